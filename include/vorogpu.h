@@ -1,0 +1,151 @@
+/* vorogpu.h — C ABI of the GB300 per-cell Voronoi engine.
+ *
+ * This is the drop-in boundary for the reference's per-particle cell path
+ * (Voro++).  Each entry point names the reference interface it replaces.
+ * All functions return an int status (VGPU_OK = 0); nothing exits, traps or
+ * prints.  Plain pointers and sizes only; host pointers unless a name says
+ * "device".  One handle = one container = one CUDA stream; handles are
+ * independent and may be used from different host threads.
+ */
+#ifndef VOROGPU_H
+#define VOROGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: 1-4 mirror VOROPP_* exit codes (src/config.hh:105-119) -- */
+#define VGPU_OK 0
+#define VGPU_ERR_FILE 1          /* VOROPP_FILE_ERROR */
+#define VGPU_ERR_MEMORY 2        /* VOROPP_MEMORY_ERROR (device allocation) */
+#define VGPU_ERR_INTERNAL 3      /* VOROPP_INTERNAL_ERROR */
+#define VGPU_ERR_ARG 16          /* bad argument / handle */
+#define VGPU_ERR_CUDA 17         /* CUDA runtime error (see vgpu_last_error) */
+#define VGPU_ERR_UNSUPPORTED 18  /* geometry not supported (e.g. sheared periodic box) */
+#define VGPU_ERR_DUPLICATE 19    /* container_periodic put of a duplicate point
+                                    (src/common.cc:14-20 exits; we return this) */
+#define VGPU_ERR_NOT_COMPUTED 20 /* results requested before vgpu_compute */
+#define VGPU_ERR_CAPACITY 21     /* a cell exceeded every engine capacity */
+#define VGPU_ERR_NO_DEVICE 22    /* no CUDA device */
+
+/* ---- container kinds (reference classes) ------------------------------- */
+#define VGPU_CONTAINER 0               /* container, src/container.hh:289-291 */
+#define VGPU_CONTAINER_POLY 1          /* container_poly, src/container.hh:511-513 */
+#define VGPU_CONTAINER_PERIODIC 2      /* container_periodic, src/container_prd.hh:213-216 */
+#define VGPU_CONTAINER_PERIODIC_POLY 3 /* container_periodic_poly, src/container_prd.hh:434-437 */
+
+/* ---- precision modes ---------------------------------------------------- */
+#define VGPU_FP64 0  /* every side test, vertex and reduction in FP64 */
+#define VGPU_MIXED 1 /* FP32 side tests under a forward error filter; filter-band
+                        hits redone in FP64; final vertices rebuilt in FP64 from
+                        their three planes; volume/centroid accumulated in FP64 */
+
+/* ---- per-cell flag bits (vgpu_get_cells, out_flags) -------------------- */
+#define VGPU_CELL_OK 1        /* compute_cell returned true (cell not deleted) */
+#define VGPU_CELL_MARGINAL 2  /* a vertex fell inside the reference tolerance band
+                                 (|plane value| <= tol): the reference would merge
+                                 vertices there; topology may differ from it */
+#define VGPU_CELL_REPAIRED 4  /* at least one FP32 test was redone in FP64 */
+
+typedef struct vgpu_container vgpu_container;
+
+/* Engine counters for the last vgpu_compute. */
+typedef struct vgpu_stats {
+    int64_t cells;            /* cells computed (stored particles) */
+    int64_t deleted;          /* cells removed entirely (compute_cell == false) */
+    int64_t marginal_cells;   /* cells flagged VGPU_CELL_MARGINAL */
+    int64_t side_tests;       /* vertex-plane side tests evaluated */
+    int64_t fp64_repairs;     /* FP32 tests redone in FP64 */
+    int64_t planes_tested;    /* candidate planes tested against a cell */
+    int64_t planes_cut;       /* candidate planes that cut a cell */
+    int64_t overflow_reruns;  /* cells re-run by the large-capacity engine */
+    int64_t failed_cells;     /* cells that overflowed every engine capacity */
+    double kernel_ms;         /* device time of the cell kernel(s), last compute */
+    double bin_ms;            /* device time of binning, last compute */
+    double step_ms;           /* device time of the whole compute (events on the handle's stream) */
+    int64_t kernel_launches;  /* engine kernels launched by the last compute */
+} vgpu_stats;
+
+/* Library / device. */
+const char *vgpu_version(void);
+int vgpu_device_count(int *count);
+/* Message for the last error on this thread. */
+const char *vgpu_last_error(void);
+
+/* Replaces the constructors container(ax,bx,ay,by,az,bz,nx,ny,nz,xper,yper,zper,
+ * init_mem) (src/container.hh:290-291), container_poly(...) (src/container.hh:512-513),
+ * container_periodic(bx,bxy,by,bxz,byz,bz,nx,ny,nz,init_mem) (src/container_prd.hh:215-216)
+ * and container_periodic_poly (src/container_prd.hh:436-437).
+ * geom: container kinds (ax,bx,ay,by,az,bz); periodic kinds (bx,bxy,by,bxz,byz,bz).
+ * grid: (nx,ny,nz) as given to the reference (it fixes the loop order of results).
+ * periodic: three flags, container kinds only (ignored for periodic kinds). */
+int vgpu_container_create(vgpu_container **out, int kind, const double geom[6],
+                          const int grid[3], const int periodic[3]);
+int vgpu_container_destroy(vgpu_container *h);
+
+/* Replaces container::put(n,x,y,z) (src/container.cc:90-97),
+ * container_poly::put(n,x,y,z,r) (src/container.cc:103-111) and
+ * container_periodic(_poly)::put (src/container_prd.cc:94-119), called n times:
+ * appends ids[i] with xyzr[4i..4i+3] = (x,y,z,r) to the container's device
+ * staging area; the copy completes before return, so the caller may reuse its
+ * arrays (r ignored for mono kinds).  Out-of-range points in non-periodic directions
+ * are dropped at compute time exactly as put_remap (src/container.cc:174-191). */
+int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyzr);
+/* Same, from device memory already resident on the container's device; the
+ * next vgpu_compute reads it in place (no host staging, no copy). */
+int vgpu_put_device(vgpu_container *h, int64_t n, const int32_t *dev_ids, const double *dev_xyzr);
+/* Replaces container::clear() (src/container.cc:385-387). */
+int vgpu_clear(vgpu_container *h);
+
+/* Replaces compute_all_cells() (src/container.cc:438-453, src/container_prd.cc:514-529):
+ * computes every cell and keeps per-cell results on the device.
+ * mode: VGPU_FP64 or VGPU_MIXED.  Synchronous. */
+int vgpu_compute(vgpu_container *h, int mode);
+/* Replaces sum_cell_volumes() (src/container.cc:459-477, src/container_prd.cc:535-546):
+ * sum of the volumes of the cells from the last compute (deleted cells add 0). */
+int vgpu_sum_cell_volumes(vgpu_container *h, double *out);
+int vgpu_get_stats(vgpu_container *h, vgpu_stats *out);
+
+/* Number of stored particles (= result records) after the last compute, in the
+ * reference's loop order (c_loop_all, src/c_loops.hh:165-210;
+ * c_loop_all_periodic, src/c_loops.hh:325-393). */
+int vgpu_num_cells(vgpu_container *h, int64_t *n);
+/* Total neighbour entries over all cells (sum of face counts). */
+int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
+
+/* Per-cell results of the last compute, in loop order; any pointer may be NULL.
+ * Replaces, per cell, the voronoicell queries the reference's callers make
+ * after compute_cell (src/container.hh:462-478):
+ *   ids      particle ID (c_loop_base::pid, src/c_loops.hh:149)
+ *   pos      stored (remapped) position, 3 doubles (c_loop_base::pos, src/c_loops.hh:123-127)
+ *   vol      voronoicell_base::volume (src/cell.cc:1584-1616)
+ *   cen      voronoicell_base::centroid, particle-relative, 3 doubles (src/cell.cc:1861-1901)
+ *   nfaces   voronoicell_base::number_of_faces (src/cell.cc:2168-2187)
+ *   nverts   voronoicell_base::p (src/cell.hh:54)
+ *   maxr2    max vertex distance squared from the particle, real units
+ *            (0.25 * voronoicell_base::max_radius_squared, src/cell.cc:1907-1917)
+ *   flags    VGPU_CELL_* bits */
+int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen,
+                   int32_t *nfaces, int32_t *nverts, double *maxr2, int32_t *flags);
+/* Neighbour lists in CSR form: offsets[n+1] (int64) and ids[total].  Each
+ * cell's list holds one ID per face, in ascending order (the reference's order,
+ * voronoicell_neighbor::neighbors src/cell.cc:2660-2678, is an artefact of
+ * plane insertion; the multiset is what is preserved).  Box walls are -1..-6
+ * (src/cell.cc:2567-2580); unit-cell faces of periodic kinds are 0
+ * (src/cell.cc:86-95). */
+int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
+
+/* Device-resident views of the results (valid until the next compute/destroy):
+ * volumes (double[n]) and face counts (int32[n]). */
+int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t **dev_nfaces);
+
+/* Engine tuning: target particles per engine block (0 = default) and warps per
+ * CTA (0 = default).  Applies from the next compute. */
+int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VOROGPU_H */

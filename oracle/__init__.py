@@ -1,0 +1,125 @@
+"""Oracle for the per-cell Voronoi path — TEST INFRASTRUCTURE ONLY.
+
+Two checkers live here; neither is part of the product and only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may use
+them:
+
+* ``RefLib``  — the unmodified reference (Voro++), compiled from its own
+  sources into ``oracle/_ref/libvoro_ref.so`` by ``oracle/Makefile``.  It only
+  exists where the reference tree exists.
+* ``PortLib`` — the CPU restatement of the reference's cell algorithm in
+  ``oracle/port/`` (built into ``oracle/_build/libvoro_port.so``).  It builds
+  anywhere and is pinned against ``RefLib`` and the committed golden fixtures.
+
+Both return per-cell records in the reference's loop order (c_loop_all,
+src/c_loops.hh:165-210; c_loop_all_periodic, src/c_loops.hh:325-393).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SO = os.path.join(HERE, "_ref", "libvoro_ref.so")
+PORT_SO = os.path.join(HERE, "_build", "libvoro_port.so")
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build_ref(quiet=True) -> bool:
+    """Builds the reference library if its sources are present."""
+    ref_src = os.environ.get("VORO_REF_SRC", "/root/reference/src")
+    if not os.path.isfile(os.path.join(ref_src, "voro++.cc")):
+        return False
+    subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return os.path.isfile(REF_SO)
+
+
+def build_port(quiet=True) -> bool:
+    subprocess.run(["make", "-C", HERE, "port"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return os.path.isfile(PORT_SO)
+
+
+class CellRecords:
+    """Per-cell results in loop order; neighbours in CSR form."""
+
+    def __init__(self, ids, pos, vol, cen, nf, nv, ok, mrs, nb, nb_off, tests=None):
+        self.ids, self.pos, self.vol, self.cen = ids, pos, vol, cen
+        self.nf, self.nv, self.ok, self.mrs = nf, nv, ok, mrs
+        self.nb, self.nb_off = nb, nb_off
+        self.tests = tests
+
+    def __len__(self):
+        return len(self.ids)
+
+    def neighbors(self, k):
+        return self.nb[self.nb_off[k]:self.nb_off[k + 1]]
+
+    def sorted_neighbors(self, k):
+        return np.sort(self.neighbors(k))
+
+    def by_id(self):
+        """Index permutation that orders records by particle ID."""
+        return np.argsort(self.ids, kind="stable")
+
+
+class _Lib:
+    path = None
+
+    def __init__(self):
+        if not os.path.isfile(self.path):
+            raise FileNotFoundError(self.path)
+        self.lib = ctypes.CDLL(self.path)
+        f = self.lib.ref_compute_cells if hasattr(self.lib, "ref_compute_cells") else None
+        self._setup(f)
+
+    def _setup(self, f):
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p,
+                      ctypes.c_int, _i32p, _f64p, _f64p, _f64p, _i32p, _i32p, _i32p, _f64p,
+                      ctypes.c_long, _i32p, _i64p]
+        self._compute = f
+
+    def compute(self, w, nb_per_cell=40) -> CellRecords:
+        n = len(w["ids"])
+        geom = np.asarray(w["geom"], dtype=np.float64)
+        grid = np.asarray(w["grid"], dtype=np.int32)
+        per = np.asarray([1 if p else 0 for p in w["periodic"]], dtype=np.int32)
+        cap = max(n, 1)
+        nb_cap = max(64, n * nb_per_cell)
+        while True:
+            ids = np.zeros(cap, np.int32); pos = np.zeros(3 * cap); vol = np.zeros(cap)
+            cen = np.zeros(3 * cap); nf = np.zeros(cap, np.int32); nv = np.zeros(cap, np.int32)
+            ok = np.zeros(cap, np.int32); mrs = np.zeros(cap)
+            nb = np.zeros(nb_cap, np.int32); nb_off = np.zeros(cap + 1, np.int64)
+            m = self._compute(int(w["kind"]), geom, grid, per, n, w["ids"], w["xyzr"], cap,
+                              ids, pos, vol, cen, nf, nv, ok, mrs, nb_cap, nb, nb_off)
+            if m >= 0:
+                break
+            if m == -2:
+                raise ValueError("bad container kind")
+            nb_cap *= 2
+        return CellRecords(ids[:m], pos[:3 * m].reshape(m, 3), vol[:m], cen[:3 * m].reshape(m, 3),
+                           nf[:m], nv[:m], ok[:m], mrs[:m], nb[:nb_off[m]], nb_off[:m + 1])
+
+
+class RefLib(_Lib):
+    path = REF_SO
+
+    def time_compute_all(self, w):
+        f = self.lib.ref_time_compute_all
+        f.restype = ctypes.c_double
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p,
+                      ctypes.POINTER(ctypes.c_double)]
+        sv = ctypes.c_double(0)
+        t = f(int(w["kind"]), np.asarray(w["geom"], np.float64), np.asarray(w["grid"], np.int32),
+              np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), len(w["ids"]),
+              w["ids"], w["xyzr"], ctypes.byref(sv))
+        return t, sv.value

@@ -1,0 +1,72 @@
+"""Loading and comparison helpers for the golden fixtures."""
+import glob
+import os
+
+import numpy as np
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(HERE, name + ".npz"))
+    w = {
+        "kind": int(z["kind"]),
+        "geom": tuple(float(v) for v in z["geom"]),
+        "grid": tuple(int(v) for v in z["grid"]),
+        "periodic": tuple(bool(v) for v in z["periodic"]),
+        "ids": z["in_ids"],
+        "xyzr": z["in_xyzr"],
+    }
+    return w, z
+
+
+def box_volume(w):
+    g = w["geom"]
+    if w["kind"] in (0, 1):
+        return (g[1] - g[0]) * (g[3] - g[2]) * (g[5] - g[4])
+    return g[0] * g[2] * g[5]
+
+
+def compare_cells(got, ref, vol_rtol, cen_rtol, label=""):
+    """got: object with ids,pos,vol,cen,nf,nv,ok and neighbors(k) sorted;
+    ref: the fixture arrays.  Returns a list of human-readable mismatches."""
+    errs = []
+    n = len(ref["ids"])
+    if len(got.ids) != n:
+        return [f"{label}: {len(got.ids)} cells vs reference {n}"]
+    if not np.array_equal(got.ids, ref["ids"]):
+        errs.append(f"{label}: loop order (ids) differs")
+    if not np.array_equal(got.pos, ref["pos"]):
+        errs.append(f"{label}: stored positions differ (max {np.abs(got.pos - ref['pos']).max():.3g})")
+    ok_ref = ref["ok"] != 0
+    ok_got = np.asarray(got.ok, dtype=bool)
+    if not np.array_equal(ok_got, ok_ref):
+        errs.append(f"{label}: deleted-cell flags differ at {np.nonzero(ok_got != ok_ref)[0][:10]}")
+    m = ok_ref & ok_got
+    bad_nf = np.nonzero((got.nf != ref["nf"]) & m)[0]
+    bad_nv = np.nonzero((got.nv != ref["nv"]) & m)[0]
+    if len(bad_nf):
+        errs.append(f"{label}: face counts differ at {len(bad_nf)} cells, e.g. {bad_nf[:5]}")
+    if len(bad_nv):
+        errs.append(f"{label}: vertex counts differ at {len(bad_nv)} cells, e.g. {bad_nv[:5]}")
+    nbad = 0
+    for k in np.nonzero(m)[0]:
+        a = np.asarray(got.neighbors(k))
+        b = ref["nb"][ref["nb_off"][k]:ref["nb_off"][k + 1]]
+        if len(a) != len(b) or not np.array_equal(np.sort(a), b):
+            nbad += 1
+    if nbad:
+        errs.append(f"{label}: neighbour lists differ at {nbad} cells")
+    v = ref["vol"][m]
+    rel = np.abs(got.vol[m] - v) / np.maximum(np.abs(v), 1e-300)
+    if len(rel) and rel.max() > vol_rtol:
+        errs.append(f"{label}: max relative volume error {rel.max():.3g} > {vol_rtol}")
+    scale = np.cbrt(np.maximum(np.abs(v), 1e-300))[:, None]
+    cerr = np.abs(got.cen[m] - ref["cen"][m]) / scale
+    if len(cerr) and cerr.max() > cen_rtol:
+        errs.append(f"{label}: max centroid error / cell size {cerr.max():.3g} > {cen_rtol}")
+    return errs

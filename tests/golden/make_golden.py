@@ -1,0 +1,81 @@
+"""Generates the golden per-cell fixtures from the unmodified reference.
+
+Run in a tree where the reference sources exist (oracle/Makefile builds
+oracle/_ref/libvoro_ref.so from them):
+
+    python tests/golden/make_golden.py
+
+Each case stores its inputs (so the fixture does not depend on a random
+number generator) and the reference's per-cell records in loop order:
+ids, stored positions, volume, centroid, face count, vertex count,
+max_radius_squared, ok flag and the neighbour lists (CSR, each list sorted).
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import RefLib, build_ref  # noqa: E402
+from voro_gb300 import workloads as W  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def cases():
+    out = {}
+    # container on the unit cube, non-periodic (the 100k shape, scaled down)
+    out["unit_cube_1000"] = W.unit_cube(n=1000, seed=2001, grid=(3, 3, 3))
+    # container_periodic, density 4 (the 4M / L=100 shape)
+    n = 2000
+    L = 100.0 * (n / 4e6) ** (1 / 3)
+    out["periodic_2000"] = W.periodic_cube(n=n, L=L, seed=2002, grid=(7, 7, 7))
+    # flag-periodic container on the same kind of box
+    out["flagperiodic_1500"] = W.periodic_cube(n=1500, L=100.0 * (1500 / 4e6) ** (1 / 3), seed=2003,
+                                              grid=(6, 6, 6), kind=W.KIND_CONTAINER)
+    # container_poly, log-normal radii (the 2M / 200^3 shape)
+    n = 1200
+    out["radical_1200"] = W.radical_box(n=n, L=200.0 * (n / 2e6) ** (1 / 3), seed=2004, grid=(6, 6, 6))
+    # jittered FCC, container_periodic
+    out["fcc_6"] = W.fcc_jitter(cells=6, sigma=1e-7, seed=2005)
+    # mixed walls: periodic in x only
+    out["xperiodic_600"] = W.small_random(600, kind=W.KIND_CONTAINER, L=2.0, periodic=(True, False, False),
+                                          grid=(4, 5, 3), seed=2006)
+    # a few particles in a mostly empty grid, including out-of-range ones that put() drops
+    w = W.small_random(40, kind=W.KIND_CONTAINER, L=2.0, grid=(6, 6, 6), seed=2007)
+    w["xyzr"][:, :3] -= 1.0  # container is [0,2]^3: about half of these fall outside and are dropped
+    w["geom"] = (-0.5, 1.0, -0.5, 1.0, -0.5, 1.0)
+    out["sparse_dropped_40"] = w
+    # container_periodic_poly
+    w = W.small_random(800, kind=W.KIND_PERIODIC_POLY, L=8.0, grid=(5, 5, 5), seed=2008, rmin=0.2, rmax=0.8)
+    out["periodic_poly_800"] = w
+    return out
+
+
+def main():
+    if not build_ref():
+        raise SystemExit("reference sources not available; cannot generate fixtures")
+    ref = RefLib()
+    for name, w in cases().items():
+        rec = ref.compute(w)
+        nb = []
+        for k in range(len(rec)):
+            nb.append(np.sort(rec.neighbors(k)))
+        nb_off = np.zeros(len(rec) + 1, np.int64)
+        nb_off[1:] = np.cumsum([len(x) for x in nb])
+        nb_flat = np.concatenate(nb).astype(np.int32) if nb else np.zeros(0, np.int32)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(
+            path, kind=w["kind"], geom=np.asarray(w["geom"]), grid=np.asarray(w["grid"], np.int32),
+            periodic=np.asarray(w["periodic"], np.int32), in_ids=w["ids"], in_xyzr=w["xyzr"],
+            ids=rec.ids, pos=rec.pos, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, ok=rec.ok, mrs=rec.mrs,
+            nb=nb_flat, nb_off=nb_off)
+        print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,50 @@
+"""Golden fixtures: produced by the unmodified reference (tests/golden/make_golden.py).
+Where the reference tree exists, the fixtures are re-derived and must match bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+from tests import _golden as G
+
+NAMES = G.names()
+
+
+def test_fixtures_present():
+    assert len(NAMES) >= 8
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_volumes_tile_the_box(name):
+    w, z = G.load(name)
+    ok = z["ok"] != 0
+    assert abs(z["vol"][ok].sum() - G.box_volume(w)) <= 1e-11 * G.box_volume(w)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_neighbour_relation_is_symmetric(name):
+    w, z = G.load(name)
+    ids = z["ids"]
+    pairs = set()
+    for k in range(len(ids)):
+        for j in z["nb"][z["nb_off"][k]:z["nb_off"][k + 1]]:
+            if j >= 0:
+                pairs.add((int(ids[k]), int(j)))
+    kept = set(int(i) for i in ids)
+    for a, b in pairs:
+        if b in kept:
+            assert (b, a) in pairs, (a, b)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fixture_rederived_from_reference(name):
+    from oracle import REF_SO, RefLib
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference library not built here")
+    w, z = G.load(name)
+    rec = RefLib().compute(w)
+    assert np.array_equal(rec.ids, z["ids"])
+    assert np.array_equal(rec.vol, z["vol"])
+    assert np.array_equal(rec.cen, z["cen"])
+    assert np.array_equal(rec.nf, z["nf"])
+    assert np.array_equal(rec.nv, z["nv"])

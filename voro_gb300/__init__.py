@@ -1,0 +1,430 @@
+"""GB300 engine for Voro++'s per-particle Voronoi cell computation.
+
+The host classes mirror the reference's container API (src/container.hh,
+src/container_prd.hh) and call the CUDA engine through its C ABI
+(include/vorogpu.h, built into ``voro_gb300/_lib/libvorogpu.so``).  There is
+no CPU fallback: if the library or a GPU is missing, construction raises.
+
+    from voro_gb300 import container
+    con = container(0, 1, 0, 1, 0, 1, 6, 6, 6, False, False, False, 8)
+    for i, (x, y, z) in enumerate(points):
+        con.put(i, x, y, z)
+    vol = con.sum_cell_volumes()
+    con.print_custom("%i %q %v %s %n", "out.vol")
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+from . import _build
+
+VGPU_OK = 0
+VGPU_FP64 = 0
+VGPU_MIXED = 1
+VGPU_CELL_OK = 1
+VGPU_CELL_MARGINAL = 2
+VGPU_CELL_REPAIRED = 4
+
+KIND_CONTAINER = 0
+KIND_CONTAINER_POLY = 1
+KIND_PERIODIC = 2
+KIND_PERIODIC_POLY = 3
+
+# Reference status codes (src/config.hh:105-119) plus the engine's own.
+STATUS_NAMES = {
+    0: "VGPU_OK", 1: "VGPU_ERR_FILE", 2: "VGPU_ERR_MEMORY", 3: "VGPU_ERR_INTERNAL", 16: "VGPU_ERR_ARG",
+    17: "VGPU_ERR_CUDA", 18: "VGPU_ERR_UNSUPPORTED", 19: "VGPU_ERR_DUPLICATE", 20: "VGPU_ERR_NOT_COMPUTED",
+    21: "VGPU_ERR_CAPACITY", 22: "VGPU_ERR_NO_DEVICE",
+}
+
+# Every symbol include/vorogpu.h declares.
+EXPORTED = [
+    "vgpu_version", "vgpu_device_count", "vgpu_last_error", "vgpu_container_create", "vgpu_container_destroy",
+    "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
+    "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
+    "vgpu_set_tuning",
+]
+
+
+class VoroError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("cells", ctypes.c_int64), ("deleted", ctypes.c_int64), ("marginal_cells", ctypes.c_int64),
+                ("side_tests", ctypes.c_int64), ("fp64_repairs", ctypes.c_int64),
+                ("planes_tested", ctypes.c_int64), ("planes_cut", ctypes.c_int64),
+                ("overflow_reruns", ctypes.c_int64), ("failed_cells", ctypes.c_int64),
+                ("kernel_ms", ctypes.c_double), ("bin_ms", ctypes.c_double), ("step_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load_library(build_if_missing=True):
+    """Loads libvorogpu.so (building it from source if absent).  Raises if it
+    cannot be built or loaded: the engine has no CPU path."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB) or (build_if_missing and not _build.up_to_date()):
+        if not build_if_missing:
+            raise RuntimeError(f"engine library missing: {_build.LIB}")
+        _build.build()
+    lib = ctypes.CDLL(_build.LIB)
+    vp = ctypes.c_void_p
+    i64 = ctypes.c_int64
+    pd = ctypes.POINTER(ctypes.c_double)
+    pi = ctypes.POINTER(ctypes.c_int32)
+    lib.vgpu_version.restype = ctypes.c_char_p
+    lib.vgpu_last_error.restype = ctypes.c_char_p
+    lib.vgpu_device_count.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    lib.vgpu_container_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, pd, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_int)]
+    lib.vgpu_container_destroy.argtypes = [vp]
+    lib.vgpu_put.argtypes = [vp, i64, vp, vp]
+    lib.vgpu_put_device.argtypes = [vp, i64, vp, vp]
+    lib.vgpu_clear.argtypes = [vp]
+    lib.vgpu_compute.argtypes = [vp, ctypes.c_int]
+    lib.vgpu_sum_cell_volumes.argtypes = [vp, pd]
+    lib.vgpu_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.vgpu_num_cells.argtypes = [vp, ctypes.POINTER(i64)]
+    lib.vgpu_num_neighbors.argtypes = [vp, ctypes.POINTER(i64)]
+    lib.vgpu_get_cells.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.vgpu_get_neighbors.argtypes = [vp, vp, vp]
+    lib.vgpu_device_results.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+    for name in EXPORTED:
+        if name not in ("vgpu_version", "vgpu_last_error"):
+            getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != VGPU_OK:
+        raise VoroError(rc, _lib.vgpu_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_count():
+    lib = load_library()
+    c = ctypes.c_int(0)
+    _check(lib.vgpu_device_count(ctypes.byref(c)))
+    return c.value
+
+
+class CellResults:
+    """Per-cell results in the reference's loop order."""
+
+    def __init__(self, ids, pos, vol, cen, nf, nv, maxr2, flags, nb=None, nb_off=None):
+        self.ids, self.pos, self.vol, self.cen = ids, pos, vol, cen
+        self.nf, self.nv, self.maxr2, self.flags = nf, nv, maxr2, flags
+        self.nb, self.nb_off = nb, nb_off
+
+    def __len__(self):
+        return len(self.ids)
+
+    @property
+    def ok(self):
+        return (self.flags & VGPU_CELL_OK) != 0
+
+    def neighbors(self, k):
+        return self.nb[self.nb_off[k]:self.nb_off[k + 1]]
+
+
+class _ContainerBase:
+    """Shared implementation of the four reference container classes."""
+
+    _kind = None
+
+    def __init__(self, kind, geom, grid, periodic, mode="mixed"):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        g = (ctypes.c_double * 6)(*[float(v) for v in geom])
+        gr = (ctypes.c_int * 3)(*[int(v) for v in grid])
+        pe = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
+        _check(self._lib.vgpu_container_create(ctypes.byref(self._h), kind, g, gr, pe))
+        self.kind = kind
+        self.geom = tuple(float(v) for v in geom)
+        self.grid = tuple(int(v) for v in grid)
+        self.periodic = tuple(bool(p) for p in periodic)
+        self.mode = mode
+        self._pending_ids = []
+        self._pending_xyzr = []
+        self._dirty = True
+        self._dev_keep = None
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._lib.vgpu_container_destroy(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    # ---- put(): src/container.cc:90-111, src/container_prd.cc:94-119
+    def _put(self, n, x, y, z, r):
+        self._pending_ids.append(int(n))
+        self._pending_xyzr.extend((float(x), float(y), float(z), float(r)))
+        self._dirty = True
+
+    def _flush_pending(self):
+        if self._pending_ids:
+            ids = np.asarray(self._pending_ids, dtype=np.int32)
+            xyzr = np.asarray(self._pending_xyzr, dtype=np.float64)
+            _check(self._lib.vgpu_put(self._h, len(ids), _ptr(ids), _ptr(xyzr)))
+            self._pending_ids = []
+            self._pending_xyzr = []
+
+    def put_array(self, ids, xyz, r=None):
+        """Vectorised put(): ids (n,), xyz (n,3), optional radii (n,)."""
+        self._flush_pending()
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        xyz = np.asarray(xyz, dtype=np.float64)
+        n = len(ids)
+        xyzr = np.empty((n, 4), dtype=np.float64)
+        xyzr[:, :3] = xyz
+        xyzr[:, 3] = 0.5 if r is None else r
+        _check(self._lib.vgpu_put(self._h, n, _ptr(ids), _ptr(xyzr)))
+        self._dirty = True
+
+    def put_xyzr(self, ids, xyzr):
+        """put() of int32 ids (n,) and float64 xyzr (n,4) without a host copy."""
+        self._flush_pending()
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        xyzr = np.ascontiguousarray(xyzr, dtype=np.float64)
+        assert xyzr.shape == (len(ids), 4)
+        _check(self._lib.vgpu_put(self._h, len(ids), _ptr(ids), _ptr(xyzr)))
+        self._dirty = True
+
+    def put_device(self, n, dev_ids_ptr, dev_xyzr_ptr, keepalive=None):
+        """Points the container at particle arrays already in device memory
+        (int32 ids, float64 (n,4) xyzr); ``keepalive`` holds their owner."""
+        self._pending_ids, self._pending_xyzr = [], []
+        _check(self._lib.vgpu_put_device(self._h, int(n), ctypes.c_void_p(dev_ids_ptr),
+                                         ctypes.c_void_p(dev_xyzr_ptr)))
+        self._dev_keep = keepalive
+        self._dirty = True
+
+    def clear(self):
+        """container::clear (src/container.cc:385-387)."""
+        self._pending_ids, self._pending_xyzr = [], []
+        self._dev_keep = None
+        _check(self._lib.vgpu_clear(self._h))
+        self._dirty = True
+
+    def set_tuning(self, particles_per_block=0.0, warps_per_cta=0):
+        _check(self._lib.vgpu_set_tuning(self._h, float(particles_per_block), int(warps_per_cta)))
+        self._dirty = True
+
+    def _mode_code(self, mode):
+        mode = mode or self.mode
+        return VGPU_FP64 if mode == "fp64" else VGPU_MIXED
+
+    # ---- compute_all_cells: src/container.cc:438-453
+    def compute_all_cells(self, mode=None):
+        self._flush_pending()
+        _check(self._lib.vgpu_compute(self._h, self._mode_code(mode)))
+        self._dirty = False
+
+    def _ensure(self):
+        if self._dirty:
+            self.compute_all_cells()
+
+    # ---- sum_cell_volumes: src/container.cc:459-477
+    def sum_cell_volumes(self):
+        self._ensure()
+        out = ctypes.c_double(0)
+        _check(self._lib.vgpu_sum_cell_volumes(self._h, ctypes.byref(out)))
+        return out.value
+
+    def stats(self):
+        st = Stats()
+        _check(self._lib.vgpu_get_stats(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def total_particles(self):
+        self._ensure()
+        n = ctypes.c_int64(0)
+        _check(self._lib.vgpu_num_cells(self._h, ctypes.byref(n)))
+        return n.value
+
+    def cells(self, neighbors=True):
+        """All per-cell results (CellResults) from the last compute."""
+        self._ensure()
+        n = self.total_particles()
+        ids = np.zeros(n, np.int32); pos = np.zeros((n, 3)); vol = np.zeros(n); cen = np.zeros((n, 3))
+        nf = np.zeros(n, np.int32); nv = np.zeros(n, np.int32); mr2 = np.zeros(n); fl = np.zeros(n, np.int32)
+        _check(self._lib.vgpu_get_cells(self._h, _ptr(ids), _ptr(pos), _ptr(vol), _ptr(cen), _ptr(nf),
+                                        _ptr(nv), _ptr(mr2), _ptr(fl)))
+        res = CellResults(ids, pos, vol, cen, nf, nv, mr2, fl)
+        if neighbors:
+            tot = ctypes.c_int64(0)
+            _check(self._lib.vgpu_num_neighbors(self._h, ctypes.byref(tot)))
+            off = np.zeros(n + 1, np.int64)
+            nb = np.zeros(max(tot.value, 1), np.int32)
+            _check(self._lib.vgpu_get_neighbors(self._h, _ptr(off), _ptr(nb)))
+            res.nb, res.nb_off = nb[:tot.value], off
+        return res
+
+    # ---- print_custom: src/container.hh:434-451, src/cell.cc:2485-2558
+    def print_custom(self, fmt, fp=None):
+        """Writes one line per computed cell with the reference's %-fields.
+        ``fp`` is a file object, a filename, or None (stdout)."""
+        res = self.cells(neighbors=("%n" in fmt))
+        close = False
+        if fp is None:
+            fp = sys.stdout
+        elif isinstance(fp, (str, os.PathLike)):
+            fp = open(fp, "w")
+            close = True
+        try:
+            radius = (lambda k: float(self._radius_of(k)))
+            for k in range(len(res)):
+                if not res.ok[k]:
+                    continue
+                fp.write(_format_custom(fmt, res, k, radius) + "\n")
+        finally:
+            if close:
+                fp.close()
+
+    def _radius_of(self, k):
+        return 0.5  # default_radius (src/config.hh:88); container_poly also prints it (container.hh:445)
+
+
+def _vec(v):
+    return " ".join(str(int(x)) for x in v)
+
+
+def _format_custom(fmt, res, k, radius):
+    out = []
+    i = 0
+    n = len(fmt)
+    while i < n:
+        ch = fmt[i]
+        if ch != "%":
+            out.append(ch)
+            i += 1
+            continue
+        i += 1
+        if i >= n:
+            break
+        f = fmt[i]
+        x, y, z = res.pos[k]
+        if f == "i":
+            out.append("%d" % res.ids[k])
+        elif f == "x":
+            out.append("%g" % x)
+        elif f == "y":
+            out.append("%g" % y)
+        elif f == "z":
+            out.append("%g" % z)
+        elif f == "q":
+            out.append("%g %g %g" % (x, y, z))
+        elif f == "r":
+            out.append("%g" % radius(k))
+        elif f == "w":
+            out.append("%d" % res.nv[k])
+        elif f == "o":
+            out.append(" ".join(["3"] * int(res.nv[k])))
+        elif f == "m":
+            out.append("%g" % res.maxr2[k])
+        elif f == "g":
+            out.append("%d" % (3 * int(res.nv[k]) // 2))
+        elif f == "s":
+            out.append("%d" % res.nf[k])
+        elif f == "n":
+            out.append(_vec(res.neighbors(k)))
+        elif f == "v":
+            out.append("%g" % res.vol[k])
+        elif f == "c":
+            out.append("%g %g %g" % tuple(res.cen[k]))
+        elif f == "C":
+            cx, cy, cz = res.cen[k]
+            out.append("%g %g %g" % (x + cx, y + cy, z + cz))
+        elif f in "pPeEFAaftl":
+            raise NotImplementedError(f"print_custom field %{f} is not produced by the engine yet")
+        else:
+            out.append("%" + f)
+        i += 1
+    return "".join(out)
+
+
+class container(_ContainerBase):
+    """container(ax,bx,ay,by,az,bz,nx,ny,nz,xperiodic,yperiodic,zperiodic,init_mem)
+    (src/container.hh:289-291)."""
+
+    def __init__(self, ax, bx, ay, by, az, bz, nx, ny, nz, xperiodic, yperiodic, zperiodic, init_mem=8,
+                 mode="mixed"):
+        super().__init__(KIND_CONTAINER, (ax, bx, ay, by, az, bz), (nx, ny, nz),
+                         (xperiodic, yperiodic, zperiodic), mode)
+
+    def put(self, n, x, y, z):
+        self._put(n, x, y, z, 0.5)
+
+
+class container_poly(_ContainerBase):
+    """container_poly(...) (src/container.hh:511-513): radical tessellation."""
+
+    def __init__(self, ax, bx, ay, by, az, bz, nx, ny, nz, xperiodic, yperiodic, zperiodic, init_mem=8,
+                 mode="mixed"):
+        super().__init__(KIND_CONTAINER_POLY, (ax, bx, ay, by, az, bz), (nx, ny, nz),
+                         (xperiodic, yperiodic, zperiodic), mode)
+
+    def put(self, n, x, y, z, r):
+        self._put(n, x, y, z, r)
+
+
+class container_periodic(_ContainerBase):
+    """container_periodic(bx,bxy,by,bxz,byz,bz,nx,ny,nz,init_mem)
+    (src/container_prd.hh:213-216); rectangular boxes (bxy=bxz=byz=0)."""
+
+    def __init__(self, bx, bxy, by, bxz, byz, bz, nx, ny, nz, init_mem=8, mode="mixed"):
+        super().__init__(KIND_PERIODIC, (bx, bxy, by, bxz, byz, bz), (nx, ny, nz), (True, True, True), mode)
+
+    def put(self, n, x, y, z):
+        self._put(n, x, y, z, 0.5)
+
+
+class container_periodic_poly(_ContainerBase):
+    """container_periodic_poly (src/container_prd.hh:434-437)."""
+
+    def __init__(self, bx, bxy, by, bxz, byz, bz, nx, ny, nz, init_mem=8, mode="mixed"):
+        super().__init__(KIND_PERIODIC_POLY, (bx, bxy, by, bxz, byz, bz), (nx, ny, nz), (True, True, True), mode)
+
+    def put(self, n, x, y, z, r):
+        self._put(n, x, y, z, r)
+
+
+def from_workload(w, mode="mixed"):
+    """Builds a container from a ``voro_gb300.workloads`` dict and puts its particles."""
+    kind = w["kind"]
+    if kind == KIND_CONTAINER:
+        c = container(*w["geom"], *w["grid"], *w["periodic"], 8, mode=mode)
+    elif kind == KIND_CONTAINER_POLY:
+        c = container_poly(*w["geom"], *w["grid"], *w["periodic"], 8, mode=mode)
+    elif kind == KIND_PERIODIC:
+        c = container_periodic(*w["geom"], *w["grid"], 8, mode=mode)
+    else:
+        c = container_periodic_poly(*w["geom"], *w["grid"], 8, mode=mode)
+    xyzr = w["xyzr"]
+    c.put_array(w["ids"], xyzr[:, :3], xyzr[:, 3])
+    return c

@@ -1,0 +1,670 @@
+// C ABI of the engine (declared in include/vorogpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "vgpu_internal.cuh"
+#include "../../include/vorogpu.h"
+
+#include <atomic>
+
+namespace vgpu {
+cudaError_t upload_box_tables();
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}
+
+using namespace vgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define VG_CUDA(expr)                                                                        \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess)                                                               \
+            return fail(_e == cudaErrorMemoryAllocation ? VGPU_ERR_MEMORY : VGPU_ERR_CUDA,   \
+                        "%s: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__, __LINE__); \
+    } while (0)
+
+// A device buffer that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t b = want + want / 8 + 256;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+std::mutex g_dev_mutex;
+bool g_box_uploaded[64] = {false};
+
+struct OffsetTable {
+    std::vector<int> codes;
+    std::vector<int> group_start;
+    std::vector<int> group_lb2;
+};
+
+const OffsetTable &offset_table() {
+    static OffsetTable t = [] {
+        OffsetTable o;
+        struct E { int lb2, r2, code; };
+        std::vector<E> es;
+        const int R = kOffsetRadius;
+        for (int dk = -R; dk <= R; dk++)
+            for (int dj = -R; dj <= R; dj++)
+                for (int di = -R; di <= R; di++) {
+                    int a = std::max(std::abs(di) - 1, 0), b = std::max(std::abs(dj) - 1, 0),
+                        c = std::max(std::abs(dk) - 1, 0);
+                    int lb2 = a * a + b * b + c * c;
+                    if (lb2 > kTableLb2Max) continue;
+                    int code = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
+                    es.push_back({lb2, di * di + dj * dj + dk * dk, code});
+                }
+        std::stable_sort(es.begin(), es.end(), [](const E &x, const E &y) {
+            if (x.lb2 != y.lb2) return x.lb2 < y.lb2;
+            return x.r2 < y.r2;
+        });
+        for (size_t i = 0; i < es.size(); i++) {
+            if (i == 0 || es[i].lb2 != es[i - 1].lb2) {
+                o.group_start.push_back((int)i);
+                o.group_lb2.push_back(es[i].lb2);
+            }
+            o.codes.push_back(es[i].code);
+        }
+        o.group_start.push_back((int)es.size());
+        return o;
+    }();
+    return t;
+}
+
+}  // namespace
+
+struct vgpu_container {
+    Geometry g;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6];
+    double target_density = 2.5;
+    int warps_per_cta = 4;
+    // particles put() so far, staged on the device in put() order
+    int64_t staged = 0;
+    // device input (either owned copies or caller's device arrays)
+    const int32_t *dev_ids_ext = nullptr;
+    const double *dev_xyzr_ext = nullptr;
+    int64_t dev_n_ext = 0;
+    bool use_device_input = false;
+    DevBuf ids_in, xyzr_in;
+    // work buffers
+    DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
+    DevBuf p64, l32, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
+    // results
+    DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, nb_off, nb_out, nb_tmp, sum_tmp;
+    int64_t ncells = 0;
+    bool computed = false;
+    vgpu_stats stats{};
+};
+
+namespace {
+
+int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int grid[3], const int periodic[3]) {
+    Geometry &g = h->g;
+    memset(&g, 0, sizeof(g));
+    g.kind = kind;
+    g.poly = (kind == VGPU_CONTAINER_POLY || kind == VGPU_CONTAINER_PERIODIC_POLY) ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        if (grid[a] < 1) return fail(VGPU_ERR_ARG, "grid[%d] = %d must be >= 1", a, grid[a]);
+        g.un[a] = grid[a];
+    }
+    double max_len_sq;
+    if (kind == VGPU_CONTAINER || kind == VGPU_CONTAINER_POLY) {
+        g.unit_cell = 0;
+        for (int a = 0; a < 3; a++) {
+            g.lo[a] = geom[2 * a];
+            g.hi[a] = geom[2 * a + 1];
+            g.len[a] = g.hi[a] - g.lo[a];
+            if (!(g.len[a] > 0)) return fail(VGPU_ERR_ARG, "empty container extent on axis %d", a);
+            g.per[a] = periodic ? (periodic[a] != 0) : 0;
+            g.ubox[a] = g.len[a] / g.un[a];   // src/container.cc:31
+            g.usp[a] = 1 / g.ubox[a];          // src/v_base.cc:26
+        }
+        // src/container.cc:34-35
+        max_len_sq = g.len[0] * g.len[0] * (g.per[0] ? 0.25 : 1) + g.len[1] * g.len[1] * (g.per[1] ? 0.25 : 1) +
+                     g.len[2] * g.len[2] * (g.per[2] ? 0.25 : 1);
+    } else if (kind == VGPU_CONTAINER_PERIODIC || kind == VGPU_CONTAINER_PERIODIC_POLY) {
+        // geom = (bx, bxy, by, bxz, byz, bz)
+        if (geom[1] != 0.0 || geom[3] != 0.0 || geom[4] != 0.0)
+            return fail(VGPU_ERR_UNSUPPORTED, "sheared periodic boxes (bxy, bxz, byz != 0) are not supported yet");
+        g.unit_cell = 1;
+        double L[3] = {geom[0], geom[2], geom[5]};
+        for (int a = 0; a < 3; a++) {
+            if (!(L[a] > 0)) return fail(VGPU_ERR_ARG, "periodic length on axis %d must be > 0", a);
+            g.lo[a] = 0;
+            g.len[a] = L[a];
+            g.hi[a] = L[a];
+            g.per[a] = 1;
+            g.ubox[a] = L[a] / g.un[a];        // src/container_prd.cc:31
+            g.usp[a] = 1 / g.ubox[a];
+        }
+        // unit_voro.max_radius_squared() of the rectangular unit cell
+        // (src/container_prd.cc:32), in the reference's doubled coordinates
+        max_len_sq = L[0] * L[0] + L[1] * L[1] + L[2] * L[2];
+    } else {
+        return fail(VGPU_ERR_ARG, "unknown container kind %d", kind);
+    }
+    double tol = 10.0 * 2.220446049250313e-16 * max_len_sq;  // src/config.hh:80, src/cell.cc:24
+    g.tol_h = 0.5 * tol;
+    g.tol_cu = tol * std::sqrt(tol);
+    return VGPU_OK;
+}
+
+void choose_engine_grid(Geometry &g, int64_t n, double density) {
+    double vol = g.len[0] * g.len[1] * g.len[2];
+    double nn = (double)std::max<int64_t>(n, 1);
+    double bs = std::cbrt(vol * density / nn);
+    long long total = 1;
+    for (int a = 0; a < 3; a++) {
+        int m = (int)std::floor(g.len[a] / bs + 0.5);
+        m = std::max(1, std::min(m, 1 << 10));
+        g.gn[a] = m;
+        total *= m;
+    }
+    while (total > (1ll << 26)) {
+        total = 1;
+        for (int a = 0; a < 3; a++) {
+            g.gn[a] = std::max(1, g.gn[a] / 2);
+            total *= g.gn[a];
+        }
+    }
+    float bmin = 3.4e38f;
+    for (int a = 0; a < 3; a++) {
+        g.gbs[a] = g.len[a] / g.gn[a];
+        g.gbs32[a] = (float)g.gbs[a];
+        bmin = std::min(bmin, g.gbs32[a]);
+    }
+    g.gbs_min = bmin * (1.0f - 1e-6f);
+}
+
+int ensure_device(vgpu_container *h) {
+    int dev = 0;
+    VG_CUDA(cudaGetDevice(&dev));
+    h->device = dev;
+    std::lock_guard<std::mutex> lock(g_dev_mutex);
+    if (dev >= 0 && dev < 64 && !g_box_uploaded[dev]) {
+        VG_CUDA(upload_box_tables());
+        g_box_uploaded[dev] = true;
+    }
+    return VGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vgpu_version(void) { return "vorogpu 0.1 (sm_103a)"; }
+
+const char *vgpu_last_error(void) { return g_last_error.c_str(); }
+
+int vgpu_device_count(int *count) {
+    if (!count) return fail(VGPU_ERR_ARG, "null count");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) c = 0;
+    *count = c;
+    return VGPU_OK;
+}
+
+int vgpu_container_create(vgpu_container **out, int kind, const double geom[6], const int grid[3],
+                          const int periodic[3]) {
+    if (!out || !geom || !grid) return fail(VGPU_ERR_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VGPU_ERR_NO_DEVICE, "no CUDA device");
+    vgpu_container *h = new vgpu_container();
+    int rc = setup_geometry(h, kind, geom, grid, periodic);
+    if (rc != VGPU_OK) {
+        delete h;
+        return rc;
+    }
+    rc = ensure_device(h);
+    if (rc != VGPU_OK) {
+        delete h;
+        return rc;
+    }
+    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(VGPU_ERR_CUDA, "stream creation failed");
+    }
+    for (int i = 0; i < 6; i++) cudaEventCreate(&h->ev[i]);
+    *out = h;
+    return VGPU_OK;
+}
+
+int vgpu_container_destroy(vgpu_container *h) {
+    if (!h) return VGPU_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    DevBuf *bufs[] = {&h->ids_in, &h->xyzr_in, &h->rem, &h->ukey, &h->gkey, &h->idx, &h->idx2, &h->keys_alt,
+                      &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64, &h->l32, &h->pid,
+                      &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
+                      &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
+                      &h->r_pos, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+    for (DevBuf *b : bufs) b->release();
+    for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return VGPU_OK;
+}
+
+int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyzr) {
+    if (!h || n < 0 || (n > 0 && (!ids || !xyzr))) return fail(VGPU_ERR_ARG, "bad put arguments");
+    if (h->use_device_input) {
+        h->use_device_input = false;
+        h->dev_ids_ext = nullptr;
+        h->dev_xyzr_ext = nullptr;
+        h->dev_n_ext = 0;
+        h->staged = 0;
+    }
+    if (n == 0) return VGPU_OK;
+    if (h->staged + n > (int64_t)INT32_MAX / 2) return fail(VGPU_ERR_MEMORY, "too many particles");
+    const size_t want = (size_t)(h->staged + n);
+    if (want * 32 > h->xyzr_in.bytes || want * 4 > h->ids_in.bytes) {
+        // grow the device staging area, keeping what is already there
+        DevBuf ni, nx;
+        size_t cap = std::max(want, (size_t)(h->staged * 2));
+        VG_CUDA(ni.ensure(cap * 4));
+        VG_CUDA(nx.ensure(cap * 32));
+        if (h->staged > 0) {
+            VG_CUDA(cudaMemcpyAsync(ni.p, h->ids_in.p, (size_t)h->staged * 4, cudaMemcpyDeviceToDevice, h->stream));
+            VG_CUDA(cudaMemcpyAsync(nx.p, h->xyzr_in.p, (size_t)h->staged * 32, cudaMemcpyDeviceToDevice, h->stream));
+            VG_CUDA(cudaStreamSynchronize(h->stream));
+        }
+        h->ids_in.release();
+        h->xyzr_in.release();
+        h->ids_in = ni;
+        h->xyzr_in = nx;
+        ni.p = nx.p = nullptr;
+    }
+    // synchronous with respect to the caller's arrays: they may be reused on return
+    VG_CUDA(cudaMemcpyAsync(h->ids_in.as<int32_t>() + h->staged, ids, (size_t)n * 4, cudaMemcpyHostToDevice,
+                            h->stream));
+    VG_CUDA(cudaMemcpyAsync(h->xyzr_in.as<double>() + 4 * h->staged, xyzr, (size_t)n * 32,
+                            cudaMemcpyHostToDevice, h->stream));
+    VG_CUDA(cudaStreamSynchronize(h->stream));
+    h->staged += n;
+    h->computed = false;
+    return VGPU_OK;
+}
+
+int vgpu_put_device(vgpu_container *h, int64_t n, const int32_t *dev_ids, const double *dev_xyzr) {
+    if (!h || n < 0 || (n > 0 && (!dev_ids || !dev_xyzr))) return fail(VGPU_ERR_ARG, "bad put_device arguments");
+    if (n > (int64_t)INT32_MAX / 2) return fail(VGPU_ERR_MEMORY, "too many particles");
+    h->staged = 0;
+    h->use_device_input = true;
+    h->dev_ids_ext = dev_ids;
+    h->dev_xyzr_ext = dev_xyzr;
+    h->dev_n_ext = n;
+    h->computed = false;
+    return VGPU_OK;
+}
+
+int vgpu_clear(vgpu_container *h) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    h->staged = 0;
+    h->use_device_input = false;
+    h->dev_ids_ext = nullptr;
+    h->dev_xyzr_ext = nullptr;
+    h->dev_n_ext = 0;
+    h->computed = false;
+    h->ncells = 0;
+    return VGPU_OK;
+}
+
+int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (particles_per_block > 0) h->target_density = particles_per_block;
+    if (warps_per_cta > 0) h->warps_per_cta = warps_per_cta;
+    return VGPU_OK;
+}
+
+int vgpu_compute(vgpu_container *h, int mode) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    cudaStream_t s = h->stream;
+    const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
+    const int n = (int)n64;
+    Geometry &g = h->g;
+    memset(&h->stats, 0, sizeof(h->stats));
+    choose_engine_grid(g, n64, h->target_density);
+    const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
+    const int nub = g.un[0] * g.un[1] * g.un[2];
+    const size_t nn = (size_t)std::max(n, 1);
+
+    // inputs
+    const int32_t *d_ids;
+    const double *d_xyzr;
+    if (h->use_device_input) {
+        d_ids = h->dev_ids_ext;
+        d_xyzr = h->dev_xyzr_ext;
+    } else {
+        VG_CUDA(h->ids_in.ensure(nn * 4));
+        VG_CUDA(h->xyzr_in.ensure(nn * 32));
+        d_ids = h->ids_in.as<int32_t>();
+        d_xyzr = h->xyzr_in.as<double>();
+    }
+    if ((reinterpret_cast<uintptr_t>(d_xyzr) & 15u) != 0)
+        return fail(VGPU_ERR_ARG, "device xyzr must be 16-byte aligned");
+
+    // work buffers
+    size_t scan_n = scan_tmp_ints(std::max<int>((int)radix_hist_ints(n), nblocks + 1)) + 64;
+    VG_CUDA(h->rem.ensure(nn * 32));
+    VG_CUDA(h->ukey.ensure(nn * 4));
+    VG_CUDA(h->gkey.ensure(nn * 4));
+    VG_CUDA(h->idx.ensure((nn + 1) * 4));
+    VG_CUDA(h->idx2.ensure(nn * 4));
+    VG_CUDA(h->keys_alt.ensure(nn * 4));
+    VG_CUDA(h->vals_alt.ensure(nn * 4));
+    VG_CUDA(h->hist.ensure(radix_hist_ints(n) * 4));
+    VG_CUDA(h->scan_tmp.ensure(scan_n * 8));
+    VG_CUDA(h->outpos_in.ensure(nn * 4));
+    VG_CUDA(h->kept.ensure(64));
+    VG_CUDA(h->counters.ensure(sizeof(Counters)));
+    VG_CUDA(h->counters2.ensure(sizeof(Counters)));
+
+    const long long launches0 = launch_count();
+    cudaEventRecord(h->ev[0], s);
+    VG_CUDA(cudaMemsetAsync(h->kept.p, 0, 64, s));
+    BinParams bp;
+    bp.g = g;
+    bp.n = n;
+    bp.ids_in = d_ids;
+    bp.xyzr_in = reinterpret_cast<const double4 *>(d_xyzr);
+    bp.rem = h->rem.as<double4>();
+    bp.ukey = h->ukey.as<unsigned>();
+    bp.gkey = h->gkey.as<unsigned>();
+    bp.idx = h->idx.as<int>();
+    int *d_kept = h->kept.as<int>();
+    unsigned long long *d_rmax = reinterpret_cast<unsigned long long *>(h->kept.as<char>() + 16);
+    VG_CUDA(launch_remap(bp, d_kept, d_rmax, s));
+    int nkept = 0;
+    unsigned long long rmax_bits = 0;
+    VG_CUDA(cudaMemcpyAsync(&nkept, d_kept, 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaMemcpyAsync(&rmax_bits, d_rmax, 8, cudaMemcpyDeviceToHost, s));
+    // identity copy for the second sort
+    if (n > 0) VG_CUDA(cudaMemcpyAsync(h->idx2.p, h->idx.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    double rmax = 0.0;
+    memcpy(&rmax, &rmax_bits, 8);
+    g.rmax = rmax;
+    g.rmax32 = (float)rmax * (1.0f + 1e-6f);
+
+    int ubits = 1, gbits = 1;
+    while ((1u << ubits) <= (unsigned)nub) ubits++;
+    while ((1u << gbits) <= (unsigned)nblocks) gbits++;
+    ubits = (ubits + 7) / 8 * 8;
+    gbits = (gbits + 7) / 8 * 8;
+    bool alt = false;
+    VG_CUDA(radix_sort_pairs(h->ukey.as<unsigned>(), h->idx.as<int>(), h->keys_alt.as<unsigned>(),
+                             h->vals_alt.as<int>(), n, ubits, h->hist.as<int>(), h->hist.bytes / 4,
+                             h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4, s, &alt));
+    const unsigned *ukey_sorted = alt ? h->keys_alt.as<unsigned>() : h->ukey.as<unsigned>();
+    const int *uorder = alt ? h->vals_alt.as<int>() : h->idx.as<int>();
+
+    // results arrays
+    const size_t nk = (size_t)std::max(nkept, 1);
+    VG_CUDA(h->r_vol.ensure(nk * 8));
+    VG_CUDA(h->r_cen.ensure(nk * 24));
+    VG_CUDA(h->r_nf.ensure(nk * 4));
+    VG_CUDA(h->r_nv.ensure(nk * 4));
+    VG_CUDA(h->r_mr2.ensure(nk * 8));
+    VG_CUDA(h->r_flags.ensure(nk * 4));
+    VG_CUDA(h->r_nb.ensure(nk * kMaxNb * 4));
+    VG_CUDA(h->r_ids.ensure(nk * 4));
+    VG_CUDA(h->r_pos.ensure(nk * 24));
+    VG_CUDA(h->p64.ensure(nk * 32));
+    VG_CUDA(h->l32.ensure(nk * 16));
+    VG_CUDA(h->pid.ensure(nk * 4));
+    VG_CUDA(h->outpos.ensure(nk * 4));
+    VG_CUDA(h->gblock.ensure(nk * 4));
+    VG_CUDA(h->bstart.ensure(((size_t)nblocks + 2) * 4));
+    VG_CUDA(h->ovf_list.ensure(nk * 4));
+
+    if (g.unit_cell && nkept > 1) {
+        int *dflag = h->kept.as<int>() + 8;
+        VG_CUDA(cudaMemsetAsync(dflag, 0, 4, s));
+        VG_CUDA(launch_duplicate_check(ukey_sorted, uorder, h->rem.as<double4>(), nkept, dflag, s));
+        int dup = 0;
+        VG_CUDA(cudaMemcpyAsync(&dup, dflag, 4, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        if (dup) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
+    }
+
+    // engine order: the u-sort consumed idx, so sort (gkey, idx2)
+    bool galt = false;
+    unsigned *gk_alt = alt ? h->ukey.as<unsigned>() : h->keys_alt.as<unsigned>();
+    int *gv_alt = alt ? h->idx.as<int>() : h->vals_alt.as<int>();
+    // keep uorder intact: the g-sort ping-pongs between gkey/idx2 and the buffers not holding uorder
+    VG_CUDA(radix_sort_pairs(h->gkey.as<unsigned>(), h->idx2.as<int>(), gk_alt, gv_alt, n, gbits,
+                             h->hist.as<int>(), h->hist.bytes / 4, h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4, s,
+                             &galt));
+    const unsigned *gkey_sorted = galt ? gk_alt : h->gkey.as<unsigned>();
+    const int *gorder = galt ? gv_alt : h->idx2.as<int>();
+    if (galt && (gk_alt == (const unsigned *)ukey_sorted || gv_alt == uorder))
+        return fail(VGPU_ERR_INTERNAL, "sort buffer aliasing");
+
+    VG_CUDA(launch_gather(g, nkept, uorder, gorder, gkey_sorted, h->rem.as<double4>(), d_ids,
+                          h->outpos_in.as<int>(), h->p64.as<double4>(), h->l32.as<float4>(), h->pid.as<int>(),
+                          h->outpos.as<int>(), h->gblock.as<int>(), h->bstart.as<int>(), nblocks,
+                          h->r_ids.as<int>(), h->r_pos.as<double>(), s));
+    cudaEventRecord(h->ev[1], s);
+
+    // cell engine
+    const OffsetTable &ot = offset_table();
+    VG_CUDA(h->offsets.ensure(ot.codes.size() * 4));
+    VG_CUDA(cudaMemcpyAsync(h->offsets.p, ot.codes.data(), ot.codes.size() * 4, cudaMemcpyHostToDevice, s));
+    VG_CUDA(cudaMemsetAsync(h->counters.p, 0, sizeof(Counters), s));
+    VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, sizeof(Counters), s));
+    CellParams cp;
+    memset(&cp, 0, sizeof(cp));
+    cp.g = g;
+    cp.a.p64 = h->p64.as<double4>();
+    cp.a.l32 = h->l32.as<float4>();
+    cp.a.pid = h->pid.as<int>();
+    cp.a.outpos = h->outpos.as<int>();
+    cp.a.gblock = h->gblock.as<int>();
+    cp.a.bstart = h->bstart.as<int>();
+    cp.r.vol = h->r_vol.as<double>();
+    cp.r.cen = h->r_cen.as<double>();
+    cp.r.nf = h->r_nf.as<int>();
+    cp.r.nv = h->r_nv.as<int>();
+    cp.r.maxr2 = h->r_mr2.as<double>();
+    cp.r.flags = h->r_flags.as<int>();
+    cp.r.nb = h->r_nb.as<int>();
+    cp.cnt = h->counters.as<Counters>();
+    cp.ncells = nkept;
+    cp.cell_list = nullptr;
+    cp.overflow_list = h->ovf_list.as<int>();
+    cp.offsets = h->offsets.as<int>();
+    cp.noffsets = (int)ot.codes.size();
+    cp.ngroups = (int)ot.group_lb2.size();
+    for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
+    for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
+    cudaEventRecord(h->ev[2], s);
+    VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
+    Counters c1;
+    VG_CUDA(cudaMemcpyAsync(&c1, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    Counters c2;
+    memset(&c2, 0, sizeof(c2));
+    if (c1.overflow > 0) {
+        CellParams cp2 = cp;
+        cp2.cnt = h->counters2.as<Counters>();
+        cp2.ncells = (int)c1.overflow;
+        cp2.cell_list = h->ovf_list.as<int>();
+        cp2.overflow_list = nullptr;
+        VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s));
+        VG_CUDA(cudaMemcpyAsync(&c2, h->counters2.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    }
+    cudaEventRecord(h->ev[3], s);
+    VG_CUDA(cudaStreamSynchronize(s));
+    VG_CUDA(cudaGetLastError());
+    float bin_ms = 0, cell_ms = 0, step_ms = 0;
+    cudaEventElapsedTime(&bin_ms, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&cell_ms, h->ev[2], h->ev[3]);
+    cudaEventElapsedTime(&step_ms, h->ev[0], h->ev[3]);
+
+    h->ncells = nkept;
+    h->stats.cells = nkept;
+    h->stats.deleted = (int64_t)(c1.deleted + c2.deleted);
+    h->stats.marginal_cells = (int64_t)(c1.marginal + c2.marginal);
+    h->stats.side_tests = (int64_t)(c1.side_tests + c2.side_tests);
+    h->stats.fp64_repairs = (int64_t)(c1.fp64_repairs + c2.fp64_repairs);
+    h->stats.planes_tested = (int64_t)(c1.planes_tested + c2.planes_tested);
+    h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
+    h->stats.overflow_reruns = (int64_t)c1.overflow;
+    h->stats.failed_cells = (int64_t)c2.overflow;
+    h->stats.kernel_ms = cell_ms;
+    h->stats.bin_ms = bin_ms;
+    h->stats.step_ms = step_ms;
+    h->stats.kernel_launches = launch_count() - launches0;
+    h->computed = true;
+    if (c2.overflow > 0)
+        return fail(VGPU_ERR_CAPACITY, "%llu cells exceeded the engine capacity", (unsigned long long)c2.overflow);
+    return VGPU_OK;
+}
+
+int vgpu_get_stats(vgpu_container *h, vgpu_stats *out) {
+    if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
+    *out = h->stats;
+    return VGPU_OK;
+}
+
+int vgpu_num_cells(vgpu_container *h, int64_t *n) {
+    if (!h || !n) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    *n = h->ncells;
+    return VGPU_OK;
+}
+
+int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen, int32_t *nfaces,
+                   int32_t *nverts, double *maxr2, int32_t *flags) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    size_t n = (size_t)h->ncells;
+    if (n == 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    if (ids) VG_CUDA(cudaMemcpyAsync(ids, h->r_ids.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (pos) VG_CUDA(cudaMemcpyAsync(pos, h->r_pos.p, n * 24, cudaMemcpyDeviceToHost, s));
+    if (vol) VG_CUDA(cudaMemcpyAsync(vol, h->r_vol.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (cen) VG_CUDA(cudaMemcpyAsync(cen, h->r_cen.p, n * 24, cudaMemcpyDeviceToHost, s));
+    if (nfaces) VG_CUDA(cudaMemcpyAsync(nfaces, h->r_nf.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (nverts) VG_CUDA(cudaMemcpyAsync(nverts, h->r_nv.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (maxr2) VG_CUDA(cudaMemcpyAsync(maxr2, h->r_mr2.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (flags) VG_CUDA(cudaMemcpyAsync(flags, h->r_flags.p, n * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    return VGPU_OK;
+}
+
+static int build_csr(vgpu_container *h, int64_t *total_out) {
+    size_t n = (size_t)h->ncells;
+    cudaStream_t s = h->stream;
+    VG_CUDA(h->nb_off.ensure((n + 1) * 8));
+    VG_CUDA(h->nb_tmp.ensure((scan_tmp_ints((int)n + 1) + 64) * 8));
+    VG_CUDA(launch_nf_to_ll(h->r_nf.as<int>(), h->nb_off.as<long long>(), (int)n, s));
+    VG_CUDA(cudaMemsetAsync(h->nb_off.as<long long>() + n, 0, 8, s));
+    VG_CUDA(exclusive_scan_ll(h->nb_off.as<long long>(), h->nb_off.as<long long>(), (int)n + 1,
+                              h->nb_tmp.as<long long>(), s));
+    long long total = 0;
+    VG_CUDA(cudaMemcpyAsync(&total, h->nb_off.as<long long>() + n, 8, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    *total_out = total;
+    return VGPU_OK;
+}
+
+int vgpu_num_neighbors(vgpu_container *h, int64_t *total) {
+    if (!h || !total) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    if (h->ncells == 0) { *total = 0; return VGPU_OK; }
+    return build_csr(h, total);
+}
+
+int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    size_t n = (size_t)h->ncells;
+    if (n == 0) {
+        if (offsets) offsets[0] = 0;
+        return VGPU_OK;
+    }
+    int64_t total = 0;
+    int rc = build_csr(h, &total);
+    if (rc != VGPU_OK) return rc;
+    cudaStream_t s = h->stream;
+    if (offsets) VG_CUDA(cudaMemcpyAsync(offsets, h->nb_off.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
+    if (ids && total > 0) {
+        VG_CUDA(h->nb_out.ensure((size_t)total * 4));
+        VG_CUDA(launch_compact_neighbors(h->r_nf.as<int>(), h->r_nb.as<int>(), h->nb_off.as<long long>(), (int)n,
+                                         h->nb_out.as<int>(), s));
+        VG_CUDA(cudaMemcpyAsync(ids, h->nb_out.p, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+    }
+    VG_CUDA(cudaStreamSynchronize(s));
+    return VGPU_OK;
+}
+
+int vgpu_sum_cell_volumes(vgpu_container *h, double *out) {
+    if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    *out = 0.0;
+    if (h->ncells == 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    VG_CUDA(h->sum_tmp.ensure(64 * 8));
+    VG_CUDA(launch_sum_volumes(h->r_vol.as<double>(), h->r_flags.as<int>(), (int)h->ncells, h->sum_tmp.as<double>(), s));
+    double part[64];
+    VG_CUDA(cudaMemcpyAsync(part, h->sum_tmp.p, sizeof(part), cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    double t = 0.0;
+    for (int i = 0; i < 64; i++) t += part[i];
+    *out = t;
+    return VGPU_OK;
+}
+
+int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t **dev_nfaces) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    if (dev_vol) *dev_vol = h->r_vol.as<double>();
+    if (dev_nfaces) *dev_nfaces = h->r_nf.as<int32_t>();
+    return VGPU_OK;
+}
+
+}  // extern "C"

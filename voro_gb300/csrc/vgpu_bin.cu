@@ -1,0 +1,178 @@
+// Binning: the device side of put().
+//
+// remap_kernel reproduces the reference's placement arithmetic exactly (same
+// IEEE double operations, no contraction):
+//   container:          put_remap          src/container.cc:174-191
+//   container_periodic: put_locate_block   src/container_prd.cc:189-216
+// and computes two keys per particle: the reference block (which fixes the
+// loop order of results) and the engine block (which fixes the search grid).
+#include "vgpu_internal.cuh"
+#include "../../include/vorogpu.h"
+
+namespace vgpu {
+
+namespace {
+
+// step_int, step_mod, step_div: src/v_base.hh:61-80
+__device__ __forceinline__ int step_int(double a) {
+    return a < 0 ? __double2int_rz(a) - 1 : __double2int_rz(a);
+}
+__device__ __forceinline__ int step_mod(int a, int b) { return a >= 0 ? a % b : b - 1 - (b - 1 - a) % b; }
+__device__ __forceinline__ int step_div(int a, int b) { return a >= 0 ? a / b : -1 + (a + 1) / b; }
+
+__global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsigned long long *rmax_bits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= bp.n) return;
+    const Geometry &g = bp.g;
+    double4 q = bp.xyzr_in[i];
+    double c[3] = {q.x, q.y, q.z};
+    int b[3];
+    bool ok = true;
+    if (g.kind == VGPU_CONTAINER || g.kind == VGPU_CONTAINER_POLY) {
+        for (int a = 0; a < 3; a++) {
+            int ijk = step_int(__dmul_rn(__dsub_rn(c[a], g.lo[a]), g.usp[a]));
+            if (g.per[a]) {
+                int l = step_mod(ijk, g.un[a]);
+                c[a] = __dadd_rn(c[a], __dmul_rn(g.ubox[a], (double)(l - ijk)));
+                ijk = l;
+            } else if (ijk < 0 || ijk >= g.un[a]) {
+                ok = false;
+            }
+            b[a] = ijk;
+        }
+    } else {
+        // rectangular periodic box: z, then y, then x (shear terms are zero)
+        for (int a = 2; a >= 0; a--) {
+            int ijk = step_int(__dmul_rn(c[a], g.usp[a]));
+            if (ijk < 0 || ijk >= g.un[a]) {
+                int ak = step_div(ijk, g.un[a]);
+                c[a] = __dsub_rn(c[a], __dmul_rn((double)ak, g.len[a]));
+                ijk -= ak * g.un[a];
+            }
+            b[a] = ijk;
+        }
+    }
+    unsigned uk, gk;
+    if (ok) {
+        uk = (unsigned)(b[0] + g.un[0] * (b[1] + g.un[1] * b[2]));
+        int e[3];
+        for (int a = 0; a < 3; a++) {
+            double t = (c[a] - g.lo[a]) / g.gbs[a];
+            int v = (int)floor(t);
+            e[a] = v < 0 ? 0 : (v >= g.gn[a] ? g.gn[a] - 1 : v);
+        }
+        gk = (unsigned)(e[0] + g.gn[0] * (e[1] + g.gn[1] * e[2]));
+        atomicAdd(kept, 1);
+        // radius_poly::max_radius over stored particles (src/container.cc:108)
+        if (g.poly) atomicMax(rmax_bits, (unsigned long long)__double_as_longlong(fmax(q.w, 0.0)));
+    } else {
+        uk = (unsigned)nub;
+        gk = (unsigned)nblocks;
+    }
+    bp.rem[i] = make_double4(c[0], c[1], c[2], q.w);
+    bp.ukey[i] = uk;
+    bp.gkey[i] = gk;
+    bp.idx[i] = i;
+}
+
+__global__ void loop_order_kernel(const int *uorder, int nkept, const int *ids_in, const double4 *rem,
+                                  int *outpos_by_input, int *res_ids, double *res_pos) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nkept) return;
+    int i = uorder[m];
+    outpos_by_input[i] = m;
+    res_ids[m] = ids_in[i];
+    double4 p = rem[i];
+    res_pos[3 * m] = p.x;
+    res_pos[3 * m + 1] = p.y;
+    res_pos[3 * m + 2] = p.z;
+}
+
+__global__ void gather_kernel(Geometry g, int nkept, const int *gorder, const unsigned *gkey_sorted,
+                              const double4 *rem, const int *ids_in, const int *outpos_by_input,
+                              double4 *p64, float4 *l32, int *pid, int *outpos, int *gblock, int *bstart,
+                              int nblocks) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nkept) return;
+    int i = gorder[k];
+    double4 p = rem[i];
+    int b = (int)gkey_sorted[k];
+    int bx = b % g.gn[0];
+    int by = (b / g.gn[0]) % g.gn[1];
+    int bz = b / (g.gn[0] * g.gn[1]);
+    double ox = g.lo[0] + bx * g.gbs[0];
+    double oy = g.lo[1] + by * g.gbs[1];
+    double oz = g.lo[2] + bz * g.gbs[2];
+    p64[k] = p;
+    l32[k] = make_float4((float)(p.x - ox), (float)(p.y - oy), (float)(p.z - oz), (float)p.w);
+    pid[k] = ids_in[i];
+    outpos[k] = outpos_by_input[i];
+    gblock[k] = b;
+    int prev = k == 0 ? -1 : (int)gkey_sorted[k - 1];
+    for (int q = prev + 1; q <= b; q++) bstart[q] = k;
+    if (k == nkept - 1)
+        for (int q = b + 1; q <= nblocks; q++) bstart[q] = nkept;
+}
+
+__global__ void empty_bstart_kernel(int *bstart, int nblocks) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q <= nblocks) bstart[q] = 0;
+}
+
+// check_duplicate (src/common.cc:14-20), applied within each reference block
+// as container_periodic::put does (src/container_prd.cc:94-101).
+__global__ void duplicate_kernel(const unsigned *ukey_sorted, const int *uorder, const double4 *rem, int nkept,
+                                 int *dup_flag) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nkept) return;
+    unsigned key = ukey_sorted[m];
+    double4 a = rem[uorder[m]];
+    for (int q = m + 1; q < nkept && ukey_sorted[q] == key; q++) {
+        double4 b = rem[uorder[q]];
+        double dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+        if (dx * dx + dy * dy + dz * dz < 1e-10) atomicExch(dup_flag, 1);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s) {
+    int nub = bp.g.un[0] * bp.g.un[1] * bp.g.un[2];
+    int nblocks = bp.g.gn[0] * bp.g.gn[1] * bp.g.gn[2];
+    int threads = 256, blocks = (bp.n + threads - 1) / threads;
+    if (blocks > 0)
+        remap_kernel<<<blocks, threads, 0, s>>>(bp, nub, nblocks, kept, rmax_bits);
+        note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
+                          const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
+                          int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
+                          int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
+                          cudaStream_t s) {
+    int threads = 256;
+    if (nkept == 0) {
+        empty_bstart_kernel<<<(nblocks + 1 + threads - 1) / threads, threads, 0, s>>>(bstart, nblocks);
+        note_launch();
+        return cudaGetLastError();
+    }
+    int blocks = (nkept + threads - 1) / threads;
+    loop_order_kernel<<<blocks, threads, 0, s>>>(uorder, nkept, ids_in, rem, outpos_by_input, res_ids, res_pos);
+    note_launch();
+    gather_kernel<<<blocks, threads, 0, s>>>(g, nkept, gorder, gkey_sorted, rem, ids_in, outpos_by_input, p64,
+                                             l32, pid, outpos, gblock, bstart, nblocks);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,
+                                   int nkept, int *dup_flag, cudaStream_t s) {
+    if (nkept == 0) return cudaSuccess;
+    int threads = 256, blocks = (nkept + threads - 1) / threads;
+    duplicate_kernel<<<blocks, threads, 0, s>>>(ukey_sorted, uorder, rem, nkept, dup_flag);
+    note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace vgpu

@@ -1,0 +1,128 @@
+// Internal types shared by the engine's translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vgpu {
+
+constexpr int kWarp = 32;
+constexpr int kMaxPlanes = 64;     // plane slots per cell (64-bit plane masks)
+constexpr int kCandBuf = 64;       // candidate buffer entries per warp
+constexpr int kMaxNb = 64;         // neighbour slots per cell in the fixed-stride output
+constexpr int kOffsetRadius = 4;   // engine search table covers Chebyshev radius <= 4
+constexpr int kTableLb2Max = 15;   // ... and lower-bound shells lb2 <= 15 (complete there)
+constexpr int kMaxGroups = 16;
+
+// Geometry of one container, in the reference's own terms plus the engine's
+// private block grid.
+struct Geometry {
+    int kind;           // VGPU_CONTAINER .. VGPU_CONTAINER_PERIODIC_POLY
+    int poly;           // radical (power) tessellation
+    int unit_cell;      // periodic kinds: initial cell is the unit Voronoi cell
+    int per[3];         // periodic flags per axis
+    double lo[3];       // domain lower corner (container: ax,ay,az; periodic kinds: 0)
+    double len[3];      // domain lengths (bx-ax, ...)
+    double hi[3];       // domain upper corner as given (bx, by, bz)
+    // reference block grid: loop order and put_remap semantics
+    int un[3];          // nx, ny, nz
+    double ubox[3];     // boxx = (bx-ax)/nx  (src/container.cc:31)
+    double usp[3];      // xsp = 1/boxx       (src/v_base.cc:26)
+    // engine block grid
+    int gn[3];
+    double gbs[3];      // engine block sizes
+    float gbs32[3];
+    float gbs_min;
+    double tol_h;       // half the reference tolerance: 0.5*10*DBL_EPSILON*max_len_sq
+    double tol_cu;      // reference tol_cu (centroid threshold, src/cell.cc:25)
+    double rmax;        // largest radius (poly kinds)
+    float rmax32;
+};
+
+// Particles in engine order (sorted by engine block).
+struct EngineArrays {
+    const double4 *p64;   // remapped position + radius (double)
+    const float4 *l32;    // position local to its engine block + radius (float)
+    const int *pid;       // particle id
+    const int *outpos;    // slot of this particle in the loop-order result arrays
+    const int *gblock;    // engine block index of this particle
+    const int *bstart;    // engine block start offsets, size nblocks+1
+};
+
+struct Results {
+    double *vol;
+    double *cen;      // 3 per cell
+    int *nf;
+    int *nv;
+    double *maxr2;
+    int *flags;
+    int *nb;          // kMaxNb per cell
+};
+
+struct Counters {
+    unsigned long long side_tests;
+    unsigned long long fp64_repairs;
+    unsigned long long planes_tested;
+    unsigned long long planes_cut;
+    unsigned long long deleted;
+    unsigned long long marginal;
+    unsigned long long overflow;   // cells appended to the overflow list
+    unsigned long long work;       // work-queue counter
+    unsigned long long overflow_work;
+};
+
+struct CellParams {
+    Geometry g;
+    EngineArrays a;
+    Results r;
+    Counters *cnt;
+    int ncells;             // cells to compute (engine order), or overflow list length
+    const int *cell_list;   // NULL: all cells 0..ncells-1; else the list of engine indices
+    int *overflow_list;     // cells that overflowed this engine's capacity
+    const int *offsets;     // packed search offsets (engine table), sorted by lb2
+    int noffsets;
+    int ngroups;
+    int group_start[kMaxGroups + 1];
+    int group_lb2[kMaxGroups];
+};
+
+// launch accounting (vgpu_api.cu)
+void note_launch(int n = 1);
+long long launch_count();
+
+// vgpu_sort.cu
+cudaError_t exclusive_scan_int(const int *in, int *out, int n, int *tmp, size_t tmp_ints, cudaStream_t s);
+size_t scan_tmp_ints(int n);
+cudaError_t radix_sort_pairs(unsigned *keys, int *vals, unsigned *keys_alt, int *vals_alt, int n,
+                             int key_bits, int *hist, size_t hist_ints, int *scan_tmp, size_t scan_tmp_n,
+                             cudaStream_t s, bool *result_in_alt);
+size_t radix_hist_ints(int n);
+
+// vgpu_bin.cu
+struct BinParams {
+    Geometry g;
+    int n;
+    const int *ids_in;
+    const double4 *xyzr_in;
+    double4 *rem;        // remapped positions (input order)
+    unsigned *ukey;      // loop-order key (reference block, or 0xffffffff dropped)
+    unsigned *gkey;      // engine block key
+    int *idx;            // identity 0..n-1
+};
+cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s);
+cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
+                          const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
+                          int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
+                          int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
+                          cudaStream_t s);
+cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,
+                                   int nkept, int *dup_flag, cudaStream_t s);
+
+// vgpu_cell.cu
+cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s);
+cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n,
+                                     int *out, cudaStream_t s);
+cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);
+cudaError_t exclusive_scan_ll(const long long *in, long long *out, int n, long long *tmp, cudaStream_t s);
+cudaError_t launch_sum_volumes(const double *vol, const int *flags, int n, double *out, cudaStream_t s);
+
+}  // namespace vgpu

@@ -123,3 +123,66 @@ class RefLib(_Lib):
               np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), len(w["ids"]),
               w["ids"], w["xyzr"], ctypes.byref(sv))
         return t, sv.value
+
+
+class PortLib(_Lib):
+    """The CPU restatement (oracle/port), same records as RefLib plus the
+    per-cell count of vertex-plane side tests."""
+    path = PORT_SO
+
+    def _setup(self, f):
+        f = self.lib.port_compute_cells
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p,
+                      ctypes.c_int, _i32p, _f64p, _f64p, _f64p, _i32p, _i32p, _i32p, _f64p,
+                      ctypes.c_long, _i32p, _i64p, _i64p]
+        self._compute_port = f
+        t = self.lib.port_time_cells
+        t.restype = ctypes.c_double
+        t.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_long,
+                      ctypes.c_long, ctypes.c_int, ctypes.POINTER(ctypes.c_long),
+                      ctypes.POINTER(ctypes.c_ulonglong)]
+        self._time = t
+
+    def compute(self, w, nb_per_cell=40) -> CellRecords:
+        n = len(w["ids"])
+        geom = np.asarray(w["geom"], dtype=np.float64)
+        grid = np.asarray(w["grid"], dtype=np.int32)
+        per = np.asarray([1 if p else 0 for p in w["periodic"]], dtype=np.int32)
+        cap = max(n, 1)
+        nb_cap = max(64, n * nb_per_cell)
+        while True:
+            ids = np.zeros(cap, np.int32); pos = np.zeros(3 * cap); vol = np.zeros(cap)
+            cen = np.zeros(3 * cap); nf = np.zeros(cap, np.int32); nv = np.zeros(cap, np.int32)
+            ok = np.zeros(cap, np.int32); mrs = np.zeros(cap)
+            nb = np.zeros(nb_cap, np.int32); nb_off = np.zeros(cap + 1, np.int64); tests = np.zeros(cap, np.int64)
+            m = self._compute_port(int(w["kind"]), geom, grid, per, n, w["ids"], w["xyzr"], cap,
+                                   ids, pos, vol, cen, nf, nv, ok, mrs, nb_cap, nb, nb_off, tests)
+            if m >= 0:
+                break
+            if m == -2:
+                raise ValueError("unsupported container for the port")
+            nb_cap *= 2
+        return CellRecords(ids[:m], pos[:3 * m].reshape(m, 3), vol[:m], cen[:3 * m].reshape(m, 3),
+                           nf[:m], nv[:m], ok[:m], mrs[:m], nb[:nb_off[m]], nb_off[:m + 1], tests[:m])
+
+    def time_cells(self, w, first=0, count=None, threads=1):
+        """Seconds to compute cells [first, first+count) of the loop order with
+        `threads` threads; returns (seconds, cells)."""
+        n = len(w["ids"])
+        count = n if count is None else count
+        done = ctypes.c_long(0)
+        tests = ctypes.c_ulonglong(0)
+        t = self._time(int(w["kind"]), np.asarray(w["geom"], np.float64), np.asarray(w["grid"], np.int32),
+                       np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), n, w["ids"], w["xyzr"],
+                       int(first), int(count), int(threads), ctypes.byref(done), ctypes.byref(tests))
+        self.last_side_tests = tests.value
+        return t, done.value
+
+    def worklists(self):
+        f = self.lib.port_worklists
+        f.restype = ctypes.c_int
+        out = np.zeros(4096, np.uint32)
+        f.argtypes = [np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS"), ctypes.c_int]
+        m = f(out, 4096)
+        return out[:m]

@@ -53,6 +53,12 @@ def cases():
     # container_periodic_poly
     w = W.small_random(800, kind=W.KIND_PERIODIC_POLY, L=8.0, grid=(5, 5, 5), seed=2008, rmin=0.2, rmax=0.8)
     out["periodic_poly_800"] = w
+    # exactly degenerate input: a simple-cubic lattice (every cell a cube with
+    # twelve further neighbours touching it only along edges and at corners)
+    g = np.arange(6, dtype=float) + 0.5
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    out["degenerate_cubic_216"] = W._pack(W.KIND_CONTAINER, (0, 6, 0, 6, 0, 6), (3, 3, 3), (False,) * 3, xyz)
     return out
 
 

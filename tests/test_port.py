@@ -1,0 +1,79 @@
+"""The CPU oracle port (oracle/port) against the reference.
+
+The port restates the reference's cell algorithm with the same arithmetic
+order; on the golden fixtures it must reproduce the reference bit for bit
+(volumes, centroids, counts and even the order of neighbour IDs).  Where the
+reference tree is present it is also compared directly on fresh inputs."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests import _golden as G
+
+
+@pytest.fixture(scope="module")
+def port():
+    from oracle import PortLib, build_port
+    assert build_port()
+    return PortLib()
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_port_matches_golden_bit_for_bit(port, name):
+    w, z = G.load(name)
+    r = port.compute(w)
+    assert np.array_equal(r.ids, z["ids"])
+    assert np.array_equal(r.pos, z["pos"])
+    assert np.array_equal(r.ok, z["ok"])
+    assert np.array_equal(r.nf, z["nf"])
+    assert np.array_equal(r.nv, z["nv"])
+    assert np.array_equal(r.vol, z["vol"])
+    assert np.array_equal(r.cen, z["cen"])
+    assert np.array_equal(r.mrs, z["mrs"])
+    for k in range(len(r.ids)):
+        assert np.array_equal(np.sort(r.neighbors(k)), z["nb"][z["nb_off"][k]:z["nb_off"][k + 1]])
+
+
+def test_port_counts_side_tests(port):
+    w, _ = G.load("periodic_2000")
+    r = port.compute(w)
+    assert r.tests.min() > 0
+    assert 200 < r.tests.mean() < 2000
+
+
+def test_port_threads_give_same_work(port):
+    w, _ = G.load("radical_1200")
+    t1, m1 = port.time_cells(w, threads=1)
+    s1 = port.last_side_tests
+    t4, m4 = port.time_cells(w, threads=4)
+    assert m1 == m4 == len(w["ids"])
+    assert port.last_side_tests == s1
+
+
+REF_WL = "/root/reference/src/v_base_wl.cc"
+
+
+def test_worklists_match_reference_table(port):
+    if not os.path.exists(REF_WL):
+        pytest.skip("reference tree not present")
+    txt = open(REF_WL).read()
+    body = txt[txt.index("{") + 1:txt.rindex("}")]
+    vals = np.array([int(t, 0) for t in re.findall(r"0x[0-9a-f]+|\b\d+\b", body)], dtype=np.uint32)
+    assert np.array_equal(vals, port.worklists())
+
+
+@pytest.mark.parametrize("kind,periodic,seed", [(0, (False,) * 3, 11), (0, (True, False, True), 12),
+                                                (1, (False,) * 3, 13), (2, (True,) * 3, 14), (3, (True,) * 3, 15)])
+def test_port_matches_reference_on_fresh_inputs(port, kind, periodic, seed):
+    from oracle import REF_SO, RefLib
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference library not built here")
+    from voro_gb300 import workloads as W
+    w = W.small_random(700, kind=kind, L=3.0, periodic=periodic, seed=seed)
+    a = port.compute(w)
+    b = RefLib().compute(w)
+    assert np.array_equal(a.vol, b.vol)
+    assert np.array_equal(a.nb, b.nb)
+    assert np.array_equal(a.nv, b.nv)

@@ -137,6 +137,12 @@ int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, do
  * (src/cell.cc:86-95). */
 int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
 
+/* Diagnostics: per-phase SM clock totals of the last compute's cell kernel,
+ * summed over warps (0 init, 1 candidate gather, 2 sort, 3 side tests,
+ * 4 cuts, 5 reductions, 7 whole kernel).  All zero unless the library was
+ * built with -DVGPU_PHASE_TIMING. */
+int vgpu_phase_cycles(vgpu_container *h, double out[8]);
+
 /* Device-resident views of the results (valid until the next compute/destroy):
  * volumes (double[n]) and face counts (int32[n]). */
 int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t **dev_nfaces);

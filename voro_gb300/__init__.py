@@ -46,7 +46,7 @@ EXPORTED = [
     "vgpu_version", "vgpu_device_count", "vgpu_last_error", "vgpu_container_create", "vgpu_container_destroy",
     "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
-    "vgpu_set_tuning",
+    "vgpu_set_tuning", "vgpu_phase_cycles",
 ]
 
 
@@ -72,7 +72,7 @@ _lib = None
 
 
 def library_path():
-    return _build.LIB
+    return os.environ.get("VORO_GB300_LIB", _build.LIB)
 
 
 def load_library(build_if_missing=True):
@@ -81,11 +81,12 @@ def load_library(build_if_missing=True):
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(_build.LIB) or (build_if_missing and not _build.up_to_date()):
+    path = library_path()
+    if path == _build.LIB and (not os.path.exists(path) or (build_if_missing and not _build.up_to_date())):
         if not build_if_missing:
-            raise RuntimeError(f"engine library missing: {_build.LIB}")
+            raise RuntimeError(f"engine library missing: {path}")
         _build.build()
-    lib = ctypes.CDLL(_build.LIB)
+    lib = ctypes.CDLL(path)
     vp = ctypes.c_void_p
     i64 = ctypes.c_int64
     pd = ctypes.POINTER(ctypes.c_double)
@@ -108,6 +109,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_get_neighbors.argtypes = [vp, vp, vp]
     lib.vgpu_device_results.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+    lib.vgpu_phase_cycles.argtypes = [vp, pd]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -260,6 +262,13 @@ class _ContainerBase:
         st = Stats()
         _check(self._lib.vgpu_get_stats(self._h, ctypes.byref(st)))
         return st.as_dict()
+
+    def phase_cycles(self):
+        """Per-phase clock totals (diagnostics builds only; zeros otherwise)."""
+        out = (ctypes.c_double * 8)()
+        _check(self._lib.vgpu_phase_cycles(self._h, out))
+        names = ["init", "gather", "sort", "test", "cut", "finish", "-", "kernel"]
+        return dict(zip(names, list(out)))
 
     def total_particles(self):
         self._ensure()

@@ -40,24 +40,27 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
-    """Compiles the library if a source is newer than it; returns its path."""
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, extra_flags=None, out=None) -> str:
+    """Compiles the library if a source is newer than it; returns its path.
+    ``out`` writes a variant library elsewhere (e.g. with other -D flags)."""
+    target = out or LIB
+    if out is None and not force and up_to_date():
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)
+    tag = "" if out is None else "_" + str(abs(hash(out)) % 100000)
     nvcc = _nvcc()
     flags = NVCC_FLAGS + list(extra_flags or [])
     objs, procs = [], []
     for src in SOURCES:
-        obj = os.path.join(LIBDIR, src.replace(".cu", ".o"))
+        obj = os.path.join(LIBDIR, src.replace(".cu", tag + ".o"))
         cmd = [nvcc] + ARCH + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
         objs.append(obj)
     errors = []
     for (src, p), obj in zip(procs, objs):
-        out, _ = p.communicate()
-        if verbose and out:
-            print(out)
+        log, _ = p.communicate()
+        if verbose and log:
+            print(log)
         if p.returncode != 0:
             # nvcc has crashed (SIGSEGV) on aarch64 hosts under parallel load: retry
             # serially, then once more without line tables
@@ -68,23 +71,23 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
                 if r.returncode == 0:
                     ok = True
                     break
-                out = r.stdout
+                log = r.stdout
             if not ok:
-                errors.append(f"{src}:\n{out}")
+                errors.append(f"{src}:\n{log}")
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    tmp = LIB + ".tmp"
+    tmp = target + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout)
-    os.replace(tmp, LIB)
+    os.replace(tmp, target)
     for o in objs:
         try:
             os.remove(o)
         except OSError:
             pass
-    return LIB
+    return target
 
 
 if __name__ == "__main__":

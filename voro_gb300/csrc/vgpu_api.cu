@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -116,7 +117,7 @@ struct vgpu_container {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6];
-    double target_density = 2.5;
+    double target_density = 1.5;
     int warps_per_cta = 4;
     // particles put() so far, staged on the device in put() order
     int64_t staged = 0;
@@ -134,6 +135,7 @@ struct vgpu_container {
     int64_t ncells = 0;
     bool computed = false;
     vgpu_stats stats{};
+    double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -207,13 +209,15 @@ void choose_engine_grid(Geometry &g, int64_t n, double density) {
             total *= g.gn[a];
         }
     }
-    float bmin = 3.4e38f;
+    float bmin = 3.4e38f, bmax = 0.0f;
     for (int a = 0; a < 3; a++) {
         g.gbs[a] = g.len[a] / g.gn[a];
         g.gbs32[a] = (float)g.gbs[a];
         bmin = std::min(bmin, g.gbs32[a]);
+        bmax = std::max(bmax, g.gbs32[a]);
     }
     g.gbs_min = bmin * (1.0f - 1e-6f);
+    g.gbs_max = bmax * (1.0f + 1e-6f);
 }
 
 int ensure_device(vgpu_container *h) {
@@ -520,6 +524,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     cp.ngroups = (int)ot.group_lb2.size();
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
+    box_tables(cp.box_tri, cp.box_adj);
     cudaEventRecord(h->ev[2], s);
     VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
     Counters c1;
@@ -554,6 +559,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
     h->stats.overflow_reruns = (int64_t)c1.overflow;
     h->stats.failed_cells = (int64_t)c2.overflow;
+    for (int i = 0; i < 8; i++) h->phase[i] = (double)(c1.phase_cycles[i] + c2.phase_cycles[i]);
     h->stats.kernel_ms = cell_ms;
     h->stats.bin_ms = bin_ms;
     h->stats.step_ms = step_ms;
@@ -656,6 +662,12 @@ int vgpu_sum_cell_volumes(vgpu_container *h, double *out) {
     double t = 0.0;
     for (int i = 0; i < 64; i++) t += part[i];
     *out = t;
+    return VGPU_OK;
+}
+
+int vgpu_phase_cycles(vgpu_container *h, double out[8]) {
+    if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
+    for (int i = 0; i < 8; i++) out[i] = h->phase[i];
     return VGPU_OK;
 }
 

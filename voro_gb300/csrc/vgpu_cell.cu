@@ -11,12 +11,14 @@
 //    the meeting point of three planes (a,b,c), stored as a "triangle" of
 //    plane indices oriented so that det(n_a,n_b,n_c) > 0 (faces counter-
 //    clockwise seen from outside), plus the three neighbouring vertices across
-//    its three edges.  Lane l owns vertex slots l, l+32, ... in registers.
+//    its three edges.  Lane l owns vertex slots l, l+32, ... in registers;
+//    an empty slot holds a NaN position, so it never tests outside a plane.
 //  * A candidate plane is tested against all vertices at once (one side test
 //    per lane and slot, then a ballot).  The common case — the plane misses —
 //    costs a handful of instructions.  A cut removes the vertices outside,
-//    finds the boundary of the removed region (a cycle of edges), and adds one
-//    new vertex per boundary edge; slots are reused through bit masks.
+//    stages the boundary of the removed region (a cycle of edges) in shared
+//    memory, and every free slot of rank r builds the new vertex for boundary
+//    edge r, so slot assignment needs only a population count.
 //  * Side tests run in FP32 (MIXED mode) under a forward error bound: a test
 //    is certain when |value| exceeds the bound plus the reference tolerance;
 //    otherwise it is redone in FP64 from the planes' double-precision source.
@@ -27,20 +29,16 @@
 //    in order of the blocks' lower-bound distance and sorted by (power)
 //    distance inside a batch, with the same radius cut-off as the reference's
 //    r_ctest / r_scale_check (src/rad_option.hh:320-341,387-431).
-//  * Final vertices are rebuilt in FP64 from their three planes; volume and
-//    centroid are accumulated in FP64 over the cell's edges.
+//  * Final vertices are rebuilt in FP64 from their three planes (one
+//    residual-correction step from the FP32 vertex); volume and centroid are
+//    accumulated in FP64 over the cell's edges, relative to one of its vertices.
 #include <cfloat>
 #include <cstdio>
-#include "vgpu_internal.cuh"
-#include "../../include/vorogpu.h"
+#include "vgpu_dev.cuh"
 
 namespace vgpu {
 
 namespace {
-
-constexpr float kU32 = 5.9604645e-08f;          // 2^-24
-constexpr double kU64 = 1.1102230246251565e-16; // 2^-53
-constexpr unsigned kFull = 0xffffffffu;
 
 // Initial box: eight corners as plane triangles and their neighbours.  Planes
 // 0..5 are -x,+x,-y,+y,-z,+z.  Filled from the host (see build_box_tables).
@@ -48,6 +46,7 @@ __constant__ unsigned c_box_tri[8];
 __constant__ unsigned c_box_adj[8];
 
 // ------------------------------------------------------------------ masks
+// Slot s of lane l is bit l+32s.
 template <int K>
 struct Mask {
     static constexpr int W = (K + 1) / 2;
@@ -57,7 +56,6 @@ struct Mask {
         for (int i = 0; i < W; i++) w[i] = 0ull;
     }
     __device__ __forceinline__ bool test(int t) const { return (w[t >> 6] >> (t & 63)) & 1ull; }
-    __device__ __forceinline__ void set(int t) { w[t >> 6] |= 1ull << (t & 63); }
     __device__ __forceinline__ int popc() const {
         int c = 0;
 #pragma unroll
@@ -76,23 +74,26 @@ struct Mask {
         for (int i = 0; i < W; i++) e = e && (w[i] == o.w[i]);
         return e;
     }
-    // position of the j-th (0-based) set bit, or -1
-    __device__ __forceinline__ int nth(int j) const {
+    // number of set bits below bit t
+    __device__ __forceinline__ int rank(int t) const {
+        int c = 0;
+        const int wi = t >> 6;
 #pragma unroll
         for (int i = 0; i < W; i++) {
-            int c = __popcll(w[i]);
-            if (j < c) {
-                unsigned long long x = w[i];
-                for (int q = 0; q < j; q++) x &= x - 1ull;
-                return i * 64 + __ffsll((long long)x) - 1;
-            }
-            j -= c;
+            if (i < wi) c += __popcll(w[i]);
+            else if (i == wi) c += __popcll(w[i] & ((1ull << (t & 63)) - 1ull));
         }
+        return c;
+    }
+    // lowest set bit, or -1
+    __device__ __forceinline__ int first() const {
+#pragma unroll
+        for (int i = 0; i < W; i++)
+            if (w[i]) return i * 64 + __ffsll((long long)w[i]) - 1;
         return -1;
     }
 };
 
-// ballot of a per-slot predicate into a mask: slot s of lane l is bit l+32s
 template <int K>
 __device__ __forceinline__ Mask<K> ballot_mask(const bool (&pred)[K]) {
     Mask<K> m;
@@ -125,52 +126,54 @@ __device__ __forceinline__ double warp_maxd(double x) {
     for (int d = 16; d > 0; d >>= 1) x = fmax(x, __shfl_xor_sync(kFull, x, d));
     return x;
 }
-
-// plane indices are always < kMaxPlanes; the mask keeps every shared-memory
-// index in bounds even if a slot held inconsistent data
-__device__ __forceinline__ int tri_plane(unsigned t, int e) { return (t >> (8 * e)) & (kMaxPlanes - 1); }
-
-// Sortable key of a float (total order as unsigned)
-__device__ __forceinline__ unsigned float_key(float f) {
-    unsigned u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+__device__ __forceinline__ int warp_incl_scan(int x, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+    }
+    return x;
 }
 
 // ------------------------------------------------------------------ shared memory per warp
-template <int K>
+template <int MODE, int K>
 struct WarpShared {
-    float4 pl[kMaxPlanes];      // plane n.x, n.y, n.z, h  (n.v <= h inside)
-    float4 pe[kMaxPlanes];      // |n|, en (abs error of n), eh (abs error of h), |h|
-    double4 pl64[kMaxPlanes];   // FP64 plane (box planes always; others when needed)
-    int pid[kMaxPlanes];        // neighbour ID of the plane
-    int psrc[kMaxPlanes];       // engine index of the generating particle, -1 for initial faces
-    int pshift[kMaxPlanes];     // packed periodic image counts
+    float4 pl[kMaxPlanes];   // plane n.x, n.y, n.z, h  (n.v <= h inside)
+    float4 pe[kMaxPlanes];   // |n|, en (abs error of n), eh (abs error of h), |h|
+    // (pl and pe are contiguous: at the end of a cell they hold the FP64 planes)
+    double4 pl64x[MODE == VGPU_FP64 ? kMaxPlanes : 1];   // FP64 planes (FP64 engine, during the search)
+    int pid[kMaxPlanes];     // neighbour ID of the plane
+    int psrc[kMaxPlanes];    // engine index of the generating particle, -1 for initial faces
+    int pshift[kMaxPlanes];  // packed periodic image counts (initial faces: face index)
     unsigned tri[32 * K];
     unsigned adj[32 * K];
+    unsigned stage[48 * K];  // boundary edges of a cut (a | b<<8 | u<<16); final stage: edge list
     unsigned char startN[kMaxPlanes];
     unsigned char endN[kMaxPlanes];
-    unsigned ck[kCandBuf];      // candidate sort keys
-    int cj[kCandBuf];           // candidate engine index
-    int cs[kCandBuf];           // candidate packed image counts
     union {
         struct {
-            float4 cd[kCandBuf];      // candidate plane (FP32): n, h
-            float4 ce[kCandBuf];      // en, eh, dist2, rs
-            double4 cd64[kCandBuf];   // candidate plane (FP64), FP64 mode
+            unsigned ck[kCandBuf];    // sort keys
+            int cj[kCandBuf];         // engine index
+            int cs[kCandBuf];         // packed periodic image counts
+            float4 cd[kCandBuf];      // plane (FP32): n, h
+            float4 ce[kCandBuf];      // en, eh, |n|, rs
+            double4 cd64[MODE == VGPU_FP64 ? kCandBuf : 1];  // plane (FP64), FP64 engine
         } c;
         struct {
-            double4 vtx[32 * K];      // final FP64 vertices (after the search)
+            double vx[32 * K], vy[32 * K], vz[32 * K];   // FP64 vertices relative to c0
+            double fx[kMaxPlanes], fy[kMaxPlanes], fz[kMaxPlanes];  // face points relative to c0
         } f;
     } u;
-    double4 foot[kMaxPlanes];   // final stage: foot point of each live plane
 };
 
 // ------------------------------------------------------------------ per-lane vertex registers
 template <int MODE, int K>
 struct Verts {
     unsigned tri[K];
-    float x[K], y[K], z[K], a[K], e[K];   // FP32 position, |v|, error bound
-    double dx[K], dy[K], dz[K];           // FP64 mode positions
+    float x[K], y[K], z[K];   // FP32 position (NaN = empty slot)
+    float a[K], e[K];         // |v| and the forward error bound of the position
+    float r2[K];              // bound on |v|^2 (0 for empty)
+    double dx[K], dy[K], dz[K];   // FP64 engine positions (NaN = empty)
 };
 
 struct CellCtx {
@@ -181,112 +184,100 @@ struct CellCtx {
     float R2;         // upper bound of max |v|^2
     float cutoff2;    // squared distance bound for candidates / blocks
     float ri2;        // particle radius squared (poly)
-    bool deleted;
-    bool overflow;
-    bool marginal;
-    bool repaired;
+    bool deleted, overflow, marginal, repaired;
     unsigned long long freeplanes;
     int ncand;
-    unsigned long long tests, repairs, ptested, pcut;
+    unsigned tests, repairs, ptested, pcut;
+#ifdef VGPU_PHASE_TIMING
+    unsigned long long phase[8];
+#endif
 };
 
-__device__ __forceinline__ int unpack_shift(int code, int a) { return ((code >> (8 * a)) & 255) - 128; }
+// ------------------------------------------------------------------ out-of-line helpers
+// The vertex solve, its FP64 refinement and the key sorts.  They are inlined by
+// default (measured faster on the 4M periodic box: 16.9M vs 15.3M cells/s);
+// -DVGPU_OUTLINE=1 keeps one out-of-line copy of each instead, which shrinks
+// the kernel's code at the price of spills around the calls.
+#ifndef VGPU_OUTLINE
+#define VGPU_OUTLINE 0
+#endif
+#if VGPU_OUTLINE
+#define VGPU_HELPER __device__ __noinline__
+#else
+#define VGPU_HELPER __device__ __forceinline__
+#endif
+struct VertexF32 {
+    float x, y, z, a, e, r2;
+    bool good;
+};
 
-// FP64 plane of a candidate (engine index j, image counts) relative to the
-// particle, with the reference's own arithmetic: x1 = p_j - (x - qx)
-// (src/v_compute.cc:383-397) and rs = x1*x1+y1*y1+z1*z1 [+ r_i^2 - r_j^2]
-// (r_scale, src/rad_option.hh:414-416).  h = rs/2 (the reference works in
-// doubled coordinates; halving is exact).
-__device__ __forceinline__ double4 plane64_from(const CellParams &P, const CellCtx &C, int j, int code) {
-    double4 q = P.a.p64[j];
-    double sx = unpack_shift(code, 0) * P.g.len[0];
-    double sy = unpack_shift(code, 1) * P.g.len[1];
-    double sz = unpack_shift(code, 2) * P.g.len[2];
-    double x1 = __dsub_rn(q.x, __dsub_rn(C.me64.x, sx));
-    double y1 = __dsub_rn(q.y, __dsub_rn(C.me64.y, sy));
-    double z1 = __dsub_rn(q.z, __dsub_rn(C.me64.z, sz));
-    double rs = __dadd_rn(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)), __dmul_rn(z1, z1));
-    if (P.g.poly) rs = __dsub_rn(__dadd_rn(rs, __dmul_rn(C.me64.w, C.me64.w)), __dmul_rn(q.w, q.w));
-    return make_double4(x1, y1, z1, 0.5 * rs);
-}
-
-template <int K>
-__device__ __forceinline__ double4 plane64_of(const CellParams &P, const CellCtx &C, WarpShared<K> &S, int p) {
-    int src = S.psrc[p];
-    if (src < 0) return S.pl64[p];
-    return plane64_from(P, C, src, S.pshift[p]);
-}
-
-// Vertex of planes (a,b,c) in FP32 with a forward error bound (absolute,
-// Euclidean) covering the planes' own storage error and the rounding of this
-// Cramer solve.  Returns false if the planes are (numerically) dependent.
-template <int K>
-__device__ __forceinline__ bool solve_f32(const WarpShared<K> &S, unsigned t, float &x, float &y, float &z,
-                                          float &va, float &ve) {
+// Vertex of planes (a,b,c) of triangle t in FP32, with a forward error bound e
+// covering the planes' own storage error (pe: |n|, en, eh, |h|) and the
+// rounding of this Cramer solve: |adj(A)| <= |n_b||n_c| + |n_c||n_a| + |n_a||n_b|
+// and every row's error is at most rho.
+VGPU_HELPER VertexF32 solve_vertex_f32(const float4 *pl, const float4 *pe, unsigned t) {
     const int a = tri_plane(t, 0), b = tri_plane(t, 1), c = tri_plane(t, 2);
-    const float4 A = S.pl[a], B = S.pl[b], Cc = S.pl[c];
-    const float4 EA = S.pe[a], EB = S.pe[b], EC = S.pe[c];
-    float bcx = B.y * Cc.z - B.z * Cc.y, bcy = B.z * Cc.x - B.x * Cc.z, bcz = B.x * Cc.y - B.y * Cc.x;
-    float cax = Cc.y * A.z - Cc.z * A.y, cay = Cc.z * A.x - Cc.x * A.z, caz = Cc.x * A.y - Cc.y * A.x;
-    float abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
-    float D = A.x * bcx + A.y * bcy + A.z * bcz;
-    float inv = 1.0f / D;
-    x = (A.w * bcx + B.w * cax + Cc.w * abx) * inv;
-    y = (A.w * bcy + B.w * cay + Cc.w * aby) * inv;
-    z = (A.w * bcz + B.w * caz + Cc.w * abz) * inv;
-    va = sqrtf(x * x + y * y + z * z);
-    float nbc = fabsf(bcx) + fabsf(bcy) + fabsf(bcz);
-    float nca = fabsf(cax) + fabsf(cay) + fabsf(caz);
-    float nab = fabsf(abx) + fabsf(aby) + fabsf(abz);
+    const float4 A = pl[a], B = pl[b], Cc = pl[c];
+    const float4 EA = pe[a], EB = pe[b], EC = pe[c];
+    const float bcx = B.y * Cc.z - B.z * Cc.y, bcy = B.z * Cc.x - B.x * Cc.z, bcz = B.x * Cc.y - B.y * Cc.x;
+    const float cax = Cc.y * A.z - Cc.z * A.y, cay = Cc.z * A.x - Cc.x * A.z, caz = Cc.x * A.y - Cc.y * A.x;
+    const float abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
+    const float D = A.x * bcx + A.y * bcy + A.z * bcz;
+    const float inv = 1.0f / D;
+    VertexF32 o;
+    o.x = (A.w * bcx + B.w * cax + Cc.w * abx) * inv;
+    o.y = (A.w * bcy + B.w * cay + Cc.w * aby) * inv;
+    o.z = (A.w * bcz + B.w * caz + Cc.w * abz) * inv;
+    o.a = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+    const float cof = fmaf(EB.x, EC.x, fmaf(EC.x, EA.x, EA.x * EB.x));
     const float r8 = 8.0f * kU32;
-    float ra = EA.z + EA.y * va + r8 * (EA.w + EA.x * va);
-    float rb = EB.z + EB.y * va + r8 * (EB.w + EB.x * va);
-    float rc = EC.z + EC.y * va + r8 * (EC.w + EC.x * va);
-    ve = 2.0f * (nbc * ra + nca * rb + nab * rc) / fabsf(D) + r8 * va;
-    bool good = D > 0.0f && isfinite(x) && isfinite(y) && isfinite(z) && isfinite(ve);
-    if (!good) { ve = 3.0e38f; }
-    return good;
+    const float ra = fmaf(EA.y, o.a, EA.z) + r8 * fmaf(EA.x, o.a, EA.w);
+    const float rb = fmaf(EB.y, o.a, EB.z) + r8 * fmaf(EB.x, o.a, EB.w);
+    const float rc = fmaf(EC.y, o.a, EC.z) + r8 * fmaf(EC.x, o.a, EC.w);
+    o.e = 2.0f * cof * fmaxf(ra, fmaxf(rb, rc)) / fabsf(D) + r8 * o.a;
+    o.good = D > 0.0f && isfinite(o.e) && isfinite(o.a);
+    if (!o.good) o.e = 3.0e38f;  // every test on it is repaired in FP64
+    const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
+    o.r2 = r * r;
+    return o;
 }
 
-// Vertex of three FP64 planes by Cramer's rule.
-__device__ __forceinline__ void solve_f64(const double4 A, const double4 B, const double4 C, double &x, double &y,
-                                          double &z, double &D, double &kappa_num) {
-    double bcx = B.y * C.z - B.z * C.y, bcy = B.z * C.x - B.x * C.z, bcz = B.x * C.y - B.y * C.x;
-    double cax = C.y * A.z - C.z * A.y, cay = C.z * A.x - C.x * A.z, caz = C.x * A.y - C.y * A.x;
-    double abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
-    D = A.x * bcx + A.y * bcy + A.z * bcz;
-    double inv = 1.0 / D;
-    x = (A.w * bcx + B.w * cax + C.w * abx) * inv;
-    y = (A.w * bcy + B.w * cay + C.w * aby) * inv;
-    z = (A.w * bcz + B.w * caz + C.w * abz) * inv;
-    // sum over rows of |cofactor row| * (|h| + |n||v|), used for the error bound
-    float vv = (float)sqrt(x * x + y * y + z * z);
-    float nbc = fabsf((float)bcx) + fabsf((float)bcy) + fabsf((float)bcz);
-    float nca = fabsf((float)cax) + fabsf((float)cay) + fabsf((float)caz);
-    float nab = fabsf((float)abx) + fabsf((float)aby) + fabsf((float)abz);
-    float na = fabsf((float)A.x) + fabsf((float)A.y) + fabsf((float)A.z);
-    float nb = fabsf((float)B.x) + fabsf((float)B.y) + fabsf((float)B.z);
-    float nc = fabsf((float)C.x) + fabsf((float)C.y) + fabsf((float)C.z);
-    kappa_num = nbc * (fabsf((float)A.w) + na * vv) + nca * (fabsf((float)B.w) + nb * vv) +
-                nab * (fabsf((float)C.w) + nc * vv);
-}
-
-// FP64 side test of one vertex against plane Q, returning 2 outside, 0 inside,
-// 1 inside the reference tolerance band (marginal).
-__device__ __forceinline__ int side64(const double4 Q, double x, double y, double z, double D, double kappa_num,
-                                      double tol_h) {
-    double s = fma(Q.x, x, fma(Q.y, y, fma(Q.z, z, -Q.w)));
-    double vv = sqrt(x * x + y * y + z * z);
-    double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
-    double verr = 16.0 * kU64 * kappa_num / fabs(D) + 64.0 * kU64 * vv;
-    double bnd = nq * verr + 8.0 * kU64 * (nq * vv + fabs(Q.w));
-    if (s > tol_h + bnd) return 2;
-    if (s < -(tol_h + bnd)) return 0;
-    return 1;
+// FP64 vertex of triangle t: one residual correction of the FP32 vertex
+// (x,y,z) against its three FP64 planes; ill-conditioned vertices are solved
+// directly in FP64.
+VGPU_HELPER double3 refine_vertex_f64(const double4 *pl64, unsigned t, float fx, float fy, float fz) {
+    const double4 A = pl64[tri_plane(t, 0)], B = pl64[tri_plane(t, 1)], Cq = pl64[tri_plane(t, 2)];
+    const double x = fx, y = fy, z = fz;
+    const double ra = A.w - fma(A.x, x, fma(A.y, y, A.z * z));
+    const double rb = B.w - fma(B.x, x, fma(B.y, y, B.z * z));
+    const double rc = Cq.w - fma(Cq.x, x, fma(Cq.y, y, Cq.z * z));
+    const float ax = (float)A.x, ay = (float)A.y, az = (float)A.z;
+    const float bx = (float)B.x, by = (float)B.y, bz = (float)B.z;
+    const float cx = (float)Cq.x, cy = (float)Cq.y, cz = (float)Cq.z;
+    const float bcx = by * cz - bz * cy, bcy = bz * cx - bx * cz, bcz = bx * cy - by * cx;
+    const float cax = cy * az - cz * ay, cay = cz * ax - cx * az, caz = cx * ay - cy * ax;
+    const float abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
+    const float D = ax * bcx + ay * bcy + az * bcz;
+    const float scale = (fabsf(ax) + fabsf(ay) + fabsf(az)) * (fabsf(bx) + fabsf(by) + fabsf(bz)) *
+                        (fabsf(cx) + fabsf(cy) + fabsf(cz));
+    double3 v;
+    if (fabsf(D) > 1e-3f * scale) {
+        // well conditioned: one correction step is exact to ~1e-14
+        const float fra = (float)ra, frb = (float)rb, frc = (float)rc;
+        const float inv = 1.0f / D;
+        v.x = x + (double)((fra * bcx + frb * cax + frc * abx) * inv);
+        v.y = y + (double)((fra * bcy + frb * cay + frc * aby) * inv);
+        v.z = z + (double)((fra * bcz + frb * caz + frc * abz) * inv);
+    } else {
+        double DD;
+        float kn;
+        solve_f64(A, B, Cq, v.x, v.y, v.z, DD, kn);
+    }
+    return v;
 }
 
 // ------------------------------------------------------------------ warp sort of candidate keys
-__device__ __forceinline__ void bitonic32(unsigned &x, int lane) {
+VGPU_HELPER unsigned bitonic32(unsigned x, int lane) {
 #pragma unroll
     for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
@@ -297,11 +288,12 @@ __device__ __forceinline__ void bitonic32(unsigned &x, int lane) {
             x = (lower == up) ? min(x, y) : max(x, y);
         }
     }
+    return x;
 }
-__device__ __forceinline__ void bitonic64(unsigned &x0, unsigned &x1, int lane) {
-#pragma unroll
+VGPU_HELPER uint2 bitonic64(unsigned x0, unsigned x1, int lane) {
+#pragma unroll 1
     for (int k = 2; k <= 64; k <<= 1) {
-#pragma unroll
+#pragma unroll 1
         for (int j = k >> 1; j > 0; j >>= 1) {
             if (j == 32) {
                 unsigned a = min(x0, x1), b = max(x0, x1);
@@ -311,45 +303,96 @@ __device__ __forceinline__ void bitonic64(unsigned &x0, unsigned &x1, int lane) 
                 unsigned y0 = __shfl_xor_sync(kFull, x0, j);
                 unsigned y1 = __shfl_xor_sync(kFull, x1, j);
                 bool lower = (lane & j) == 0;
-                bool up0 = ((lane)&k) == 0;
+                bool up0 = (lane & k) == 0;
                 bool up1 = ((lane + 32) & k) == 0;
                 x0 = (lower == up0) ? min(x0, y0) : max(x0, y0);
                 x1 = (lower == up1) ? min(x1, y1) : max(x1, y1);
             }
         }
     }
+    return make_uint2(x0, x1);
 }
+
+// FP64 plane of an existing plane slot of a cell
+template <int MODE, int K>
+__device__ __forceinline__ double4 plane64_slot(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int p) {
+    const int src = S.psrc[p];
+    if (src >= 0) return plane64_from(P, me, src, S.pshift[p]);
+    return face64(P, me, S.pshift[p]);
+}
+
+// FP64 re-test of the vertices whose FP32 test against candidate cb was
+// uncertain (bit s of uncbits: slot s of this lane, vertex planes tri_s).
+// Returns the outside bits; *marginal is set for tolerance-band hits.
+template <int MODE, int K>
+__device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int cb,
+                                              unsigned uncbits, unsigned tri0, unsigned tri1, unsigned tri2,
+                                              unsigned tri3, bool *marginal) {
+    unsigned outbits = 0;
+    bool anym = false;
+    if (uncbits) {
+        const double4 Q = plane64_from(P, me, S.u.c.cj[cb], S.u.c.cs[cb]);
+        for (int s = 0; s < K; s++) {
+            if (!((uncbits >> s) & 1u)) continue;
+            const unsigned t = s == 0 ? tri0 : (s == 1 ? tri1 : (s == 2 ? tri2 : tri3));
+            const double4 A = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 0));
+            const double4 B = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 1));
+            const double4 Cq = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 2));
+            double x, y, z, D;
+            float kn;
+            solve_f64(A, B, Cq, x, y, z, D, kn);
+            const double v = fma(Q.x, x, fma(Q.y, y, fma(Q.z, z, -Q.w)));
+            const double vv = sqrt(x * x + y * y + z * z);
+            const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
+            const double verr = 16.0 * kU64 * (double)kn / fabs(D) + 64.0 * kU64 * vv;
+            const double bnd = nq * verr + 8.0 * kU64 * (nq * vv + fabs(Q.w)) + P.g.tol_h;
+            if (!(D > 0.0)) anym = true;
+            else if (v > bnd) outbits |= 1u << s;
+            else if (v >= -bnd) anym = true;
+        }
+    }
+    *marginal = anym;
+    return outbits;
+}
+
+// Optional per-phase clock accounting (diagnostics builds: -DVGPU_PHASE_TIMING).
+// Phases: 0 init, 1 block/candidate gather, 2 sort, 3 side tests, 4 cuts, 5 finish.
+#ifdef VGPU_PHASE_TIMING
+#define PHASE_BEGIN(v) const long long v = clock64()
+#define PHASE_END(v, ph) C.phase[ph] += (unsigned long long)(clock64() - (v))
+#else
+#define PHASE_BEGIN(v)
+#define PHASE_END(v, ph)
+#endif
 
 // ------------------------------------------------------------------ the engine
 template <int MODE, int K>
 struct Engine {
     const CellParams &P;
-    WarpShared<K> &S;
+    WarpShared<MODE, K> &S;
     const int *offsets;   // shared copy of the offset table
-    int lane;
+    const int lane;
     Verts<MODE, K> V;
     Mask<K> Vm;           // valid vertex slots
     CellCtx C;
 
-    __device__ Engine(const CellParams &p, WarpShared<K> &s, const int *off, int l) : P(p), S(s), offsets(off), lane(l) {}
+    __device__ Engine(const CellParams &p, WarpShared<MODE, K> &s, const int *off, int l)
+        : P(p), S(s), offsets(off), lane(l) {}
+
+    __device__ __forceinline__ void clear_slot(int s) {
+        V.x[s] = V.y[s] = V.z[s] = __int_as_float(0x7fffffff);
+        V.a[s] = V.e[s] = 0.0f;
+        V.r2[s] = 0.0f;
+        V.tri[s] = 0;
+        if (MODE == VGPU_FP64) V.dx[s] = V.dy[s] = V.dz[s] = __longlong_as_double(0x7ff8000000000000ll);
+    }
 
     // ---- bound of max |v|^2 and the candidate cut-off
-    __device__ void update_radius() {
-        float m = 0.0f;
+    __device__ __forceinline__ void update_radius() {
+        float m = V.r2[0];
 #pragma unroll
-        for (int s = 0; s < K; s++) {
-            if (Vm.test(lane + 32 * s)) {
-                float r;
-                if (MODE == VGPU_FP64) {
-                    r = (float)sqrt(V.dx[s] * V.dx[s] + V.dy[s] * V.dy[s] + V.dz[s] * V.dz[s]);
-                    r = r * (1.0f + 4.0f * kU32);
-                } else {
-                    r = (V.a[s] + V.e[s]) * (1.0f + 4.0f * kU32);
-                }
-                m = fmaxf(m, r * r);
-            }
-        }
-        C.R2 = warp_maxf(m) * (1.0f + 4.0f * kU32);
+        for (int s = 1; s < K; s++) m = fmaxf(m, V.r2[s]);
+        C.R2 = warp_maxf(m);
         if (P.g.poly) {
             float R = sqrtf(C.R2);
             float q = C.R2 + P.g.rmax32 * P.g.rmax32 - C.ri2;
@@ -360,13 +403,38 @@ struct Engine {
         }
     }
 
+    // ---- vertex of slot s from the three planes of V.tri[s]
+    __device__ __forceinline__ void compute_vertex(int s) {
+        const unsigned t = V.tri[s];
+        const int a = tri_plane(t, 0), b = tri_plane(t, 1), c = tri_plane(t, 2);
+        if (MODE == VGPU_FP64) {
+            double D;
+            float kn;
+            solve_f64(S.pl64x[a], S.pl64x[b], S.pl64x[c], V.dx[s], V.dy[s], V.dz[s], D, kn);
+            const float vv = sqrtf((float)(V.dx[s] * V.dx[s] + V.dy[s] * V.dy[s] + V.dz[s] * V.dz[s]));
+            V.e[s] = (float)(16.0 * kU64 * (double)kn / fabs(D)) + (float)(64.0 * kU64) * vv;
+            V.a[s] = vv;
+            if (!(D > 0.0)) C.marginal = true;
+            const float r = vv * (1.0f + 4.0f * kU32) + V.e[s];
+            V.r2[s] = r * r;
+            return;
+        }
+        const VertexF32 o = solve_vertex_f32(S.pl, S.pe, t);
+        V.x[s] = o.x;
+        V.y[s] = o.y;
+        V.z[s] = o.z;
+        V.a[s] = o.a;
+        V.e[s] = o.e;
+        V.r2[s] = o.r2;
+    }
+
     // ---- initial cell: container box (src/container.hh:191-203, src/cell.cc:294-318,2567-2580)
     //      or the periodic unit cell (src/container_prd.hh:124-131)
     __device__ void init_cell(int k) {
         C.k = k;
         C.me64 = P.a.p64[k];
         C.me32 = P.a.l32[k];
-        int b = P.a.gblock[k];
+        const int b = P.a.gblock[k];
         C.bi = b % P.g.gn[0];
         C.bj = (b / P.g.gn[0]) % P.g.gn[1];
         C.bk = b / (P.g.gn[0] * P.g.gn[1]);
@@ -376,266 +444,228 @@ struct Engine {
         C.ncand = 0;
         C.tests = C.repairs = C.ptested = C.pcut = 0;
         if (lane < 6) {
-            int ax = lane >> 1;
-            bool hiside = lane & 1;
-            double xa = ax == 0 ? C.me64.x : (ax == 1 ? C.me64.y : C.me64.z);
-            double h;
-            if (P.g.unit_cell || P.g.per[ax]) {
-                h = 0.5 * P.g.len[ax];
-            } else {
-                h = hiside ? __dsub_rn(P.g.hi[ax], xa) : -__dsub_rn(P.g.lo[ax], xa);
-            }
-            double n = hiside ? 1.0 : -1.0;
-            double4 q = make_double4(ax == 0 ? n : 0.0, ax == 1 ? n : 0.0, ax == 2 ? n : 0.0, h);
-            S.pl64[lane] = q;
-            S.pl[lane] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)h);
-            float hf = fabsf((float)h);
+            const double4 q = face64(P, C.me64, lane);
+            if (MODE == VGPU_FP64) S.pl64x[lane] = q;
+            S.pl[lane] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+            const float hf = fabsf((float)q.w);
             S.pe[lane] = make_float4(1.0f, 0.0f, 2.0f * kU32 * hf, hf);
             S.pid[lane] = P.g.unit_cell ? 0 : -(lane + 1);
             S.psrc[lane] = -1;
-            S.pshift[lane] = 0;
+            S.pshift[lane] = lane;
         }
         Vm.clear();
+        Vm.w[0] = 0xffull;
 #pragma unroll
-        for (int s = 0; s < K; s++) V.tri[s] = 0;
+        for (int s = 0; s < K; s++) clear_slot(s);
         if (lane < 8) {
             S.tri[lane] = c_box_tri[lane];
             S.adj[lane] = c_box_adj[lane];
             V.tri[0] = c_box_tri[lane];
         }
-        for (int t = 0; t < 8; t++) Vm.set(t);
         __syncwarp();
         if (lane < 8) compute_vertex(0);
         update_radius();
     }
 
-    // ---- vertex of slot s (planes from shared memory)
-    __device__ void compute_vertex(int s) {
-        unsigned t = V.tri[s];
-        if (MODE == VGPU_FP64) {
-            double D, kn;
-            solve_f64(S.pl64[tri_plane(t, 0)], S.pl64[tri_plane(t, 1)], S.pl64[tri_plane(t, 2)], V.dx[s], V.dy[s],
-                      V.dz[s], D, kn);
-            V.e[s] = (float)(16.0 * kU64 * kn / fabs(D) + 64.0 * kU64 * sqrt(V.dx[s] * V.dx[s] + V.dy[s] * V.dy[s] + V.dz[s] * V.dz[s]));
-            V.a[s] = (float)D;   // orientation check value
-            if (!(D > 0.0)) C.marginal = true;
-        } else {
-            bool ok = solve_f32<K>(S, t, V.x[s], V.y[s], V.z[s], V.a[s], V.e[s]);
-            (void)ok;  // a dependent triple leaves an infinite error bound: every test on it is repaired in FP64
-        }
-    }
-
     // ---- plane slot allocation with recycling of dead planes
-    __device__ int alloc_plane() {
+    __device__ __forceinline__ int alloc_plane() {
         if (C.freeplanes == 0ull) {
             unsigned long long live = 0ull;
 #pragma unroll
             for (int s = 0; s < K; s++)
                 if (Vm.test(lane + 32 * s)) {
-                    unsigned t = V.tri[s];
+                    const unsigned t = V.tri[s];
                     live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
                 }
-            live = warp_or64(live);
-            C.freeplanes = ~live;
+            C.freeplanes = ~warp_or64(live);
             if (C.freeplanes == 0ull) return -1;
         }
-        int p = __ffsll((long long)C.freeplanes) - 1;
+        const int p = __ffsll((long long)C.freeplanes) - 1;
         C.freeplanes &= ~(1ull << p);
         return p;
     }
 
     // ---- test candidate (buffer slot cb) and cut the cell if it intersects.
-    __device__ void test_and_cut(int cb) {
-        const float4 Q = S.u.c.cd[cb];
-        const float4 E = S.u.c.ce[cb];
+    __device__ __forceinline__ void test_and_cut(int cb) {
+        PHASE_BEGIN(t_test);
         C.ptested++;
-        bool out[K], unc[K];
-        const int nvalid = Vm.popc();
-        C.tests += nvalid;
+        C.tests += (unsigned)Vm.popc();
+        bool out[K];
+        unsigned uncbits = 0;
         if (MODE == VGPU_FP64) {
-            const double4 Q64 = S.u.c.cd64[cb];
+            const double4 Q = S.u.c.cd64[cb];
+            const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
 #pragma unroll
             for (int s = 0; s < K; s++) {
-                out[s] = unc[s] = false;
-                if (Vm.test(lane + 32 * s)) {
-                    double v = fma(Q64.x, V.dx[s], fma(Q64.y, V.dy[s], fma(Q64.z, V.dz[s], -Q64.w)));
-                    double vv = sqrt(V.dx[s] * V.dx[s] + V.dy[s] * V.dy[s] + V.dz[s] * V.dz[s]);
-                    double nq = fabs(Q64.x) + fabs(Q64.y) + fabs(Q64.z);
-                    double bnd = nq * (double)V.e[s] + 8.0 * kU64 * (nq * vv + fabs(Q64.w)) + P.g.tol_h;
-                    out[s] = v > bnd;
-                    if (!out[s] && v >= -bnd) { unc[s] = true; }
-                }
+                const double v = fma(Q.x, V.dx[s], fma(Q.y, V.dy[s], fma(Q.z, V.dz[s], -Q.w)));
+                const double bnd = nq * (double)V.e[s] + 8.0 * kU64 * (nq * (double)V.a[s] + fabs(Q.w)) + P.g.tol_h;
+                out[s] = v > bnd;
+                if (!out[s] && v >= -bnd) uncbits |= 1u << s;
             }
-            Mask<K> Um = ballot_mask<K>(unc);
-            if (Um.any()) C.marginal = true;   // inside the tolerance band: kept, cell flagged
+            if (__any_sync(kFull, uncbits != 0)) C.marginal = true;   // tolerance band: kept, cell flagged
         } else {
-            const float nabs = sqrtf(E.z);
-            const float A = E.x + 3.0f * kU32 * nabs;
-            const float Cq = E.y + 3.0f * kU32 * fabsf(Q.w) + (float)P.g.tol_h;
+            const float4 Q = S.u.c.cd[cb];
+            const float4 E = S.u.c.ce[cb];
+            const float A = fmaf(3.0f * kU32, E.z, E.x);
+            const float Cq = fmaf(3.0f * kU32, fabsf(Q.w), E.y) + (float)P.g.tol_h;
 #pragma unroll
             for (int s = 0; s < K; s++) {
-                out[s] = unc[s] = false;
-                if (Vm.test(lane + 32 * s)) {
-                    float v = fmaf(Q.x, V.x[s], fmaf(Q.y, V.y[s], fmaf(Q.z, V.z[s], -Q.w)));
-                    float bnd = 1.5f * fmaf(A, V.a[s], fmaf(nabs, V.e[s], Cq));
-                    out[s] = v > bnd;
-                    unc[s] = !out[s] && v >= -bnd;
-                }
+                const float v = fmaf(Q.x, V.x[s], fmaf(Q.y, V.y[s], fmaf(Q.z, V.z[s], -Q.w)));
+                const float bnd = 1.5f * fmaf(A, V.a[s], fmaf(E.z, V.e[s], Cq));
+                out[s] = v > bnd;
+                if (!(v > bnd) && v >= -bnd) uncbits |= 1u << s;
             }
-            Mask<K> Um = ballot_mask<K>(unc);
-            if (Um.any()) {
-                // FP64 repair of the uncertain tests
+            const unsigned ub = __ballot_sync(kFull, uncbits != 0);
+            if (ub) {
                 C.repaired = true;
-                C.repairs += Um.popc();
-                bool anym = false;
+                C.repairs += __popc(ub);
+                bool m = false;
+                const unsigned ob = repair_tests<MODE, K>(P, S, C.me64, cb, uncbits, V.tri[0], K > 1 ? V.tri[K > 1 ? 1 : 0] : 0u,
+                                                          K > 2 ? V.tri[K > 2 ? 2 : 0] : 0u, K > 3 ? V.tri[K > 3 ? 3 : 0] : 0u, &m);
+                if (__any_sync(kFull, m)) C.marginal = true;
 #pragma unroll
-                for (int s = 0; s < K; s++) {
-                    if (unc[s]) {
-                        unsigned t = V.tri[s];
-                        double4 Q64 = plane64_from(P, C, S.cj[cb], S.cs[cb]);
-                        double4 A64 = plane64_of<K>(P, C, S, tri_plane(t, 0));
-                        double4 B64 = plane64_of<K>(P, C, S, tri_plane(t, 1));
-                        double4 C64 = plane64_of<K>(P, C, S, tri_plane(t, 2));
-                        double x, y, z, D, kn;
-                        solve_f64(A64, B64, C64, x, y, z, D, kn);
-                        int side = side64(Q64, x, y, z, D, kn, P.g.tol_h);
-                        if (!(D > 0.0)) side = 1;
-                        out[s] = side == 2;
-                        if (side == 1) anym = true;
-                    }
-                }
-                if (__any_sync(kFull, anym)) C.marginal = true;
+                for (int s = 0; s < K; s++)
+                    if ((uncbits >> s) & 1u) out[s] = (ob >> s) & 1u;
             }
         }
-        Mask<K> Rm = ballot_mask<K>(out);
+        const Mask<K> Rm = ballot_mask<K>(out);
+        PHASE_END(t_test, 3);
         if (!Rm.any()) return;
         if (Rm.equals(Vm)) {
             C.deleted = true;
             return;
         }
+        PHASE_BEGIN(t_cut);
         C.pcut++;
-        int p = alloc_plane();
+        const int p = alloc_plane();
         if (p < 0) {
             C.overflow = true;
             return;
         }
-        const int j = S.cj[cb];
         if (lane == 0) {
+            const float4 Q = S.u.c.cd[cb];
+            const float4 E = S.u.c.ce[cb];
+            const int j = S.u.c.cj[cb];
             S.pl[p] = Q;
-            S.pe[p] = make_float4(sqrtf(E.z), E.x, E.y, fabsf(Q.w));
+            S.pe[p] = make_float4(E.z, E.x, E.y, fabsf(Q.w));
             S.pid[p] = P.a.pid[j];
             S.psrc[p] = j;
-            S.pshift[p] = S.cs[cb];
-            if (MODE == VGPU_FP64) S.pl64[p] = S.u.c.cd64[cb];
+            S.pshift[p] = S.u.c.cs[cb];
+            if (MODE == VGPU_FP64) S.pl64x[p] = S.u.c.cd64[cb];
         }
         cut(p, Rm);
+        PHASE_END(t_cut, 4);
     }
 
     // ---- remove the vertices in Rm and close the hole with the face of plane p
-    __device__ void cut(int p, const Mask<K> &Rm) {
-        // Phase A: boundary edges of the removed region
-        unsigned be[3 * K];
+    __device__ __forceinline__ void cut(int p, const Mask<K> &Rm) {
+        // Phase A: count boundary edges (edges from a removed vertex to a kept one)
+        unsigned bnd[K];
         int nbe = 0;
         bool broken = false;
 #pragma unroll
         for (int s = 0; s < K; s++) {
-            int t = lane + 32 * s;
+            bnd[s] = 0;
+            const int t = lane + 32 * s;
             if (Rm.test(t)) {
-                unsigned T = V.tri[s];
-                unsigned A3 = S.adj[t];
+                const unsigned A3 = S.adj[t];
 #pragma unroll
                 for (int e = 0; e < 3; e++) {
-                    int u = (A3 >> (8 * e)) & 255u;
-                    if (u >= 32 * K) { broken = true; continue; }
-                    if (!Rm.test(u)) {
-                        int a = tri_plane(T, e), b = tri_plane(T, e == 2 ? 0 : e + 1);
-                        be[nbe++] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)u << 16);
-                    }
+                    const int u = (A3 >> (8 * e)) & 255u;
+                    if (u >= 32 * K) broken = true;
+                    else if (!Rm.test(u)) bnd[s] |= 1u << e;
                 }
+                nbe += __popc(bnd[s]);
             }
         }
-        // exclusive prefix of per-lane counts
-        int incl = nbe;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            int y = __shfl_up_sync(kFull, incl, d);
-            if (lane >= d) incl += y;
-        }
+        const int incl = warp_incl_scan(nbe, lane);
         const int total = __shfl_sync(kFull, incl, 31);
-        const int base = incl - nbe;
         if (__any_sync(kFull, broken)) {  // inconsistent adjacency: hand the cell to the large engine
             C.overflow = true;
+            return;
+        }
+        if (total < 3) {  // not a closed boundary: inconsistent side decisions
+            C.marginal = true;
             return;
         }
         Mask<K> Fm;
 #pragma unroll
         for (int i = 0; i < Mask<K>::W; i++) Fm.w[i] = ~Vm.w[i] | Rm.w[i];
-        if (total < 3) {  // not a closed boundary: inconsistent side decisions
-            C.marginal = true;
-            return;
-        }
         if (Fm.popc() < total) {
             C.overflow = true;
             return;
         }
-        __syncwarp();
-        // Phase B: new triangles (a, b, p) in the first free slots
-        int fslot[3 * K];
-        for (int q = 0; q < nbe; q++) {
-            unsigned E = be[q];
-            int a = E & 255u, b = (E >> 8) & 255u, u = (E >> 16) & 255u;
-            int f = Fm.nth(base + q);
-            fslot[q] = f;
-            S.tri[f] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)p << 16);
-            S.adj[f] = (unsigned)u;
-            S.startN[a] = (unsigned char)f;
-            S.endN[b] = (unsigned char)f;
-            unsigned Tu = S.tri[u];
+        // stage the boundary edges (a -> b, kept neighbour u) in lane order
+        {
+            int q = incl - nbe;
 #pragma unroll
-            for (int e = 0; e < 3; e++) {
-                if (tri_plane(Tu, e) == b && tri_plane(Tu, e == 2 ? 0 : e + 1) == a)
-                    reinterpret_cast<unsigned char *>(&S.adj[u])[e] = (unsigned char)f;
+            for (int s = 0; s < K; s++) {
+                if (bnd[s]) {
+                    const unsigned T = V.tri[s];
+                    const unsigned A3 = S.adj[lane + 32 * s];
+#pragma unroll
+                    for (int e = 0; e < 3; e++)
+                        if ((bnd[s] >> e) & 1u) {
+                            const int a = tri_plane(T, e), b = tri_plane(T, e == 2 ? 0 : e + 1);
+                            const unsigned u = (A3 >> (8 * e)) & 255u;
+                            S.stage[q++] = (unsigned)a | ((unsigned)b << 8) | (u << 16);
+                        }
+                }
             }
         }
         __syncwarp();
-        // Phase C: link the new triangles around the new face
+        // Phase B: the free slot of rank r hosts the new vertex (a, b, p) of boundary edge r
+        bool host[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) {
+            const int t = lane + 32 * s;
+            host[s] = false;
+            if (Fm.test(t)) {
+                const int r = Fm.rank(t);
+                if (r < total) {
+                    host[s] = true;
+                    const unsigned E = S.stage[r];
+                    const int a = E & 255u, b = (E >> 8) & 255u, u = (E >> 16) & 255u;
+                    const unsigned T = (unsigned)a | ((unsigned)b << 8) | ((unsigned)p << 16);
+                    V.tri[s] = T;
+                    S.tri[t] = T;
+                    S.adj[t] = (unsigned)u;
+                    S.startN[a] = (unsigned char)t;
+                    S.endN[b] = (unsigned char)t;
+                    const unsigned Tu = S.tri[u];
+#pragma unroll
+                    for (int e = 0; e < 3; e++)
+                        if (tri_plane(Tu, e) == b && tri_plane(Tu, e == 2 ? 0 : e + 1) == a)
+                            reinterpret_cast<unsigned char *>(&S.adj[u])[e] = (unsigned char)t;
+                }
+            }
+        }
+        __syncwarp();
+        // Phase C: link the new vertices around the new face; clear freed slots
         bool bad = false;
-        for (int q = 0; q < nbe; q++) {
-            unsigned E = be[q];
-            int a = E & 255u, b = (E >> 8) & 255u;
-            int f = fslot[q];
-            if (S.startN[a] != f) bad = true;
-            unsigned char *ab = reinterpret_cast<unsigned char *>(&S.adj[f]);
-            ab[1] = S.startN[b];
-            ab[2] = S.endN[a];
+#pragma unroll
+        for (int s = 0; s < K; s++) {
+            if (host[s]) {
+                const int t = lane + 32 * s;
+                const unsigned T = V.tri[s];
+                const int a = T & 255u, b = (T >> 8) & 255u;
+                if (S.startN[a] != t) bad = true;
+                unsigned char *ab = reinterpret_cast<unsigned char *>(&S.adj[t]);
+                ab[1] = S.startN[b];
+                ab[2] = S.endN[a];
+            } else if (Rm.test(lane + 32 * s)) {
+                clear_slot(s);
+            }
         }
         if (__any_sync(kFull, bad)) C.marginal = true;
-        // new valid mask: removed slots cleared, first `total` free slots set
-        Mask<K> Nm;
-        Nm.clear();
-        if (total > 0) {
-            int last = Fm.nth(total - 1);
-#pragma unroll
-            for (int i = 0; i < Mask<K>::W; i++) {
-                unsigned long long lim;
-                if (last >= i * 64 + 63) lim = ~0ull;
-                else if (last < i * 64) lim = 0ull;
-                else lim = (2ull << (last - i * 64)) - 1ull;
-                Nm.w[i] = Fm.w[i] & lim;
-            }
-        }
+        const Mask<K> Nm = ballot_mask<K>(host);
 #pragma unroll
         for (int i = 0; i < Mask<K>::W; i++) Vm.w[i] = (Vm.w[i] & ~Rm.w[i]) | Nm.w[i];
         __syncwarp();
         // Phase D: positions of the new vertices
 #pragma unroll
-        for (int s = 0; s < K; s++) {
-            int t = lane + 32 * s;
-            if (Nm.test(t)) {
-                V.tri[s] = S.tri[t];
-                compute_vertex(s);
-            }
-        }
+        for (int s = 0; s < K; s++)
+            if (host[s]) compute_vertex(s);
         update_radius();
     }
 
@@ -643,20 +673,27 @@ struct Engine {
     __device__ void flush() {
         const int n = C.ncand;
         if (n == 0) return;
+        PHASE_BEGIN(t_sort);
         __syncwarp();
-        unsigned k0 = lane < n ? S.ck[lane] : 0xffffffffu;
-        unsigned k1 = lane + 32 < n ? S.ck[lane + 32] : 0xffffffffu;
-        if (n > 32) bitonic64(k0, k1, lane);
-        else bitonic32(k0, lane);
+        unsigned k0 = lane < n ? S.u.c.ck[lane] : 0xffffffffu;
+        unsigned k1 = lane + 32 < n ? S.u.c.ck[lane + 32] : 0xffffffffu;
+        if (n > 32) {
+            const uint2 kk = bitonic64(k0, k1, lane);
+            k0 = kk.x;
+            k1 = kk.y;
+        } else {
+            k0 = bitonic32(k0, lane);
+        }
+        PHASE_END(t_sort, 2);
         for (int i = 0; i < n; i++) {
-            unsigned key = __shfl_sync(kFull, i < 32 ? k0 : k1, i & 31);
-            int cb = key & 63u;
-            float4 E = S.u.c.ce[cb];
+            const unsigned key = __shfl_sync(kFull, i < 32 ? k0 : k1, i & 31);
+            const int cb = key & 63u;
+            const float4 E = S.u.c.ce[cb];
             if (P.g.poly) {
-                float rs = E.w;
-                if (!(rs <= 0.0f || rs * rs < 4.0f * C.R2 * E.z * (1.0f + 16.0f * kU32))) continue;
+                const float rs = E.w;
+                if (!(rs <= 0.0f || rs * rs < 4.0f * C.R2 * E.z * E.z * (1.0f + 16.0f * kU32))) continue;
             } else {
-                if (E.z >= C.cutoff2 * (1.0f + 1e-4f)) break;
+                if (E.w >= C.cutoff2 * (1.0f + 1e-4f)) break;
             }
             test_and_cut(cb);
             if (C.deleted || C.overflow) break;
@@ -665,103 +702,103 @@ struct Engine {
         __syncwarp();
     }
 
-    // ---- evaluate one block offset for this lane: wrap/skip, block distance
+    // ---- candidates from a range of block offsets: wrap/skip, block distance,
+    //      then one lane per candidate particle
     __device__ void gather_offsets(int e_begin, int e_end, bool from_table, int shell_r) {
-        const float l[3] = {C.me32.x, C.me32.y, C.me32.z};
+        const float l0 = C.me32.x, l1 = C.me32.y, l2 = C.me32.z;
         for (int base = e_begin; base < e_end; base += 32) {
-            int e = base + lane;
+            const int e = base + lane;
             int di = 0, dj = 0, dk = 0;
             bool ok = e < e_end;
             if (ok) {
                 if (from_table) {
-                    int code = offsets[e];
+                    const int code = offsets[e];
                     di = (code & 31) - 16;
                     dj = ((code >> 5) & 31) - 16;
                     dk = ((code >> 10) & 31) - 16;
                 } else {
-                    int w = 2 * shell_r + 1;
+                    const int w = 2 * shell_r + 1;
                     di = e % w - shell_r;
                     dj = (e / w) % w - shell_r;
                     dk = e / (w * w) - shell_r;
-                    int m = max(abs(di), max(abs(dj), abs(dk)));
-                    int l2 = max(abs(di) - 1, 0) * max(abs(di) - 1, 0) + max(abs(dj) - 1, 0) * max(abs(dj) - 1, 0) +
-                             max(abs(dk) - 1, 0) * max(abs(dk) - 1, 0);
-                    ok = (m == shell_r) && (l2 > kTableLb2Max);
+                    const int m = max(abs(di), max(abs(dj), abs(dk)));
+                    const int a = max(abs(di) - 1, 0), b = max(abs(dj) - 1, 0), c = max(abs(dk) - 1, 0);
+                    ok = (m == shell_r) && (a * a + b * b + c * c > kTableLb2Max);
                 }
             }
-            int d[3] = {di, dj, dk};
-            int cb[3] = {C.bi + di, C.bj + dj, C.bk + dk};
-            int wrapped[3], img[3];
-            float md2 = 0.0f;
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                int n = P.g.gn[a];
-                int c = cb[a];
-                if (P.g.per[a]) {
-                    int w = c % n;
-                    if (w < 0) w += n;
-                    img[a] = (c - w) / n;
-                    wrapped[a] = w;
-                } else {
-                    img[a] = 0;
-                    wrapped[a] = c;
-                    if (c < 0 || c >= n) ok = false;
-                }
-                float bs = P.g.gbs32[a];
-                float t = d[a] > 0 ? (float)d[a] * bs - l[a] : (d[a] < 0 ? l[a] - (float)(d[a] + 1) * bs : 0.0f);
-                t = fmaxf(t, 0.0f);
-                md2 = fmaf(t, t, md2);
-            }
-            if (ok && md2 * (1.0f - 1e-5f) >= C.cutoff2) ok = false;
             int cnt = 0, st = 0, code = 0;
-            if (ok) {
-                int b = wrapped[0] + P.g.gn[0] * (wrapped[1] + P.g.gn[1] * wrapped[2]);
-                st = P.a.bstart[b];
-                cnt = P.a.bstart[b + 1] - st;
-                code = (img[0] + 128) | ((img[1] + 128) << 8) | ((img[2] + 128) << 16);
-            }
-            int incl = cnt;
+            {
+                const int d[3] = {di, dj, dk};
+                const int cb[3] = {C.bi + di, C.bj + dj, C.bk + dk};
+                const float l[3] = {l0, l1, l2};
+                int wr[3], img[3];
+                float md2 = 0.0f;
 #pragma unroll
-            for (int q = 1; q < 32; q <<= 1) {
-                int y = __shfl_up_sync(kFull, incl, q);
-                if (lane >= q) incl += y;
+                for (int a = 0; a < 3; a++) {
+                    const int n = P.g.gn[a];
+                    int c = cb[a];
+                    img[a] = 0;
+                    if (P.g.per[a]) {
+                        if (from_table && n > 2 * kOffsetRadius) {
+                            if (c < 0) { c += n; img[a] = -1; }
+                            else if (c >= n) { c -= n; img[a] = 1; }
+                        } else {
+                            int w = c % n;
+                            if (w < 0) w += n;
+                            img[a] = (c - w) / n;
+                            c = w;
+                        }
+                    } else if (c < 0 || c >= n) {
+                        ok = false;
+                    }
+                    wr[a] = c;
+                    const float bs = P.g.gbs32[a];
+                    float t = d[a] > 0 ? (float)d[a] * bs - l[a] : (d[a] < 0 ? l[a] - (float)(d[a] + 1) * bs : 0.0f);
+                    t = fmaxf(t, 0.0f);
+                    md2 = fmaf(t, t, md2);
+                }
+                if (ok && md2 * (1.0f - 1e-5f) >= C.cutoff2) ok = false;
+                if (ok) {
+                    const int b = wr[0] + P.g.gn[0] * (wr[1] + P.g.gn[1] * wr[2]);
+                    st = P.a.bstart[b];
+                    cnt = P.a.bstart[b + 1] - st;
+                    code = (img[0] + 128) | ((img[1] + 128) << 8) | ((img[2] + 128) << 16);
+                }
             }
+            const int incl = warp_incl_scan(cnt, lane);
             const int tot = __shfl_sync(kFull, incl, 31);
             const int packed_d = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
             for (int c0 = 0; c0 < tot; c0 += 32) {
                 if (C.ncand > kCandBuf - 32) flush();
                 if (C.deleted || C.overflow) return;
-                int c = c0 + lane;
-                bool has = c < tot;
+                const int c = c0 + lane;
                 // owner lane: number of lanes whose inclusive prefix is <= c
                 int pos = 0;
 #pragma unroll
                 for (int w = 16; w >= 1; w >>= 1) {
-                    int v = __shfl_sync(kFull, incl, pos + w - 1);
+                    const int v = __shfl_sync(kFull, incl, pos + w - 1);
                     if (v <= c) pos += w;
                 }
                 pos = min(pos, 31);
-                int o_incl = __shfl_sync(kFull, incl, pos);
-                int o_cnt = __shfl_sync(kFull, cnt, pos);
-                int o_st = __shfl_sync(kFull, st, pos);
-                int o_code = __shfl_sync(kFull, code, pos);
-                int o_d = __shfl_sync(kFull, packed_d, pos);
+                const int o_incl = __shfl_sync(kFull, incl, pos);
+                const int o_cnt = __shfl_sync(kFull, cnt, pos);
+                const int o_st = __shfl_sync(kFull, st, pos);
+                const int o_code = __shfl_sync(kFull, code, pos);
+                const int o_d = __shfl_sync(kFull, packed_d, pos);
                 bool pass = false;
                 unsigned key = 0;
                 float4 cd = make_float4(0, 0, 0, 0), ce = make_float4(0, 0, 0, 0);
-                int j = 0;
-                if (has) {
-                    j = o_st + (c - (o_incl - o_cnt));
-                    int ddi = (o_d & 31) - 16, ddj = ((o_d >> 5) & 31) - 16, ddk = ((o_d >> 10) & 31) - 16;
-                    bool self = (j == C.k) && ddi == 0 && ddj == 0 && ddk == 0;
+                const int j = o_st + (c - (o_incl - o_cnt));
+                if (c < tot) {
+                    const int ddi = (o_d & 31) - 16, ddj = ((o_d >> 5) & 31) - 16, ddk = ((o_d >> 10) & 31) - 16;
+                    const bool self = (j == C.k) && ddi == 0 && ddj == 0 && ddk == 0;
                     if (!self) {
-                        float4 lj = P.a.l32[j];
-                        float dx = fmaf((float)ddi, P.g.gbs32[0], lj.x - C.me32.x);
-                        float dy = fmaf((float)ddj, P.g.gbs32[1], lj.y - C.me32.y);
-                        float dz = fmaf((float)ddk, P.g.gbs32[2], lj.z - C.me32.z);
-                        float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        float rs = d2;
-                        float rr = 0.0f;
+                        const float4 lj = P.a.l32[j];
+                        const float dx = fmaf((float)ddi, P.g.gbs32[0], lj.x - l0);
+                        const float dy = fmaf((float)ddj, P.g.gbs32[1], lj.y - l1);
+                        const float dz = fmaf((float)ddk, P.g.gbs32[2], lj.z - l2);
+                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        float rs = d2, rr = 0.0f;
                         if (P.g.poly) {
                             rr = C.ri2 + lj.w * lj.w;
                             rs = d2 + (C.ri2 - lj.w * lj.w);
@@ -769,25 +806,26 @@ struct Engine {
                         } else {
                             pass = d2 < C.cutoff2 * (1.0f + 1e-5f);
                         }
-                        int M = max(abs(ddi), max(abs(ddj), abs(ddk)));
-                        float bsmax = fmaxf(P.g.gbs32[0], fmaxf(P.g.gbs32[1], P.g.gbs32[2]));
-                        float dn = sqrtf(d2);
-                        float en = kU32 * (1.75f * (float)(M + 3) * bsmax + 1.01f * dn) + 1e-12f * bsmax;
-                        float eh = dn * en + 2.0f * kU32 * (d2 + rr) + 0.5f * en * en;
+                        // forward error of the FP32 plane: local coordinates and block
+                        // offsets each carry at most u*bs; the sum one more rounding
+                        const int M = max(abs(ddi), max(abs(ddj), abs(ddk)));
+                        const float dn = sqrtf(d2);
+                        const float en = kU32 * (1.75f * (float)(M + 3) * P.g.gbs_max + 1.01f * dn) + 1e-12f * P.g.gbs_max;
+                        const float eh = dn * en + 2.0f * kU32 * (d2 + rr) + 0.5f * en * en;
                         cd = make_float4(dx, dy, dz, 0.5f * rs);
-                        ce = make_float4(en, eh, d2, rs);
-                        key = float_key(P.g.poly ? rs : d2);
+                        ce = make_float4(en, eh, dn, rs);
+                        key = float_key(rs);
                     }
                 }
-                unsigned bal = __ballot_sync(kFull, pass);
+                const unsigned bal = __ballot_sync(kFull, pass);
                 if (pass) {
-                    int slot = C.ncand + __popc(bal & ((1u << lane) - 1u));
-                    S.ck[slot] = (key & ~63u) | (unsigned)slot;
-                    S.cj[slot] = j;
-                    S.cs[slot] = o_code;
+                    const int slot = C.ncand + __popc(bal & ((1u << lane) - 1u));
+                    S.u.c.ck[slot] = (key & ~63u) | (unsigned)slot;
+                    S.u.c.cj[slot] = j;
+                    S.u.c.cs[slot] = o_code;
                     S.u.c.cd[slot] = cd;
                     S.u.c.ce[slot] = ce;
-                    if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C, j, o_code);
+                    if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C.me64, j, o_code);
                 }
                 C.ncand += __popc(bal);
             }
@@ -795,32 +833,40 @@ struct Engine {
     }
 
     // ---- the search: blocks in order of lower-bound distance (src/v_compute.cc:289-621
-    //      does the same with its 64 worklists, mrad cut-offs and the block queue)
+    //      does the same with its 64 worklists, mrad cut-offs and the block queue).
+    //      Segments 0..ngroups-1 are the table's distance groups; after them come
+    //      Chebyshev shells r = kOffsetRadius, ... with what the table covered skipped.
     __device__ void search() {
         const float bmin2 = P.g.gbs_min * P.g.gbs_min;
-        bool done = false;
-        for (int g = 0; g < P.ngroups && !done; g++) {
-            if ((float)P.group_lb2[g] * bmin2 >= C.cutoff2 * (1.0f + 1e-5f)) { done = true; break; }
-            gather_offsets(P.group_start[g], P.group_start[g + 1], true, 0);
+        const int rmax_grid = max(P.g.gn[0], max(P.g.gn[1], P.g.gn[2]));
+        const bool any_periodic = P.g.per[0] || P.g.per[1] || P.g.per[2];
+        const int rlim = min(4 * rmax_grid + 8, 40);
+        for (int seg = 0;; seg++) {
+            const bool table = seg < P.ngroups;
+            int b0 = 0, b1 = 0, r = 0;
+            float lb2;
+            if (table) {
+                lb2 = (float)P.group_lb2[seg] * bmin2;
+                b0 = P.group_start[seg];
+                b1 = P.group_start[seg + 1];
+            } else {
+                r = kOffsetRadius + (seg - P.ngroups);
+                if (r >= rlim) {
+                    C.overflow = true;  // search did not terminate
+                    return;
+                }
+                if (!any_periodic && r > rmax_grid + 1) return;
+                lb2 = (float)((r - 1) * (r - 1)) * bmin2;
+                b1 = (2 * r + 1) * (2 * r + 1) * (2 * r + 1);
+            }
+            if (lb2 >= C.cutoff2 * (1.0f + 1e-5f)) return;
+            PHASE_BEGIN(t_g);
+            gather_offsets(b0, b1, table, r);
+            PHASE_END(t_g, 1);
             if (C.deleted || C.overflow) return;
             flush();
             if (C.deleted || C.overflow) return;
         }
-        if (done) return;
-        // beyond the table: Chebyshev shells, skipping what the table covered
-        int rmax_grid = max(P.g.gn[0], max(P.g.gn[1], P.g.gn[2]));
-        for (int r = 2; r < 4 * rmax_grid + 8; r++) {
-            float lb = (float)(r - 1) * P.g.gbs_min;
-            if (lb * lb >= C.cutoff2 * (1.0f + 1e-5f)) return;
-            bool any_periodic = P.g.per[0] || P.g.per[1] || P.g.per[2];
-            if (!any_periodic && r > rmax_grid + 1) return;
-            int w = 2 * r + 1;
-            gather_offsets(0, w * w * w, false, r);
-            if (C.deleted || C.overflow) return;
-            flush();
-            if (C.deleted || C.overflow) return;
-        }
-        C.overflow = true;  // search did not terminate
     }
 
     // ---- reductions: vertex/face counts, neighbours, FP64 volume and centroid
@@ -842,85 +888,128 @@ struct Engine {
 #pragma unroll
         for (int s = 0; s < K; s++)
             if (Vm.test(lane + 32 * s)) {
-                unsigned t = V.tri[s];
+                const unsigned t = V.tri[s];
                 live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
             }
         live = warp_or64(live);
         const int nf = __popcll(live);
         const int nv = Vm.popc();
-        // neighbours, ascending plane order; FP64 planes of the live faces
-        for (int q = lane; q < nf; q += 32) {
-            unsigned long long x = live;
-            for (int i = 0; i < q; i++) x &= x - 1ull;
-            int p = __ffsll((long long)x) - 1;
-            P.r.nb[(size_t)out * kMaxNb + q] = S.pid[p];
-            S.pl64[p] = plane64_of<K>(P, C, S, p);
+        // neighbours (ascending plane slot order) and the FP64 planes of the live
+        // faces, written over the FP32 plane arrays
+        double4 *pl64 = MODE == VGPU_FP64 ? S.pl64x : reinterpret_cast<double4 *>(S.pl);
+        double4 mine[2];
+        bool has[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int p = lane + 32 * h;
+            has[h] = (live >> p) & 1ull;
+            if (has[h]) {
+                const int q = __popcll(live & ((1ull << p) - 1ull));
+                P.r.nb[(size_t)out * kMaxNb + q] = S.pid[p];
+                if (MODE != VGPU_FP64) mine[h] = plane64_slot<MODE, K>(P, S, C.me64, p);
+            }
+        }
+        if (MODE != VGPU_FP64) {
+            __syncwarp();
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (has[h]) pl64[lane + 32 * h] = mine[h];
         }
         __syncwarp();
-        // FP64 vertices, rebuilt from their three planes
+        // FP64 vertices: one residual correction of the FP32 vertex against its
+        // three FP64 planes (FP64 engine: already FP64)
+        double vx[K], vy[K], vz[K];
         double mr2 = 0.0;
 #pragma unroll
         for (int s = 0; s < K; s++) {
-            int t = lane + 32 * s;
-            if (Vm.test(t)) {
-                double x, y, z;
+            vx[s] = vy[s] = vz[s] = 0.0;
+            if (Vm.test(lane + 32 * s)) {
                 if (MODE == VGPU_FP64) {
-                    x = V.dx[s]; y = V.dy[s]; z = V.dz[s];
+                    vx[s] = V.dx[s]; vy[s] = V.dy[s]; vz[s] = V.dz[s];
                 } else {
-                    unsigned T = V.tri[s];
-                    double D, kn;
-                    solve_f64(S.pl64[tri_plane(T, 0)], S.pl64[tri_plane(T, 1)], S.pl64[tri_plane(T, 2)], x, y, z, D, kn);
+                    const double3 r = refine_vertex_f64(pl64, V.tri[s], V.x[s], V.y[s], V.z[s]);
+                    vx[s] = r.x; vy[s] = r.y; vz[s] = r.z;
                 }
-                S.u.f.vtx[t] = make_double4(x, y, z, 0.0);
-                mr2 = fmax(mr2, x * x + y * y + z * z);
+                mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
             }
         }
-        __syncwarp();
-        // Origin for the volume sums: one vertex of the cell, so that every term
-        // scales with the cell size rather than its distance from the particle.
-        const double4 c0 = S.u.f.vtx[Vm.nth(0)];
-        for (int q = lane; q < nf; q += 32) {
-            unsigned long long x = live;
-            for (int i = 0; i < q; i++) x &= x - 1ull;
-            int p = __ffsll((long long)x) - 1;
-            double4 pl = S.pl64[p];
-            double nn = pl.x * pl.x + pl.y * pl.y + pl.z * pl.z;
-            double f = (pl.w - (pl.x * c0.x + pl.y * c0.y + pl.z * c0.z)) / nn;
-            S.foot[p] = make_double4(pl.x * f, pl.y * f, pl.z * f, 0.0);  // closest point of face p to c0, relative to c0
-        }
-        __syncwarp();
-        // volume and centroid over edges (t,u) owned by the lower slot:
-        // sum over edges of (p_y - p_x).(v_t x v_u), p_f a point of face f
-        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+        // origin of the volume sums: one vertex of the cell, so that every term
+        // scales with the cell size rather than its distance from the particle
+        const int t0 = Vm.first();
+        double c0x = 0, c0y = 0, c0z = 0;
 #pragma unroll
         for (int s = 0; s < K; s++) {
-            int t = lane + 32 * s;
+            const double sx = __shfl_sync(kFull, vx[s], t0 & 31);
+            const double sy = __shfl_sync(kFull, vy[s], t0 & 31);
+            const double sz = __shfl_sync(kFull, vz[s], t0 & 31);
+            if ((t0 >> 5) == s) { c0x = sx; c0y = sy; c0z = sz; }
+        }
+        // vertices relative to c0, and the owned edges (t < u) listed compactly
+        int ne = 0;
+        unsigned own[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) {
+            own[s] = 0;
+            const int t = lane + 32 * s;
             if (Vm.test(t)) {
-                unsigned T = V.tri[s];
-                unsigned A3 = S.adj[t];
-                double4 vt = S.u.f.vtx[t];
-                vt.x -= c0.x; vt.y -= c0.y; vt.z -= c0.z;
+                S.u.f.vx[t] = vx[s] - c0x;
+                S.u.f.vy[t] = vy[s] - c0y;
+                S.u.f.vz[t] = vz[s] - c0z;
+                const unsigned A3 = S.adj[t];
 #pragma unroll
                 for (int e = 0; e < 3; e++) {
-                    int u = (A3 >> (8 * e)) & 255u;
-                    if (u > t && u < 32 * K) {
-                        double4 vu = S.u.f.vtx[u];
-                        vu.x -= c0.x; vu.y -= c0.y; vu.z -= c0.z;
-                        double4 px = S.foot[tri_plane(T, e)];
-                        double4 py = S.foot[tri_plane(T, e == 2 ? 0 : e + 1)];
-                        double wx = vt.y * vu.z - vt.z * vu.y;
-                        double wy = vt.z * vu.x - vt.x * vu.z;
-                        double wz = vt.x * vu.y - vt.y * vu.x;
-                        double ty = py.x * wx + py.y * wy + py.z * wz;
-                        double tx = px.x * wx + px.y * wy + px.z * wz;
-                        double dd = ty - tx;
-                        vs += dd;
-                        cx += dd * (vt.x + vu.x) + ty * py.x - tx * px.x;
-                        cy += dd * (vt.y + vu.y) + ty * py.y - tx * px.y;
-                        cz += dd * (vt.z + vu.z) + ty * py.z - tx * px.z;
-                    }
+                    const int u = (A3 >> (8 * e)) & 255u;
+                    if (u > t && u < 32 * K) own[s] |= 1u << e;
                 }
+                ne += __popc(own[s]);
             }
+        }
+        // face points: the point of each live face closest to c0, relative to c0
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (has[h]) {
+                const int p = lane + 32 * h;
+                const double4 pl = pl64[p];
+                const double nn = pl.x * pl.x + pl.y * pl.y + pl.z * pl.z;
+                const double f = (pl.w - (pl.x * c0x + pl.y * c0y + pl.z * c0z)) / nn;
+                S.u.f.fx[p] = pl.x * f;
+                S.u.f.fy[p] = pl.y * f;
+                S.u.f.fz[p] = pl.z * f;
+            }
+        }
+        const int eincl = warp_incl_scan(ne, lane);
+        const int etot = __shfl_sync(kFull, eincl, 31);
+        {
+            int q = eincl - ne;
+#pragma unroll
+            for (int s = 0; s < K; s++)
+#pragma unroll
+                for (int e = 0; e < 3; e++)
+                    if ((own[s] >> e) & 1u) S.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
+        }
+        __syncwarp();
+        // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a point of face f
+        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int i = lane; i < etot; i += 32) {
+            const unsigned E = S.stage[i];
+            const int t = E & 255u, e = E >> 8;
+            const unsigned T = S.tri[t];
+            const int u = (S.adj[t] >> (8 * e)) & 255u;
+            const int px = tri_plane(T, e), py = tri_plane(T, e == 2 ? 0 : e + 1);
+            const double tx = S.u.f.vx[t], ty = S.u.f.vy[t], tz = S.u.f.vz[t];
+            const double ux = S.u.f.vx[u], uy = S.u.f.vy[u], uz = S.u.f.vz[u];
+            const double wx = ty * uz - tz * uy;
+            const double wy = tz * ux - tx * uz;
+            const double wz = tx * uy - ty * ux;
+            const double ax = S.u.f.fx[px], ay = S.u.f.fy[px], az = S.u.f.fz[px];
+            const double bx = S.u.f.fx[py], by = S.u.f.fy[py], bz = S.u.f.fz[py];
+            const double dy = bx * wx + by * wy + bz * wz;
+            const double dx = ax * wx + ay * wy + az * wz;
+            const double dd = dy - dx;
+            vs += dd;
+            cx += dd * (tx + ux) + dy * bx - dx * ax;
+            cy += dd * (ty + uy) + dy * by - dx * ay;
+            cz += dd * (tz + uz) + dy * bz - dx * az;
         }
         vs = warp_sumd(vs);
         cx = warp_sumd(cx);
@@ -928,14 +1017,14 @@ struct Engine {
         cz = warp_sumd(cz);
         mr2 = warp_maxd(mr2);
         if (lane == 0) {
-            double vol = vs / 6.0;
+            const double vol = vs / 6.0;
             P.r.vol[out] = vol;
             // centroid threshold as src/cell.cc:1895 (raw doubled-coordinate sum = 48*volume)
             if (48.0 * vol > P.g.tol_cu) {
-                double f = 1.0 / (4.0 * vs);
-                P.r.cen[3 * out] = c0.x + cx * f;
-                P.r.cen[3 * out + 1] = c0.y + cy * f;
-                P.r.cen[3 * out + 2] = c0.z + cz * f;
+                const double f = 1.0 / (4.0 * vs);
+                P.r.cen[3 * out] = c0x + cx * f;
+                P.r.cen[3 * out + 1] = c0y + cy * f;
+                P.r.cen[3 * out + 2] = c0z + cz * f;
             } else {
                 P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
             }
@@ -944,45 +1033,65 @@ struct Engine {
             P.r.maxr2[out] = mr2;
             P.r.flags[out] = VGPU_CELL_OK | (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
         }
+        __syncwarp();
     }
 
     __device__ void run(int k) {
+#ifdef VGPU_PHASE_TIMING
+        for (int i = 0; i < 8; i++) C.phase[i] = 0;
+#endif
+        PHASE_BEGIN(t_init);
         init_cell(k);
+        PHASE_END(t_init, 0);
         search();
+        PHASE_BEGIN(t_fin);
         finish();
+        PHASE_END(t_fin, 5);
     }
 };
 
+// CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot) engine;
+// it fixes the register budget (65536 / (128 * blocks)).
+#ifndef VGPU_MIN_BLOCKS
+#define VGPU_MIN_BLOCKS 4
+#endif
 template <int MODE, int K>
-__global__ void __launch_bounds__(128) cell_kernel(CellParams P) {
+constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
+
+template <int MODE, int K>
+__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int warps = blockDim.x >> 5;
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *offsets = reinterpret_cast<int *>(smem_raw);
-    size_t off_bytes = ((size_t)P.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    WarpShared<K> *ws = reinterpret_cast<WarpShared<K> *>(smem_raw + off_bytes);
+    const size_t off_bytes = ((size_t)P.noffsets * sizeof(int) + 15) & ~(size_t)15;
+    WarpShared<MODE, K> *ws = reinterpret_cast<WarpShared<MODE, K> *>(smem_raw + off_bytes);
     for (int i = threadIdx.x; i < P.noffsets; i += blockDim.x) offsets[i] = P.offsets[i];
     __syncthreads();
-    (void)warps;
-    WarpShared<K> &S = ws[wid];
-    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0, overflow = 0;
+    WarpShared<MODE, K> &S = ws[wid];
+    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0;
+#ifdef VGPU_PHASE_TIMING
+    unsigned long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const long long t_kernel0 = clock64();
+#endif
     unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
     for (;;) {
         int w = 0;
         if (lane == 0) w = (int)atomicAdd(work, 1ull);
         w = __shfl_sync(kFull, w, 0);
         if (w >= P.ncells) break;
-        int k = P.cell_list ? P.cell_list[w] : w;
+        const int k = P.cell_list ? P.cell_list[w] : w;
         Engine<MODE, K> eng(P, S, offsets, lane);
         eng.run(k);
         tests += eng.C.tests;
         repairs += eng.C.repairs;
         ptested += eng.C.ptested;
         pcut += eng.C.pcut;
+#ifdef VGPU_PHASE_TIMING
+        for (int i = 0; i < 8; i++) ph[i] += eng.C.phase[i];
+#endif
         if (eng.C.overflow) {
-            overflow++;
             if (lane == 0) {
-                unsigned long long slot = atomicAdd(&P.cnt->overflow, 1ull);
+                const unsigned long long slot = atomicAdd(&P.cnt->overflow, 1ull);
                 if (P.overflow_list) P.overflow_list[slot] = k;
             }
         } else {
@@ -998,6 +1107,10 @@ __global__ void __launch_bounds__(128) cell_kernel(CellParams P) {
         atomicAdd(&P.cnt->planes_cut, pcut);
         atomicAdd(&P.cnt->deleted, deleted);
         atomicAdd(&P.cnt->marginal, marginal);
+#ifdef VGPU_PHASE_TIMING
+        ph[7] = (unsigned long long)(clock64() - t_kernel0);
+        for (int i = 0; i < 8; i++) atomicAdd(&P.cnt->phase_cycles[i], ph[i]);
+#endif
     }
 }
 
@@ -1042,16 +1155,16 @@ __global__ void sum_volumes_kernel(const double *vol, const int *flags, int n, d
 template <int MODE, int K>
 cudaError_t launch_one(const CellParams &cp, int sms, cudaStream_t s) {
     const int warps = 4;
-    size_t off_bytes = ((size_t)cp.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    size_t smem = off_bytes + warps * sizeof(WarpShared<K>);
+    const size_t off_bytes = ((size_t)cp.noffsets * sizeof(int) + 15) & ~(size_t)15;
+    const size_t smem = off_bytes + warps * sizeof(WarpShared<MODE, K>);
     cudaError_t e = cudaFuncSetAttribute(cell_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_kernel<MODE, K>, warps * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
-    long long want = (long long)sms * per_sm;
-    long long need = (cp.ncells + warps - 1) / warps;
+    const long long want = (long long)sms * per_sm;
+    const long long need = (cp.ncells + warps - 1) / warps;
     int grid = (int)(want < need ? want : need);
     if (grid < 1) grid = 1;
     cell_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(cp);
@@ -1088,6 +1201,8 @@ static void build_box_tables(unsigned tri[8], unsigned adj[8]) {
         adj[c] = a3;
     }
 }
+
+void box_tables(unsigned tri[8], unsigned adj[8]) { build_box_tables(tri, adj); }
 
 cudaError_t upload_box_tables() {
     unsigned tri[8], adj[8];

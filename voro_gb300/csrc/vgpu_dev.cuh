@@ -1,0 +1,77 @@
+// Device helpers shared by the engine's cell kernels.
+#pragma once
+#include "vgpu_internal.cuh"
+#include "../../include/vorogpu.h"
+
+namespace vgpu {
+
+static constexpr float kU32 = 5.9604645e-08f;          // 2^-24
+static constexpr double kU64 = 1.1102230246251565e-16; // 2^-53
+static constexpr unsigned kFull = 0xffffffffu;
+
+// plane indices are always < kMaxPlanes; the mask keeps every shared-memory
+// index in bounds even if a slot held inconsistent data
+static __device__ __forceinline__ int tri_plane(unsigned t, int e) { return (t >> (8 * e)) & (kMaxPlanes - 1); }
+
+// Sortable key of a float (total order as unsigned)
+static __device__ __forceinline__ unsigned float_key(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+static __device__ __forceinline__ int unpack_shift(int code, int a) { return ((code >> (8 * a)) & 255) - 128; }
+
+// FP64 plane of a candidate (engine index j, image counts) relative to the
+// particle, with the reference's own arithmetic: x1 = p_j - (x - qx)
+// (src/v_compute.cc:383-397) and rs = x1*x1+y1*y1+z1*z1 [+ r_i^2 - r_j^2]
+// (r_scale, src/rad_option.hh:414-416).  h = rs/2 (the reference works in
+// doubled coordinates; halving is exact).
+static __device__ __noinline__ double4 plane64_from(const CellParams &P, double4 me, int j, int code) {
+    double4 q = P.a.p64[j];
+    double sx = unpack_shift(code, 0) * P.g.len[0];
+    double sy = unpack_shift(code, 1) * P.g.len[1];
+    double sz = unpack_shift(code, 2) * P.g.len[2];
+    double x1 = __dsub_rn(q.x, __dsub_rn(me.x, sx));
+    double y1 = __dsub_rn(q.y, __dsub_rn(me.y, sy));
+    double z1 = __dsub_rn(q.z, __dsub_rn(me.z, sz));
+    double rs = __dadd_rn(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)), __dmul_rn(z1, z1));
+    if (P.g.poly) rs = __dsub_rn(__dadd_rn(rs, __dmul_rn(me.w, me.w)), __dmul_rn(q.w, q.w));
+    return make_double4(x1, y1, z1, 0.5 * rs);
+}
+
+// FP64 plane of an initial face (f = 2*axis + side) of the particle's cell
+static __device__ __forceinline__ double4 face64(const CellParams &P, double4 me, int f) {
+    const int ax = f >> 1;
+    const bool hiside = f & 1;
+    const double xa = ax == 0 ? me.x : (ax == 1 ? me.y : me.z);
+    double h;
+    if (P.g.unit_cell || P.g.per[ax]) h = 0.5 * P.g.len[ax];
+    else h = hiside ? __dsub_rn(P.g.hi[ax], xa) : -__dsub_rn(P.g.lo[ax], xa);
+    const double n = hiside ? 1.0 : -1.0;
+    return make_double4(ax == 0 ? n : 0.0, ax == 1 ? n : 0.0, ax == 2 ? n : 0.0, h);
+}
+
+// Vertex of three FP64 planes by Cramer's rule; kn = sum over rows of
+// |cofactor row| * (|h| + |n||v|), the scale of its rounding error.
+static __device__ __forceinline__ void solve_f64(const double4 A, const double4 B, const double4 C, double &x, double &y,
+                                          double &z, double &D, float &kn) {
+    double bcx = B.y * C.z - B.z * C.y, bcy = B.z * C.x - B.x * C.z, bcz = B.x * C.y - B.y * C.x;
+    double cax = C.y * A.z - C.z * A.y, cay = C.z * A.x - C.x * A.z, caz = C.x * A.y - C.y * A.x;
+    double abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
+    D = A.x * bcx + A.y * bcy + A.z * bcz;
+    double inv = 1.0 / D;
+    x = (A.w * bcx + B.w * cax + C.w * abx) * inv;
+    y = (A.w * bcy + B.w * cay + C.w * aby) * inv;
+    z = (A.w * bcz + B.w * caz + C.w * abz) * inv;
+    float vv = sqrtf((float)(x * x + y * y + z * z));
+    float nbc = fabsf((float)bcx) + fabsf((float)bcy) + fabsf((float)bcz);
+    float nca = fabsf((float)cax) + fabsf((float)cay) + fabsf((float)caz);
+    float nab = fabsf((float)abx) + fabsf((float)aby) + fabsf((float)abz);
+    float na = fabsf((float)A.x) + fabsf((float)A.y) + fabsf((float)A.z);
+    float nb = fabsf((float)B.x) + fabsf((float)B.y) + fabsf((float)B.z);
+    float nc = fabsf((float)C.x) + fabsf((float)C.y) + fabsf((float)C.z);
+    kn = nbc * (fabsf((float)A.w) + na * vv) + nca * (fabsf((float)B.w) + nb * vv) + nab * (fabsf((float)C.w) + nc * vv);
+}
+
+
+}  // namespace vgpu

@@ -32,6 +32,7 @@ struct Geometry {
     double gbs[3];      // engine block sizes
     float gbs32[3];
     float gbs_min;
+    float gbs_max;
     double tol_h;       // half the reference tolerance: 0.5*10*DBL_EPSILON*max_len_sq
     double tol_cu;      // reference tol_cu (centroid threshold, src/cell.cc:25)
     double rmax;        // largest radius (poly kinds)
@@ -68,6 +69,7 @@ struct Counters {
     unsigned long long overflow;   // cells appended to the overflow list
     unsigned long long work;       // work-queue counter
     unsigned long long overflow_work;
+    unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
 };
 
 struct CellParams {
@@ -83,6 +85,8 @@ struct CellParams {
     int ngroups;
     int group_start[kMaxGroups + 1];
     int group_lb2[kMaxGroups];
+    unsigned box_tri[8];    // initial box: corner triangles and neighbours
+    unsigned box_adj[8];
 };
 
 // launch accounting (vgpu_api.cu)
@@ -124,5 +128,7 @@ cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long lo
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);
 cudaError_t exclusive_scan_ll(const long long *in, long long *out, int n, long long *tmp, cudaStream_t s);
 cudaError_t launch_sum_volumes(const double *vol, const int *flags, int n, double *out, cudaStream_t s);
+void box_tables(unsigned tri[8], unsigned adj[8]);
+
 
 }  // namespace vgpu

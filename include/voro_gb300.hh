@@ -1,0 +1,430 @@
+// Drop-in C++ host API for the GB300 Voronoi cell engine.
+//
+// A program written against the reference's container API (src/voro++.hh:
+// container, container_poly, container_periodic, container_periodic_poly,
+// c_loop_all, c_loop_all_periodic, voronoicell, voronoicell_neighbor) builds
+// against this header instead by replacing
+//     #include "voro++.hh"            ->   #include "voro_gb300.hh"
+//     -lvoro++                        ->   -lvorogpu
+// The classes keep the reference's names, constructor arguments and
+// semantics; every cell is computed on the GPU through the C ABI of
+// vorogpu.h, once per compute_all_cells() (or lazily on first use).
+//
+// What a cell exposes after compute_cell(c, vl) is what the engine returns per
+// cell: volume(), centroid(), number_of_faces(), number_of_edges(), p (vertex
+// count), max_radius_squared() and, for voronoicell_neighbor, neighbors().
+// Queries that need the polytope itself (vertices(), face_areas(), ...) are
+// not provided, so code using them fails to compile rather than silently
+// differing.
+//
+// Errors follow the reference (src/common.cc:27-30): the message is printed
+// and the process exits with the status code, unless VORO_GB300_THROW is
+// defined, in which case voro::gpu_error is thrown instead.
+#ifndef VORO_GB300_HH
+#define VORO_GB300_HH
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "vorogpu.h"
+
+namespace voro {
+
+// Status codes and the default radius of the reference (src/config.hh:88-119).
+const int VOROPP_FILE_ERROR = 1;
+const int VOROPP_MEMORY_ERROR = 2;
+const int VOROPP_INTERNAL_ERROR = 3;
+const int VOROPP_CMD_LINE_ERROR = 4;
+const double default_radius = 0.5;
+
+struct gpu_error : std::runtime_error {
+    int status;
+    gpu_error(const std::string &m, int s) : std::runtime_error(m), status(s) {}
+};
+
+inline void voro_fatal_error(const char *p, int status) {
+#ifdef VORO_GB300_THROW
+    throw gpu_error(p, status);
+#else
+    fprintf(stderr, "voro++: %s\n", p);
+    exit(status);
+#endif
+}
+
+namespace gpu_detail {
+// Argument packs for the C ABI's fixed-size arrays (temporaries that live
+// until the end of the constructor call that uses them).
+struct d6 {
+    double v[6];
+};
+struct i3 {
+    int v[3];
+};
+inline void check(int rc, const char *what) {
+    if (rc == VGPU_OK) return;
+    std::string m = std::string(what) + ": " + vgpu_last_error();
+    // engine codes 1..3 are the reference's; the GPU-specific ones map to an internal error
+    voro_fatal_error(m.c_str(), rc <= VOROPP_INTERNAL_ERROR ? rc : VOROPP_INTERNAL_ERROR);
+}
+}  // namespace gpu_detail
+
+class container_gpu_base;
+
+// Per-cell results of one compute_cell call (voronoicell, src/cell.hh:93-350).
+class voronoicell {
+  public:
+    int p = 0;   // vertex count (voronoicell_base::p)
+    voronoicell() {}
+    template <class C>
+    explicit voronoicell(C &) {}
+    double volume() const { return vol_; }
+    void centroid(double &cx, double &cy, double &cz) const {
+        cx = cen_[0];
+        cy = cen_[1];
+        cz = cen_[2];
+    }
+    int number_of_faces() const { return nf_; }
+    // every vertex the engine produces has order 3 (E = 3p/2)
+    int number_of_edges() const { return 3 * p / 2; }
+    void vertex_orders(std::vector<int> &v) const { v.assign(p, 3); }
+    // in the reference's doubled coordinates (src/cell.cc:1907-1917)
+    double max_radius_squared() const { return 4.0 * mr2_; }
+
+  protected:
+    friend class container_gpu_base;
+    double vol_ = 0, cen_[3] = {0, 0, 0}, mr2_ = 0;
+    int nf_ = 0;
+};
+
+// voronoicell_neighbor (src/cell.hh:470-560): adds the neighbour ID per face.
+class voronoicell_neighbor : public voronoicell {
+  public:
+    voronoicell_neighbor() {}
+    template <class C>
+    explicit voronoicell_neighbor(C &) {}
+    // one ID per face, ascending (the reference lists them in face order)
+    void neighbors(std::vector<int> &v) const { v = nb_; }
+
+  protected:
+    friend class container_gpu_base;
+    std::vector<int> nb_;
+};
+
+// Shared implementation of the four container classes.
+class container_gpu_base {
+  public:
+    container_gpu_base(const container_gpu_base &) = delete;
+    container_gpu_base &operator=(const container_gpu_base &) = delete;
+    ~container_gpu_base() {
+        if (h_) vgpu_container_destroy(h_);
+    }
+
+    // Precision of the engine: VGPU_MIXED (default) or VGPU_FP64.
+    void set_mode(int mode) {
+        mode_ = mode;
+        dirty_ = true;
+    }
+
+    // container::clear (src/container.cc:385-387)
+    void clear() {
+        ids_in_.clear();
+        xyzr_in_.clear();
+        gpu_detail::check(vgpu_clear(h_), "clear");
+        dirty_ = true;
+    }
+
+    // container::compute_all_cells (src/container.cc:438-453)
+    void compute_all_cells() {
+        flush();
+        gpu_detail::check(vgpu_compute(h_, mode_), "compute_all_cells");
+        int64_t n = 0;
+        gpu_detail::check(vgpu_num_cells(h_, &n), "compute_all_cells");
+        n_ = n;
+        ids_.resize(n);
+        pos_.resize(3 * n);
+        vol_.resize(n);
+        cen_.resize(3 * n);
+        nf_.resize(n);
+        nv_.resize(n);
+        mr2_.resize(n);
+        flags_.resize(n);
+        rad_.resize(n);
+        if (n > 0) {
+            gpu_detail::check(vgpu_get_cells(h_, ids_.data(), pos_.data(), vol_.data(), cen_.data(), nf_.data(),
+                                             nv_.data(), mr2_.data(), flags_.data()),
+                              "compute_all_cells");
+            gpu_detail::check(vgpu_get_radii(h_, rad_.data()), "compute_all_cells");
+        }
+        have_nb_ = false;
+        dirty_ = false;
+    }
+
+    // container::sum_cell_volumes (src/container.cc:459-465)
+    double sum_cell_volumes() {
+        ensure();
+        double s = 0;
+        gpu_detail::check(vgpu_sum_cell_volumes(h_, &s), "sum_cell_volumes");
+        return s;
+    }
+
+    // container_base::total_particles (src/container.hh:150-155)
+    int total_particles() {
+        ensure();
+        return (int)n_;
+    }
+
+    // compute_cell (src/container.hh:462-465): fills c with cell k of the loop
+    // and returns false if the cell was cut away entirely.
+    template <class c_loop>
+    bool compute_cell(voronoicell &c, c_loop &vl) {
+        ensure();
+        return fill(c, vl.index());
+    }
+    template <class c_loop>
+    bool compute_cell(voronoicell_neighbor &c, c_loop &vl) {
+        ensure();
+        ensure_neighbors();
+        if (!fill(c, vl.index())) return false;
+        const int64_t k = vl.index();
+        c.nb_.assign(nb_.begin() + off_[k], nb_.begin() + off_[k + 1]);
+        return true;
+    }
+
+    // container::print_custom (src/container.hh:434-451; fields
+    // src/cell.cc:2485-2558)
+    void print_custom(const char *format, FILE *fp = stdout) {
+        ensure();
+        if (contains_neighbor(format)) ensure_neighbors();
+        for (int64_t k = 0; k < n_; k++)
+            if (flags_[k] & VGPU_CELL_OK) output_custom(format, k, fp);
+    }
+    void print_custom(const char *format, const char *filename) {
+        FILE *fp = fopen(filename, "w");
+        if (!fp) voro_fatal_error("Unable to open file", VOROPP_FILE_ERROR);
+        print_custom(format, fp);
+        fclose(fp);
+    }
+
+    // Loop-order record access used by c_loop_all.
+    int64_t size() {
+        ensure();
+        return n_;
+    }
+    int pid_at(int64_t k) const { return ids_[k]; }
+    const double *pos_at(int64_t k) const { return &pos_[3 * k]; }
+    double radius_at(int64_t k) const { return poly_ ? rad_[k] : default_radius; }
+
+    vgpu_container *handle() { return h_; }
+
+  protected:
+    container_gpu_base(int kind, const double geom[6], const int grid[3], const int per[3])
+        : poly_(kind == VGPU_CONTAINER_POLY || kind == VGPU_CONTAINER_PERIODIC_POLY) {
+        gpu_detail::check(vgpu_container_create(&h_, kind, geom, grid, per), "container");
+    }
+
+    void stage(int n, double x, double y, double z, double r) {
+        ids_in_.push_back(n);
+        xyzr_in_.push_back(x);
+        xyzr_in_.push_back(y);
+        xyzr_in_.push_back(z);
+        xyzr_in_.push_back(r);
+        dirty_ = true;
+    }
+
+    // container::import (src/container.cc:333-376): "id x y z" (+ " r") per line
+    void import_stream(FILE *fp, bool with_r) {
+        int i, j;
+        double x, y, z, r = default_radius;
+        while ((j = with_r ? fscanf(fp, "%d %lg %lg %lg %lg", &i, &x, &y, &z, &r)
+                           : fscanf(fp, "%d %lg %lg %lg", &i, &x, &y, &z)) == (with_r ? 5 : 4))
+            stage(i, x, y, z, r);
+        if (j != EOF) voro_fatal_error("File import error", VOROPP_FILE_ERROR);
+    }
+    void import_file(const char *filename, bool with_r) {
+        FILE *fp = fopen(filename, "r");
+        if (!fp) voro_fatal_error("Unable to open file", VOROPP_FILE_ERROR);
+        import_stream(fp, with_r);
+        fclose(fp);
+    }
+
+  private:
+    vgpu_container *h_ = nullptr;
+    bool poly_;
+    int mode_ = VGPU_MIXED;
+    bool dirty_ = true, have_nb_ = false;
+    std::vector<int32_t> ids_in_;
+    std::vector<double> xyzr_in_;
+    int64_t n_ = 0;
+    std::vector<int32_t> ids_, nf_, nv_, flags_, nb_;
+    std::vector<double> pos_, vol_, cen_, mr2_, rad_;
+    std::vector<int64_t> off_;
+
+    void flush() {
+        if (!ids_in_.empty()) {
+            gpu_detail::check(vgpu_put(h_, (int64_t)ids_in_.size(), ids_in_.data(), xyzr_in_.data()), "put");
+            ids_in_.clear();
+            xyzr_in_.clear();
+        }
+    }
+    void ensure() {
+        if (dirty_) compute_all_cells();
+    }
+    void ensure_neighbors() {
+        if (have_nb_) return;
+        int64_t tot = 0;
+        gpu_detail::check(vgpu_num_neighbors(h_, &tot), "neighbors");
+        off_.assign(n_ + 1, 0);
+        nb_.resize(tot > 0 ? tot : 1);
+        gpu_detail::check(vgpu_get_neighbors(h_, off_.data(), nb_.data()), "neighbors");
+        nb_.resize(tot);
+        have_nb_ = true;
+    }
+    bool fill(voronoicell &c, int64_t k) {
+        c.p = nv_[k];
+        c.vol_ = vol_[k];
+        c.cen_[0] = cen_[3 * k];
+        c.cen_[1] = cen_[3 * k + 1];
+        c.cen_[2] = cen_[3 * k + 2];
+        c.nf_ = nf_[k];
+        c.mr2_ = mr2_[k];
+        return (flags_[k] & VGPU_CELL_OK) != 0;
+    }
+    static bool contains_neighbor(const char *format) {
+        for (const char *f = format; *f; f++)
+            if (f[0] == '%' && f[1] == 'n') return true;
+        return false;
+    }
+    void output_custom(const char *format, int64_t k, FILE *fp) {
+        const double x = pos_[3 * k], y = pos_[3 * k + 1], z = pos_[3 * k + 2];
+        const double *c = &cen_[3 * k];
+        for (const char *f = format; *f; f++) {
+            if (*f != '%') {
+                putc(*f, fp);
+                continue;
+            }
+            f++;
+            switch (*f) {
+                case 'i': fprintf(fp, "%d", ids_[k]); break;
+                case 'x': fprintf(fp, "%g", x); break;
+                case 'y': fprintf(fp, "%g", y); break;
+                case 'z': fprintf(fp, "%g", z); break;
+                case 'q': fprintf(fp, "%g %g %g", x, y, z); break;
+                case 'r': fprintf(fp, "%g", radius_at(k)); break;
+                case 'w': fprintf(fp, "%d", nv_[k]); break;
+                case 'o':
+                    for (int v = 0; v < nv_[k]; v++) fputs(v ? " 3" : "3", fp);
+                    break;
+                case 'm': fprintf(fp, "%g", mr2_[k]); break;
+                case 'g': fprintf(fp, "%d", 3 * nv_[k] / 2); break;
+                case 's': fprintf(fp, "%d", nf_[k]); break;
+                case 'n':
+                    for (int64_t q = off_[k]; q < off_[k + 1]; q++)
+                        fprintf(fp, q > off_[k] ? " %d" : "%d", nb_[q]);
+                    break;
+                case 'v': fprintf(fp, "%g", vol_[k]); break;
+                case 'c': fprintf(fp, "%g %g %g", c[0], c[1], c[2]); break;
+                case 'C': fprintf(fp, "%g %g %g", x + c[0], y + c[1], z + c[2]); break;
+                case 'p': case 'P': case 'E': case 'e': case 'F': case 'A': case 'a': case 'f': case 't': case 'l':
+                    voro_fatal_error("print_custom: this field needs the cell polytope, which the GPU engine "
+                                     "does not return", VOROPP_INTERNAL_ERROR);
+                    break;
+                case 0: f--; break;
+                default:
+                    putc('%', fp);
+                    putc(*f, fp);
+            }
+        }
+        fputs("\n", fp);
+    }
+};
+
+// container (src/container.hh:289-291)
+class container : public container_gpu_base {
+  public:
+    container(double ax_, double bx_, double ay_, double by_, double az_, double bz_, int nx_, int ny_, int nz_,
+              bool xperiodic_, bool yperiodic_, bool zperiodic_, int /*init_mem*/)
+        : container_gpu_base(VGPU_CONTAINER, gpu_detail::d6{{ax_, bx_, ay_, by_, az_, bz_}}.v,
+                             gpu_detail::i3{{nx_, ny_, nz_}}.v, gpu_detail::i3{{xperiodic_, yperiodic_, zperiodic_}}.v) {}
+    void put(int n, double x, double y, double z) { stage(n, x, y, z, default_radius); }
+    void import(FILE *fp = stdin) { import_stream(fp, false); }
+    void import(const char *filename) { import_file(filename, false); }
+};
+
+// container_poly (src/container.hh:511-513)
+class container_poly : public container_gpu_base {
+  public:
+    container_poly(double ax_, double bx_, double ay_, double by_, double az_, double bz_, int nx_, int ny_, int nz_,
+                   bool xperiodic_, bool yperiodic_, bool zperiodic_, int /*init_mem*/)
+        : container_gpu_base(VGPU_CONTAINER_POLY, gpu_detail::d6{{ax_, bx_, ay_, by_, az_, bz_}}.v,
+                             gpu_detail::i3{{nx_, ny_, nz_}}.v, gpu_detail::i3{{xperiodic_, yperiodic_, zperiodic_}}.v) {}
+    void put(int n, double x, double y, double z, double r) { stage(n, x, y, z, r); }
+    void import(FILE *fp = stdin) { import_stream(fp, true); }
+    void import(const char *filename) { import_file(filename, true); }
+};
+
+// container_periodic (src/container_prd.hh:213-216); rectangular boxes only
+// (bxy = bxz = byz = 0), anything else is VGPU_ERR_UNSUPPORTED.
+class container_periodic : public container_gpu_base {
+  public:
+    container_periodic(double bx_, double bxy_, double by_, double bxz_, double byz_, double bz_, int nx_, int ny_,
+                       int nz_, int /*init_mem*/)
+        : container_gpu_base(VGPU_CONTAINER_PERIODIC, gpu_detail::d6{{bx_, bxy_, by_, bxz_, byz_, bz_}}.v,
+                             gpu_detail::i3{{nx_, ny_, nz_}}.v, gpu_detail::i3{{1, 1, 1}}.v) {}
+    void put(int n, double x, double y, double z) { stage(n, x, y, z, default_radius); }
+    void import(FILE *fp = stdin) { import_stream(fp, false); }
+    void import(const char *filename) { import_file(filename, false); }
+};
+
+// container_periodic_poly (src/container_prd.hh:434-437)
+class container_periodic_poly : public container_gpu_base {
+  public:
+    container_periodic_poly(double bx_, double bxy_, double by_, double bxz_, double byz_, double bz_, int nx_,
+                            int ny_, int nz_, int /*init_mem*/)
+        : container_gpu_base(VGPU_CONTAINER_PERIODIC_POLY, gpu_detail::d6{{bx_, bxy_, by_, bxz_, byz_, bz_}}.v,
+                             gpu_detail::i3{{nx_, ny_, nz_}}.v, gpu_detail::i3{{1, 1, 1}}.v) {}
+    void put(int n, double x, double y, double z, double r) { stage(n, x, y, z, r); }
+    void import(FILE *fp = stdin) { import_stream(fp, true); }
+    void import(const char *filename) { import_file(filename, true); }
+};
+
+// c_loop_all (src/c_loops.hh:165-210) and c_loop_all_periodic (325-393): the
+// reference's loop order, which is the order of the engine's records.
+class c_loop_all {
+  public:
+    template <class C>
+    explicit c_loop_all(C &con) : con_(&con) {}
+    bool start() {
+        k_ = 0;
+        return con_->size() > 0;
+    }
+    bool inc() { return ++k_ < con_->size(); }
+    int pid() const { return con_->pid_at(k_); }
+    void pos(double &x, double &y, double &z) const {
+        const double *p = con_->pos_at(k_);
+        x = p[0];
+        y = p[1];
+        z = p[2];
+    }
+    void pos(int &pid_, double &x, double &y, double &z, double &r) const {
+        pid_ = pid();
+        pos(x, y, z);
+        r = con_->radius_at(k_);
+    }
+    double x() const { return con_->pos_at(k_)[0]; }
+    double y() const { return con_->pos_at(k_)[1]; }
+    double z() const { return con_->pos_at(k_)[2]; }
+    int64_t index() const { return k_; }
+
+  private:
+    container_gpu_base *con_;
+    int64_t k_ = 0;
+};
+typedef c_loop_all c_loop_all_periodic;
+
+}  // namespace voro
+
+#endif

@@ -129,6 +129,10 @@ int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
  *   flags    VGPU_CELL_* bits */
 int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen,
                    int32_t *nfaces, int32_t *nverts, double *maxr2, int32_t *flags);
+/* Stored radius of every cell's particle, in loop order (the r argument of
+ * put; what container_poly::print_custom prints for %r, src/container.hh:
+ * 660-671, reading p[ijk][4q+3]). */
+int vgpu_get_radii(vgpu_container *h, double *radii);
 /* Neighbour lists in CSR form: offsets[n+1] (int64) and ids[total].  Each
  * cell's list holds one ID per face, in ascending order (the reference's order,
  * voronoicell_neighbor::neighbors src/cell.cc:2660-2678, is an artefact of

@@ -166,6 +166,32 @@ class PortLib(_Lib):
         return CellRecords(ids[:m], pos[:3 * m].reshape(m, 3), vol[:m], cen[:3 * m].reshape(m, 3),
                            nf[:m], nv[:m], ok[:m], mrs[:m], nb[:nb_off[m]], nb_off[:m + 1], tests[:m])
 
+    def compute_selected(self, w, sel, nb_per_cell=40) -> CellRecords:
+        """Records of the cells at loop-order positions ``sel`` only."""
+        f = self.lib.port_compute_selected
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_int, _i64p,
+                      _i32p, _f64p, _f64p, _f64p, _i32p, _i32p, _i32p, _f64p, ctypes.c_long, _i32p, _i64p]
+        sel = np.ascontiguousarray(sel, dtype=np.int64)
+        m = len(sel)
+        cap = max(m, 1)
+        nb_cap = max(64, m * nb_per_cell)
+        while True:
+            ids = np.zeros(cap, np.int32); pos = np.zeros(3 * cap); vol = np.zeros(cap)
+            cen = np.zeros(3 * cap); nf = np.zeros(cap, np.int32); nv = np.zeros(cap, np.int32)
+            ok = np.zeros(cap, np.int32); mrs = np.zeros(cap)
+            nb = np.zeros(nb_cap, np.int32); nb_off = np.zeros(cap + 1, np.int64)
+            r = f(int(w["kind"]), np.asarray(w["geom"], np.float64), np.asarray(w["grid"], np.int32),
+                  np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), len(w["ids"]), w["ids"], w["xyzr"],
+                  m, sel, ids, pos, vol, cen, nf, nv, ok, mrs, nb_cap, nb, nb_off)
+            if r >= 0:
+                break
+            if r != -1:
+                raise ValueError(f"port_compute_selected failed ({r})")
+            nb_cap *= 2
+        return CellRecords(ids[:m], pos[:3 * m].reshape(m, 3), vol[:m], cen[:3 * m].reshape(m, 3),
+                           nf[:m], nv[:m], ok[:m], mrs[:m], nb[:nb_off[m]], nb_off[:m + 1])
+
     def time_cells(self, w, first=0, count=None, threads=1):
         """Seconds to compute cells [first, first+count) of the loop order with
         `threads` threads; returns (seconds, cells)."""

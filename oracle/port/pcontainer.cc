@@ -1052,6 +1052,48 @@ extern "C" {
 
 // Same records and layout as ref_compute_cells (oracle/ref_capi.cc), plus the
 // per-cell count of vertex-plane side tests when out_tests is not NULL.
+// Computes the cells at loop-order positions sel[0..m) and writes their
+// records at output rows 0..m; returns m, -1 if nb_cap is too small.
+static int record_cells(Container &con, const std::vector<int> &blk, const std::vector<int> &slot,
+                        const std::vector<int> &ci, const std::vector<int> &cj, const std::vector<int> &ck,
+                        const long *sel, int m, int *out_id, double *out_pos, double *out_vol, double *out_cen,
+                        int *out_nf, int *out_nv, int *out_ok, double *out_mrs, long nb_cap, int *out_nb,
+                        long *out_nb_off, long long *out_tests) {
+    Computer comp(con);
+    std::vector<int> v;
+    long used = 0;
+    for (int r = 0; r < m; r++) {
+        const long t = sel ? sel[r] : r;
+        int ijk = blk[t], q = slot[t];
+        out_id[r] = con.ids(ijk)[q];
+        out_pos[3 * r] = con.pp(ijk)[con.ps * q];
+        out_pos[3 * r + 1] = con.pp(ijk)[con.ps * q + 1];
+        out_pos[3 * r + 2] = con.pp(ijk)[con.ps * q + 2];
+        out_nb_off[r] = used;
+        uint64_t t0 = comp.c.side_tests;
+        bool ok = comp.compute_cell(ijk, q, ci[t], cj[t], ck[t]);
+        if (out_tests) out_tests[r] = (long long)(comp.c.side_tests - t0);
+        out_ok[r] = ok ? 1 : 0;
+        if (ok) {
+            out_vol[r] = comp.c.volume();
+            comp.c.centroid(out_cen[3 * r], out_cen[3 * r + 1], out_cen[3 * r + 2]);
+            out_nf[r] = comp.c.number_of_faces();
+            out_nv[r] = comp.c.p;
+            out_mrs[r] = comp.c.max_radius_squared();
+            comp.c.neighbors(v);
+            for (int x : v) {
+                if (used >= nb_cap) return -1;
+                out_nb[used++] = x;
+            }
+        } else {
+            out_vol[r] = 0; out_cen[3 * r] = out_cen[3 * r + 1] = out_cen[3 * r + 2] = 0;
+            out_nf[r] = 0; out_nv[r] = 0; out_mrs[r] = 0;
+        }
+    }
+    out_nb_off[m] = used;
+    return m;
+}
+
 int port_compute_cells(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
                        const double *xyzr, int cap, int *out_id, double *out_pos, double *out_vol, double *out_cen,
                        int *out_nf, int *out_nv, int *out_ok, double *out_mrs, long nb_cap, int *out_nb,
@@ -1062,38 +1104,25 @@ int port_compute_cells(int kind, const double *geom, const int *grid, const int 
     con.loop_order(blk, slot, ci, cj, ck);
     int m = (int)blk.size();
     if (m > cap) return -1;
-    Computer comp(con);
-    std::vector<int> v;
-    long used = 0;
-    for (int t = 0; t < m; t++) {
-        int ijk = blk[t], q = slot[t];
-        out_id[t] = con.ids(ijk)[q];
-        out_pos[3 * t] = con.pp(ijk)[con.ps * q];
-        out_pos[3 * t + 1] = con.pp(ijk)[con.ps * q + 1];
-        out_pos[3 * t + 2] = con.pp(ijk)[con.ps * q + 2];
-        out_nb_off[t] = used;
-        uint64_t t0 = comp.c.side_tests;
-        bool ok = comp.compute_cell(ijk, q, ci[t], cj[t], ck[t]);
-        if (out_tests) out_tests[t] = (long long)(comp.c.side_tests - t0);
-        out_ok[t] = ok ? 1 : 0;
-        if (ok) {
-            out_vol[t] = comp.c.volume();
-            comp.c.centroid(out_cen[3 * t], out_cen[3 * t + 1], out_cen[3 * t + 2]);
-            out_nf[t] = comp.c.number_of_faces();
-            out_nv[t] = comp.c.p;
-            out_mrs[t] = comp.c.max_radius_squared();
-            comp.c.neighbors(v);
-            for (int x : v) {
-                if (used >= nb_cap) return -1;
-                out_nb[used++] = x;
-            }
-        } else {
-            out_vol[t] = 0; out_cen[3 * t] = out_cen[3 * t + 1] = out_cen[3 * t + 2] = 0;
-            out_nf[t] = 0; out_nv[t] = 0; out_mrs[t] = 0;
-        }
-    }
-    out_nb_off[m] = used;
-    return m;
+    return record_cells(con, blk, slot, ci, cj, ck, nullptr, m, out_id, out_pos, out_vol, out_cen, out_nf, out_nv,
+                        out_ok, out_mrs, nb_cap, out_nb, out_nb_off, out_tests);
+}
+
+// The records of the cells at loop-order positions sel[0..nsel) only (a
+// sample of a container too large to compute whole on the CPU).  Returns
+// nsel, -1 if nb_cap is too small, -3 if a position is out of range.
+int port_compute_selected(int kind, const double *geom, const int *grid, const int *periodic, int n,
+                          const int *ids, const double *xyzr, int nsel, const long *sel, int *out_id,
+                          double *out_pos, double *out_vol, double *out_cen, int *out_nf, int *out_nv, int *out_ok,
+                          double *out_mrs, long nb_cap, int *out_nb, long *out_nb_off) {
+    Container con;
+    if (!build(con, kind, geom, grid, periodic, n, ids, xyzr)) return -2;
+    std::vector<int> blk, slot, ci, cj, ck;
+    con.loop_order(blk, slot, ci, cj, ck);
+    for (int r = 0; r < nsel; r++)
+        if (sel[r] < 0 || sel[r] >= (long)blk.size()) return -3;
+    return record_cells(con, blk, slot, ci, cj, ck, sel, nsel, out_id, out_pos, out_vol, out_cen, out_nf, out_nv,
+                        out_ok, out_mrs, nb_cap, out_nb, out_nb_off, nullptr);
 }
 
 // Times compute_cell over the cells [first, first+count) of the loop order

@@ -1,0 +1,120 @@
+"""The C++ drop-in header (include/voro_gb300.hh): a reference-style program
+(container / c_loop_all / voronoicell_neighbor / compute_cell / print_custom,
+as the reference's examples are written) compiles against it and, on a GPU,
+reproduces the reference's golden per-cell records and the Python API's
+print_custom output."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import voro_gb300 as vg
+from tests import _golden as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "shim_cells.cc")
+LIBDIR = os.path.dirname(vg.library_path())
+
+
+def _compile(tmp_path, extra=()):
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    vg.load_library()  # builds libvorogpu.so if needed
+    exe = str(tmp_path / "shim_cells")
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", f"-I{ROOT}/include", SRC,
+           f"-L{LIBDIR}", "-lvorogpu", f"-Wl,-rpath,{LIBDIR}", "-o", exe, *extra]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def _write_input(path, w):
+    g, gr, per = w["geom"], w["grid"], w["periodic"]
+    with open(path, "w") as f:
+        f.write(f"{w['kind']} " + " ".join(repr(float(v)) for v in g) + " " + " ".join(str(v) for v in gr) + " " +
+                " ".join(str(int(p)) for p in per) + f" {len(w['ids'])}\n")
+        for i, (x, y, z, r) in zip(w["ids"], w["xyzr"]):
+            f.write(f"{int(i)} {float(x)!r} {float(y)!r} {float(z)!r} {float(r)!r}\n")
+
+
+class _Parsed:
+    def __init__(self, path):
+        ids, ok, pos, vol, cen, nf, nv, mrs, nbs = [], [], [], [], [], [], [], [], []
+        self.sum = None
+        for line in open(path):
+            t = line.split()
+            if t[0] == "sum":
+                self.sum = float(t[1])
+                continue
+            ids.append(int(t[0]))
+            ok.append(int(t[1]))
+            pos.append([float(v) for v in t[2:5]])
+            if t[1] == "1":
+                vol.append(float(t[5])); cen.append([float(v) for v in t[6:9]])
+                nf.append(int(t[9])); nv.append(int(t[10])); mrs.append(float(t[11]))
+                nbs.append(np.sort(np.array([int(v) for v in t[12:]], np.int32)))
+            else:
+                vol.append(0.0); cen.append([0, 0, 0]); nf.append(0); nv.append(0); mrs.append(0.0)
+                nbs.append(np.zeros(0, np.int32))
+        self.ids = np.array(ids, np.int32)
+        self.ok = np.array(ok, bool)
+        self.pos = np.array(pos)
+        self.vol = np.array(vol)
+        self.cen = np.array(cen, float)
+        self.nf = np.array(nf, np.int32)
+        self.nv = np.array(nv, np.int32)
+        self.mrs = np.array(mrs)
+        self._nb = nbs
+
+    def neighbors(self, k):
+        return self._nb[k]
+
+
+def test_shim_compiles(tmp_path):
+    _compile(tmp_path)
+    _compile(tmp_path, ["-DVORO_GB300_THROW"])
+
+
+def test_shim_reports_errors_like_the_reference(tmp_path):
+    """Without a GPU the engine's status reaches the program as the
+    reference's fatal-error path: a 'voro++:' message and a VOROPP_* exit code."""
+    try:
+        if vg.device_count() > 0:
+            pytest.skip("a GPU is present: the no-device path cannot be exercised")
+    except vg.VoroError:
+        pass
+    exe = _compile(tmp_path)
+    w, _ = G.load("unit_cube_1000")
+    inp = tmp_path / "in.txt"
+    _write_input(inp, w)
+    r = subprocess.run([exe, str(inp), str(tmp_path / "out.txt")], capture_output=True, text=True)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    assert r.stderr.startswith("voro++: container:")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["unit_cube_1000", "periodic_2000", "radical_1200", "periodic_poly_800",
+                                  "sparse_dropped_40"])
+def test_shim_matches_reference_records(gpu, tmp_path, name):
+    exe = _compile(tmp_path)
+    w, z = G.load(name)
+    inp = tmp_path / "in.txt"
+    _write_input(inp, w)
+    out = tmp_path / "out.txt"
+    custom = tmp_path / "custom.txt"
+    fmt = "%i %q %r %v %s %w %g %m %c %C %n %% %"
+    r = subprocess.run([exe, str(inp), str(out), fmt, str(custom)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = _Parsed(out)
+    errs = G.compare_cells(got, z, 1e-10, 1e-10, label=f"shim/{name}")
+    assert not errs, "\n".join(errs)
+    m = got.ok
+    assert np.allclose(got.mrs[m], z["mrs"][m], rtol=1e-10, atol=0)
+    assert abs(got.sum - G.box_volume(w)) <= 1e-9 * G.box_volume(w)
+    # print_custom from C++ and from the Python mirror agree character for character
+    con = vg.from_workload(w, mode="mixed")
+    py = tmp_path / "custom_py.txt"
+    con.print_custom(fmt, str(py))
+    assert open(custom).read() == open(py).read()

@@ -1,0 +1,94 @@
+"""Full-size workloads (the bench configurations) checked by size-independent
+properties, plus bit-exact topology against the CPU port on a seeded sample:
+
+* Σ cell volumes = container volume;
+* neighbour relation symmetric with multiplicity (j lists i as often as i
+  lists j — periodic images included);
+* Euler's relation for simple polyhedra, V = 2F − 4 (every vertex the engine
+  produces has order 3);
+* MIXED and FP64 engines give the same topology (4M periodic box);
+* a seeded sample of cells matches the CPU port (which is bit-exact with the
+  reference) in face count, vertex count and neighbour multiset, with volume
+  and centroid within the engine's tolerance."""
+import numpy as np
+import pytest
+
+import oracle
+import voro_gb300 as vg
+from tests import _golden as G
+from voro_gb300 import workloads as W
+
+CASES = {
+    "unit_cube_100k": (lambda: W.unit_cube(), "fp64"),
+    "periodic_4m": (lambda: W.periodic_cube(), "mixed"),
+    "radical_2m": (lambda: W.radical_box(), "mixed"),
+    "fcc_jitter_1m": (lambda: W.fcc_jitter(), "mixed"),
+}
+TOL = {"fp64": 1e-12, "mixed": 1e-10}
+SAMPLE = 1500
+
+
+def _symmetric(res):
+    ids = res.ids.astype(np.int64)
+    owner = np.repeat(ids, np.diff(res.nb_off))
+    m = res.nb >= 0
+    a, b = owner[m], res.nb[m].astype(np.int64)
+    n = int(ids.max()) + 1
+    return np.array_equal(np.sort(a * n + b), np.sort(b * n + a))
+
+
+@pytest.fixture(scope="module")
+def port():
+    oracle.build_port()
+    return oracle.PortLib()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
+def test_full_size_invariants_and_sample_parity(gpu, port, name):
+    make, mode = CASES[name]
+    w = make()
+    con = vg.from_workload(w, mode=mode)
+    con.compute_all_cells()
+    st = con.stats()
+    assert st["failed_cells"] == 0
+    res = con.cells()
+    ok = res.ok
+    vbox = G.box_volume(w)
+    assert abs(con.sum_cell_volumes() - vbox) <= 1e-9 * vbox
+    assert np.array_equal(res.nv[ok], 2 * res.nf[ok] - 4), "Euler relation V = 2F - 4"
+    assert _symmetric(res), "neighbour relation not symmetric"
+
+    rng = np.random.default_rng(7)
+    sel = np.sort(rng.choice(len(res), size=min(SAMPLE, len(res)), replace=False))
+    ref = port.compute_selected(w, sel)
+    assert np.array_equal(res.ids[sel], ref.ids)
+    assert np.array_equal(res.pos[sel], ref.pos)
+    assert np.array_equal(ok[sel], ref.ok != 0)
+    m = ref.ok != 0
+    assert np.array_equal(res.nf[sel][m], ref.nf[m])
+    assert np.array_equal(res.nv[sel][m], ref.nv[m])
+    for r, k in enumerate(sel):
+        if m[r]:
+            assert np.array_equal(np.sort(res.neighbors(k)), np.sort(ref.neighbors(r))), f"cell {k}"
+    rel = np.abs(res.vol[sel][m] - ref.vol[m]) / ref.vol[m]
+    assert rel.max() <= TOL[mode]
+    scale = np.cbrt(ref.vol[m])[:, None]
+    assert (np.abs(res.cen[sel][m] - ref.cen[m]) / scale).max() <= TOL[mode]
+
+
+@pytest.mark.gpu
+def test_mixed_and_fp64_agree_on_the_4m_periodic_box(gpu):
+    w = W.periodic_cube()
+    a = vg.from_workload(w, mode="mixed")
+    b = vg.from_workload(w, mode="fp64")
+    ra, rb = a.cells(), b.cells()
+    assert np.array_equal(ra.nf, rb.nf)
+    assert np.array_equal(ra.nv, rb.nv)
+    assert np.array_equal(ra.nb_off, rb.nb_off)
+    assert np.array_equal(ra.nb, rb.nb)
+    assert (np.abs(ra.vol - rb.vol) / rb.vol).max() <= 1e-10
+    sa, sb = a.stats(), b.stats()
+    # the FP64 fallback rate of the mixed engine
+    assert sa["fp64_repairs"] <= 0.01 * sa["side_tests"]
+    assert sb["marginal_cells"] == 0

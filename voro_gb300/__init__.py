@@ -46,7 +46,7 @@ EXPORTED = [
     "vgpu_version", "vgpu_device_count", "vgpu_last_error", "vgpu_container_create", "vgpu_container_destroy",
     "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
-    "vgpu_set_tuning", "vgpu_phase_cycles",
+    "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
 ]
 
 
@@ -110,6 +110,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_device_results.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
+    lib.vgpu_get_radii.argtypes = [vp, vp]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -140,6 +141,7 @@ class CellResults:
         self.ids, self.pos, self.vol, self.cen = ids, pos, vol, cen
         self.nf, self.nv, self.maxr2, self.flags = nf, nv, maxr2, flags
         self.nb, self.nb_off = nb, nb_off
+        self.rad = None   # stored radii (put's r), filled by cells()
 
     def __len__(self):
         return len(self.ids)
@@ -285,6 +287,9 @@ class _ContainerBase:
         _check(self._lib.vgpu_get_cells(self._h, _ptr(ids), _ptr(pos), _ptr(vol), _ptr(cen), _ptr(nf),
                                         _ptr(nv), _ptr(mr2), _ptr(fl)))
         res = CellResults(ids, pos, vol, cen, nf, nv, mr2, fl)
+        rad = np.zeros(n)
+        _check(self._lib.vgpu_get_radii(self._h, _ptr(rad)))
+        res.rad = rad
         if neighbors:
             tot = ctypes.c_int64(0)
             _check(self._lib.vgpu_num_neighbors(self._h, ctypes.byref(tot)))
@@ -306,7 +311,8 @@ class _ContainerBase:
             fp = open(fp, "w")
             close = True
         try:
-            radius = (lambda k: float(self._radius_of(k)))
+            poly = self.kind in (KIND_CONTAINER_POLY, KIND_PERIODIC_POLY)
+            radius = (lambda k: float(res.rad[k]) if poly else 0.5)
             for k in range(len(res)):
                 if not res.ok[k]:
                     continue
@@ -314,9 +320,6 @@ class _ContainerBase:
         finally:
             if close:
                 fp.close()
-
-    def _radius_of(self, k):
-        return 0.5  # default_radius (src/config.hh:88); container_poly also prints it (container.hh:445)
 
 
 def _vec(v):

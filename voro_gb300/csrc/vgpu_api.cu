@@ -131,7 +131,7 @@ struct vgpu_container {
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, l32, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
-    DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, nb_off, nb_out, nb_tmp, sum_tmp;
+    DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
     bool computed = false;
     vgpu_stats stats{};
@@ -283,7 +283,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64, &h->l32, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
-                      &h->r_pos, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+                      &h->r_pos, &h->r_rad, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -456,6 +456,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     VG_CUDA(h->r_nb.ensure(nk * kMaxNb * 4));
     VG_CUDA(h->r_ids.ensure(nk * 4));
     VG_CUDA(h->r_pos.ensure(nk * 24));
+    VG_CUDA(h->r_rad.ensure(nk * 8));
     VG_CUDA(h->p64.ensure(nk * 32));
     VG_CUDA(h->l32.ensure(nk * 16));
     VG_CUDA(h->pid.ensure(nk * 4));
@@ -490,7 +491,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     VG_CUDA(launch_gather(g, nkept, uorder, gorder, gkey_sorted, h->rem.as<double4>(), d_ids,
                           h->outpos_in.as<int>(), h->p64.as<double4>(), h->l32.as<float4>(), h->pid.as<int>(),
                           h->outpos.as<int>(), h->gblock.as<int>(), h->bstart.as<int>(), nblocks,
-                          h->r_ids.as<int>(), h->r_pos.as<double>(), s));
+                          h->r_ids.as<int>(), h->r_pos.as<double>(), h->r_rad.as<double>(), s));
     cudaEventRecord(h->ev[1], s);
 
     // cell engine
@@ -599,6 +600,16 @@ int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, do
     if (maxr2) VG_CUDA(cudaMemcpyAsync(maxr2, h->r_mr2.p, n * 8, cudaMemcpyDeviceToHost, s));
     if (flags) VG_CUDA(cudaMemcpyAsync(flags, h->r_flags.p, n * 4, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
+    return VGPU_OK;
+}
+
+int vgpu_get_radii(vgpu_container *h, double *radii) {
+    if (!h || !radii) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    size_t n = (size_t)h->ncells;
+    if (n == 0) return VGPU_OK;
+    VG_CUDA(cudaMemcpyAsync(radii, h->r_rad.p, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    VG_CUDA(cudaStreamSynchronize(h->stream));
     return VGPU_OK;
 }
 

@@ -76,7 +76,7 @@ __global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsi
 }
 
 __global__ void loop_order_kernel(const int *uorder, int nkept, const int *ids_in, const double4 *rem,
-                                  int *outpos_by_input, int *res_ids, double *res_pos) {
+                                  int *outpos_by_input, int *res_ids, double *res_pos, double *res_rad) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nkept) return;
     int i = uorder[m];
@@ -86,6 +86,7 @@ __global__ void loop_order_kernel(const int *uorder, int nkept, const int *ids_i
     res_pos[3 * m] = p.x;
     res_pos[3 * m + 1] = p.y;
     res_pos[3 * m + 2] = p.z;
+    res_rad[m] = p.w;
 }
 
 __global__ void gather_kernel(Geometry g, int nkept, const int *gorder, const unsigned *gkey_sorted,
@@ -140,9 +141,10 @@ cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rma
     int nub = bp.g.un[0] * bp.g.un[1] * bp.g.un[2];
     int nblocks = bp.g.gn[0] * bp.g.gn[1] * bp.g.gn[2];
     int threads = 256, blocks = (bp.n + threads - 1) / threads;
-    if (blocks > 0)
+    if (blocks > 0) {
         remap_kernel<<<blocks, threads, 0, s>>>(bp, nub, nblocks, kept, rmax_bits);
         note_launch();
+    }
     return cudaGetLastError();
 }
 
@@ -150,7 +152,7 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
                           int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
-                          cudaStream_t s) {
+                          double *res_rad, cudaStream_t s) {
     int threads = 256;
     if (nkept == 0) {
         empty_bstart_kernel<<<(nblocks + 1 + threads - 1) / threads, threads, 0, s>>>(bstart, nblocks);
@@ -158,7 +160,8 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
         return cudaGetLastError();
     }
     int blocks = (nkept + threads - 1) / threads;
-    loop_order_kernel<<<blocks, threads, 0, s>>>(uorder, nkept, ids_in, rem, outpos_by_input, res_ids, res_pos);
+    loop_order_kernel<<<blocks, threads, 0, s>>>(uorder, nkept, ids_in, rem, outpos_by_input, res_ids, res_pos,
+                                                  res_rad);
     note_launch();
     gather_kernel<<<blocks, threads, 0, s>>>(g, nkept, gorder, gkey_sorted, rem, ids_in, outpos_by_input, p64,
                                              l32, pid, outpos, gblock, bstart, nblocks);

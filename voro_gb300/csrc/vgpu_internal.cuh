@@ -117,7 +117,7 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
                           int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
-                          cudaStream_t s);
+                          double *res_rad, cudaStream_t s);
 cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,
                                    int nkept, int *dup_flag, cudaStream_t s);
 

@@ -155,6 +155,19 @@ int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t
  * CTA (0 = default).  Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
 
+/* Σ of n device-resident cell volumes (e.g. vgpu_device_results' dev_vol;
+ * deleted cells hold volume 0) written to dev_out (one double, device memory),
+ * launched on the caller's stream (a cudaStream_t; NULL = legacy default
+ * stream) and not waited for.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory — it calls no allocator and
+ * keeps its partial sums in a fixed 64 KB static device array, so n is limited
+ * to 33,554,432 (larger n: VGPU_ERR_ARG).  The first call on each device, with
+ * that device current, does a one-time set-up (the scratch address lookup);
+ * make it before any stream capture.  Nothing has to be zeroed beforehand.
+ * Calls that overlap on one device share the scratch and race: serialise them.
+ * The summation order is fixed, so repeated calls give identical results. */
+int vgpu_sum_volumes_noalloc(const double *dev_vol, int64_t n, double *dev_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

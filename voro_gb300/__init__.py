@@ -47,6 +47,7 @@ EXPORTED = [
     "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
+    "vgpu_sum_volumes_noalloc",
 ]
 
 
@@ -111,6 +112,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
+    lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
             getattr(lib, name).restype = ctypes.c_int

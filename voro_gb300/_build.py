@@ -15,7 +15,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libvorogpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu"]
+SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu", "vgpu_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "1444"]
 

@@ -36,6 +36,21 @@ int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+// Error reporting for the library's other translation units.
+int vgpu::report_error(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+namespace {
+
 #define VG_CUDA(expr)                                                                        \
     do {                                                                                     \
         cudaError_t _e = (expr);                                                             \

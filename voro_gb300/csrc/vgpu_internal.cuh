@@ -92,6 +92,8 @@ struct CellParams {
 // launch accounting (vgpu_api.cu)
 void note_launch(int n = 1);
 long long launch_count();
+// sets the message vgpu_last_error returns; returns code
+int report_error(int code, const char *fmt, ...);
 
 // vgpu_sort.cu
 cudaError_t exclusive_scan_int(const int *in, int *out, int n, int *tmp, size_t tmp_ints, cudaStream_t s);

@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default="periodic", choices=["periodic", "batched"],
+                    help="periodic: the 4M periodic box (the headline); batched: many containers")
+    ap.add_argument("--count", type=int, default=4096, help="batched: number of containers")
+    ap.add_argument("--nmax", type=int, default=100_000, help="batched: largest container")
     return ap.parse_args()
 
 
@@ -158,6 +162,20 @@ def cpu_baseline(w, seconds, threads=None):
     return {"value": m / t, "unit": "cells/s", "cores": threads, "kind": "port",
             "sample": f"first {m} cells (loop order) of the {n_total}-particle container, "
                       f"{threads} threads, {t:.2f} s"}, None
+
+
+def reference_tests_per_cell(w, cells=20000):
+    """T_cell of the flop model: the reference algorithm's vertex-plane side
+    tests (m_calc calls, src/cell.cc:2050-2059) per cell, counted by the CPU
+    port on the first cells of the same container."""
+    try:
+        from oracle import PortLib, build_port
+        build_port()
+        port = PortLib()
+        _, m = port.time_cells(w, first=0, count=min(cells, len(w["ids"])), threads=os.cpu_count() or 1)
+        return port.last_side_tests / max(m, 1), m
+    except Exception:  # noqa: BLE001
+        return None, 0
 
 
 def run_reference(args):
@@ -303,7 +321,9 @@ def run_ours(args):
     prof = load_profile_summary() or {}
     traffic = prof.get("dram_bytes_per_launch_scaled")
     side_tests_per_cell = st["side_tests"] / max(st["cells"], 1)
-    flops_cell = 6.0 * side_tests_per_cell + 40.0 * 27.0
+    t_ref, t_cells = reference_tests_per_cell(w)
+    v_mean = float(np.mean(con.cells(neighbors=False).nv))
+    flops_cell = 6.0 * (t_ref if t_ref is not None else side_tests_per_cell) + 40.0 * v_mean
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     line = {
         "metric": "cells/s (Voronoi cells computed per second)",
@@ -320,7 +340,10 @@ def run_ours(args):
                      "note": "issue/latency-bound kernel; algorithmic bytes 136 B/cell",
                      "pipe": {"unit": "TFLOP/s", "achieved": flops_cell * n / (kms / 1000.0) / 1e12,
                               "peak": fp32_peak, "peak_kind": "nominal FP32",
-                              "flops_per_cell": flops_cell}},
+                              "flops_per_cell": flops_cell,
+                              "model": "F_cell = 6 T_cell + 40 V_cell; T_cell = reference side tests per cell "
+                                       f"({t_ref if t_ref is not None else float('nan'):.1f}, CPU port on "
+                                       f"{t_cells} cells), V_cell = mean vertices ({v_mean:.2f})"}},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks,
@@ -341,10 +364,75 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Many containers (log-uniform sizes, mixed kinds): one vgpu_batch_compute
+    (binning per container + one persistent launch for every cell) against a
+    loop of per-container computes on the same containers."""
+    import torch
+    torch.cuda.set_device(0)
+    import voro_gb300 as vg
+    from voro_gb300 import workloads as W
+    ws = W.batched(count=args.count, nmin=64, nmax=args.nmax, seed=1005)
+    total = sum(len(w["ids"]) for w in ws)
+    cons = [vg.from_workload(w, mode=args.mode) for w in ws]
+    b = vg.batch(cons)
+    for _ in range(args.warmup):
+        b.compute_all_cells(mode=args.mode)
+    wall, kern, binms = [], [], []
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.compute_all_cells(mode=args.mode)
+            wall.append(time.perf_counter() - t0)
+            st = b.stats()
+            kern.append(st["kernel_ms"])
+            binms.append(st["bin_ms"])
+    st = b.stats()
+    # the same containers one compute at a time
+    loop = []
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in cons:
+            c.compute_all_cells(mode=args.mode)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            loop.append(time.perf_counter() - t0)
+    def box_volume(w):
+        g = w["geom"]
+        return (g[1] - g[0]) * (g[3] - g[2]) * (g[5] - g[4]) if w["kind"] < 2 else g[0] * g[2] * g[5]
+
+    vol_ok = all(abs(c.sum_cell_volumes() - box_volume(w)) <= 1e-9 * box_volume(w) for c, w in zip(cons, ws))
+    wt = statistics.mean(wall)
+    line = {
+        "metric": "cells/s (Voronoi cells computed per second), batched containers",
+        "value": total / wt, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * wt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.mode == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": f"{args.count} containers, N log-uniform [64, {args.nmax}] (seed 1005), half "
+                               f"container_periodic, a quarter radical; {total} particles",
+                   "timing": "host wall clock around vgpu_batch_compute (binning + one persistent launch)"},
+        "kernel_only_cells_per_s": total / (statistics.mean(kern) / 1000.0),
+        "batched_kernel_ms": statistics.mean(kern), "batched_bin_ms": statistics.mean(binms),
+        "per_container_loop": {"value": total / statistics.mean(loop), "unit": "cells/s",
+                               "ms_per_step": 1000.0 * statistics.mean(loop)},
+        "speedup_vs_loop": statistics.mean(loop) / wt,
+        "gpu_launches": int(st["kernel_launches"]),
+        "clocks": clk.summary(),
+        "engine": {"cells": st["cells"], "failed_cells": st["failed_cells"], "overflow_reruns": st["overflow_reruns"],
+                   "marginal_cells": st["marginal_cells"], "sum_volume_ok": bool(vol_ok)},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

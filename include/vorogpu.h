@@ -48,6 +48,12 @@ extern "C" {
                                  (|plane value| <= tol): the reference would merge
                                  vertices there; topology may differ from it */
 #define VGPU_CELL_REPAIRED 4  /* at least one FP32 test was redone in FP64 */
+#define VGPU_CELL_FAILED 8    /* the cell exceeded every engine capacity; bits 8-11 give why: */
+#define VGPU_FAIL_PLANES 1    /*   more than 64 plane slots in use */
+#define VGPU_FAIL_ADJACENCY 2 /*   inconsistent vertex adjacency after a cut */
+#define VGPU_FAIL_VERTICES 3  /*   more vertices than the engine's slots */
+#define VGPU_FAIL_SEARCH 4    /*   the neighbour search did not terminate */
+#define VGPU_FAIL_RECORDS 5   /*   the polytope record store was full */
 
 typedef struct vgpu_container vgpu_container;
 
@@ -154,6 +160,23 @@ int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t
 /* Engine tuning: target particles per engine block (0 = default) and warps per
  * CTA (0 = default).  Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
+
+/* ---- batches: many containers computed by one persistent launch ----
+ * The reference computes containers one at a time (compute_all_cells per
+ * container, src/container.cc:438-453).  A batch bins every member container
+ * (each on its own stream) and then runs all their cells in one launch of the
+ * cell engine with a single device work queue, so thousands of small and
+ * large containers share the GPU.  Results land in each member container and
+ * are read with the usual getters.  Containers stay owned by the caller and
+ * must outlive the batch's computes. */
+typedef struct vgpu_batch vgpu_batch;
+int vgpu_batch_create(vgpu_batch **out);
+int vgpu_batch_add(vgpu_batch *b, vgpu_container *h);
+int vgpu_batch_compute(vgpu_batch *b, int mode);
+/* Sums over the members; kernel_ms = the batched launch(es), bin_ms = the
+ * members' binning (host wall time), step_ms = the whole call (wall time). */
+int vgpu_batch_get_stats(vgpu_batch *b, vgpu_stats *out);
+int vgpu_batch_destroy(vgpu_batch *b);
 
 /* Σ of n device-resident cell volumes (e.g. vgpu_device_results' dev_vol;
  * deleted cells hold volume 0) written to dev_out (one double, device memory),

@@ -1,0 +1,64 @@
+"""Batched containers (vgpu_batch_*): many containers computed by one
+persistent launch give exactly the per-container results."""
+import numpy as np
+import pytest
+
+import voro_gb300 as vg
+from tests import _golden as G
+from voro_gb300 import workloads as W
+
+TOL = {"fp64": (1e-12, 1e-12), "mixed": (1e-10, 1e-10)}
+
+
+def test_batch_needs_a_device():
+    try:
+        if vg.device_count() > 0:
+            pytest.skip("a GPU is present")
+    except vg.VoroError:
+        pass
+    with pytest.raises(vg.VoroError):
+        vg.batch()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_batch_of_golden_fixtures_matches_reference(gpu, mode):
+    names = G.names()
+    cons, refs = [], []
+    for name in names:
+        w, z = G.load(name)
+        cons.append(vg.from_workload(w, mode=mode))
+        refs.append((w, z))
+    b = vg.batch(cons)
+    b.compute_all_cells(mode=mode)
+    st = b.stats()
+    assert st["cells"] == sum(len(z["ids"]) for _, z in refs)
+    assert st["failed_cells"] == 0
+    for name, con, (w, z) in zip(names, cons, refs):
+        errs = G.compare_cells(con.cells(), z, *TOL[mode], label=f"batch/{name}/{mode}")
+        assert not errs, "\n".join(errs)
+        assert abs(con.sum_cell_volumes() - G.box_volume(w)) <= 1e-9 * G.box_volume(w)
+
+
+@pytest.mark.gpu
+def test_batch_equals_one_container_at_a_time(gpu):
+    ws = W.batched(count=48, nmin=64, nmax=20000, seed=77)
+    single = []
+    for w in ws:
+        c = vg.from_workload(w, mode="mixed")
+        c.compute_all_cells()
+        single.append(c.cells())
+    cons = [vg.from_workload(w, mode="mixed") for w in ws]
+    b = vg.batch(cons)
+    b.compute_all_cells(mode="mixed")
+    for k, (c, a) in enumerate(zip(cons, single)):
+        r = c.cells()
+        assert np.array_equal(r.ids, a.ids), k
+        assert np.array_equal(r.flags, a.flags), k
+        assert np.array_equal(r.vol, a.vol), k
+        assert np.array_equal(r.cen, a.cen), k
+        assert np.array_equal(r.nb_off, a.nb_off), k
+        assert np.array_equal(r.nb, a.nb), k
+    # a second compute of the same batch gives the same again
+    b.compute_all_cells(mode="mixed")
+    assert np.array_equal(cons[3].cells().vol, single[3].vol)

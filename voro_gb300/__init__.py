@@ -28,6 +28,7 @@ VGPU_MIXED = 1
 VGPU_CELL_OK = 1
 VGPU_CELL_MARGINAL = 2
 VGPU_CELL_REPAIRED = 4
+VGPU_CELL_FAILED = 8   # bits 8-11: reason (1 planes, 2 adjacency, 3 vertices, 4 search)
 
 KIND_CONTAINER = 0
 KIND_CONTAINER_POLY = 1
@@ -47,7 +48,8 @@ EXPORTED = [
     "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
-    "vgpu_sum_volumes_noalloc",
+    "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
+    "vgpu_batch_get_stats", "vgpu_batch_destroy",
 ]
 
 
@@ -113,6 +115,11 @@ def load_library(build_if_missing=True):
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
     lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
+    lib.vgpu_batch_create.argtypes = [ctypes.POINTER(vp)]
+    lib.vgpu_batch_add.argtypes = [vp, vp]
+    lib.vgpu_batch_compute.argtypes = [vp, ctypes.c_int]
+    lib.vgpu_batch_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    lib.vgpu_batch_destroy.argtypes = [vp]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -426,6 +433,45 @@ class container_periodic_poly(_ContainerBase):
 
     def put(self, n, x, y, z, r):
         self._put(n, x, y, z, r)
+
+
+class batch:
+    """Many containers computed together by one persistent launch of the cell
+    engine (vgpu_batch_*).  Members keep their own results (``cells()``,
+    ``sum_cell_volumes()``, ``print_custom``)."""
+
+    def __init__(self, containers=()):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        _check(self._lib.vgpu_batch_create(ctypes.byref(self._h)))
+        self.members = []
+        for c in containers:
+            self.add(c)
+
+    def add(self, con):
+        con._flush_pending()
+        _check(self._lib.vgpu_batch_add(self._h, con._h))
+        self.members.append(con)
+
+    def compute_all_cells(self, mode="mixed"):
+        for c in self.members:
+            c._flush_pending()
+        _check(self._lib.vgpu_batch_compute(self._h, VGPU_FP64 if mode == "fp64" else VGPU_MIXED))
+        for c in self.members:
+            c._dirty = False
+
+    def stats(self):
+        st = Stats()
+        _check(self._lib.vgpu_batch_get_stats(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._lib.vgpu_batch_destroy(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
 
 
 def from_workload(w, mode="mixed"):

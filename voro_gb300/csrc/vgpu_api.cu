@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -126,6 +127,11 @@ const OffsetTable &offset_table() {
 
 }  // namespace
 
+// Polytope record store of the split finish, words per cell (the mean record
+// of a uniform periodic box is about 215 words; a cell that finds the store
+// full is redone by the larger engine, which finishes inline).
+constexpr unsigned long long kRecWordsPerCell = 256;
+
 struct vgpu_container {
     Geometry g;
     int device = 0;
@@ -146,8 +152,11 @@ struct vgpu_container {
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, l32, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
+    DevBuf rec, rec_off;
     DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
+    int nkept = 0;              // cells of the compute in progress
+    long long launches0 = 0;    // launch counter at its start
     bool computed = false;
     vgpu_stats stats{};
     double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -298,7 +307,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64, &h->l32, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
-                      &h->r_pos, &h->r_rad, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+                      &h->r_pos, &h->r_rad, &h->rec, &h->rec_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -377,19 +386,25 @@ int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per
     return VGPU_OK;
 }
 
-int vgpu_compute(vgpu_container *h, int mode) {
-    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+}  // extern "C"
+
+namespace {
+
+// Everything of a compute before the cell kernel: remap, loop-order sort,
+// duplicate check, engine-order sort and gather; fills cp for the engine.
+// Leaves the gather queued on the handle's stream (event ev[1] after it).
+int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
     cudaStream_t s = h->stream;
     const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
     const int n = (int)n64;
     Geometry &g = h->g;
     memset(&h->stats, 0, sizeof(h->stats));
+    h->computed = false;
     choose_engine_grid(g, n64, h->target_density);
     const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
     const int nub = g.un[0] * g.un[1] * g.un[2];
     const size_t nn = (size_t)std::max(n, 1);
-
     // inputs
     const int32_t *d_ids;
     const double *d_xyzr;
@@ -421,7 +436,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     VG_CUDA(h->counters.ensure(sizeof(Counters)));
     VG_CUDA(h->counters2.ensure(sizeof(Counters)));
 
-    const long long launches0 = launch_count();
+    h->launches0 = launch_count();
     cudaEventRecord(h->ev[0], s);
     VG_CUDA(cudaMemsetAsync(h->kept.p, 0, 64, s));
     BinParams bp;
@@ -509,13 +524,12 @@ int vgpu_compute(vgpu_container *h, int mode) {
                           h->r_ids.as<int>(), h->r_pos.as<double>(), h->r_rad.as<double>(), s));
     cudaEventRecord(h->ev[1], s);
 
-    // cell engine
+    // cell engine parameters
     const OffsetTable &ot = offset_table();
     VG_CUDA(h->offsets.ensure(ot.codes.size() * 4));
     VG_CUDA(cudaMemcpyAsync(h->offsets.p, ot.codes.data(), ot.codes.size() * 4, cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemsetAsync(h->counters.p, 0, sizeof(Counters), s));
     VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, sizeof(Counters), s));
-    CellParams cp;
     memset(&cp, 0, sizeof(cp));
     cp.g = g;
     cp.a.p64 = h->p64.as<double4>();
@@ -541,8 +555,61 @@ int vgpu_compute(vgpu_container *h, int mode) {
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
     box_tables(cp.box_tri, cp.box_adj);
+    h->nkept = nkept;
+    return VGPU_OK;
+}
+
+// Counters of the last compute into the handle's stats; marks it computed.
+int finish_compute(vgpu_container *h, const Counters &c1, const Counters &c2, float cell_ms) {
+    float bin_ms = 0, step_ms = 0;
+    cudaEventElapsedTime(&bin_ms, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&step_ms, h->ev[0], h->ev[3]);
+    h->ncells = h->nkept;
+    h->stats.cells = h->nkept;
+    h->stats.deleted = (int64_t)(c1.deleted + c2.deleted);
+    h->stats.marginal_cells = (int64_t)(c1.marginal + c2.marginal);
+    h->stats.side_tests = (int64_t)(c1.side_tests + c2.side_tests);
+    h->stats.fp64_repairs = (int64_t)(c1.fp64_repairs + c2.fp64_repairs);
+    h->stats.planes_tested = (int64_t)(c1.planes_tested + c2.planes_tested);
+    h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
+    h->stats.overflow_reruns = (int64_t)c1.overflow;
+    h->stats.failed_cells = (int64_t)(c2.overflow + c1.failed);
+    for (int i = 0; i < 8; i++) h->phase[i] = (double)(c1.phase_cycles[i] + c2.phase_cycles[i]);
+    h->stats.kernel_ms = cell_ms;
+    h->stats.bin_ms = bin_ms;
+    h->stats.step_ms = step_ms;
+    h->stats.kernel_launches = launch_count() - h->launches0;
+    h->computed = true;
+    if (h->stats.failed_cells > 0)
+        return fail(VGPU_ERR_CAPACITY, "%lld cells exceeded the engine capacity", (long long)h->stats.failed_cells);
+    return VGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgpu_compute(vgpu_container *h, int mode) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    CellParams cp;
+    int rc = prepare_cells(h, mode, cp);
+    if (rc != VGPU_OK) return rc;
+    cudaStream_t s = h->stream;
+    if (mode == VGPU_MIXED && h->nkept > 0) {
+        // split finish: the clipping kernel writes polytope records, the finish kernel reduces them
+        const unsigned long long cap = std::min<unsigned long long>(
+            (unsigned long long)h->nkept * kRecWordsPerCell + (1u << 20), 0xfffffff0ull);
+        VG_CUDA(h->rec.ensure(cap * 4));
+        VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 4));
+        VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 4, s));
+        cp.rec = h->rec.as<unsigned>();
+        cp.rec_cap = cap;
+        cp.rec_used = &h->counters.as<Counters>()->rec_used;
+        cp.rec_off = h->rec_off.as<unsigned>();
+    }
     cudaEventRecord(h->ev[2], s);
     VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
+    VG_CUDA(launch_finish(cp, h->sms, s));
     Counters c1;
     VG_CUDA(cudaMemcpyAsync(&c1, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
@@ -554,36 +621,16 @@ int vgpu_compute(vgpu_container *h, int mode) {
         cp2.ncells = (int)c1.overflow;
         cp2.cell_list = h->ovf_list.as<int>();
         cp2.overflow_list = nullptr;
+        cp2.rec = nullptr;   // the larger engine finishes its cells inline
         VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s));
         VG_CUDA(cudaMemcpyAsync(&c2, h->counters2.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     }
     cudaEventRecord(h->ev[3], s);
     VG_CUDA(cudaStreamSynchronize(s));
     VG_CUDA(cudaGetLastError());
-    float bin_ms = 0, cell_ms = 0, step_ms = 0;
-    cudaEventElapsedTime(&bin_ms, h->ev[0], h->ev[1]);
+    float cell_ms = 0;
     cudaEventElapsedTime(&cell_ms, h->ev[2], h->ev[3]);
-    cudaEventElapsedTime(&step_ms, h->ev[0], h->ev[3]);
-
-    h->ncells = nkept;
-    h->stats.cells = nkept;
-    h->stats.deleted = (int64_t)(c1.deleted + c2.deleted);
-    h->stats.marginal_cells = (int64_t)(c1.marginal + c2.marginal);
-    h->stats.side_tests = (int64_t)(c1.side_tests + c2.side_tests);
-    h->stats.fp64_repairs = (int64_t)(c1.fp64_repairs + c2.fp64_repairs);
-    h->stats.planes_tested = (int64_t)(c1.planes_tested + c2.planes_tested);
-    h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
-    h->stats.overflow_reruns = (int64_t)c1.overflow;
-    h->stats.failed_cells = (int64_t)c2.overflow;
-    for (int i = 0; i < 8; i++) h->phase[i] = (double)(c1.phase_cycles[i] + c2.phase_cycles[i]);
-    h->stats.kernel_ms = cell_ms;
-    h->stats.bin_ms = bin_ms;
-    h->stats.step_ms = step_ms;
-    h->stats.kernel_launches = launch_count() - launches0;
-    h->computed = true;
-    if (c2.overflow > 0)
-        return fail(VGPU_ERR_CAPACITY, "%llu cells exceeded the engine capacity", (unsigned long long)c2.overflow);
-    return VGPU_OK;
+    return finish_compute(h, c1, c2, cell_ms);
 }
 
 int vgpu_get_stats(vgpu_container *h, vgpu_stats *out) {
@@ -702,6 +749,161 @@ int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t
     if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
     if (dev_vol) *dev_vol = h->r_vol.as<double>();
     if (dev_nfaces) *dev_nfaces = h->r_nf.as<int32_t>();
+    return VGPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- batches
+
+struct vgpu_batch {
+    std::vector<vgpu_container *> members;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[2];
+    DevBuf cps, starts, counters, work, ovf_list;
+    vgpu_stats stats{};
+};
+
+extern "C" {
+
+int vgpu_batch_create(vgpu_batch **out) {
+    if (!out) return fail(VGPU_ERR_ARG, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(VGPU_ERR_NO_DEVICE, "no CUDA device");
+    vgpu_batch *b = new vgpu_batch();
+    VG_CUDA(cudaGetDevice(&b->device));
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        return fail(VGPU_ERR_CUDA, "stream creation failed");
+    }
+    for (int i = 0; i < 2; i++) cudaEventCreate(&b->ev[i]);
+    *out = b;
+    return VGPU_OK;
+}
+
+int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
+    if (!b || !h) return fail(VGPU_ERR_ARG, "null argument");
+    if (h->device != b->device) return fail(VGPU_ERR_ARG, "container and batch are on different devices");
+    b->members.push_back(h);
+    return VGPU_OK;
+}
+
+int vgpu_batch_destroy(vgpu_batch *b) {
+    if (!b) return VGPU_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list};
+    for (DevBuf *d : bufs) d->release();
+    for (int i = 0; i < 2; i++) cudaEventDestroy(b->ev[i]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return VGPU_OK;
+}
+
+int vgpu_batch_compute(vgpu_batch *b, int mode) {
+    if (!b) return fail(VGPU_ERR_ARG, "null handle");
+    if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    const auto t0 = std::chrono::steady_clock::now();
+    memset(&b->stats, 0, sizeof(b->stats));
+    const long long launches0 = launch_count();
+    const int nc = (int)b->members.size();
+    if (nc == 0) return VGPU_OK;
+    cudaStream_t s = b->stream;
+    VG_CUDA(b->counters.ensure((size_t)nc * sizeof(Counters)));
+    VG_CUDA(cudaMemsetAsync(b->counters.p, 0, (size_t)nc * sizeof(Counters), s));
+    // binning of every container on its own stream; the batch stream waits for each gather
+    std::vector<CellParams> cps(nc);
+    std::vector<long long> starts(nc + 1, 0);
+    for (int i = 0; i < nc; i++) {
+        vgpu_container *h = b->members[i];
+        memset(&cps[i], 0, sizeof(CellParams));
+        int rc = prepare_cells(h, mode, cps[i]);
+        if (rc != VGPU_OK) return rc;
+        cps[i].cnt = b->counters.as<Counters>() + i;
+        cps[i].cell_list = nullptr;
+        cps[i].overflow_list = nullptr;
+        starts[i + 1] = starts[i] + h->nkept;
+        cudaEventRecord(h->ev[2], h->stream);   // after the gather and the offsets upload
+        VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
+    }
+    const long long total = starts[nc];
+    const auto t1 = std::chrono::steady_clock::now();
+    VG_CUDA(b->cps.ensure((size_t)nc * sizeof(CellParams)));
+    VG_CUDA(b->starts.ensure((size_t)(nc + 1) * 8));
+    VG_CUDA(b->work.ensure(64));
+    VG_CUDA(b->ovf_list.ensure((size_t)std::max<long long>(total, 1) * 8));
+    const OffsetTable &ot = offset_table();
+    VG_CUDA(cudaMemcpyAsync(b->cps.p, cps.data(), (size_t)nc * sizeof(CellParams), cudaMemcpyHostToDevice, s));
+    VG_CUDA(cudaMemcpyAsync(b->starts.p, starts.data(), (size_t)(nc + 1) * 8, cudaMemcpyHostToDevice, s));
+    VG_CUDA(cudaMemsetAsync(b->work.p, 0, 64, s));
+    BatchParams bp;
+    memset(&bp, 0, sizeof(bp));
+    bp.cps = b->cps.as<CellParams>();
+    bp.cell_start = b->starts.as<long long>();
+    bp.ncont = nc;
+    bp.ncells = total;
+    bp.cell_list = nullptr;
+    bp.overflow_list = b->ovf_list.as<long long>();
+    unsigned long long *wk = b->work.as<unsigned long long>();
+    bp.work = wk;
+    bp.overflow_count = wk + 1;
+    bp.offsets = cps[0].offsets;   // the same table for every container
+    bp.noffsets = (int)ot.codes.size();
+    cudaEventRecord(b->ev[0], s);
+    VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
+    unsigned long long novf = 0;
+    VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    if (novf > 0) {
+        BatchParams bp2 = bp;
+        bp2.ncells = (long long)novf;
+        bp2.cell_list = b->ovf_list.as<long long>();
+        bp2.overflow_list = nullptr;
+        bp2.work = wk + 2;
+        VG_CUDA(launch_cells_batch(bp2, mode, 1, b->sms, s));
+    }
+    cudaEventRecord(b->ev[1], s);
+    for (int i = 0; i < nc; i++) cudaEventRecord(b->members[i]->ev[3], s);
+    std::vector<Counters> cs(nc);
+    VG_CUDA(cudaMemcpyAsync(cs.data(), b->counters.p, (size_t)nc * sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    VG_CUDA(cudaGetLastError());
+    float cell_ms = 0;
+    cudaEventElapsedTime(&cell_ms, b->ev[0], b->ev[1]);
+    Counters zero;
+    memset(&zero, 0, sizeof(zero));
+    int first_err = VGPU_OK;
+    for (int i = 0; i < nc; i++) {
+        vgpu_container *h = b->members[i];
+        int rc = finish_compute(h, cs[i], zero, cell_ms);
+        if (rc != VGPU_OK && first_err == VGPU_OK) first_err = rc;
+        vgpu_stats &t = b->stats;
+        t.cells += h->stats.cells;
+        t.deleted += h->stats.deleted;
+        t.marginal_cells += h->stats.marginal_cells;
+        t.side_tests += h->stats.side_tests;
+        t.fp64_repairs += h->stats.fp64_repairs;
+        t.planes_tested += h->stats.planes_tested;
+        t.planes_cut += h->stats.planes_cut;
+        t.overflow_reruns += h->stats.overflow_reruns;
+        t.failed_cells += h->stats.failed_cells;
+    }
+    const auto t2 = std::chrono::steady_clock::now();
+    b->stats.kernel_ms = cell_ms;
+    b->stats.bin_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    b->stats.step_ms = std::chrono::duration<double, std::milli>(t2 - t0).count();
+    b->stats.kernel_launches = launch_count() - launches0;
+    if (first_err != VGPU_OK)
+        return fail(first_err, "%lld cells exceeded the engine capacity", (long long)b->stats.failed_cells);
+    return VGPU_OK;
+}
+
+int vgpu_batch_get_stats(vgpu_batch *b, vgpu_stats *out) {
+    if (!b || !out) return fail(VGPU_ERR_ARG, "null argument");
+    *out = b->stats;
     return VGPU_OK;
 }
 

@@ -185,6 +185,7 @@ struct CellCtx {
     float cutoff2;    // squared distance bound for candidates / blocks
     float ri2;        // particle radius squared (poly)
     bool deleted, overflow, marginal, repaired;
+    int fail_reason;  // why overflow was set (VGPU_FAIL_*)
     unsigned long long freeplanes;
     int ncand;
     unsigned tests, repairs, ptested, pcut;
@@ -355,6 +356,40 @@ __device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpSha
     return outbits;
 }
 
+// A vertex whose FP32 solve is ill-conditioned (error bound above
+// kVertexTrust of its distance, or the determinant's sign lost) is solved in
+// FP64 from the planes' double-precision source instead and rounded to FP32;
+// its error bound is then the FP64 solve's plus that rounding.  Only nearly
+// degenerate plane triples (as in jittered lattices) get here: FP64 runs at a
+// small fraction of the FP32 rate, so the threshold is high and the code is
+// kept out of line.  (At 1e-4 about 1 % of vertices came here and the 4M
+// periodic box ran 1.8x slower.)
+constexpr float kVertexTrust = 1e-2f;
+
+template <int MODE, int K>
+__device__ __noinline__ VertexF32 vertex_f64_fallback(const CellParams &P, const WarpShared<MODE, K> &S, double4 me,
+                                                      unsigned t) {
+    const double4 A = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 0));
+    const double4 B = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 1));
+    const double4 Cq = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 2));
+    double x, y, z, D;
+    float kn;
+    solve_f64(A, B, Cq, x, y, z, D, kn);
+    VertexF32 o;
+    const double vv = sqrt(x * x + y * y + z * z);
+    o.x = (float)x;
+    o.y = (float)y;
+    o.z = (float)z;
+    o.a = (float)vv;
+    const double verr = 16.0 * kU64 * (double)kn / fabs(D) + 64.0 * kU64 * vv;
+    o.e = (float)(verr * (1.0 + 1e-6)) + 4.0f * kU32 * o.a;
+    o.good = D > 0.0 && isfinite(o.e) && isfinite(o.a);
+    if (!o.good) o.e = 3.0e38f;   // every test on it is repaired in FP64
+    const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
+    o.r2 = r * r;
+    return o;
+}
+
 // Optional per-phase clock accounting (diagnostics builds: -DVGPU_PHASE_TIMING).
 // Phases: 0 init, 1 block/candidate gather, 2 sort, 3 side tests, 4 cuts, 5 finish.
 #ifdef VGPU_PHASE_TIMING
@@ -419,7 +454,8 @@ struct Engine {
             V.r2[s] = r * r;
             return;
         }
-        const VertexF32 o = solve_vertex_f32(S.pl, S.pe, t);
+        VertexF32 o = solve_vertex_f32(S.pl, S.pe, t);
+        if (!(o.e <= kVertexTrust * o.a)) o = vertex_f64_fallback<MODE, K>(P, S, C.me64, t);
         V.x[s] = o.x;
         V.y[s] = o.y;
         V.z[s] = o.z;
@@ -440,6 +476,7 @@ struct Engine {
         C.bk = b / (P.g.gn[0] * P.g.gn[1]);
         C.ri2 = C.me32.w * C.me32.w;
         C.deleted = C.overflow = C.marginal = C.repaired = false;
+        C.fail_reason = 0;
         C.freeplanes = ~0x3full;
         C.ncand = 0;
         C.tests = C.repairs = C.ptested = C.pcut = 0;
@@ -540,6 +577,7 @@ struct Engine {
         const int p = alloc_plane();
         if (p < 0) {
             C.overflow = true;
+            C.fail_reason = VGPU_FAIL_PLANES;
             return;
         }
         if (lane == 0) {
@@ -582,6 +620,7 @@ struct Engine {
         const int total = __shfl_sync(kFull, incl, 31);
         if (__any_sync(kFull, broken)) {  // inconsistent adjacency: hand the cell to the large engine
             C.overflow = true;
+            C.fail_reason = VGPU_FAIL_ADJACENCY;
             return;
         }
         if (total < 3) {  // not a closed boundary: inconsistent side decisions
@@ -593,6 +632,7 @@ struct Engine {
         for (int i = 0; i < Mask<K>::W; i++) Fm.w[i] = ~Vm.w[i] | Rm.w[i];
         if (Fm.popc() < total) {
             C.overflow = true;
+            C.fail_reason = VGPU_FAIL_VERTICES;
             return;
         }
         // stage the boundary edges (a -> b, kept neighbour u) in lane order
@@ -853,6 +893,7 @@ struct Engine {
                 r = kOffsetRadius + (seg - P.ngroups);
                 if (r >= rlim) {
                     C.overflow = true;  // search did not terminate
+                    C.fail_reason = VGPU_FAIL_SEARCH;
                     return;
                 }
                 if (!any_periodic && r > rmax_grid + 1) return;
@@ -872,7 +913,18 @@ struct Engine {
     // ---- reductions: vertex/face counts, neighbours, FP64 volume and centroid
     __device__ void finish() {
         const int out = P.a.outpos[C.k];
-        if (C.overflow) return;
+        if (C.overflow) {
+            // a larger engine reruns the cell and overwrites this; if none does, it stays failed
+            if (lane == 0) {
+                P.r.vol[out] = 0.0;
+                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+                P.r.nf[out] = 0;
+                P.r.nv[out] = 0;
+                P.r.maxr2[out] = 0.0;
+                P.r.flags[out] = VGPU_CELL_FAILED | (C.fail_reason << 8);
+            }
+            return;
+        }
         if (C.deleted) {
             if (lane == 0) {
                 P.r.vol[out] = 0.0;
@@ -1045,8 +1097,68 @@ struct Engine {
         PHASE_END(t_init, 0);
         search();
         PHASE_BEGIN(t_fin);
+        if (MODE == VGPU_MIXED && K == 2 && P.rec != nullptr && !C.overflow && !C.deleted) {
+            // the finish kernel completes the cell from its record
+            if (emit_record()) {
+                PHASE_END(t_fin, 5);
+                return;
+            }
+            C.overflow = true;   // record store full: the larger engine redoes the cell inline
+            C.fail_reason = VGPU_FAIL_RECORDS;
+        }
         finish();
         PHASE_END(t_fin, 5);
+    }
+
+    // ---- the finished polytope as a record for the finish kernel (layout
+    //      in CellParams); false if the record store is full
+    __device__ bool emit_record() {
+        unsigned long long live = 0ull;
+#pragma unroll
+        for (int s = 0; s < K; s++)
+            if (Vm.test(lane + 32 * s)) {
+                const unsigned t = V.tri[s];
+                live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+            }
+        live = warp_or64(live);
+        const int np = 64 - __clzll((long long)live);
+        int ns = 0;
+#pragma unroll
+        for (int i = 0; i < Mask<K>::W; i++)
+            if (Vm.w[i]) ns = 64 * i + 64 - __clzll((long long)Vm.w[i]);
+        const unsigned words = (unsigned)(kRecHeader + 5 * ns + 3 * np);
+        unsigned long long off = 0;
+        if (lane == 0) off = atomicAdd(P.rec_used, (unsigned long long)words);
+        off = __shfl_sync(kFull, off, 0);
+        if (off + words > P.rec_cap) return false;
+        unsigned *R = P.rec + off;
+        if (lane == 0) {
+            R[0] = (unsigned)ns;
+            R[1] = (unsigned)np;
+            R[2] = (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
+            R[3] = (unsigned)Vm.w[0];
+            R[4] = (unsigned)(Vm.w[0] >> 32);
+        }
+        unsigned *rv = R + kRecHeader;
+#pragma unroll
+        for (int s = 0; s < K; s++) {
+            const int t = lane + 32 * s;
+            if (t < ns) {
+                rv[t] = V.tri[s];
+                rv[ns + t] = S.adj[t];
+                rv[2 * ns + t] = __float_as_uint(V.x[s]);
+                rv[3 * ns + t] = __float_as_uint(V.y[s]);
+                rv[4 * ns + t] = __float_as_uint(V.z[s]);
+            }
+        }
+        unsigned *rp = rv + 5 * ns;
+        for (int q = lane; q < np; q += 32) {
+            rp[q] = (unsigned)S.psrc[q];
+            rp[np + q] = (unsigned)S.pshift[q];
+            rp[2 * np + q] = (unsigned)S.pid[q];
+        }
+        if (lane == 0) P.rec_off[C.k] = (unsigned)off;
+        return true;
     }
 };
 
@@ -1114,6 +1226,284 @@ __global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_kernel(const 
     }
 }
 
+// Many containers in one persistent launch.  A warp takes global cell indices
+// from one queue (container-major, so neighbouring warps share blocks); when
+// a cell belongs to another container than the warp's previous one, the warp
+// copies that container's parameters into its shared slot and flushes its
+// counters to the previous container's.
+template <int MODE, int K>
+__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warps = blockDim.x >> 5;
+    int *offsets = reinterpret_cast<int *>(smem_raw);
+    const size_t off_bytes = ((size_t)B.noffsets * sizeof(int) + 15) & ~(size_t)15;
+    constexpr size_t cp_slot = (sizeof(CellParams) + 15) & ~(size_t)15;
+    CellParams *cps = reinterpret_cast<CellParams *>(smem_raw + off_bytes);
+    WarpShared<MODE, K> *ws = reinterpret_cast<WarpShared<MODE, K> *>(smem_raw + off_bytes + cp_slot * warps);
+    for (int i = threadIdx.x; i < B.noffsets; i += blockDim.x) offsets[i] = B.offsets[i];
+    __syncthreads();
+    CellParams &P = *reinterpret_cast<CellParams *>(reinterpret_cast<unsigned char *>(cps) + cp_slot * wid);
+    WarpShared<MODE, K> &S = ws[wid];
+    int cur = -1;
+    long long cbeg = 0, cend = 0;
+    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0, ovf = 0;
+    auto flush = [&]() {
+        if (cur >= 0 && lane == 0) {
+            Counters *c = B.cps[cur].cnt;
+            atomicAdd(&c->side_tests, tests);
+            atomicAdd(&c->fp64_repairs, repairs);
+            atomicAdd(&c->planes_tested, ptested);
+            atomicAdd(&c->planes_cut, pcut);
+            atomicAdd(&c->deleted, deleted);
+            atomicAdd(&c->marginal, marginal);
+            if (ovf) atomicAdd(B.overflow_list ? &c->overflow : &c->failed, ovf);
+        }
+        tests = repairs = ptested = pcut = deleted = marginal = ovf = 0;
+    };
+    for (;;) {
+        long long w = 0;
+        if (lane == 0) w = (long long)atomicAdd(B.work, 1ull);
+        w = __shfl_sync(kFull, w, 0);
+        if (w >= B.ncells) break;
+        const long long gidx = B.cell_list ? B.cell_list[w] : w;
+        if (gidx < cbeg || gidx >= cend) {
+            flush();
+            // the container c with cell_start[c] <= gidx < cell_start[c+1]
+            int lo = 0, hi = B.ncont;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (B.cell_start[mid] <= gidx) lo = mid;
+                else hi = mid;
+            }
+            cur = lo;
+            cbeg = B.cell_start[lo];
+            cend = B.cell_start[lo + 1];
+            __syncwarp();
+            const unsigned *src = reinterpret_cast<const unsigned *>(B.cps + cur);
+            unsigned *dst = reinterpret_cast<unsigned *>(&P);
+            for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
+        }
+        const int k = (int)(gidx - cbeg);
+        Engine<MODE, K> eng(P, S, offsets, lane);
+        eng.run(k);
+        tests += eng.C.tests;
+        repairs += eng.C.repairs;
+        ptested += eng.C.ptested;
+        pcut += eng.C.pcut;
+        if (eng.C.overflow) {
+            ovf++;
+            if (lane == 0 && B.overflow_list) {
+                const unsigned long long slot = atomicAdd(B.overflow_count, 1ull);
+                B.overflow_list[slot] = gidx;
+            }
+        } else {
+            deleted += eng.C.deleted ? 1 : 0;
+            marginal += eng.C.marginal ? 1 : 0;
+        }
+        __syncwarp();
+    }
+    flush();
+}
+
+// ------------------------------------------------------------------ split finish
+// The FP64 reductions of cells whose polytope the clipping kernel wrote as a
+// record (layout in CellParams).  Kept out of the clipping kernel so that
+// its hot loop keeps the instruction cache to itself; the arithmetic is the
+// same as Engine::finish.
+struct FinishShared {
+    unsigned tri[64];
+    unsigned adj[64];
+    int psrc[64], pshift[64], pid[64];
+    double4 pl64[64];
+    double vx[64], vy[64], vz[64];   // FP64 vertices relative to c0
+    double fx[64], fy[64], fz[64];   // face points relative to c0
+    unsigned stage[96];              // owned edges (t < u)
+};
+
+__device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
+    const int src = F.psrc[p];
+    if (src >= 0) return plane64_from(P, me, src, F.pshift[p]);
+    return face64(P, me, F.pshift[p]);
+}
+
+__global__ void __launch_bounds__(128) finish_kernel(const __grid_constant__ CellParams P) {
+    __shared__ FinishShared fsh[4];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    FinishShared &F = fsh[wid];
+    const int nwarps = gridDim.x * 4;
+    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) {
+        const unsigned off = P.rec_off[k];
+        if (off == kNoRecord) continue;
+        const unsigned *R = P.rec + off;
+        const int ns = (int)R[0], np = (int)R[1];
+        const unsigned fl = R[2];
+        const unsigned long long vm = (unsigned long long)R[3] | ((unsigned long long)R[4] << 32);
+        const unsigned *rv = R + kRecHeader;
+        const unsigned *rp = rv + 5 * ns;
+        unsigned tri[2];
+        float x[2], y[2], z[2];
+        bool valid[2];
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            const int t = lane + 32 * s;
+            valid[s] = (vm >> t) & 1ull;
+            tri[s] = 0;
+            x[s] = y[s] = z[s] = 0.0f;
+            if (t < ns) {
+                tri[s] = rv[t];
+                F.tri[t] = tri[s];
+                F.adj[t] = rv[ns + t];
+                x[s] = __uint_as_float(rv[2 * ns + t]);
+                y[s] = __uint_as_float(rv[3 * ns + t]);
+                z[s] = __uint_as_float(rv[4 * ns + t]);
+            }
+        }
+        for (int q = lane; q < np; q += 32) {
+            F.psrc[q] = (int)rp[q];
+            F.pshift[q] = (int)rp[np + q];
+            F.pid[q] = (int)rp[2 * np + q];
+        }
+        __syncwarp();
+        const double4 me = P.a.p64[k];
+        const int out = P.a.outpos[k];
+        unsigned long long live = 0ull;
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+            if (valid[s]) live |= (1ull << tri_plane(tri[s], 0)) | (1ull << tri_plane(tri[s], 1)) |
+                                  (1ull << tri_plane(tri[s], 2));
+        live = warp_or64(live);
+        const int nf = __popcll(live);
+        const int nv = __popcll(vm);
+        // neighbours (ascending plane slot order) and FP64 planes of the live faces
+        bool has[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int p = lane + 32 * h;
+            has[h] = (live >> p) & 1ull;
+            if (has[h]) {
+                const int q = __popcll(live & ((1ull << p) - 1ull));
+                P.r.nb[(size_t)out * kMaxNb + q] = F.pid[p];
+                F.pl64[p] = plane64_rec(P, F, me, p);
+            }
+        }
+        __syncwarp();
+        double vx[2], vy[2], vz[2];
+        double mr2 = 0.0;
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            vx[s] = vy[s] = vz[s] = 0.0;
+            if (valid[s]) {
+                const double3 r = refine_vertex_f64(F.pl64, tri[s], x[s], y[s], z[s]);
+                vx[s] = r.x;
+                vy[s] = r.y;
+                vz[s] = r.z;
+                mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
+            }
+        }
+        const int t0 = __ffsll((long long)vm) - 1;
+        double c0x = 0, c0y = 0, c0z = 0;
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            const double sx = __shfl_sync(kFull, vx[s], t0 & 31);
+            const double sy = __shfl_sync(kFull, vy[s], t0 & 31);
+            const double sz = __shfl_sync(kFull, vz[s], t0 & 31);
+            if ((t0 >> 5) == s) {
+                c0x = sx;
+                c0y = sy;
+                c0z = sz;
+            }
+        }
+        int ne = 0;
+        unsigned own[2];
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            own[s] = 0;
+            const int t = lane + 32 * s;
+            if (valid[s]) {
+                F.vx[t] = vx[s] - c0x;
+                F.vy[t] = vy[s] - c0y;
+                F.vz[t] = vz[s] - c0z;
+                const unsigned A3 = F.adj[t];
+#pragma unroll
+                for (int e = 0; e < 3; e++) {
+                    const int u = (A3 >> (8 * e)) & 255u;
+                    if (u > t && u < 64) own[s] |= 1u << e;
+                }
+                ne += __popc(own[s]);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (has[h]) {
+                const int p = lane + 32 * h;
+                const double4 pl = F.pl64[p];
+                const double nn = pl.x * pl.x + pl.y * pl.y + pl.z * pl.z;
+                const double f = (pl.w - (pl.x * c0x + pl.y * c0y + pl.z * c0z)) / nn;
+                F.fx[p] = pl.x * f;
+                F.fy[p] = pl.y * f;
+                F.fz[p] = pl.z * f;
+            }
+        }
+        const int eincl = warp_incl_scan(ne, lane);
+        const int etot = __shfl_sync(kFull, eincl, 31);
+        {
+            int q = eincl - ne;
+#pragma unroll
+            for (int s = 0; s < 2; s++)
+#pragma unroll
+                for (int e = 0; e < 3; e++)
+                    if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
+        }
+        __syncwarp();
+        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int i = lane; i < etot; i += 32) {
+            const unsigned E = F.stage[i];
+            const int t = E & 255u, e = E >> 8;
+            const unsigned T = F.tri[t];
+            const int u = (F.adj[t] >> (8 * e)) & 255u;
+            const int px = tri_plane(T, e), py = tri_plane(T, e == 2 ? 0 : e + 1);
+            const double tx = F.vx[t], ty = F.vy[t], tz = F.vz[t];
+            const double ux = F.vx[u], uy = F.vy[u], uz = F.vz[u];
+            const double wx = ty * uz - tz * uy;
+            const double wy = tz * ux - tx * uz;
+            const double wz = tx * uy - ty * ux;
+            const double ax = F.fx[px], ay = F.fy[px], az = F.fz[px];
+            const double bx = F.fx[py], by = F.fy[py], bz = F.fz[py];
+            const double dy = bx * wx + by * wy + bz * wz;
+            const double dx = ax * wx + ay * wy + az * wz;
+            const double dd = dy - dx;
+            vs += dd;
+            cx += dd * (tx + ux) + dy * bx - dx * ax;
+            cy += dd * (ty + uy) + dy * by - dx * ay;
+            cz += dd * (tz + uz) + dy * bz - dx * az;
+        }
+        vs = warp_sumd(vs);
+        cx = warp_sumd(cx);
+        cy = warp_sumd(cy);
+        cz = warp_sumd(cz);
+        mr2 = warp_maxd(mr2);
+        if (lane == 0) {
+            const double vol = vs / 6.0;
+            P.r.vol[out] = vol;
+            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
+                const double f = 1.0 / (4.0 * vs);
+                P.r.cen[3 * out] = c0x + cx * f;
+                P.r.cen[3 * out + 1] = c0y + cy * f;
+                P.r.cen[3 * out + 2] = c0z + cz * f;
+            } else {
+                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+            }
+            P.r.nf[out] = nf;
+            P.r.nv[out] = nv;
+            P.r.maxr2[out] = mr2;
+            P.r.flags[out] = VGPU_CELL_OK | (int)fl;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void nf_to_ll_kernel(const int *nf, long long *out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = nf[i];
@@ -1172,6 +1562,28 @@ cudaError_t launch_one(const CellParams &cp, int sms, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int MODE, int K>
+cudaError_t launch_batch_one(const BatchParams &bp, int sms, cudaStream_t s) {
+    const int warps = 4;
+    const size_t off_bytes = ((size_t)bp.noffsets * sizeof(int) + 15) & ~(size_t)15;
+    const size_t cp_slot = (sizeof(CellParams) + 15) & ~(size_t)15;
+    const size_t smem = off_bytes + warps * (cp_slot + sizeof(WarpShared<MODE, K>));
+    cudaError_t e =
+        cudaFuncSetAttribute(cell_batch_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_batch_kernel<MODE, K>, warps * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long want = (long long)sms * per_sm;
+    const long long need = (bp.ncells + warps - 1) / warps;
+    int grid = (int)(want < need ? want : need);
+    if (grid < 1) grid = 1;
+    cell_batch_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(bp);
+    note_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 // Box tables: corner (sx,sy,sz) uses faces x:(sx>0), y:2+(sy>0), z:4+(sz>0),
@@ -1218,6 +1630,28 @@ cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaS
         return big ? launch_one<VGPU_FP64, 4>(cp, sms, s) : launch_one<VGPU_FP64, 2>(cp, sms, s);
     }
     return big ? launch_one<VGPU_MIXED, 4>(cp, sms, s) : launch_one<VGPU_MIXED, 2>(cp, sms, s);
+}
+
+cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s) {
+    if (bp.ncells <= 0) return cudaSuccess;
+    if (mode == VGPU_FP64) {
+        return big ? launch_batch_one<VGPU_FP64, 4>(bp, sms, s) : launch_batch_one<VGPU_FP64, 2>(bp, sms, s);
+    }
+    return big ? launch_batch_one<VGPU_MIXED, 4>(bp, sms, s) : launch_batch_one<VGPU_MIXED, 2>(bp, sms, s);
+}
+
+cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s) {
+    if (cp.ncells <= 0 || cp.rec == nullptr) return cudaSuccess;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel, 128, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long want = (long long)sms * per_sm;
+    const long long need = (cp.ncells + 3) / 4;
+    const int grid = (int)(want < need ? want : need);
+    finish_kernel<<<grid, 128, 0, s>>>(cp);
+    note_launch();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s) {

@@ -69,6 +69,8 @@ struct Counters {
     unsigned long long overflow;   // cells appended to the overflow list
     unsigned long long work;       // work-queue counter
     unsigned long long overflow_work;
+    unsigned long long failed;     // batched launches: cells that overflowed every capacity
+    unsigned long long rec_used;   // words of the polytope record store in use
     unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
 };
 
@@ -87,6 +89,33 @@ struct CellParams {
     int group_lb2[kMaxGroups];
     unsigned box_tri[8];    // initial box: corner triangles and neighbours
     unsigned box_adj[8];
+    // Split finish (MIXED engine): the clipping kernel writes each finished
+    // polytope as a record here and a separate kernel does the FP64
+    // reductions; NULL: reductions inline.  Record layout (32-bit words):
+    // [ns, np, flags, vmask_lo, vmask_hi, tri[ns], adj[ns], x[ns], y[ns], z[ns],
+    //  psrc[np], pshift[np], pid[np]] with ns / np one past the highest used
+    // vertex / plane slot.
+    unsigned *rec;
+    unsigned long long rec_cap;     // words
+    unsigned long long *rec_used;   // bump allocator (words)
+    unsigned *rec_off;              // per engine index: record offset, kNoRecord if none
+};
+constexpr unsigned kNoRecord = 0xffffffffu;
+constexpr int kRecHeader = 5;
+
+// Many containers in one persistent launch: cells are numbered globally,
+// container c owning [cell_start[c], cell_start[c+1]).
+struct BatchParams {
+    const CellParams *cps;          // per-container parameters (device array)
+    const long long *cell_start;    // ncont + 1 prefix sums of cells
+    int ncont;
+    long long ncells;               // cells in this pass
+    const long long *cell_list;     // NULL: global cells 0..ncells-1; else global indices
+    long long *overflow_list;       // first pass: cells that need the larger engine; NULL: rerun
+    unsigned long long *overflow_count;
+    unsigned long long *work;       // work-queue counter (starts at 0)
+    const int *offsets;             // the engine's offset table (same for every container)
+    int noffsets;
 };
 
 // launch accounting (vgpu_api.cu)
@@ -125,6 +154,8 @@ cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorde
 
 // vgpu_cell.cu
 cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s);
+cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
+cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s);
 cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n,
                                      int *out, cudaStream_t s);
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);

@@ -97,8 +97,9 @@ def fcc_jitter(cells=64, sigma=1e-7, seed=1004, kind=KIND_PERIODIC):
 
 def batched(count=4096, nmin=64, nmax=1_000_000, seed=1005):
     """Many independent containers: N log-uniform in [nmin, nmax], unit density
-    (box side N^(1/3)), blocks round((N/5)^(1/3)); even-indexed containers are
-    periodic, odd ones walled; every fourth is radical with radii U[0.3, 1.0]."""
+    (box side N^(1/3)), blocks round((N/5)^(1/3)).  Even-indexed containers are
+    container_periodic, odd ones walled containers; every fourth (index 1 mod
+    4, walled) is radical with radii U[0.3, 1.0]."""
     rng = np.random.default_rng(seed)
     out = []
     for c in range(count):
@@ -106,11 +107,13 @@ def batched(count=4096, nmin=64, nmax=1_000_000, seed=1005):
         L = n ** (1.0 / 3.0)
         g = max(1, int(round((n / 5.0) ** (1.0 / 3.0))))
         xyz = rng.random((n, 3)) * L
-        periodic = (c % 2 == 0)
-        poly = (c % 4 == 1)
-        r = rng.uniform(0.3, 1.0, size=n) if poly else None
-        kind = KIND_CONTAINER_POLY if poly else KIND_CONTAINER
-        out.append(_pack(kind, (0, L, 0, L, 0, L), (g, g, g), (periodic,) * 3, xyz, r))
+        if c % 2 == 0:
+            out.append(_pack(KIND_PERIODIC, (L, 0, L, 0, 0, L), (g, g, g), (True,) * 3, xyz))
+        elif c % 4 == 1:
+            r = rng.uniform(0.3, 1.0, size=n)
+            out.append(_pack(KIND_CONTAINER_POLY, (0, L, 0, L, 0, L), (g, g, g), (False,) * 3, xyz, r))
+        else:
+            out.append(_pack(KIND_CONTAINER, (0, L, 0, L, 0, L), (g, g, g), (False,) * 3, xyz))
     return out
 
 

@@ -559,6 +559,24 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     return VGPU_OK;
 }
 
+// Split finish (MIXED engine): the clipping kernel writes polytope records,
+// the finish kernel reduces them.  Sets up the record store of h for cp.
+int setup_records(vgpu_container *h, int mode, CellParams &cp, unsigned long long *used_counter) {
+    cp.rec = nullptr;
+    if (mode != VGPU_MIXED || h->nkept <= 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    const unsigned long long cap =
+        std::min<unsigned long long>((unsigned long long)h->nkept * kRecWordsPerCell + (1u << 20), 0xfffffff0ull);
+    VG_CUDA(h->rec.ensure(cap * 4));
+    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 4));
+    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 4, s));
+    cp.rec = h->rec.as<unsigned>();
+    cp.rec_cap = cap;
+    cp.rec_used = used_counter;
+    cp.rec_off = h->rec_off.as<unsigned>();
+    return VGPU_OK;
+}
+
 // Counters of the last compute into the handle's stats; marks it computed.
 int finish_compute(vgpu_container *h, const Counters &c1, const Counters &c2, float cell_ms) {
     float bin_ms = 0, step_ms = 0;
@@ -595,18 +613,8 @@ int vgpu_compute(vgpu_container *h, int mode) {
     int rc = prepare_cells(h, mode, cp);
     if (rc != VGPU_OK) return rc;
     cudaStream_t s = h->stream;
-    if (mode == VGPU_MIXED && h->nkept > 0) {
-        // split finish: the clipping kernel writes polytope records, the finish kernel reduces them
-        const unsigned long long cap = std::min<unsigned long long>(
-            (unsigned long long)h->nkept * kRecWordsPerCell + (1u << 20), 0xfffffff0ull);
-        VG_CUDA(h->rec.ensure(cap * 4));
-        VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 4));
-        VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 4, s));
-        cp.rec = h->rec.as<unsigned>();
-        cp.rec_cap = cap;
-        cp.rec_used = &h->counters.as<Counters>()->rec_used;
-        cp.rec_off = h->rec_off.as<unsigned>();
-    }
+    rc = setup_records(h, mode, cp, &h->counters.as<Counters>()->rec_used);
+    if (rc != VGPU_OK) return rc;
     cudaEventRecord(h->ev[2], s);
     VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
     VG_CUDA(launch_finish(cp, h->sms, s));
@@ -825,6 +833,8 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         cps[i].cnt = b->counters.as<Counters>() + i;
         cps[i].cell_list = nullptr;
         cps[i].overflow_list = nullptr;
+        rc = setup_records(h, mode, cps[i], &cps[i].cnt->rec_used);
+        if (rc != VGPU_OK) return rc;
         starts[i + 1] = starts[i] + h->nkept;
         cudaEventRecord(h->ev[2], h->stream);   // after the gather and the offsets upload
         VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
@@ -854,6 +864,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     bp.noffsets = (int)ot.codes.size();
     cudaEventRecord(b->ev[0], s);
     VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
+    if (mode == VGPU_MIXED) VG_CUDA(launch_finish_batch(bp, b->sms, s));
     unsigned long long novf = 0;
     VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));

@@ -1110,8 +1110,10 @@ struct Engine {
         PHASE_END(t_fin, 5);
     }
 
-    // ---- the finished polytope as a record for the finish kernel (layout
-    //      in CellParams); false if the record store is full
+    // ---- the finished polytope as a compact record for the finish kernel
+    //      (layout in CellParams): valid vertices and live planes only, in
+    //      slot order, with plane and vertex indices renumbered to match;
+    //      false if the record store is full
     __device__ bool emit_record() {
         unsigned long long live = 0ull;
 #pragma unroll
@@ -1121,41 +1123,61 @@ struct Engine {
                 live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
             }
         live = warp_or64(live);
-        const int np = 64 - __clzll((long long)live);
-        int ns = 0;
-#pragma unroll
-        for (int i = 0; i < Mask<K>::W; i++)
-            if (Vm.w[i]) ns = 64 * i + 64 - __clzll((long long)Vm.w[i]);
-        const unsigned words = (unsigned)(kRecHeader + 5 * ns + 3 * np);
+        const int nf = __popcll(live);
+        const int nv = Vm.popc();
+        const unsigned words = (unsigned)(kRecHeader + 5 * nv + 3 * nf);
         unsigned long long off = 0;
         if (lane == 0) off = atomicAdd(P.rec_used, (unsigned long long)words);
         off = __shfl_sync(kFull, off, 0);
         if (off + words > P.rec_cap) return false;
         unsigned *R = P.rec + off;
         if (lane == 0) {
-            R[0] = (unsigned)ns;
-            R[1] = (unsigned)np;
+            R[0] = (unsigned)nv;
+            R[1] = (unsigned)nf;
             R[2] = (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
-            R[3] = (unsigned)Vm.w[0];
-            R[4] = (unsigned)(Vm.w[0] >> 32);
+            R[3] = 0;
+            R[4] = 0;
         }
+        // new indices: vertex slot -> rank among valid slots (startN), plane
+        // slot -> rank among live planes (endN); both tables are free now
+#pragma unroll
+        for (int s = 0; s < K; s++) {
+            const int t = lane + 32 * s;
+            if (Vm.test(t)) S.startN[t] = (unsigned char)Vm.rank(t);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = lane + 32 * h;
+            if ((live >> q) & 1ull) S.endN[q] = (unsigned char)__popcll(live & ((1ull << q) - 1ull));
+        }
+        __syncwarp();
         unsigned *rv = R + kRecHeader;
 #pragma unroll
         for (int s = 0; s < K; s++) {
             const int t = lane + 32 * s;
-            if (t < ns) {
-                rv[t] = V.tri[s];
-                rv[ns + t] = S.adj[t];
-                rv[2 * ns + t] = __float_as_uint(V.x[s]);
-                rv[3 * ns + t] = __float_as_uint(V.y[s]);
-                rv[4 * ns + t] = __float_as_uint(V.z[s]);
+            if (Vm.test(t)) {
+                const int r = S.startN[t];
+                const unsigned T = V.tri[s];
+                const unsigned A3 = S.adj[t];
+                rv[r] = (unsigned)S.endN[tri_plane(T, 0)] | ((unsigned)S.endN[tri_plane(T, 1)] << 8) |
+                        ((unsigned)S.endN[tri_plane(T, 2)] << 16);
+                rv[nv + r] = (unsigned)S.startN[A3 & 255u] | ((unsigned)S.startN[(A3 >> 8) & 255u] << 8) |
+                             ((unsigned)S.startN[(A3 >> 16) & 255u] << 16);
+                rv[2 * nv + r] = __float_as_uint(V.x[s]);
+                rv[3 * nv + r] = __float_as_uint(V.y[s]);
+                rv[4 * nv + r] = __float_as_uint(V.z[s]);
             }
         }
-        unsigned *rp = rv + 5 * ns;
-        for (int q = lane; q < np; q += 32) {
-            rp[q] = (unsigned)S.psrc[q];
-            rp[np + q] = (unsigned)S.pshift[q];
-            rp[2 * np + q] = (unsigned)S.pid[q];
+        unsigned *rp = rv + 5 * nv;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = lane + 32 * h;
+            if ((live >> q) & 1ull) {
+                const int r = S.endN[q];
+                rp[r] = (unsigned)S.psrc[q];
+                rp[nf + r] = (unsigned)S.pshift[q];
+                rp[2 * nf + r] = (unsigned)S.pid[q];
+            }
         }
         if (lane == 0) P.rec_off[C.k] = (unsigned)off;
         return true;
@@ -1309,16 +1331,18 @@ __global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_batch_kernel(
 
 // ------------------------------------------------------------------ split finish
 // The FP64 reductions of cells whose polytope the clipping kernel wrote as a
-// record (layout in CellParams).  Kept out of the clipping kernel so that
-// its hot loop keeps the instruction cache to itself; the arithmetic is the
-// same as Engine::finish.
+// compact record (layout in CellParams).  Kept out of the clipping kernel so
+// that its hot loop keeps the instruction cache to itself.  Same sums as
+// Engine::finish, except that each face's reference point is one of its own
+// vertices (the one of lowest index) rather than the plane's foot point, which
+// saves the FP64 divisions (the edge formula holds for any point of the face).
 struct FinishShared {
     unsigned tri[64];
     unsigned adj[64];
-    int psrc[64], pshift[64], pid[64];
+    int psrc[64], pshift[64];
+    int rep[64];                     // per face: its lowest vertex
     double4 pl64[64];
     double vx[64], vy[64], vz[64];   // FP64 vertices relative to c0
-    double fx[64], fy[64], fz[64];   // face points relative to c0
     unsigned stage[96];              // owned edges (t < u)
 };
 
@@ -1328,179 +1352,160 @@ __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const Finish
     return face64(P, me, F.pshift[p]);
 }
 
+// The reductions of cell k (engine order) from its record, if it has one.
+__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int lane) {
+    const unsigned off = P.rec_off[k];
+    if (off == kNoRecord) return;
+    const unsigned *R = P.rec + off;
+    const int nv = (int)R[0], nf = (int)R[1];
+    const unsigned fl = R[2];
+    const unsigned *rv = R + kRecHeader;
+    const unsigned *rp = rv + 5 * nv;
+    const double4 me = P.a.p64[k];
+    const int out = P.a.outpos[k];
+    // planes: neighbour IDs (plane order), sources, FP64 planes
+    for (int q = lane; q < nf; q += 32) {
+        F.psrc[q] = (int)rp[q];
+        F.pshift[q] = (int)rp[nf + q];
+        F.rep[q] = 0x7fffffff;
+        P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
+        F.pl64[q] = plane64_rec(P, F, me, q);
+    }
+    __syncwarp();
+    unsigned tri[2];
+    double vx[2], vy[2], vz[2];
+    double mr2 = 0.0;
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const int t = lane + 32 * s;
+        tri[s] = 0;
+        vx[s] = vy[s] = vz[s] = 0.0;
+        if (t < nv) {
+            tri[s] = rv[t];
+            F.tri[t] = tri[s];
+            F.adj[t] = rv[nv + t];
+            const double3 r = refine_vertex_f64(F.pl64, tri[s], __uint_as_float(rv[2 * nv + t]),
+                                                __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
+            vx[s] = r.x;
+            vy[s] = r.y;
+            vz[s] = r.z;
+            mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
+            atomicMin(&F.rep[tri_plane(tri[s], 0)], t);
+            atomicMin(&F.rep[tri_plane(tri[s], 1)], t);
+            atomicMin(&F.rep[tri_plane(tri[s], 2)], t);
+        }
+    }
+    // origin of the sums: vertex 0
+    const double c0x = __shfl_sync(kFull, vx[0], 0);
+    const double c0y = __shfl_sync(kFull, vy[0], 0);
+    const double c0z = __shfl_sync(kFull, vz[0], 0);
+    int ne = 0;
+    unsigned own[2];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        own[s] = 0;
+        const int t = lane + 32 * s;
+        if (t < nv) {
+            F.vx[t] = vx[s] - c0x;
+            F.vy[t] = vy[s] - c0y;
+            F.vz[t] = vz[s] - c0z;
+            const unsigned A3 = F.adj[t];
+#pragma unroll
+            for (int e = 0; e < 3; e++)
+                if ((int)((A3 >> (8 * e)) & 255u) > t) own[s] |= 1u << e;
+            ne += __popc(own[s]);
+        }
+    }
+    const int eincl = warp_incl_scan(ne, lane);
+    const int etot = __shfl_sync(kFull, eincl, 31);
+    {
+        int q = eincl - ne;
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+#pragma unroll
+            for (int e = 0; e < 3; e++)
+                if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
+    }
+    __syncwarp();
+    // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
+    double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int i = lane; i < etot; i += 32) {
+        const unsigned E = F.stage[i];
+        const int t = E & 255u, e = E >> 8;
+        const unsigned T = F.tri[t];
+        const int u = (F.adj[t] >> (8 * e)) & 255u;
+        const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
+        const double tx = F.vx[t], ty = F.vy[t], tz = F.vz[t];
+        const double ux = F.vx[u], uy = F.vy[u], uz = F.vz[u];
+        const double wx = ty * uz - tz * uy;
+        const double wy = tz * ux - tx * uz;
+        const double wz = tx * uy - ty * ux;
+        const double ax = F.vx[rx], ay = F.vy[rx], az = F.vz[rx];
+        const double bx = F.vx[ry], by = F.vy[ry], bz = F.vz[ry];
+        const double dy = bx * wx + by * wy + bz * wz;
+        const double dx = ax * wx + ay * wy + az * wz;
+        const double dd = dy - dx;
+        vs += dd;
+        cx += dd * (tx + ux) + dy * bx - dx * ax;
+        cy += dd * (ty + uy) + dy * by - dx * ay;
+        cz += dd * (tz + uz) + dy * bz - dx * az;
+    }
+    vs = warp_sumd(vs);
+    cx = warp_sumd(cx);
+    cy = warp_sumd(cy);
+    cz = warp_sumd(cz);
+    mr2 = warp_maxd(mr2);
+    if (lane == 0) {
+        const double vol = vs / 6.0;
+        P.r.vol[out] = vol;
+        if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
+            const double f = 1.0 / (4.0 * vs);
+            P.r.cen[3 * out] = c0x + cx * f;
+            P.r.cen[3 * out + 1] = c0y + cy * f;
+            P.r.cen[3 * out + 2] = c0z + cz * f;
+        } else {
+            P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+        }
+        P.r.nf[out] = nf;
+        P.r.nv[out] = nv;
+        P.r.maxr2[out] = mr2;
+        P.r.flags[out] = VGPU_CELL_OK | (int)fl;
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(128) finish_kernel(const __grid_constant__ CellParams P) {
     __shared__ FinishShared fsh[4];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    FinishShared &F = fsh[wid];
     const int nwarps = gridDim.x * 4;
-    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) {
-        const unsigned off = P.rec_off[k];
-        if (off == kNoRecord) continue;
-        const unsigned *R = P.rec + off;
-        const int ns = (int)R[0], np = (int)R[1];
-        const unsigned fl = R[2];
-        const unsigned long long vm = (unsigned long long)R[3] | ((unsigned long long)R[4] << 32);
-        const unsigned *rv = R + kRecHeader;
-        const unsigned *rp = rv + 5 * ns;
-        unsigned tri[2];
-        float x[2], y[2], z[2];
-        bool valid[2];
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            const int t = lane + 32 * s;
-            valid[s] = (vm >> t) & 1ull;
-            tri[s] = 0;
-            x[s] = y[s] = z[s] = 0.0f;
-            if (t < ns) {
-                tri[s] = rv[t];
-                F.tri[t] = tri[s];
-                F.adj[t] = rv[ns + t];
-                x[s] = __uint_as_float(rv[2 * ns + t]);
-                y[s] = __uint_as_float(rv[3 * ns + t]);
-                z[s] = __uint_as_float(rv[4 * ns + t]);
+    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) finish_record(P, fsh[wid], k, lane);
+}
+
+// The same over the cells of a batch (global numbering as cell_batch_kernel).
+__global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant__ BatchParams B) {
+    __shared__ FinishShared fsh[4];
+    __shared__ __align__(16) unsigned char cpw[4][(sizeof(CellParams) + 15) & ~(size_t)15];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    CellParams &P = *reinterpret_cast<CellParams *>(cpw[wid]);
+    const long long nwarps = (long long)gridDim.x * 4;
+    long long cbeg = 0, cend = 0;
+    for (long long g = (long long)blockIdx.x * 4 + wid; g < B.ncells; g += nwarps) {
+        if (g < cbeg || g >= cend) {
+            int lo = 0, hi = B.ncont;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (B.cell_start[mid] <= g) lo = mid;
+                else hi = mid;
             }
+            cbeg = B.cell_start[lo];
+            cend = B.cell_start[lo + 1];
+            __syncwarp();
+            const unsigned *src = reinterpret_cast<const unsigned *>(B.cps + lo);
+            unsigned *dst = reinterpret_cast<unsigned *>(&P);
+            for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
         }
-        for (int q = lane; q < np; q += 32) {
-            F.psrc[q] = (int)rp[q];
-            F.pshift[q] = (int)rp[np + q];
-            F.pid[q] = (int)rp[2 * np + q];
-        }
-        __syncwarp();
-        const double4 me = P.a.p64[k];
-        const int out = P.a.outpos[k];
-        unsigned long long live = 0ull;
-#pragma unroll
-        for (int s = 0; s < 2; s++)
-            if (valid[s]) live |= (1ull << tri_plane(tri[s], 0)) | (1ull << tri_plane(tri[s], 1)) |
-                                  (1ull << tri_plane(tri[s], 2));
-        live = warp_or64(live);
-        const int nf = __popcll(live);
-        const int nv = __popcll(vm);
-        // neighbours (ascending plane slot order) and FP64 planes of the live faces
-        bool has[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int p = lane + 32 * h;
-            has[h] = (live >> p) & 1ull;
-            if (has[h]) {
-                const int q = __popcll(live & ((1ull << p) - 1ull));
-                P.r.nb[(size_t)out * kMaxNb + q] = F.pid[p];
-                F.pl64[p] = plane64_rec(P, F, me, p);
-            }
-        }
-        __syncwarp();
-        double vx[2], vy[2], vz[2];
-        double mr2 = 0.0;
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            vx[s] = vy[s] = vz[s] = 0.0;
-            if (valid[s]) {
-                const double3 r = refine_vertex_f64(F.pl64, tri[s], x[s], y[s], z[s]);
-                vx[s] = r.x;
-                vy[s] = r.y;
-                vz[s] = r.z;
-                mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
-            }
-        }
-        const int t0 = __ffsll((long long)vm) - 1;
-        double c0x = 0, c0y = 0, c0z = 0;
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            const double sx = __shfl_sync(kFull, vx[s], t0 & 31);
-            const double sy = __shfl_sync(kFull, vy[s], t0 & 31);
-            const double sz = __shfl_sync(kFull, vz[s], t0 & 31);
-            if ((t0 >> 5) == s) {
-                c0x = sx;
-                c0y = sy;
-                c0z = sz;
-            }
-        }
-        int ne = 0;
-        unsigned own[2];
-#pragma unroll
-        for (int s = 0; s < 2; s++) {
-            own[s] = 0;
-            const int t = lane + 32 * s;
-            if (valid[s]) {
-                F.vx[t] = vx[s] - c0x;
-                F.vy[t] = vy[s] - c0y;
-                F.vz[t] = vz[s] - c0z;
-                const unsigned A3 = F.adj[t];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    const int u = (A3 >> (8 * e)) & 255u;
-                    if (u > t && u < 64) own[s] |= 1u << e;
-                }
-                ne += __popc(own[s]);
-            }
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            if (has[h]) {
-                const int p = lane + 32 * h;
-                const double4 pl = F.pl64[p];
-                const double nn = pl.x * pl.x + pl.y * pl.y + pl.z * pl.z;
-                const double f = (pl.w - (pl.x * c0x + pl.y * c0y + pl.z * c0z)) / nn;
-                F.fx[p] = pl.x * f;
-                F.fy[p] = pl.y * f;
-                F.fz[p] = pl.z * f;
-            }
-        }
-        const int eincl = warp_incl_scan(ne, lane);
-        const int etot = __shfl_sync(kFull, eincl, 31);
-        {
-            int q = eincl - ne;
-#pragma unroll
-            for (int s = 0; s < 2; s++)
-#pragma unroll
-                for (int e = 0; e < 3; e++)
-                    if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
-        }
-        __syncwarp();
-        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-        for (int i = lane; i < etot; i += 32) {
-            const unsigned E = F.stage[i];
-            const int t = E & 255u, e = E >> 8;
-            const unsigned T = F.tri[t];
-            const int u = (F.adj[t] >> (8 * e)) & 255u;
-            const int px = tri_plane(T, e), py = tri_plane(T, e == 2 ? 0 : e + 1);
-            const double tx = F.vx[t], ty = F.vy[t], tz = F.vz[t];
-            const double ux = F.vx[u], uy = F.vy[u], uz = F.vz[u];
-            const double wx = ty * uz - tz * uy;
-            const double wy = tz * ux - tx * uz;
-            const double wz = tx * uy - ty * ux;
-            const double ax = F.fx[px], ay = F.fy[px], az = F.fz[px];
-            const double bx = F.fx[py], by = F.fy[py], bz = F.fz[py];
-            const double dy = bx * wx + by * wy + bz * wz;
-            const double dx = ax * wx + ay * wy + az * wz;
-            const double dd = dy - dx;
-            vs += dd;
-            cx += dd * (tx + ux) + dy * bx - dx * ax;
-            cy += dd * (ty + uy) + dy * by - dx * ay;
-            cz += dd * (tz + uz) + dy * bz - dx * az;
-        }
-        vs = warp_sumd(vs);
-        cx = warp_sumd(cx);
-        cy = warp_sumd(cy);
-        cz = warp_sumd(cz);
-        mr2 = warp_maxd(mr2);
-        if (lane == 0) {
-            const double vol = vs / 6.0;
-            P.r.vol[out] = vol;
-            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
-                const double f = 1.0 / (4.0 * vs);
-                P.r.cen[3 * out] = c0x + cx * f;
-                P.r.cen[3 * out + 1] = c0y + cy * f;
-                P.r.cen[3 * out + 2] = c0z + cz * f;
-            } else {
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-            }
-            P.r.nf[out] = nf;
-            P.r.nv[out] = nv;
-            P.r.maxr2[out] = mr2;
-            P.r.flags[out] = VGPU_CELL_OK | (int)fl;
-        }
-        __syncwarp();
+        if (P.rec != nullptr) finish_record(P, fsh[wid], (int)(g - cbeg), lane);
     }
 }
 
@@ -1650,6 +1655,20 @@ cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s) {
     const long long need = (cp.ncells + 3) / 4;
     const int grid = (int)(want < need ? want : need);
     finish_kernel<<<grid, 128, 0, s>>>(cp);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish_batch(const BatchParams &bp, int sms, cudaStream_t s) {
+    if (bp.ncells <= 0) return cudaSuccess;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel, 128, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long want = (long long)sms * per_sm;
+    const long long need = (bp.ncells + 3) / 4;
+    const int grid = (int)(want < need ? want : need);
+    finish_batch_kernel<<<grid, 128, 0, s>>>(bp);
     note_launch();
     return cudaGetLastError();
 }

@@ -156,6 +156,7 @@ cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorde
 cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s);
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
 cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s);
+cudaError_t launch_finish_batch(const BatchParams &bp, int sms, cudaStream_t s);
 cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n,
                                      int *out, cudaStream_t s);
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);

@@ -911,29 +911,26 @@ struct Engine {
     }
 
     // ---- reductions: vertex/face counts, neighbours, FP64 volume and centroid
+    // ---- results of a cell with no polytope: deleted (compute_cell false), or
+    //      overflowed (a larger engine reruns it and overwrites this; if none
+    //      does, it stays failed)
+    __device__ __forceinline__ void write_empty() {
+        const int out = P.a.outpos[C.k];
+        if (lane == 0) {
+            P.r.vol[out] = 0.0;
+            P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+            P.r.nf[out] = 0;
+            P.r.nv[out] = 0;
+            P.r.maxr2[out] = 0.0;
+            P.r.flags[out] = C.overflow ? (VGPU_CELL_FAILED | (C.fail_reason << 8))
+                                        : ((C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0));
+        }
+    }
+
     __device__ void finish() {
         const int out = P.a.outpos[C.k];
-        if (C.overflow) {
-            // a larger engine reruns the cell and overwrites this; if none does, it stays failed
-            if (lane == 0) {
-                P.r.vol[out] = 0.0;
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-                P.r.nf[out] = 0;
-                P.r.nv[out] = 0;
-                P.r.maxr2[out] = 0.0;
-                P.r.flags[out] = VGPU_CELL_FAILED | (C.fail_reason << 8);
-            }
-            return;
-        }
-        if (C.deleted) {
-            if (lane == 0) {
-                P.r.vol[out] = 0.0;
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-                P.r.nf[out] = 0;
-                P.r.nv[out] = 0;
-                P.r.maxr2[out] = 0.0;
-                P.r.flags[out] = (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
-            }
+        if (C.overflow || C.deleted) {
+            write_empty();
             return;
         }
         unsigned long long live = 0ull;
@@ -1097,16 +1094,23 @@ struct Engine {
         PHASE_END(t_init, 0);
         search();
         PHASE_BEGIN(t_fin);
-        if (MODE == VGPU_MIXED && K == 2 && P.rec != nullptr && !C.overflow && !C.deleted) {
-            // the finish kernel completes the cell from its record
-            if (emit_record()) {
-                PHASE_END(t_fin, 5);
-                return;
+        if (MODE == VGPU_MIXED && K == 2) {
+            // the main mixed engine never reduces inline: the finish kernel
+            // completes the cell from its record (the FP64 code stays out of
+            // this kernel); a full record store hands the cell to the larger
+            // engine, which finishes inline
+            if (!C.overflow && !C.deleted) {
+                if (emit_record()) {
+                    PHASE_END(t_fin, 5);
+                    return;
+                }
+                C.overflow = true;
+                C.fail_reason = VGPU_FAIL_RECORDS;
             }
-            C.overflow = true;   // record store full: the larger engine redoes the cell inline
-            C.fail_reason = VGPU_FAIL_RECORDS;
+            write_empty();
+        } else {
+            finish();
         }
-        finish();
         PHASE_END(t_fin, 5);
     }
 
@@ -1342,6 +1346,7 @@ struct FinishShared {
     int psrc[64], pshift[64];
     int rep[64];                     // per face: its lowest vertex
     double4 pl64[64];
+    float4 pn[64];                   // the FP64 plane normals rounded to FP32
     double vx[64], vy[64], vz[64];   // FP64 vertices relative to c0
     unsigned stage[96];              // owned edges (t < u)
 };
@@ -1350,6 +1355,37 @@ __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const Finish
     const int src = F.psrc[p];
     if (src >= 0) return plane64_from(P, me, src, F.pshift[p]);
     return face64(P, me, F.pshift[p]);
+}
+
+// refine_vertex_f64 with the planes' FP32 normals taken from F.pn (rounded
+// once per plane rather than once per vertex and plane).
+__device__ __forceinline__ double3 refine_vertex_rec(const FinishShared &F, unsigned t, float fx, float fy, float fz) {
+    const int ia = tri_plane(t, 0), ib = tri_plane(t, 1), ic = tri_plane(t, 2);
+    const double4 A = F.pl64[ia], B = F.pl64[ib], Cq = F.pl64[ic];
+    const float4 a = F.pn[ia], b = F.pn[ib], c = F.pn[ic];
+    const double x = fx, y = fy, z = fz;
+    const double ra = A.w - fma(A.x, x, fma(A.y, y, A.z * z));
+    const double rb = B.w - fma(B.x, x, fma(B.y, y, B.z * z));
+    const double rc = Cq.w - fma(Cq.x, x, fma(Cq.y, y, Cq.z * z));
+    const float bcx = b.y * c.z - b.z * c.y, bcy = b.z * c.x - b.x * c.z, bcz = b.x * c.y - b.y * c.x;
+    const float cax = c.y * a.z - c.z * a.y, cay = c.z * a.x - c.x * a.z, caz = c.x * a.y - c.y * a.x;
+    const float abx = a.y * b.z - a.z * b.y, aby = a.z * b.x - a.x * b.z, abz = a.x * b.y - a.y * b.x;
+    const float D = a.x * bcx + a.y * bcy + a.z * bcz;
+    const float scale = (fabsf(a.x) + fabsf(a.y) + fabsf(a.z)) * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z)) *
+                        (fabsf(c.x) + fabsf(c.y) + fabsf(c.z));
+    double3 v;
+    if (fabsf(D) > 1e-3f * scale) {
+        const float fra = (float)ra, frb = (float)rb, frc = (float)rc;
+        const float inv = 1.0f / D;
+        v.x = x + (double)((fra * bcx + frb * cax + frc * abx) * inv);
+        v.y = y + (double)((fra * bcy + frb * cay + frc * aby) * inv);
+        v.z = z + (double)((fra * bcz + frb * caz + frc * abz) * inv);
+    } else {
+        double DD;
+        float kn;
+        solve_f64(A, B, Cq, v.x, v.y, v.z, DD, kn);
+    }
+    return v;
 }
 
 // The reductions of cell k (engine order) from its record, if it has one.
@@ -1369,7 +1405,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         F.pshift[q] = (int)rp[nf + q];
         F.rep[q] = 0x7fffffff;
         P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
-        F.pl64[q] = plane64_rec(P, F, me, q);
+        const double4 pl = plane64_rec(P, F, me, q);
+        F.pl64[q] = pl;
+        F.pn[q] = make_float4((float)pl.x, (float)pl.y, (float)pl.z, 0.0f);
     }
     __syncwarp();
     unsigned tri[2];
@@ -1384,7 +1422,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             tri[s] = rv[t];
             F.tri[t] = tri[s];
             F.adj[t] = rv[nv + t];
-            const double3 r = refine_vertex_f64(F.pl64, tri[s], __uint_as_float(rv[2 * nv + t]),
+            const double3 r = refine_vertex_rec(F, tri[s], __uint_as_float(rv[2 * nv + t]),
                                                 __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
             vx[s] = r.x;
             vy[s] = r.y;

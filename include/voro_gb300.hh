@@ -13,9 +13,14 @@
 // What a cell exposes after compute_cell(c, vl) is what the engine returns per
 // cell: volume(), centroid(), number_of_faces(), number_of_edges(), p (vertex
 // count), max_radius_squared() and, for voronoicell_neighbor, neighbors().
-// Queries that need the polytope itself (vertices(), face_areas(), ...) are
-// not provided, so code using them fails to compile rather than silently
-// differing.
+// The queries that need the polytope itself (vertices(), face_vertices(),
+// face_areas(), face_orders(), face_perimeters(), normals(), surface_area(),
+// total_edge_distance(), vertex_orders(), face_freq_table()) work once the
+// container keeps polytopes: con.set_polytopes(true) before computing
+// (print_custom switches it on by itself for the fields that need it).
+// Vertex and face numbering is the engine's own: faces are listed in the
+// order of neighbors() (ascending neighbour ID), each as a vertex loop
+// clockwise seen from outside like the reference's.
 //
 // Errors follow the reference (src/common.cc:27-30): the message is printed
 // and the process exits with the status code, unless VORO_GB300_THROW is
@@ -23,9 +28,12 @@
 #ifndef VORO_GB300_HH
 #define VORO_GB300_HH
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -90,14 +98,138 @@ class voronoicell {
     int number_of_faces() const { return nf_; }
     // every vertex the engine produces has order 3 (E = 3p/2)
     int number_of_edges() const { return 3 * p / 2; }
-    void vertex_orders(std::vector<int> &v) const { v.assign(p, 3); }
     // in the reference's doubled coordinates (src/cell.cc:1907-1917)
     double max_radius_squared() const { return 4.0 * mr2_; }
+
+    // ---- polytope queries (src/cell.hh:132-184); need set_polytopes(true)
+    void vertices(std::vector<double> &v) const {
+        need_poly();
+        v = verts_;
+    }
+    void vertices(double x, double y, double z, std::vector<double> &v) const {
+        need_poly();
+        v = verts_;
+        for (size_t i = 0; i < v.size(); i += 3) {
+            v[i] += x;
+            v[i + 1] += y;
+            v[i + 2] += z;
+        }
+    }
+    // per face: vertex count, then the loop (as voronoicell_base::face_vertices)
+    void face_vertices(std::vector<int> &v) const {
+        need_poly();
+        v.clear();
+        for (size_t f = 0; f < fstart_.size(); f++) {
+            v.push_back(forder(f));
+            for (int j = 0; j < forder(f); j++) v.push_back(floops_[fstart_[f] + j]);
+        }
+    }
+    void face_orders(std::vector<int> &v) const {
+        need_poly();
+        v.resize(fstart_.size());
+        for (size_t f = 0; f < fstart_.size(); f++) v[f] = forder(f);
+    }
+    void face_areas(std::vector<double> &v) const {
+        need_poly();
+        v.resize(fstart_.size());
+        for (size_t f = 0; f < fstart_.size(); f++) {
+            double n[3];
+            newell(f, n);
+            v[f] = 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        }
+    }
+    void face_perimeters(std::vector<double> &v) const {
+        need_poly();
+        v.resize(fstart_.size());
+        for (size_t f = 0; f < fstart_.size(); f++) {
+            double per = 0;
+            for (int j = 0; j < forder(f); j++) {
+                const double *a = vert(floops_[fstart_[f] + j]);
+                const double *b = vert(floops_[fstart_[f] + (j + 1) % forder(f)]);
+                per += std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) +
+                                 (a[2] - b[2]) * (a[2] - b[2]));
+            }
+            v[f] = per;
+        }
+    }
+    // outward unit normals, three per face
+    void normals(std::vector<double> &v) const {
+        need_poly();
+        v.resize(3 * fstart_.size());
+        for (size_t f = 0; f < fstart_.size(); f++) {
+            double n[3];
+            newell(f, n);
+            const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int a = 0; a < 3; a++) v[3 * f + a] = l > 0 ? -n[a] / l : 0.0;
+        }
+    }
+    double surface_area() const {
+        std::vector<double> a;
+        face_areas(a);
+        double s = 0;
+        for (double x : a) s += x;
+        return s;
+    }
+    double total_edge_distance() const {
+        std::vector<double> p_;
+        face_perimeters(p_);
+        double s = 0;
+        for (double x : p_) s += x;
+        return 0.5 * s;   // every edge bounds two faces
+    }
+    void vertex_orders(std::vector<int> &v) const {
+        if (!has_poly_) {
+            v.assign(p, 3);   // every vertex the engine produces has order 3
+            return;
+        }
+        v.assign(p, 0);
+        for (int x : floops_) v[x]++;
+    }
+    void face_freq_table(std::vector<int> &v) const {
+        std::vector<int> o;
+        face_orders(o);
+        v.clear();
+        for (int k : o) {
+            if ((int)v.size() <= k) v.resize(k + 1, 0);
+            v[k]++;
+        }
+    }
 
   protected:
     friend class container_gpu_base;
     double vol_ = 0, cen_[3] = {0, 0, 0}, mr2_ = 0;
     int nf_ = 0;
+    bool has_poly_ = false;
+    std::vector<double> verts_;   // 3 per vertex, particle-relative
+    std::vector<int> fstart_;     // per face (neighbour order): start in floops_
+    std::vector<int> floops_;     // concatenated vertex loops
+    std::vector<int> fnb_;        // per face: neighbour ID
+    int forder(size_t f) const {
+        return (f + 1 < fstart_.size() ? fstart_[f + 1] : (int)floops_.size()) - fstart_[f];
+    }
+    const double *vert(int i) const { return &verts_[3 * i]; }
+    // twice the face's vector area, from vectors relative to its first vertex
+    // (small faces keep their precision)
+    void newell(size_t f, double n[3]) const {
+        n[0] = n[1] = n[2] = 0;
+        const int m = forder(f);
+        const double *o = vert(floops_[fstart_[f]]);
+        for (int j = 1; j + 1 < m; j++) {
+            const double *pa = vert(floops_[fstart_[f] + j]);
+            const double *pb = vert(floops_[fstart_[f] + j + 1]);
+            const double a[3] = {pa[0] - o[0], pa[1] - o[1], pa[2] - o[2]};
+            const double b[3] = {pb[0] - o[0], pb[1] - o[1], pb[2] - o[2]};
+            n[0] += a[1] * b[2] - a[2] * b[1];
+            n[1] += a[2] * b[0] - a[0] * b[2];
+            n[2] += a[0] * b[1] - a[1] * b[0];
+        }
+    }
+    void need_poly() const {
+        if (!has_poly_)
+            voro_fatal_error("this query needs the cell polytope: call set_polytopes(true) on the container "
+                             "before computing",
+                             VOROPP_INTERNAL_ERROR);
+    }
 };
 
 // voronoicell_neighbor (src/cell.hh:470-560): adds the neighbour ID per face.
@@ -121,6 +253,15 @@ class container_gpu_base {
     container_gpu_base &operator=(const container_gpu_base &) = delete;
     ~container_gpu_base() {
         if (h_) vgpu_container_destroy(h_);
+    }
+
+    // Keep every cell's polytope from the next compute on (needed by the
+    // voronoicell vertex/face queries; no counterpart in the reference, whose
+    // cells always carry their polytope).
+    void set_polytopes(bool on) {
+        gpu_detail::check(vgpu_set_output(h_, on ? VGPU_OUTPUT_POLYTOPES : 0), "set_polytopes");
+        poly_on_ = on;
+        dirty_ = true;
     }
 
     // Precision of the engine: VGPU_MIXED (default) or VGPU_FP64.
@@ -160,6 +301,14 @@ class container_gpu_base {
             gpu_detail::check(vgpu_get_radii(h_, rad_.data()), "compute_all_cells");
         }
         have_nb_ = false;
+        poff_.clear();
+        pdata_.clear();
+        if (poly_on_ && n > 0) {
+            poff_.assign(n + 1, 0);
+            gpu_detail::check(vgpu_get_polytopes(h_, poff_.data(), nullptr), "polytopes");
+            pdata_.resize(poff_[n] > 0 ? poff_[n] : 1);
+            gpu_detail::check(vgpu_get_polytopes(h_, poff_.data(), pdata_.data()), "polytopes");
+        }
         dirty_ = false;
     }
 
@@ -197,6 +346,7 @@ class container_gpu_base {
     // container::print_custom (src/container.hh:434-451; fields
     // src/cell.cc:2485-2558)
     void print_custom(const char *format, FILE *fp = stdout) {
+        if (needs_polytope(format) && !poly_on_) set_polytopes(true);
         ensure();
         if (contains_neighbor(format)) ensure_neighbors();
         for (int64_t k = 0; k < n_; k++)
@@ -254,6 +404,9 @@ class container_gpu_base {
   private:
     vgpu_container *h_ = nullptr;
     bool poly_;
+    bool poly_on_ = false;
+    std::vector<int64_t> poff_;
+    std::vector<double> pdata_;
     int mode_ = VGPU_MIXED;
     bool dirty_ = true, have_nb_ = false;
     std::vector<int32_t> ids_in_;
@@ -284,6 +437,8 @@ class container_gpu_base {
         have_nb_ = true;
     }
     bool fill(voronoicell &c, int64_t k) {
+        c.has_poly_ = false;
+        if (poly_on_ && !poff_.empty() && poff_[k + 1] > poff_[k]) load_polytope(c, &pdata_[poff_[k]]);
         c.p = nv_[k];
         c.vol_ = vol_[k];
         c.cen_[0] = cen_[3 * k];
@@ -293,11 +448,87 @@ class container_gpu_base {
         c.mr2_ = mr2_[k];
         return (flags_[k] & VGPU_CELL_OK) != 0;
     }
+    // [nv, nf, vertices, per face: neighbour, m, loop] -> faces in neighbour order
+    static void load_polytope(voronoicell &c, const double *d) {
+        const int nv = (int)d[0], nf = (int)d[1];
+        c.verts_.assign(d + 2, d + 2 + 3 * nv);
+        std::vector<int> fs(nf), order(nf);
+        int i = 2 + 3 * nv;
+        for (int f = 0; f < nf; f++) {
+            fs[f] = i;
+            order[f] = f;
+            i += 2 + (int)d[i + 1];
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return d[fs[a]] < d[fs[b]]; });
+        c.fstart_.clear();
+        c.floops_.clear();
+        c.fnb_.clear();
+        for (int f : order) {
+            c.fstart_.push_back((int)c.floops_.size());
+            c.fnb_.push_back((int)d[fs[f]]);
+            const int m = (int)d[fs[f] + 1];
+            for (int j = 0; j < m; j++) c.floops_.push_back((int)d[fs[f] + 2 + j]);
+        }
+        c.has_poly_ = true;
+    }
+    static bool needs_polytope(const char *format) {
+        for (const char *f = format; *f; f++)
+            if (f[0] == '%' && f[1]) {
+                if (strchr("pPEeFAaftl", f[1])) return true;
+                f++;
+            }
+        return false;
+    }
     static bool contains_neighbor(const char *format) {
         for (const char *f = format; *f; f++)
             if (f[0] == '%' && f[1] == 'n') return true;
         return false;
     }
+    // the polytope fields of output_custom (src/cell.cc:2485-2558), printed
+    // as the reference's printers do (src/common.cc:37-136)
+    void poly_field(char f, int64_t k, double x, double y, double z, FILE *fp) {
+        voronoicell c;
+        load_polytope(c, &pdata_[poff_[k]]);
+        c.p = (int)(c.verts_.size() / 3);
+        std::vector<double> d;
+        std::vector<int> iv;
+        auto print_d = [&](const std::vector<double> &v) {
+            for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %g" : "%g", v[i]);
+        };
+        auto print_i = [&](const std::vector<int> &v) {
+            for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %d" : "%d", v[i]);
+        };
+        auto print_xyz = [&](const std::vector<double> &v, double ox, double oy, double oz) {
+            for (size_t i = 0; i < v.size(); i += 3)
+                fprintf(fp, i ? " (%g,%g,%g)" : "(%g,%g,%g)", ox + v[i], oy + v[i + 1], oz + v[i + 2]);
+        };
+        switch (f) {
+            case 'p': c.vertices(d); print_xyz(d, 0, 0, 0); break;
+            case 'P': c.vertices(d); print_xyz(d, x, y, z); break;
+            case 'o': c.vertex_orders(iv); print_i(iv); break;
+            case 'E': fprintf(fp, "%g", c.total_edge_distance()); break;
+            case 'e': c.face_perimeters(d); print_d(d); break;
+            case 'F': fprintf(fp, "%g", c.surface_area()); break;
+            case 'A': c.face_freq_table(iv); print_i(iv); break;
+            case 'a': c.face_orders(iv); print_i(iv); break;
+            case 'f': c.face_areas(d); print_d(d); break;
+            case 't': {
+                c.face_vertices(iv);
+                size_t i = 0;
+                bool first = true;
+                while (i < iv.size()) {
+                    const int m = iv[i++];
+                    fputs(first ? "(" : " (", fp);
+                    first = false;
+                    for (int j = 0; j < m; j++) fprintf(fp, j ? ",%d" : "%d", iv[i + j]);
+                    fputs(")", fp);
+                    i += m;
+                }
+            } break;
+            case 'l': c.normals(d); print_xyz(d, 0, 0, 0); break;
+        }
+    }
+
     void output_custom(const char *format, int64_t k, FILE *fp) {
         const double x = pos_[3 * k], y = pos_[3 * k + 1], z = pos_[3 * k + 2];
         const double *c = &cen_[3 * k];
@@ -316,7 +547,11 @@ class container_gpu_base {
                 case 'r': fprintf(fp, "%g", radius_at(k)); break;
                 case 'w': fprintf(fp, "%d", nv_[k]); break;
                 case 'o':
-                    for (int v = 0; v < nv_[k]; v++) fputs(v ? " 3" : "3", fp);
+                    if (poly_on_ && !poff_.empty()) {
+                        poly_field('o', k, x, y, z, fp);
+                    } else {   // every vertex the engine produces has order 3
+                        for (int v = 0; v < nv_[k]; v++) fputs(v ? " 3" : "3", fp);
+                    }
                     break;
                 case 'm': fprintf(fp, "%g", mr2_[k]); break;
                 case 'g': fprintf(fp, "%d", 3 * nv_[k] / 2); break;
@@ -329,8 +564,7 @@ class container_gpu_base {
                 case 'c': fprintf(fp, "%g %g %g", c[0], c[1], c[2]); break;
                 case 'C': fprintf(fp, "%g %g %g", x + c[0], y + c[1], z + c[2]); break;
                 case 'p': case 'P': case 'E': case 'e': case 'F': case 'A': case 'a': case 'f': case 't': case 'l':
-                    voro_fatal_error("print_custom: this field needs the cell polytope, which the GPU engine "
-                                     "does not return", VOROPP_INTERNAL_ERROR);
+                    poly_field(*f, k, x, y, z, fp);
                     break;
                 case 0: f--; break;
                 default:

@@ -72,6 +72,8 @@ typedef struct vgpu_stats {
     double bin_ms;            /* device time of binning, last compute */
     double step_ms;           /* device time of the whole compute (events on the handle's stream) */
     int64_t kernel_launches;  /* engine kernels launched by the last compute */
+    double clip_ms;           /* of kernel_ms: the main clipping kernel alone */
+    double finish_ms;         /* of kernel_ms: the FP64 finish kernel (mixed engine) */
 } vgpu_stats;
 
 /* Library / device. */
@@ -135,6 +137,21 @@ int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
  *   flags    VGPU_CELL_* bits */
 int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen,
                    int32_t *nfaces, int32_t *nverts, double *maxr2, int32_t *flags);
+/* Optional outputs of vgpu_compute (flags; default 0).  VGPU_OUTPUT_POLYTOPES
+ * keeps every cell's polytope — FP64 vertices and ordered face loops — for
+ * the queries that need the cell itself (voronoicell_base::vertices,
+ * face_vertices, face_areas, normals, ... src/cell.hh:132-184, and the
+ * print_custom fields %p %P %o %g %E %e %F %A %a %f %t %l, src/cell.cc:
+ * 2485-2558).  Applies from the next compute. */
+#define VGPU_OUTPUT_POLYTOPES 1
+int vgpu_set_output(vgpu_container *h, int flags);
+/* The polytopes of the last compute in loop order, CSR: offsets[n+1] (int64,
+ * in doubles) and data.  Cell k is data[offsets[k] .. offsets[k+1]):
+ *   nv, nf, vertices (3 nv doubles, relative to the particle), then per face:
+ *   neighbour ID, vertex count m, m vertex indices (a loop, clockwise seen
+ *   from outside, as the reference's face_vertices).
+ * Deleted and failed cells are empty.  data may be NULL to get the offsets. */
+int vgpu_get_polytopes(vgpu_container *h, int64_t *offsets, double *data);
 /* Stored radius of every cell's particle, in loop order (the r argument of
  * put; what container_poly::print_custom prints for %r, src/container.hh:
  * 660-671, reading p[ijk][4q+3]). */

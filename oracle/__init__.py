@@ -113,6 +113,28 @@ class _Lib:
 class RefLib(_Lib):
     path = REF_SO
 
+    def polytopes(self, w):
+        """The reference's polytope of every cell (parse_polytopes format)."""
+        f = self.lib.ref_polytopes
+        f.restype = ctypes.c_long
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_long, _f64p]
+        cap = max(1024, 300 * len(w["ids"]))
+        while True:
+            out = np.zeros(cap)
+            m = f(*_args(w), cap, out)
+            if m >= 0:
+                return parse_polytopes(out[:m])
+            cap = -m
+
+    def print_custom(self, w, fmt, path):
+        """The reference's container::print_custom(fmt, path) output."""
+        f = self.lib.ref_print_custom
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_char_p,
+                      ctypes.c_char_p]
+        if f(*_args(w), fmt.encode(), str(path).encode()) != 0:
+            raise ValueError("bad container kind")
+
     def time_compute_all(self, w):
         f = self.lib.ref_time_compute_all
         f.restype = ctypes.c_double
@@ -123,6 +145,37 @@ class RefLib(_Lib):
               np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), len(w["ids"]),
               w["ids"], w["xyzr"], ctypes.byref(sv))
         return t, sv.value
+
+
+def parse_polytopes(flat):
+    """Splits a flat polytope stream (see ref_polytopes in oracle/ref_capi.cc)
+    into per-cell dicts: ok, verts (nv,3), sa, ted, faces [(nb, area,
+    perimeter, normal(3), [vertex indices])]."""
+    cells = []
+    i = 0
+    n = len(flat)
+    while i < n:
+        ok, nv, nf, sa, ted = flat[i:i + 5]
+        i += 5
+        nv, nf = int(nv), int(nf)
+        verts = np.asarray(flat[i:i + 3 * nv]).reshape(nv, 3)
+        i += 3 * nv
+        faces = []
+        for _ in range(nf):
+            nb, order, area, perim, nx, ny, nz = flat[i:i + 7]
+            i += 7
+            order = int(order)
+            faces.append((int(nb), float(area), float(perim), (float(nx), float(ny), float(nz)),
+                          [int(v) for v in flat[i:i + order]]))
+            i += order
+        cells.append({"ok": bool(ok), "verts": verts, "sa": float(sa), "ted": float(ted), "faces": faces})
+    return cells
+
+
+def _args(w):
+    return (int(w["kind"]), np.asarray(w["geom"], np.float64), np.asarray(w["grid"], np.int32),
+            np.asarray([1 if p else 0 for p in w["periodic"]], np.int32), len(w["ids"]),
+            np.ascontiguousarray(w["ids"], np.int32), np.ascontiguousarray(w["xyzr"], np.float64))
 
 
 class PortLib(_Lib):

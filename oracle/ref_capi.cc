@@ -10,6 +10,7 @@
 //   3 container_periodic_poly (src/container_prd.hh:434-655)
 // Per-cell records follow the reference's own loop order: c_loop_all
 // (src/c_loops.hh:165-210) or c_loop_all_periodic (src/c_loops.hh:325-393).
+#include <algorithm>
 #include <chrono>
 #include <vector>
 #include "voro++.hh"
@@ -69,9 +70,107 @@ void run_cells(con_t &con, loop_t &vl, rec_sink &s) {
     if (s.nb_off) s.nb_off[s.n] = s.nb_used;
 }
 
+// Builds the container of the given kind, puts the particles, and calls
+// f(con, loop).  Returns false on an unknown kind.
+template <class F>
+bool with_container(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
+                    const double *xyzr, F f) {
+    if (kind == 0) {
+        container con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
+                      periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
+        for (int i = 0; i < n; i++) con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2]);
+        c_loop_all vl(con);
+        f(con, vl);
+    } else if (kind == 1) {
+        container_poly con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
+                           periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
+        for (int i = 0; i < n; i++)
+            con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2], xyzr[4 * i + 3]);
+        c_loop_all vl(con);
+        f(con, vl);
+    } else if (kind == 2) {
+        container_periodic con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2], 8);
+        for (int i = 0; i < n; i++) con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2]);
+        c_loop_all_periodic vl(con);
+        f(con, vl);
+    } else if (kind == 3) {
+        container_periodic_poly con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2], 8);
+        for (int i = 0; i < n; i++)
+            con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2], xyzr[4 * i + 3]);
+        c_loop_all_periodic vl(con);
+        f(con, vl);
+    } else {
+        return false;
+    }
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
+
+// The polytope of every cell in loop order, flattened into doubles:
+//   ok, nv, nf, surface_area, total_edge_distance, vertices (3 nv, particle-
+//   relative), then per face: neighbour, order, area, perimeter, normal (3),
+//   vertex indices (order)
+// with the faces in the reference's own traversal order (the one
+// neighbors / face_areas / face_vertices share, src/cell.cc:2189-2308).
+// Returns the number of doubles, or -(needed) if cap is too small.
+long ref_polytopes(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
+                   const double *xyzr, long cap, double *out) {
+    std::vector<double> buf;
+    bool ok = with_container(kind, geom, grid, periodic, n, ids, xyzr, [&](auto &con, auto &vl) {
+        voronoicell_neighbor c(con);
+        std::vector<int> nb, fv, fo;
+        std::vector<double> vs, fa, fp, nm;
+        if (!vl.start()) return;
+        do {
+            if (!con.compute_cell(c, vl)) {
+                buf.insert(buf.end(), {0.0, 0.0, 0.0, 0.0, 0.0});
+                continue;
+            }
+            c.vertices(vs);
+            c.neighbors(nb);
+            c.face_vertices(fv);
+            c.face_orders(fo);
+            c.face_areas(fa);
+            c.face_perimeters(fp);
+            c.normals(nm);
+            buf.push_back(1.0);
+            buf.push_back((double)c.p);
+            buf.push_back((double)nb.size());
+            buf.push_back(c.surface_area());
+            buf.push_back(c.total_edge_distance());
+            buf.insert(buf.end(), vs.begin(), vs.end());
+            size_t q = 0;
+            for (size_t f = 0; f < nb.size(); f++) {
+                const int ord = fv[q];
+                buf.push_back((double)nb[f]);
+                buf.push_back((double)ord);
+                buf.push_back(fa[f]);
+                buf.push_back(fp[f]);
+                buf.push_back(nm[3 * f]);
+                buf.push_back(nm[3 * f + 1]);
+                buf.push_back(nm[3 * f + 2]);
+                for (int j = 0; j < ord; j++) buf.push_back((double)fv[q + 1 + j]);
+                q += 1 + ord;
+            }
+        } while (vl.inc());
+    });
+    if (!ok) return 0;
+    if ((long)buf.size() > cap) return -(long)buf.size();
+    std::copy(buf.begin(), buf.end(), out);
+    return (long)buf.size();
+}
+
+// The reference's own print_custom output for every cell, written to path
+// (container::print_custom(format, filename), src/container.cc:401-417).
+int ref_print_custom(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
+                     const double *xyzr, const char *format, const char *path) {
+    bool ok = with_container(kind, geom, grid, periodic, n, ids, xyzr,
+                             [&](auto &con, auto &) { con.print_custom(format, path); });
+    return ok ? 0 : -2;
+}
 
 // Computes every cell with the reference and writes one record per stored
 // particle.  Returns the number of records, or -1 if a capacity was too small.

@@ -8,7 +8,75 @@ HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz")))
+    """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
+                  if not os.path.basename(p).startswith("poly_"))
+
+
+def poly_names():
+    return sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(HERE, "poly_*.npz")))
+
+
+def load_poly(name):
+    """The reference's polytopes of the first cells of fixture ``name`` (list
+    of dicts: ok, verts, sa, ted, faces [(nb, area, perimeter, normal, loop)])
+    and its print_custom text over every cell for the stored format."""
+    z = np.load(os.path.join(HERE, f"poly_{name}.npz"))
+    flat = z["flat"]
+    cells = []
+    i = 0
+    while i < len(flat):
+        ok, nv, nf, sa, ted = flat[i:i + 5]
+        i += 5
+        nv, nf = int(nv), int(nf)
+        verts = flat[i:i + 3 * nv].reshape(nv, 3)
+        i += 3 * nv
+        faces = []
+        for _ in range(nf):
+            nb, m, area, perim, nx, ny, nz = flat[i:i + 7]
+            i += 7
+            m = int(m)
+            faces.append((int(nb), float(area), float(perim), np.array([nx, ny, nz]), [int(v) for v in flat[i:i + m]]))
+            i += m
+        cells.append({"ok": bool(ok), "verts": verts, "sa": float(sa), "ted": float(ted), "faces": faces})
+    return cells, str(z["custom_format"]), str(z["custom_text"])
+
+
+def compare_custom_text(got, ref, rtol=2e-6, atol=1e-12):
+    """Line-by-line, token-by-token comparison of print_custom outputs: tokens
+    equal as text, or numbers equal to the last printed digit (%g prints six
+    significant digits, so values within rounding of a boundary may differ in
+    it)."""
+    import re
+    gl, rl = got.splitlines(), ref.splitlines()
+    if len(gl) != len(rl):
+        return [f"{len(gl)} lines vs reference {len(rl)}"]
+    num = re.compile(r"[-+0-9.eE]+")
+    errs = []
+    for li, (a, b) in enumerate(zip(gl, rl)):
+        if a == b:
+            continue
+        ta = re.split(r"([ (),])", a)
+        tb = re.split(r"([ (),])", b)
+        if len(ta) != len(tb):
+            errs.append(f"line {li}: {a!r} vs {b!r}")
+            continue
+        for x, y in zip(ta, tb):
+            if x == y:
+                continue
+            if num.fullmatch(x) and num.fullmatch(y):
+                try:
+                    fx, fy = float(x), float(y)
+                except ValueError:
+                    errs.append(f"line {li}: {x!r} vs {y!r}")
+                    break
+                if abs(fx - fy) <= max(rtol * max(abs(fx), abs(fy)), atol):
+                    continue
+            errs.append(f"line {li}: {x!r} vs {y!r} in {a!r} / {b!r}")
+            break
+        if len(errs) > 10:
+            break
+    return errs
 
 
 def load(name):

@@ -62,10 +62,44 @@ def cases():
     return out
 
 
+# Polytope fixtures: the reference's own polytope of the first POLY_CELLS cells
+# (vertices, faces in its traversal order with neighbour, area, perimeter,
+# normal and vertex loop; surface area; total edge distance) and its
+# print_custom output for every cell over the fields that do not depend on
+# vertex or face numbering.
+POLY_NAMES = ["unit_cube_1000", "radical_1200", "periodic_poly_800", "sparse_dropped_40", "degenerate_cubic_216"]
+POLY_CELLS = 200
+CUSTOM_FORMAT = "%i %q %r %w %s %v %c %C %m %g %F %E %A %o"
+
+
+def make_poly_fixtures(ref, all_cases):
+    import tempfile
+    for name in POLY_NAMES:
+        w = all_cases[name]
+        cells = ref.polytopes(w)[:POLY_CELLS]
+        flat = []
+        for c in cells:
+            flat += [1.0 if c["ok"] else 0.0, len(c["verts"]), len(c["faces"]), c["sa"], c["ted"]]
+            flat += list(np.asarray(c["verts"]).ravel())
+            for nb, area, perim, nrm, loop in c["faces"]:
+                flat += [nb, len(loop), area, perim, *nrm, *loop]
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "custom.txt")
+            ref.print_custom(w, CUSTOM_FORMAT, path)
+            text = open(path).read()
+        out = os.path.join(HERE, f"poly_{name}.npz")
+        np.savez_compressed(out, flat=np.asarray(flat, np.float64), ncells=len(cells),
+                            custom_format=np.array(CUSTOM_FORMAT), custom_text=np.array(text))
+        print(f"poly_{name}: {len(cells)} cells, {os.path.getsize(out)} bytes")
+
+
 def main():
     if not build_ref():
         raise SystemExit("reference sources not available; cannot generate fixtures")
     ref = RefLib()
+    if "--poly-only" in sys.argv:
+        make_poly_fixtures(ref, cases())
+        return
     for name, w in cases().items():
         rec = ref.compute(w)
         nb = []
@@ -81,6 +115,7 @@ def main():
             ids=rec.ids, pos=rec.pos, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, ok=rec.ok, mrs=rec.mrs,
             nb=nb_flat, nb_off=nb_off)
         print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
+    make_poly_fixtures(ref, cases())
 
 
 if __name__ == "__main__":

@@ -118,3 +118,30 @@ def test_shim_matches_reference_records(gpu, tmp_path, name):
     py = tmp_path / "custom_py.txt"
     con.print_custom(fmt, str(py))
     assert open(custom).read() == open(py).read()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["radical_1200", "unit_cube_1000"])
+def test_shim_polytope_fields(gpu, tmp_path, name):
+    """print_custom's polytope fields from the C++ header agree with the
+    Python mirror, and its numbering-independent fields with the reference."""
+    exe = _compile(tmp_path)
+    w, z = G.load(name)
+    _, ref_fmt, ref_text = G.load_poly(name)
+    inp = tmp_path / "in.txt"
+    _write_input(inp, w)
+    for fmt, ref in [("%i %p %P %o %g %E %e %F %A %a %f %t %l %n", None), (ref_fmt, ref_text)]:
+        custom = tmp_path / "custom.txt"
+        r = subprocess.run([exe, str(inp), str(tmp_path / "out.txt"), fmt, str(custom)], capture_output=True,
+                           text=True)
+        assert r.returncode == 0, r.stderr
+        got = open(custom).read()
+        if ref is None:
+            con = vg.from_workload(w, mode="mixed")
+            py = tmp_path / "custom_py.txt"
+            con.print_custom(fmt, str(py))
+            # unit normals of faces with areas near 1e-12 are only resolved to ~1e-10
+            errs = G.compare_custom_text(got, open(py).read(), atol=1e-9)
+        else:
+            errs = G.compare_custom_text(got, ref)
+        assert not errs, "\n".join(errs[:10])

@@ -1,0 +1,90 @@
+"""Cell polytopes from the engine (VGPU_OUTPUT_POLYTOPES) against the
+reference's own: same vertices (up to numbering), same faces with the same
+neighbour, area, perimeter, outward normal and vertex loop (up to rotation,
+same orientation), and print_custom output over the numbering-independent
+fields equal to the reference's text."""
+import numpy as np
+import pytest
+
+import voro_gb300 as vg
+from tests import _golden as G
+
+TOL = {"fp64": 1e-12, "mixed": 1e-10}
+
+
+def _is_rotation(a, b):
+    if len(a) != len(b):
+        return False
+    if not a:
+        return True
+    try:
+        i = b.index(a[0])
+    except ValueError:
+        return False
+    return b[i:] + b[:i] == a
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+@pytest.mark.parametrize("name", G.poly_names())
+def test_polytopes_match_reference(gpu, tmp_path, name, mode):
+    w, z = G.load(name)
+    cells, fmt, text = G.load_poly(name)
+    con = vg.from_workload(w, mode=mode)
+    con.set_polytopes(True)
+    con.compute_all_cells()
+    res = con.cells()
+    tol = TOL[mode]
+    for k, c in enumerate(cells):
+        pt = res.polytope(k)
+        if not c["ok"]:
+            assert pt is None
+            continue
+        rv = c["verts"]
+        assert pt.p == len(rv), f"cell {k}: {pt.p} vertices vs {len(rv)}"
+        scale = np.cbrt(z["vol"][k])
+        d = np.linalg.norm(pt.verts[:, None, :] - rv[None, :, :], axis=2)
+        m = d.argmin(axis=1)
+        assert d[np.arange(len(m)), m].max() <= tol * scale * 10, f"cell {k}: vertex positions"
+        assert len(set(m.tolist())) == len(m), f"cell {k}: vertex matching not one to one"
+        rf = sorted(c["faces"], key=lambda f: f[0])
+        assert [f[0] for f in pt.faces] == [f[0] for f in rf], f"cell {k}: neighbours"
+        areas, perims, normals = pt.face_areas(), pt.face_perimeters(), pt.normals()
+        nbs = [f[0] for f in rf]
+        for j, ((nb, loop), (rnb, ra, rp, rn, rloop)) in enumerate(zip(pt.faces, rf)):
+            if nbs.count(nb) > 1:
+                continue   # faces sharing a neighbour ID are matched as a group below
+            assert _is_rotation([int(m[v]) for v in loop], rloop), f"cell {k} face {nb}: loop"
+            assert abs(areas[j] - ra) <= tol * max(ra, scale * scale) * 10
+            assert abs(perims[j] - rp) <= tol * max(rp, scale) * 10
+            if ra > 1e-6 * scale * scale:
+                assert np.allclose(normals[j], rn, atol=1e-8)
+        for nb in set(nbs):
+            if nbs.count(nb) > 1:
+                ga = sorted(a for (n, _), a in zip(pt.faces, areas) if n == nb)
+                gr = sorted(f[1] for f in rf if f[0] == nb)
+                assert np.allclose(ga, gr, rtol=tol * 10, atol=tol * scale * scale * 10)
+        assert abs(pt.surface_area() - c["sa"]) <= tol * c["sa"] * 10
+        assert abs(pt.total_edge_distance() - c["ted"]) <= tol * c["ted"] * 10
+    out = tmp_path / "custom.txt"
+    con.print_custom(fmt, str(out))
+    errs = G.compare_custom_text(open(out).read(), text)
+    assert not errs, "\n".join(errs[:10])
+
+
+@pytest.mark.gpu
+def test_polytopes_through_a_batch(gpu):
+    name = "radical_1200"
+    w, z = G.load(name)
+    cells, _, _ = G.load_poly(name)
+    a = vg.from_workload(w, mode="mixed")
+    a.set_polytopes(True)
+    b = vg.batch([a])
+    b.compute_all_cells()
+    res = a.cells()
+    for k, c in enumerate(cells[:50]):
+        pt = res.polytope(k)
+        assert (pt is None) == (not c["ok"])
+        if pt is not None:
+            assert pt.p == len(c["verts"])
+            assert abs(pt.surface_area() - c["sa"]) <= 1e-9 * c["sa"]

@@ -1,0 +1,33 @@
+"""Host-side polytope queries (voro_gb300.Polytope, the basis of the
+print_custom fields %p %P %o %g %E %e %F %A %a %f %t %l and of the C++
+header's voronoicell queries) against the reference's own values, on the
+reference's polytopes: no GPU needed."""
+import numpy as np
+import pytest
+
+import voro_gb300 as vg
+from tests import _golden as G
+
+
+@pytest.mark.parametrize("name", G.poly_names())
+def test_polytope_queries_match_reference(name):
+    cells, _, _ = G.load_poly(name)
+    checked = 0
+    for c in cells:
+        if not c["ok"]:
+            continue
+        pt = vg.Polytope(c["verts"], [(f[0], f[4]) for f in c["faces"]])
+        areas = pt.face_areas()
+        perims = pt.face_perimeters()
+        normals = pt.normals()
+        for (nb, area, perim, nrm, loop), a, p_, n in zip(c["faces"], areas, perims, normals):
+            assert abs(a - area) <= 1e-12 * max(area, 1e-300) + 1e-14
+            assert abs(p_ - perim) <= 1e-12 * perim
+            if area > 1e-10:
+                assert np.allclose(n, nrm, atol=1e-9), (n, nrm)
+        assert abs(pt.surface_area() - c["sa"]) <= 1e-12 * c["sa"]
+        assert abs(pt.total_edge_distance() - c["ted"]) <= 1e-12 * c["ted"]
+        assert pt.number_of_edges() == sum(pt.vertex_orders()) // 2
+        assert sum(pt.face_freq_table()) == len(c["faces"])
+        checked += 1
+    assert checked > 0

@@ -28,6 +28,7 @@ VGPU_MIXED = 1
 VGPU_CELL_OK = 1
 VGPU_CELL_MARGINAL = 2
 VGPU_CELL_REPAIRED = 4
+VGPU_OUTPUT_POLYTOPES = 1
 VGPU_CELL_FAILED = 8   # bits 8-11: reason (1 planes, 2 adjacency, 3 vertices, 4 search)
 
 KIND_CONTAINER = 0
@@ -49,7 +50,7 @@ EXPORTED = [
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
-    "vgpu_batch_get_stats", "vgpu_batch_destroy",
+    "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_set_output", "vgpu_get_polytopes",
 ]
 
 
@@ -65,7 +66,8 @@ class Stats(ctypes.Structure):
                 ("planes_tested", ctypes.c_int64), ("planes_cut", ctypes.c_int64),
                 ("overflow_reruns", ctypes.c_int64), ("failed_cells", ctypes.c_int64),
                 ("kernel_ms", ctypes.c_double), ("bin_ms", ctypes.c_double), ("step_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("clip_ms", ctypes.c_double),
+                ("finish_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -115,6 +117,8 @@ def load_library(build_if_missing=True):
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
     lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
+    lib.vgpu_set_output.argtypes = [vp, ctypes.c_int]
+    lib.vgpu_get_polytopes.argtypes = [vp, vp, vp]
     lib.vgpu_batch_create.argtypes = [ctypes.POINTER(vp)]
     lib.vgpu_batch_add.argtypes = [vp, vp]
     lib.vgpu_batch_compute.argtypes = [vp, ctypes.c_int]
@@ -151,6 +155,8 @@ class CellResults:
         self.nf, self.nv, self.maxr2, self.flags = nf, nv, maxr2, flags
         self.nb, self.nb_off = nb, nb_off
         self.rad = None   # stored radii (put's r), filled by cells()
+        self.poly_off = None   # polytope CSR (VGPU_OUTPUT_POLYTOPES), filled by cells()
+        self.poly_data = None
 
     def __len__(self):
         return len(self.ids)
@@ -161,6 +167,100 @@ class CellResults:
 
     def neighbors(self, k):
         return self.nb[self.nb_off[k]:self.nb_off[k + 1]]
+
+    def polytope(self, k):
+        """Cell k's Polytope (needs the container's polytope output)."""
+        if self.poly_off is None:
+            raise ValueError("polytope output was not requested: call set_polytopes(True) before computing")
+        a, b = self.poly_off[k], self.poly_off[k + 1]
+        return Polytope.from_stream(self.poly_data[a:b]) if b > a else None
+
+
+class Polytope:
+    """One cell's polytope as the engine returns it (VGPU_OUTPUT_POLYTOPES):
+    vertices relative to the particle and faces as vertex loops, ordered by
+    neighbour ID like ``neighbors()``.  The query names follow
+    voronoicell_base (src/cell.hh:132-211) and compute the same quantities."""
+
+    def __init__(self, verts, faces):
+        self.verts = verts                      # (nv, 3)
+        self.faces = faces                      # [(neighbour, [vertex indices])]
+
+    @classmethod
+    def from_stream(cls, d):
+        nv, nf = int(d[0]), int(d[1])
+        verts = np.asarray(d[2:2 + 3 * nv]).reshape(nv, 3)
+        faces = []
+        i = 2 + 3 * nv
+        for _ in range(nf):
+            nb, m = int(d[i]), int(d[i + 1])
+            faces.append((nb, [int(v) for v in d[i + 2:i + 2 + m]]))
+            i += 2 + m
+        faces.sort(key=lambda f: f[0])          # stable: the order of neighbors()
+        return cls(verts, faces)
+
+    @property
+    def p(self):
+        return len(self.verts)
+
+    def vertices(self, x=0.0, y=0.0, z=0.0):
+        return self.verts + np.array([x, y, z])
+
+    def neighbors(self):
+        return [f[0] for f in self.faces]
+
+    def face_vertices(self):
+        return [f[1] for f in self.faces]
+
+    def face_orders(self):
+        return [len(f[1]) for f in self.faces]
+
+    def _newell(self, loop):
+        # twice the vector area, from vectors relative to the first vertex
+        # (small faces keep their precision)
+        P = self.verts[loop] - self.verts[loop[0]]
+        return np.cross(P[1:-1], P[2:]).sum(axis=0) if len(loop) > 2 else np.zeros(3)
+
+    def face_areas(self):
+        return [0.5 * float(np.linalg.norm(self._newell(f[1]))) for f in self.faces]
+
+    def normals(self):
+        """Outward unit normals (the loops run clockwise seen from outside)."""
+        out = []
+        for f in self.faces:
+            nrm = -self._newell(f[1])
+            ln = float(np.linalg.norm(nrm))
+            out.append(tuple(nrm / ln) if ln > 0 else (0.0, 0.0, 0.0))
+        return out
+
+    def face_perimeters(self):
+        out = []
+        for f in self.faces:
+            P = self.verts[f[1]]
+            out.append(float(np.linalg.norm(P - np.roll(P, -1, axis=0), axis=1).sum()))
+        return out
+
+    def surface_area(self):
+        return float(sum(self.face_areas()))
+
+    def total_edge_distance(self):
+        return 0.5 * float(sum(self.face_perimeters()))   # every edge bounds two faces
+
+    def vertex_orders(self):
+        cnt = np.zeros(len(self.verts), np.int64)
+        for f in self.faces:
+            cnt[f[1]] += 1
+        return [int(c) for c in cnt]
+
+    def number_of_edges(self):
+        return sum(self.vertex_orders()) // 2
+
+    def face_freq_table(self):
+        orders = self.face_orders()
+        v = [0] * (max(orders) + 1 if orders else 0)
+        for o in orders:
+            v[o] += 1
+        return v
 
 
 class _ContainerBase:
@@ -184,6 +284,16 @@ class _ContainerBase:
         self._pending_xyzr = []
         self._dirty = True
         self._dev_keep = None
+        self._polytopes = False
+
+    def set_polytopes(self, on=True):
+        """Keep every cell's polytope (vertices, face loops) from the next
+        compute on (VGPU_OUTPUT_POLYTOPES): what voronoicell's vertex and face
+        queries and the print_custom fields %p %P %o %g %E %e %F %A %a %f %t %l
+        need."""
+        self._polytopes = bool(on)
+        _check(self._lib.vgpu_set_output(self._h, VGPU_OUTPUT_POLYTOPES if on else 0))
+        self._dirty = True
 
     def __del__(self):
         try:
@@ -306,12 +416,21 @@ class _ContainerBase:
             nb = np.zeros(max(tot.value, 1), np.int32)
             _check(self._lib.vgpu_get_neighbors(self._h, _ptr(off), _ptr(nb)))
             res.nb, res.nb_off = nb[:tot.value], off
+        if self._polytopes:
+            poff = np.zeros(n + 1, np.int64)
+            _check(self._lib.vgpu_get_polytopes(self._h, _ptr(poff), None))
+            data = np.zeros(max(int(poff[-1]), 1))
+            _check(self._lib.vgpu_get_polytopes(self._h, _ptr(poff), _ptr(data)))
+            res.poly_off, res.poly_data = poff, data
         return res
 
     # ---- print_custom: src/container.hh:434-451, src/cell.cc:2485-2558
     def print_custom(self, fmt, fp=None):
         """Writes one line per computed cell with the reference's %-fields.
-        ``fp`` is a file object, a filename, or None (stdout)."""
+        ``fp`` is a file object, a filename, or None (stdout).  Fields that
+        need the polytope switch its output on and recompute."""
+        if _needs_polytope(fmt) and not self._polytopes:
+            self.set_polytopes(True)
         res = self.cells(neighbors=("%n" in fmt))
         close = False
         if fp is None:
@@ -329,6 +448,53 @@ class _ContainerBase:
         finally:
             if close:
                 fp.close()
+
+
+_POLY_FIELDS = "pPoEeFAaftl"
+
+
+def _needs_polytope(fmt):
+    i = 0
+    while i < len(fmt) - 1:
+        if fmt[i] == "%":
+            if fmt[i + 1] in _POLY_FIELDS and fmt[i + 1] != "o":
+                return True
+            i += 2
+        else:
+            i += 1
+    return False
+
+
+def _g(v):
+    return "%g" % v
+
+
+def _poly_field(f, c, x, y, z):
+    """A polytope field of output_custom (src/cell.cc:2485-2558), formatted as
+    the reference's printers (src/common.cc:37-136)."""
+    if f == "p":
+        return " ".join("(%g,%g,%g)" % tuple(v) for v in c.verts)
+    if f == "P":
+        return " ".join("(%g,%g,%g)" % (x + v[0], y + v[1], z + v[2]) for v in c.verts)
+    if f == "o":
+        return " ".join(str(o) for o in c.vertex_orders())
+    if f == "E":
+        return _g(c.total_edge_distance())
+    if f == "e":
+        return " ".join(_g(v) for v in c.face_perimeters())
+    if f == "F":
+        return _g(c.surface_area())
+    if f == "A":
+        return " ".join(str(v) for v in c.face_freq_table())
+    if f == "a":
+        return " ".join(str(v) for v in c.face_orders())
+    if f == "f":
+        return " ".join(_g(v) for v in c.face_areas())
+    if f == "t":
+        return " ".join("(" + ",".join(str(i) for i in loop) + ")" for loop in c.face_vertices())
+    if f == "l":
+        return " ".join("(%g,%g,%g)" % n for n in c.normals())
+    raise ValueError(f)
 
 
 def _vec(v):
@@ -365,7 +531,10 @@ def _format_custom(fmt, res, k, radius):
         elif f == "w":
             out.append("%d" % res.nv[k])
         elif f == "o":
-            out.append(" ".join(["3"] * int(res.nv[k])))
+            if res.poly_off is not None:
+                out.append(_poly_field("o", res.polytope(k), x, y, z))
+            else:   # every vertex the engine produces has order 3
+                out.append(" ".join(["3"] * int(res.nv[k])))
         elif f == "m":
             out.append("%g" % res.maxr2[k])
         elif f == "g":
@@ -381,8 +550,8 @@ def _format_custom(fmt, res, k, radius):
         elif f == "C":
             cx, cy, cz = res.cen[k]
             out.append("%g %g %g" % (x + cx, y + cy, z + cz))
-        elif f in "pPeEFAaftl":
-            raise NotImplementedError(f"print_custom field %{f} is not produced by the engine yet")
+        elif f in "pPEeFAaftl":
+            out.append(_poly_field(f, res.polytope(k), x, y, z))
         else:
             out.append("%" + f)
         i += 1

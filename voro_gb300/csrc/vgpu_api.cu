@@ -127,10 +127,13 @@ const OffsetTable &offset_table() {
 
 }  // namespace
 
-// Polytope record store of the split finish, words per cell (the mean record
-// of a uniform periodic box is about 215 words; a cell that finds the store
-// full is redone by the larger engine, which finishes inline).
-constexpr unsigned long long kRecWordsPerCell = 256;
+// Polytope record store, words per cell: the mean record of a uniform
+// periodic box is about 186 words with FP32 vertices (MIXED engine) and 268
+// with FP64 ones; a cell that finds the store full fails with
+// VGPU_FAIL_RECORDS.  Polytope output: 2 + 6 nv + 2 nf doubles per cell
+// (about 195).
+constexpr unsigned long long kRecWordsPerCell[2] = {384, 256};   // FP64, MIXED
+constexpr unsigned long long kPolyDoublesPerCell = 256;
 
 struct vgpu_container {
     Geometry g;
@@ -152,10 +155,12 @@ struct vgpu_container {
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, l32, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
-    DevBuf rec, rec_off;
+    DevBuf rec, rec_off, poly, poly_off;
     DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
     int nkept = 0;              // cells of the compute in progress
+    int output = 0;             // VGPU_OUTPUT_* flags
+    unsigned long long poly_used = 0;   // doubles of polytope output of the last compute
     long long launches0 = 0;    // launch counter at its start
     bool computed = false;
     vgpu_stats stats{};
@@ -307,7 +312,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64, &h->l32, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
-                      &h->r_pos, &h->r_rad, &h->rec, &h->rec_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+                      &h->r_pos, &h->r_rad, &h->rec, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -559,21 +564,32 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     return VGPU_OK;
 }
 
-// Split finish (MIXED engine): the clipping kernel writes polytope records,
-// the finish kernel reduces them.  Sets up the record store of h for cp.
-int setup_records(vgpu_container *h, int mode, CellParams &cp, unsigned long long *used_counter) {
+// The record store the clipping kernels write and the finish kernel reads,
+// and the optional polytope output, for the compute of h described by cp.
+int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt) {
     cp.rec = nullptr;
-    if (mode != VGPU_MIXED || h->nkept <= 0) return VGPU_OK;
+    cp.poly = nullptr;
+    if (h->nkept <= 0) return VGPU_OK;
     cudaStream_t s = h->stream;
-    const unsigned long long cap =
-        std::min<unsigned long long>((unsigned long long)h->nkept * kRecWordsPerCell + (1u << 20), 0xfffffff0ull);
+    const unsigned long long cap = std::min<unsigned long long>(
+        (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), 0xfffffff0ull);
     VG_CUDA(h->rec.ensure(cap * 4));
     VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 4));
     VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 4, s));
     cp.rec = h->rec.as<unsigned>();
     cp.rec_cap = cap;
-    cp.rec_used = used_counter;
+    cp.rec_used = &cnt->rec_used;
     cp.rec_off = h->rec_off.as<unsigned>();
+    if (h->output & VGPU_OUTPUT_POLYTOPES) {
+        const unsigned long long pcap = (unsigned long long)h->nkept * kPolyDoublesPerCell + (1u << 16);
+        VG_CUDA(h->poly.ensure(pcap * 8));
+        VG_CUDA(h->poly_off.ensure((size_t)h->nkept * 8));
+        VG_CUDA(cudaMemsetAsync(h->poly_off.p, 0xff, (size_t)h->nkept * 8, s));
+        cp.poly = h->poly.as<double>();
+        cp.poly_cap = pcap;
+        cp.poly_used = &cnt->poly_used;
+        cp.poly_off = h->poly_off.as<long long>();
+    }
     return VGPU_OK;
 }
 
@@ -613,11 +629,12 @@ int vgpu_compute(vgpu_container *h, int mode) {
     int rc = prepare_cells(h, mode, cp);
     if (rc != VGPU_OK) return rc;
     cudaStream_t s = h->stream;
-    rc = setup_records(h, mode, cp, &h->counters.as<Counters>()->rec_used);
+    rc = setup_records(h, mode, cp, h->counters.as<Counters>());
     if (rc != VGPU_OK) return rc;
+    // clipping (64-vertex engine, then the 128-vertex one for the cells that
+    // overflowed), then the finish kernel over every record
     cudaEventRecord(h->ev[2], s);
     VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
-    VG_CUDA(launch_finish(cp, h->sms, s));
     Counters c1;
     VG_CUDA(cudaMemcpyAsync(&c1, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
@@ -629,16 +646,64 @@ int vgpu_compute(vgpu_container *h, int mode) {
         cp2.ncells = (int)c1.overflow;
         cp2.cell_list = h->ovf_list.as<int>();
         cp2.overflow_list = nullptr;
-        cp2.rec = nullptr;   // the larger engine finishes its cells inline
         VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s));
         VG_CUDA(cudaMemcpyAsync(&c2, h->counters2.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     }
+    cudaEventRecord(h->ev[4], s);
+    VG_CUDA(launch_finish(cp, mode, h->sms, s));
     cudaEventRecord(h->ev[3], s);
+    unsigned long long pused = 0;
+    VG_CUDA(cudaMemcpyAsync(&pused, &h->counters.as<Counters>()->poly_used, 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
+    h->poly_used = pused;
     VG_CUDA(cudaGetLastError());
-    float cell_ms = 0;
+    float cell_ms = 0, clip_ms = 0, fin_ms = 0;
     cudaEventElapsedTime(&cell_ms, h->ev[2], h->ev[3]);
-    return finish_compute(h, c1, c2, cell_ms);
+    cudaEventElapsedTime(&clip_ms, h->ev[2], h->ev[4]);
+    cudaEventElapsedTime(&fin_ms, h->ev[4], h->ev[3]);
+    rc = finish_compute(h, c1, c2, cell_ms);
+    h->stats.clip_ms = clip_ms;
+    h->stats.finish_ms = fin_ms;
+    return rc;
+}
+
+int vgpu_set_output(vgpu_container *h, int flags) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (flags & ~VGPU_OUTPUT_POLYTOPES) return fail(VGPU_ERR_ARG, "unknown output flags 0x%x", flags);
+    h->output = flags;
+    h->computed = false;
+    return VGPU_OK;
+}
+
+int vgpu_get_polytopes(vgpu_container *h, int64_t *offsets, double *data) {
+    if (!h || !offsets) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    if (!(h->output & VGPU_OUTPUT_POLYTOPES))
+        return fail(VGPU_ERR_ARG, "polytope output was not requested (vgpu_set_output) for the last compute");
+    const size_t n = (size_t)h->ncells;
+    offsets[0] = 0;
+    if (n == 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    std::vector<long long> off(n);
+    VG_CUDA(cudaMemcpyAsync(off.data(), h->poly_off.p, n * 8, cudaMemcpyDeviceToHost, s));
+    const unsigned long long used = std::min<unsigned long long>(h->poly_used, h->poly.bytes / 8);
+    std::vector<double> store(used);
+    if (used > 0) VG_CUDA(cudaMemcpyAsync(store.data(), h->poly.p, used * 8, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < n; k++) {
+        if (off[k] == -2) return fail(VGPU_ERR_CAPACITY, "polytope output store full");
+        int64_t len = 0;
+        if (off[k] >= 0) {
+            if ((unsigned long long)off[k] + 2 > used)
+                return fail(VGPU_ERR_INTERNAL, "polytope offset %lld beyond the store (%llu)", off[k], used);
+            len = 2 + 6 * (int64_t)store[off[k]] + 2 * (int64_t)store[off[k] + 1];
+            if ((unsigned long long)(off[k] + len) > used)
+                return fail(VGPU_ERR_INTERNAL, "polytope of cell %zu runs beyond the store", k);
+        }
+        offsets[k + 1] = offsets[k] + len;
+        if (data && len > 0) memcpy(data + offsets[k], store.data() + off[k], (size_t)len * 8);
+    }
+    return VGPU_OK;
 }
 
 int vgpu_get_stats(vgpu_container *h, vgpu_stats *out) {
@@ -769,7 +834,7 @@ struct vgpu_batch {
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[2];
+    cudaEvent_t ev[4];
     DevBuf cps, starts, counters, work, ovf_list;
     vgpu_stats stats{};
 };
@@ -788,7 +853,7 @@ int vgpu_batch_create(vgpu_batch **out) {
         delete b;
         return fail(VGPU_ERR_CUDA, "stream creation failed");
     }
-    for (int i = 0; i < 2; i++) cudaEventCreate(&b->ev[i]);
+    for (int i = 0; i < 4; i++) cudaEventCreate(&b->ev[i]);
     *out = b;
     return VGPU_OK;
 }
@@ -805,7 +870,7 @@ int vgpu_batch_destroy(vgpu_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list};
     for (DevBuf *d : bufs) d->release();
-    for (int i = 0; i < 2; i++) cudaEventDestroy(b->ev[i]);
+    for (int i = 0; i < 4; i++) cudaEventDestroy(b->ev[i]);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return VGPU_OK;
@@ -833,7 +898,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         cps[i].cnt = b->counters.as<Counters>() + i;
         cps[i].cell_list = nullptr;
         cps[i].overflow_list = nullptr;
-        rc = setup_records(h, mode, cps[i], &cps[i].cnt->rec_used);
+        rc = setup_records(h, mode, cps[i], cps[i].cnt);
         if (rc != VGPU_OK) return rc;
         starts[i + 1] = starts[i] + h->nkept;
         cudaEventRecord(h->ev[2], h->stream);   // after the gather and the offsets upload
@@ -864,7 +929,6 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     bp.noffsets = (int)ot.codes.size();
     cudaEventRecord(b->ev[0], s);
     VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
-    if (mode == VGPU_MIXED) VG_CUDA(launch_finish_batch(bp, b->sms, s));
     unsigned long long novf = 0;
     VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
@@ -876,6 +940,8 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         bp2.work = wk + 2;
         VG_CUDA(launch_cells_batch(bp2, mode, 1, b->sms, s));
     }
+    cudaEventRecord(b->ev[2], s);
+    VG_CUDA(launch_finish_batch(bp, mode, b->sms, s));
     cudaEventRecord(b->ev[1], s);
     for (int i = 0; i < nc; i++) cudaEventRecord(b->members[i]->ev[3], s);
     std::vector<Counters> cs(nc);
@@ -889,6 +955,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     int first_err = VGPU_OK;
     for (int i = 0; i < nc; i++) {
         vgpu_container *h = b->members[i];
+        h->poly_used = cs[i].poly_used;
         int rc = finish_compute(h, cs[i], zero, cell_ms);
         if (rc != VGPU_OK && first_err == VGPU_OK) first_err = rc;
         vgpu_stats &t = b->stats;
@@ -904,6 +971,11 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     }
     const auto t2 = std::chrono::steady_clock::now();
     b->stats.kernel_ms = cell_ms;
+    float clip_ms = 0, fin_ms = 0;
+    cudaEventElapsedTime(&clip_ms, b->ev[0], b->ev[2]);
+    cudaEventElapsedTime(&fin_ms, b->ev[2], b->ev[1]);
+    b->stats.clip_ms = clip_ms;
+    b->stats.finish_ms = fin_ms;
     b->stats.bin_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     b->stats.step_ms = std::chrono::duration<double, std::milli>(t2 - t0).count();
     b->stats.kernel_launches = launch_count() - launches0;

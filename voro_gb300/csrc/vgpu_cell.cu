@@ -148,6 +148,7 @@ struct WarpShared {
     unsigned tri[32 * K];
     unsigned adj[32 * K];
     unsigned stage[48 * K];  // boundary edges of a cut (a | b<<8 | u<<16); final stage: edge list
+    unsigned char vmap[32 * K];   // finished cell: vertex slot -> compact index
     unsigned char startN[kMaxPlanes];
     unsigned char endN[kMaxPlanes];
     union {
@@ -927,164 +928,6 @@ struct Engine {
         }
     }
 
-    __device__ void finish() {
-        const int out = P.a.outpos[C.k];
-        if (C.overflow || C.deleted) {
-            write_empty();
-            return;
-        }
-        unsigned long long live = 0ull;
-#pragma unroll
-        for (int s = 0; s < K; s++)
-            if (Vm.test(lane + 32 * s)) {
-                const unsigned t = V.tri[s];
-                live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
-            }
-        live = warp_or64(live);
-        const int nf = __popcll(live);
-        const int nv = Vm.popc();
-        // neighbours (ascending plane slot order) and the FP64 planes of the live
-        // faces, written over the FP32 plane arrays
-        double4 *pl64 = MODE == VGPU_FP64 ? S.pl64x : reinterpret_cast<double4 *>(S.pl);
-        double4 mine[2];
-        bool has[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int p = lane + 32 * h;
-            has[h] = (live >> p) & 1ull;
-            if (has[h]) {
-                const int q = __popcll(live & ((1ull << p) - 1ull));
-                P.r.nb[(size_t)out * kMaxNb + q] = S.pid[p];
-                if (MODE != VGPU_FP64) mine[h] = plane64_slot<MODE, K>(P, S, C.me64, p);
-            }
-        }
-        if (MODE != VGPU_FP64) {
-            __syncwarp();
-#pragma unroll
-            for (int h = 0; h < 2; h++)
-                if (has[h]) pl64[lane + 32 * h] = mine[h];
-        }
-        __syncwarp();
-        // FP64 vertices: one residual correction of the FP32 vertex against its
-        // three FP64 planes (FP64 engine: already FP64)
-        double vx[K], vy[K], vz[K];
-        double mr2 = 0.0;
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            vx[s] = vy[s] = vz[s] = 0.0;
-            if (Vm.test(lane + 32 * s)) {
-                if (MODE == VGPU_FP64) {
-                    vx[s] = V.dx[s]; vy[s] = V.dy[s]; vz[s] = V.dz[s];
-                } else {
-                    const double3 r = refine_vertex_f64(pl64, V.tri[s], V.x[s], V.y[s], V.z[s]);
-                    vx[s] = r.x; vy[s] = r.y; vz[s] = r.z;
-                }
-                mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
-            }
-        }
-        // origin of the volume sums: one vertex of the cell, so that every term
-        // scales with the cell size rather than its distance from the particle
-        const int t0 = Vm.first();
-        double c0x = 0, c0y = 0, c0z = 0;
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            const double sx = __shfl_sync(kFull, vx[s], t0 & 31);
-            const double sy = __shfl_sync(kFull, vy[s], t0 & 31);
-            const double sz = __shfl_sync(kFull, vz[s], t0 & 31);
-            if ((t0 >> 5) == s) { c0x = sx; c0y = sy; c0z = sz; }
-        }
-        // vertices relative to c0, and the owned edges (t < u) listed compactly
-        int ne = 0;
-        unsigned own[K];
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            own[s] = 0;
-            const int t = lane + 32 * s;
-            if (Vm.test(t)) {
-                S.u.f.vx[t] = vx[s] - c0x;
-                S.u.f.vy[t] = vy[s] - c0y;
-                S.u.f.vz[t] = vz[s] - c0z;
-                const unsigned A3 = S.adj[t];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    const int u = (A3 >> (8 * e)) & 255u;
-                    if (u > t && u < 32 * K) own[s] |= 1u << e;
-                }
-                ne += __popc(own[s]);
-            }
-        }
-        // face points: the point of each live face closest to c0, relative to c0
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            if (has[h]) {
-                const int p = lane + 32 * h;
-                const double4 pl = pl64[p];
-                const double nn = pl.x * pl.x + pl.y * pl.y + pl.z * pl.z;
-                const double f = (pl.w - (pl.x * c0x + pl.y * c0y + pl.z * c0z)) / nn;
-                S.u.f.fx[p] = pl.x * f;
-                S.u.f.fy[p] = pl.y * f;
-                S.u.f.fz[p] = pl.z * f;
-            }
-        }
-        const int eincl = warp_incl_scan(ne, lane);
-        const int etot = __shfl_sync(kFull, eincl, 31);
-        {
-            int q = eincl - ne;
-#pragma unroll
-            for (int s = 0; s < K; s++)
-#pragma unroll
-                for (int e = 0; e < 3; e++)
-                    if ((own[s] >> e) & 1u) S.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
-        }
-        __syncwarp();
-        // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a point of face f
-        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-        for (int i = lane; i < etot; i += 32) {
-            const unsigned E = S.stage[i];
-            const int t = E & 255u, e = E >> 8;
-            const unsigned T = S.tri[t];
-            const int u = (S.adj[t] >> (8 * e)) & 255u;
-            const int px = tri_plane(T, e), py = tri_plane(T, e == 2 ? 0 : e + 1);
-            const double tx = S.u.f.vx[t], ty = S.u.f.vy[t], tz = S.u.f.vz[t];
-            const double ux = S.u.f.vx[u], uy = S.u.f.vy[u], uz = S.u.f.vz[u];
-            const double wx = ty * uz - tz * uy;
-            const double wy = tz * ux - tx * uz;
-            const double wz = tx * uy - ty * ux;
-            const double ax = S.u.f.fx[px], ay = S.u.f.fy[px], az = S.u.f.fz[px];
-            const double bx = S.u.f.fx[py], by = S.u.f.fy[py], bz = S.u.f.fz[py];
-            const double dy = bx * wx + by * wy + bz * wz;
-            const double dx = ax * wx + ay * wy + az * wz;
-            const double dd = dy - dx;
-            vs += dd;
-            cx += dd * (tx + ux) + dy * bx - dx * ax;
-            cy += dd * (ty + uy) + dy * by - dx * ay;
-            cz += dd * (tz + uz) + dy * bz - dx * az;
-        }
-        vs = warp_sumd(vs);
-        cx = warp_sumd(cx);
-        cy = warp_sumd(cy);
-        cz = warp_sumd(cz);
-        mr2 = warp_maxd(mr2);
-        if (lane == 0) {
-            const double vol = vs / 6.0;
-            P.r.vol[out] = vol;
-            // centroid threshold as src/cell.cc:1895 (raw doubled-coordinate sum = 48*volume)
-            if (48.0 * vol > P.g.tol_cu) {
-                const double f = 1.0 / (4.0 * vs);
-                P.r.cen[3 * out] = c0x + cx * f;
-                P.r.cen[3 * out + 1] = c0y + cy * f;
-                P.r.cen[3 * out + 2] = c0z + cz * f;
-            } else {
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-            }
-            P.r.nf[out] = nf;
-            P.r.nv[out] = nv;
-            P.r.maxr2[out] = mr2;
-            P.r.flags[out] = VGPU_CELL_OK | (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
-        }
-        __syncwarp();
-    }
-
     __device__ void run(int k) {
 #ifdef VGPU_PHASE_TIMING
         for (int i = 0; i < 8; i++) C.phase[i] = 0;
@@ -1094,23 +937,18 @@ struct Engine {
         PHASE_END(t_init, 0);
         search();
         PHASE_BEGIN(t_fin);
-        if (MODE == VGPU_MIXED && K == 2) {
-            // the main mixed engine never reduces inline: the finish kernel
-            // completes the cell from its record (the FP64 code stays out of
-            // this kernel); a full record store hands the cell to the larger
-            // engine, which finishes inline
-            if (!C.overflow && !C.deleted) {
-                if (emit_record()) {
-                    PHASE_END(t_fin, 5);
-                    return;
-                }
-                C.overflow = true;
-                C.fail_reason = VGPU_FAIL_RECORDS;
+        // no reductions here: the finish kernel completes the cell from its
+        // record, which keeps the FP64 code out of this kernel's instruction
+        // stream; a full record store fails the cell
+        if (!C.overflow && !C.deleted) {
+            if (emit_record()) {
+                PHASE_END(t_fin, 5);
+                return;
             }
-            write_empty();
-        } else {
-            finish();
+            C.overflow = true;
+            C.fail_reason = VGPU_FAIL_RECORDS;
         }
+        write_empty();
         PHASE_END(t_fin, 5);
     }
 
@@ -1119,6 +957,7 @@ struct Engine {
     //      slot order, with plane and vertex indices renumbered to match;
     //      false if the record store is full
     __device__ bool emit_record() {
+        constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;   // words per vertex position
         unsigned long long live = 0ull;
 #pragma unroll
         for (int s = 0; s < K; s++)
@@ -1129,7 +968,7 @@ struct Engine {
         live = warp_or64(live);
         const int nf = __popcll(live);
         const int nv = Vm.popc();
-        const unsigned words = (unsigned)(kRecHeader + 5 * nv + 3 * nf);
+        const unsigned words = (unsigned)(kRecHeader + (2 + VW) * nv + 3 * nf);
         unsigned long long off = 0;
         if (lane == 0) off = atomicAdd(P.rec_used, (unsigned long long)words);
         off = __shfl_sync(kFull, off, 0);
@@ -1142,12 +981,12 @@ struct Engine {
             R[3] = 0;
             R[4] = 0;
         }
-        // new indices: vertex slot -> rank among valid slots (startN), plane
-        // slot -> rank among live planes (endN); both tables are free now
+        // compact indices: vertex slot -> rank among valid slots (vmap),
+        // plane slot -> rank among live planes (endN, free once the cell is done)
 #pragma unroll
         for (int s = 0; s < K; s++) {
             const int t = lane + 32 * s;
-            if (Vm.test(t)) S.startN[t] = (unsigned char)Vm.rank(t);
+            if (Vm.test(t)) S.vmap[t] = (unsigned char)Vm.rank(t);
         }
 #pragma unroll
         for (int h = 0; h < 2; h++) {
@@ -1160,19 +999,29 @@ struct Engine {
         for (int s = 0; s < K; s++) {
             const int t = lane + 32 * s;
             if (Vm.test(t)) {
-                const int r = S.startN[t];
+                const int r = S.vmap[t];
                 const unsigned T = V.tri[s];
                 const unsigned A3 = S.adj[t];
                 rv[r] = (unsigned)S.endN[tri_plane(T, 0)] | ((unsigned)S.endN[tri_plane(T, 1)] << 8) |
                         ((unsigned)S.endN[tri_plane(T, 2)] << 16);
-                rv[nv + r] = (unsigned)S.startN[A3 & 255u] | ((unsigned)S.startN[(A3 >> 8) & 255u] << 8) |
-                             ((unsigned)S.startN[(A3 >> 16) & 255u] << 16);
-                rv[2 * nv + r] = __float_as_uint(V.x[s]);
-                rv[3 * nv + r] = __float_as_uint(V.y[s]);
-                rv[4 * nv + r] = __float_as_uint(V.z[s]);
+                rv[nv + r] = (unsigned)S.vmap[A3 & 255u] | ((unsigned)S.vmap[(A3 >> 8) & 255u] << 8) |
+                             ((unsigned)S.vmap[(A3 >> 16) & 255u] << 16);
+                if (MODE == VGPU_FP64) {
+                    const double c[3] = {V.dx[s], V.dy[s], V.dz[s]};
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        const unsigned long long b = (unsigned long long)__double_as_longlong(c[a]);
+                        rv[(2 + 2 * a) * nv + 2 * r] = (unsigned)b;
+                        rv[(2 + 2 * a) * nv + 2 * r + 1] = (unsigned)(b >> 32);
+                    }
+                } else {
+                    rv[2 * nv + r] = __float_as_uint(V.x[s]);
+                    rv[3 * nv + r] = __float_as_uint(V.y[s]);
+                    rv[4 * nv + r] = __float_as_uint(V.z[s]);
+                }
             }
         }
-        unsigned *rp = rv + 5 * nv;
+        unsigned *rp = rv + (2 + VW) * nv;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int q = lane + 32 * h;
@@ -1333,22 +1182,28 @@ __global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_batch_kernel(
     flush();
 }
 
-// ------------------------------------------------------------------ split finish
-// The FP64 reductions of cells whose polytope the clipping kernel wrote as a
-// compact record (layout in CellParams).  Kept out of the clipping kernel so
-// that its hot loop keeps the instruction cache to itself.  Same sums as
-// Engine::finish, except that each face's reference point is one of its own
-// vertices (the one of lowest index) rather than the plane's foot point, which
-// saves the FP64 divisions (the edge formula holds for any point of the face).
+// ------------------------------------------------------------------ finish
+// The FP64 reductions of every cell from the compact record its clipping
+// kernel wrote (layout in CellParams).  They run as a separate kernel so that
+// the clipping loop keeps the instruction cache to itself.  Vertices: the
+// MIXED engine's FP32 vertices get one FP64 residual correction against their
+// three FP64 planes (refine_vertex_rec); the FP64 engine's are used as they
+// are.  Volume and centroid: FP64 sums over edges relative to vertex 0 with
+// each face's reference point one of its own vertices (the edge formula holds
+// for any point of the face).  Optionally the polytope itself is written out.
+constexpr int kFinMaxV = 128;   // vertices (the 128-slot engine's capacity)
+constexpr int kFinMaxE = 192;   // edges (3 * kFinMaxV / 2)
+
 struct FinishShared {
-    unsigned tri[64];
-    unsigned adj[64];
-    int psrc[64], pshift[64];
-    int rep[64];                     // per face: its lowest vertex
-    double4 pl64[64];
-    float4 pn[64];                   // the FP64 plane normals rounded to FP32
-    double vx[64], vy[64], vz[64];   // FP64 vertices relative to c0
-    unsigned stage[96];              // owned edges (t < u)
+    unsigned tri[kFinMaxV];
+    unsigned adj[kFinMaxV];
+    int psrc[kMaxPlanes], pshift[kMaxPlanes];
+    int rep[kMaxPlanes];             // per face: its lowest vertex
+    int ford[kMaxPlanes];            // per face: its vertex count
+    double4 pl64[kMaxPlanes];
+    float4 pn[kMaxPlanes];           // the FP64 plane normals rounded to FP32
+    double vx[kFinMaxV], vy[kFinMaxV], vz[kFinMaxV];   // FP64 vertices relative to c0
+    unsigned stage[kFinMaxE];        // owned edges (t < u)
 };
 
 __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
@@ -1388,15 +1243,54 @@ __device__ __forceinline__ double3 refine_vertex_rec(const FinishShared &F, unsi
     return v;
 }
 
+// Warp sums of four values with few FP64 additions (the FP64 pipe bounds the
+// finish kernel): halves of the warp first fold different pairs, then
+// quarters different singles, then each quarter folds its own; the four sums
+// end in lanes 0, 8, 16, 24 and are broadcast.  Fixed order: deterministic.
+__device__ __forceinline__ void warp_sum4(double &a, double &b, double &c, double &d, int lane) {
+    const bool lo = lane < 16;
+    double k0 = lo ? a : c, k1 = lo ? b : d;
+    const double s0 = lo ? c : a, s1 = lo ? d : b;
+    k0 += __shfl_xor_sync(kFull, s0, 16);
+    k1 += __shfl_xor_sync(kFull, s1, 16);
+    const bool lo8 = (lane & 8) == 0;
+    double k = lo8 ? k0 : k1;
+    k += __shfl_xor_sync(kFull, lo8 ? k1 : k0, 8);
+    k += __shfl_xor_sync(kFull, k, 4);
+    k += __shfl_xor_sync(kFull, k, 2);
+    k += __shfl_xor_sync(kFull, k, 1);
+    a = __shfl_sync(kFull, k, 0);
+    b = __shfl_sync(kFull, k, 8);
+    c = __shfl_sync(kFull, k, 16);
+    d = __shfl_sync(kFull, k, 24);
+}
+
+// Warp maximum of non-negative doubles by their bit patterns (ordered like
+// the values), on the integer reduction unit instead of the FP64 pipe.
+__device__ __forceinline__ double warp_max_nonneg(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned mhi = __reduce_max_sync(kFull, hi);
+    const unsigned mlo = __reduce_max_sync(kFull, hi == mhi ? lo : 0u);
+    return __longlong_as_double((long long)(((unsigned long long)mhi << 32) | mlo));
+}
+
+__device__ __forceinline__ double rec_double(const unsigned *w) {
+    return __longlong_as_double((long long)((unsigned long long)w[0] | ((unsigned long long)w[1] << 32)));
+}
+
 // The reductions of cell k (engine order) from its record, if it has one.
+template <int MODE>
 __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int lane) {
+    constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;
+    constexpr int SL = kFinMaxV / 32;
     const unsigned off = P.rec_off[k];
     if (off == kNoRecord) return;
     const unsigned *R = P.rec + off;
     const int nv = (int)R[0], nf = (int)R[1];
     const unsigned fl = R[2];
     const unsigned *rv = R + kRecHeader;
-    const unsigned *rp = rv + 5 * nv;
+    const unsigned *rp = rv + (2 + VW) * nv;
     const double4 me = P.a.p64[k];
     const int out = P.a.outpos[k];
     // planes: neighbour IDs (plane order), sources, FP64 planes
@@ -1404,17 +1298,18 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         F.psrc[q] = (int)rp[q];
         F.pshift[q] = (int)rp[nf + q];
         F.rep[q] = 0x7fffffff;
+        F.ford[q] = 0;
         P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
         const double4 pl = plane64_rec(P, F, me, q);
         F.pl64[q] = pl;
         F.pn[q] = make_float4((float)pl.x, (float)pl.y, (float)pl.z, 0.0f);
     }
     __syncwarp();
-    unsigned tri[2];
-    double vx[2], vy[2], vz[2];
+    unsigned tri[SL];
+    double vx[SL], vy[SL], vz[SL];
     double mr2 = 0.0;
 #pragma unroll
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < SL; s++) {
         const int t = lane + 32 * s;
         tri[s] = 0;
         vx[s] = vy[s] = vz[s] = 0.0;
@@ -1422,15 +1317,23 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             tri[s] = rv[t];
             F.tri[t] = tri[s];
             F.adj[t] = rv[nv + t];
-            const double3 r = refine_vertex_rec(F, tri[s], __uint_as_float(rv[2 * nv + t]),
-                                                __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
-            vx[s] = r.x;
-            vy[s] = r.y;
-            vz[s] = r.z;
+            if (MODE == VGPU_FP64) {
+                vx[s] = rec_double(rv + 2 * nv + 2 * t);
+                vy[s] = rec_double(rv + 4 * nv + 2 * t);
+                vz[s] = rec_double(rv + 6 * nv + 2 * t);
+            } else {
+                const double3 r = refine_vertex_rec(F, tri[s], __uint_as_float(rv[2 * nv + t]),
+                                                    __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
+                vx[s] = r.x;
+                vy[s] = r.y;
+                vz[s] = r.z;
+            }
             mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
-            atomicMin(&F.rep[tri_plane(tri[s], 0)], t);
-            atomicMin(&F.rep[tri_plane(tri[s], 1)], t);
-            atomicMin(&F.rep[tri_plane(tri[s], 2)], t);
+#pragma unroll
+            for (int e = 0; e < 3; e++) {
+                atomicMin(&F.rep[tri_plane(tri[s], e)], t);
+                atomicAdd(&F.ford[tri_plane(tri[s], e)], 1);
+            }
         }
     }
     // origin of the sums: vertex 0
@@ -1438,9 +1341,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     const double c0y = __shfl_sync(kFull, vy[0], 0);
     const double c0z = __shfl_sync(kFull, vz[0], 0);
     int ne = 0;
-    unsigned own[2];
+    unsigned own[SL];
 #pragma unroll
-    for (int s = 0; s < 2; s++) {
+    for (int s = 0; s < SL; s++) {
         own[s] = 0;
         const int t = lane + 32 * s;
         if (t < nv) {
@@ -1459,7 +1362,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     {
         int q = eincl - ne;
 #pragma unroll
-        for (int s = 0; s < 2; s++)
+        for (int s = 0; s < SL; s++)
 #pragma unroll
             for (int e = 0; e < 3; e++)
                 if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
@@ -1488,11 +1391,8 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         cy += dd * (ty + uy) + dy * by - dx * ay;
         cz += dd * (tz + uz) + dy * bz - dx * az;
     }
-    vs = warp_sumd(vs);
-    cx = warp_sumd(cx);
-    cy = warp_sumd(cy);
-    cz = warp_sumd(cz);
-    mr2 = warp_maxd(mr2);
+    warp_sum4(vs, cx, cy, cz, lane);
+    mr2 = warp_max_nonneg(mr2);
     if (lane == 0) {
         const double vol = vs / 6.0;
         P.r.vol[out] = vol;
@@ -1509,17 +1409,70 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         P.r.maxr2[out] = mr2;
         P.r.flags[out] = VGPU_CELL_OK | (int)fl;
     }
+    if (P.poly != nullptr) {
+        // the polytope: [nv, nf, vertices (3 nv, particle-relative), then per
+        // face (plane order): neighbour ID, vertex count, vertex loop]; each
+        // loop walks the face by the edges that start on it, which orders the
+        // vertices clockwise seen from outside, as the reference's
+        // face_vertices does (src/cell.cc:2285-2308)
+        const unsigned long long need = 2ull + 6ull * (unsigned long long)nv + 2ull * (unsigned long long)nf;
+        unsigned long long po = 0;
+        if (lane == 0) po = atomicAdd(P.poly_used, need);
+        po = __shfl_sync(kFull, po, 0);
+        if (po + need <= P.poly_cap) {
+            double *D = P.poly + po;
+            if (lane == 0) {
+                D[0] = (double)nv;
+                D[1] = (double)nf;
+            }
+#pragma unroll
+            for (int s = 0; s < SL; s++) {
+                const int t = lane + 32 * s;
+                if (t < nv) {
+                    D[2 + 3 * t] = vx[s];
+                    D[3 + 3 * t] = vy[s];
+                    D[4 + 3 * t] = vz[s];
+                }
+            }
+            double *DF = D + 2 + 3 * nv;
+            for (int q0 = 0; q0 < nf; q0 += 32) {
+                const int q = q0 + lane;
+                const int ord = q < nf ? F.ford[q] : 0;
+                // faces before q: q0 * 2 header words plus their orders
+                int before = 0;
+                for (int j = 0; j < q0; j++) before += F.ford[j];
+                const int incl = warp_incl_scan(ord, lane);
+                if (q < nf) {
+                    double *df = DF + 2 * q + before + (incl - ord);
+                    df[0] = (double)P.r.nb[(size_t)out * kMaxNb + q];
+                    df[1] = (double)ord;
+                    int t = F.rep[q];
+                    for (int j = 0; j < ord; j++) {
+                        df[2 + j] = (double)t;
+                        const unsigned T = F.tri[t];
+                        const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
+                        t = (F.adj[t] >> (8 * e)) & 255u;
+                    }
+                }
+            }
+            if (lane == 0) P.poly_off[out] = (long long)po;
+        } else if (lane == 0) {
+            P.poly_off[out] = -2;   // store full
+        }
+    }
     __syncwarp();
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(128) finish_kernel(const __grid_constant__ CellParams P) {
     __shared__ FinishShared fsh[4];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * 4;
-    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) finish_record(P, fsh[wid], k, lane);
+    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) finish_record<MODE>(P, fsh[wid], k, lane);
 }
 
 // The same over the cells of a batch (global numbering as cell_batch_kernel).
+template <int MODE>
 __global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant__ BatchParams B) {
     __shared__ FinishShared fsh[4];
     __shared__ __align__(16) unsigned char cpw[4][(sizeof(CellParams) + 15) & ~(size_t)15];
@@ -1543,7 +1496,7 @@ __global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant
             for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
             __syncwarp();
         }
-        if (P.rec != nullptr) finish_record(P, fsh[wid], (int)(g - cbeg), lane);
+        finish_record<MODE>(P, fsh[wid], (int)(g - cbeg), lane);
     }
 }
 
@@ -1683,32 +1636,43 @@ cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms
     return big ? launch_batch_one<VGPU_MIXED, 4>(bp, sms, s) : launch_batch_one<VGPU_MIXED, 2>(bp, sms, s);
 }
 
-cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s) {
-    if (cp.ncells <= 0 || cp.rec == nullptr) return cudaSuccess;
+template <int MODE>
+cudaError_t launch_finish_t(const CellParams &cp, int sms, cudaStream_t s) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel<MODE>, 128, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
     const long long need = (cp.ncells + 3) / 4;
     const int grid = (int)(want < need ? want : need);
-    finish_kernel<<<grid, 128, 0, s>>>(cp);
+    finish_kernel<MODE><<<grid, 128, 0, s>>>(cp);
     note_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_finish_batch(const BatchParams &bp, int sms, cudaStream_t s) {
-    if (bp.ncells <= 0) return cudaSuccess;
+cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s) {
+    if (cp.ncells <= 0 || cp.rec == nullptr) return cudaSuccess;
+    return mode == VGPU_FP64 ? launch_finish_t<VGPU_FP64>(cp, sms, s) : launch_finish_t<VGPU_MIXED>(cp, sms, s);
+}
+
+template <int MODE>
+cudaError_t launch_finish_batch_t(const BatchParams &bp, int sms, cudaStream_t s) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel<MODE>, 128, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
     const long long need = (bp.ncells + 3) / 4;
     const int grid = (int)(want < need ? want : need);
-    finish_batch_kernel<<<grid, 128, 0, s>>>(bp);
+    finish_batch_kernel<MODE><<<grid, 128, 0, s>>>(bp);
     note_launch();
     return cudaGetLastError();
+}
+
+cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s) {
+    if (bp.ncells <= 0) return cudaSuccess;
+    return mode == VGPU_FP64 ? launch_finish_batch_t<VGPU_FP64>(bp, sms, s)
+                             : launch_finish_batch_t<VGPU_MIXED>(bp, sms, s);
 }
 
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s) {

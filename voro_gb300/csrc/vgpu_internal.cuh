@@ -71,6 +71,7 @@ struct Counters {
     unsigned long long overflow_work;
     unsigned long long failed;     // batched launches: cells that overflowed every capacity
     unsigned long long rec_used;   // words of the polytope record store in use
+    unsigned long long poly_used;  // doubles of the polytope output in use
     unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
 };
 
@@ -89,16 +90,22 @@ struct CellParams {
     int group_lb2[kMaxGroups];
     unsigned box_tri[8];    // initial box: corner triangles and neighbours
     unsigned box_adj[8];
-    // Split finish (MIXED engine): the clipping kernel writes each finished
-    // polytope as a record here and a separate kernel does the FP64
-    // reductions; NULL: reductions inline.  Record layout (32-bit words):
-    // [ns, np, flags, vmask_lo, vmask_hi, tri[ns], adj[ns], x[ns], y[ns], z[ns],
-    //  psrc[np], pshift[np], pid[np]] with ns / np one past the highest used
-    // vertex / plane slot.
+    // The clipping kernels write each finished polytope as a record here and
+    // the finish kernel does the FP64 reductions.  Record layout (32-bit words):
+    // [nv, nf, flags, 0, 0, tri[nv], adj[nv], positions, psrc[nf], pshift[nf],
+    //  pid[nf]] over the cell's valid vertices and live planes, renumbered
+    // compactly; positions are x[nv], y[nv], z[nv] as FP32 (MIXED engine) or
+    // as FP64 word pairs (FP64 engine).
     unsigned *rec;
     unsigned long long rec_cap;     // words
     unsigned long long *rec_used;   // bump allocator (words)
     unsigned *rec_off;              // per engine index: record offset, kNoRecord if none
+    // Optional polytope output (written by the finish kernel), NULL: none.
+    // Per cell [nv, nf, vertices (3 nv), per face: neighbour, count, loop].
+    double *poly;
+    unsigned long long poly_cap;    // doubles
+    unsigned long long *poly_used;  // bump allocator (doubles)
+    long long *poly_off;            // per loop-order cell: offset, -1 none, -2 store full
 };
 constexpr unsigned kNoRecord = 0xffffffffu;
 constexpr int kRecHeader = 5;
@@ -155,8 +162,8 @@ cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorde
 // vgpu_cell.cu
 cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s);
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
-cudaError_t launch_finish(const CellParams &cp, int sms, cudaStream_t s);
-cudaError_t launch_finish_batch(const BatchParams &bp, int sms, cudaStream_t s);
+cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s);
+cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s);
 cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n,
                                      int *out, cudaStream_t s);
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);

@@ -289,13 +289,16 @@ def run_ours(args):
         h2d = ids_pin.nbytes + xyzr_pin.nbytes
         d2h = 0
         times = []
+        pinned = lambda shape, dt: torch.empty(tuple(shape), dtype=getattr(torch, np.dtype(dt).name),
+                                               pin_memory=True).numpy()
+        res = None
         for it in range(args.warmup + args.steps):
             barrier()
             t0 = time.perf_counter()
             con2.clear()
             con2.put_xyzr(ids_pin, xyzr_pin)
             con2.compute_all_cells()
-            res = con2.cells(neighbors=True)
+            res = con2.cells(neighbors=True, out=res, alloc=pinned)
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             if it >= args.warmup:

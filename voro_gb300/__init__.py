@@ -397,25 +397,42 @@ class _ContainerBase:
         _check(self._lib.vgpu_num_cells(self._h, ctypes.byref(n)))
         return n.value
 
-    def cells(self, neighbors=True):
-        """All per-cell results (CellResults) from the last compute."""
+    def cells(self, neighbors=True, out=None, alloc=None):
+        """All per-cell results (CellResults) from the last compute.
+        ``out``: the CellResults of an earlier call, whose arrays are reused
+        when they fit; ``alloc(shape, dtype)``: allocator for new arrays (for
+        example pinned host memory, which the device copies faster)."""
         self._ensure()
         n = self.total_particles()
-        ids = np.zeros(n, np.int32); pos = np.zeros((n, 3)); vol = np.zeros(n); cen = np.zeros((n, 3))
-        nf = np.zeros(n, np.int32); nv = np.zeros(n, np.int32); mr2 = np.zeros(n); fl = np.zeros(n, np.int32)
+        alloc = alloc or (lambda shape, dt: np.empty(shape, dt))
+
+        def get(name, shape, dt, at_least=False):
+            a = getattr(out, "_buf_" + name, None) if out is not None else None
+            size = int(np.prod(shape))
+            if a is not None and a.dtype == np.dtype(dt) and (a.size >= size if at_least else a.shape == shape):
+                return a
+            return alloc(shape, dt)
+
+        ids = get("ids", (n,), np.int32); pos = get("pos", (n, 3), np.float64); vol = get("vol", (n,), np.float64)
+        cen = get("cen", (n, 3), np.float64); nf = get("nf", (n,), np.int32); nv = get("nv", (n,), np.int32)
+        mr2 = get("mr2", (n,), np.float64); fl = get("fl", (n,), np.int32)
         _check(self._lib.vgpu_get_cells(self._h, _ptr(ids), _ptr(pos), _ptr(vol), _ptr(cen), _ptr(nf),
                                         _ptr(nv), _ptr(mr2), _ptr(fl)))
         res = CellResults(ids, pos, vol, cen, nf, nv, mr2, fl)
-        rad = np.zeros(n)
+        rad = get("rad", (n,), np.float64)
         _check(self._lib.vgpu_get_radii(self._h, _ptr(rad)))
         res.rad = rad
+        for name, a in (("ids", ids), ("pos", pos), ("vol", vol), ("cen", cen), ("nf", nf), ("nv", nv),
+                        ("mr2", mr2), ("fl", fl), ("rad", rad)):
+            setattr(res, "_buf_" + name, a)
         if neighbors:
             tot = ctypes.c_int64(0)
             _check(self._lib.vgpu_num_neighbors(self._h, ctypes.byref(tot)))
-            off = np.zeros(n + 1, np.int64)
-            nb = np.zeros(max(tot.value, 1), np.int32)
-            _check(self._lib.vgpu_get_neighbors(self._h, _ptr(off), _ptr(nb)))
-            res.nb, res.nb_off = nb[:tot.value], off
+            off = get("nb_off", (n + 1,), np.int64)
+            nbuf = get("nb", (max(tot.value, 1),), np.int32, at_least=True)
+            _check(self._lib.vgpu_get_neighbors(self._h, _ptr(off), _ptr(nbuf)))
+            res.nb, res.nb_off = nbuf[:tot.value], off
+            res._buf_nb, res._buf_nb_off = nbuf, off
         if self._polytopes:
             poff = np.zeros(n + 1, np.int64)
             _check(self._lib.vgpu_get_polytopes(self._h, _ptr(poff), None))

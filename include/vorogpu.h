@@ -137,6 +137,12 @@ int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
  *   flags    VGPU_CELL_* bits */
 int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen,
                    int32_t *nfaces, int32_t *nverts, double *maxr2, int32_t *flags);
+/* Autotuner: times vgpu_compute over a set of engine-grid densities
+ * (particles per engine block) on this container's own particles, keeps the
+ * fastest (as vgpu_set_tuning would) and leaves the results of a compute with
+ * it.  No counterpart in the reference (a tuning choice of this engine). */
+int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms);
+
 /* Optional outputs of vgpu_compute (flags; default 0).  VGPU_OUTPUT_POLYTOPES
  * keeps every cell's polytope — FP64 vertices and ordered face loops — for
  * the queries that need the cell itself (voronoicell_base::vertices,
@@ -174,8 +180,9 @@ int vgpu_phase_cycles(vgpu_container *h, double out[8]);
  * volumes (double[n]) and face counts (int32[n]). */
 int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t **dev_nfaces);
 
-/* Engine tuning: target particles per engine block (0 = default) and warps per
- * CTA (0 = default).  Applies from the next compute. */
+/* Engine tuning: target particles per engine block (0 = default 1.5) and warps
+ * (cells in flight) per CTA of the clipping kernel, 1-4 (0 = default 4).
+ * Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
 
 /* ---- batches: many containers computed by one persistent launch ----

@@ -50,3 +50,14 @@ def test_recompute_is_deterministic(gpu):
     b = con.cells()
     assert np.array_equal(a.vol, b.vol)
     assert np.array_equal(a.nb, b.nb)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results(gpu):
+    """The engine-grid density changes the search, never the cells."""
+    w, z = G.load("periodic_2000")
+    con = vg.from_workload(w, mode="mixed")
+    d, ms = con.autotune()
+    assert 0.3 <= d <= 3.0 and ms > 0
+    errs = G.compare_cells(con.cells(), z, *TOL["mixed"], label="autotuned")
+    assert not errs, "\n".join(errs)

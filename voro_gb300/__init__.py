@@ -51,6 +51,7 @@ EXPORTED = [
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
     "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_set_output", "vgpu_get_polytopes",
+    "vgpu_autotune",
 ]
 
 
@@ -118,6 +119,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_get_radii.argtypes = [vp, vp]
     lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
     lib.vgpu_set_output.argtypes = [vp, ctypes.c_int]
+    lib.vgpu_autotune.argtypes = [vp, ctypes.c_int, pd, pd]
     lib.vgpu_get_polytopes.argtypes = [vp, vp, vp]
     lib.vgpu_batch_create.argtypes = [ctypes.POINTER(vp)]
     lib.vgpu_batch_add.argtypes = [vp, vp]
@@ -353,6 +355,16 @@ class _ContainerBase:
         self._dev_keep = None
         _check(self._lib.vgpu_clear(self._h))
         self._dirty = True
+
+    def autotune(self, mode=None):
+        """Times the compute over a set of engine-grid densities on this
+        container's particles and keeps the fastest; returns
+        (particles per block, ms per compute)."""
+        self._flush_pending()
+        d, t = ctypes.c_double(0), ctypes.c_double(0)
+        _check(self._lib.vgpu_autotune(self._h, self._mode_code(mode), ctypes.byref(d), ctypes.byref(t)))
+        self._dirty = False
+        return d.value, t.value
 
     def set_tuning(self, particles_per_block=0.0, warps_per_cta=0):
         _check(self._lib.vgpu_set_tuning(self._h, float(particles_per_block), int(warps_per_cta)))

@@ -387,6 +387,7 @@ int vgpu_clear(vgpu_container *h) {
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
     if (particles_per_block > 0) h->target_density = particles_per_block;
+    if (warps_per_cta > 4) return fail(VGPU_ERR_ARG, "at most 4 warps per CTA (got %d)", warps_per_cta);
     if (warps_per_cta > 0) h->warps_per_cta = warps_per_cta;
     return VGPU_OK;
 }
@@ -634,7 +635,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     // clipping (64-vertex engine, then the 128-vertex one for the cells that
     // overflowed), then the finish kernel over every record
     cudaEventRecord(h->ev[2], s);
-    VG_CUDA(launch_cells(cp, mode, 0, h->sms, s));
+    VG_CUDA(launch_cells(cp, mode, 0, h->sms, s, h->warps_per_cta));
     Counters c1;
     VG_CUDA(cudaMemcpyAsync(&c1, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
@@ -646,7 +647,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
         cp2.ncells = (int)c1.overflow;
         cp2.cell_list = h->ovf_list.as<int>();
         cp2.overflow_list = nullptr;
-        VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s));
+        VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s, h->warps_per_cta));
         VG_CUDA(cudaMemcpyAsync(&c2, h->counters2.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     }
     cudaEventRecord(h->ev[4], s);
@@ -664,6 +665,33 @@ int vgpu_compute(vgpu_container *h, int mode) {
     rc = finish_compute(h, c1, c2, cell_ms);
     h->stats.clip_ms = clip_ms;
     h->stats.finish_ms = fin_ms;
+    return rc;
+}
+
+int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    // engine-grid densities to try (particles per block); the search visits
+    // fewer, fuller blocks as the density grows, and the best point depends
+    // on the container's shape and particle count
+    static const double kDensities[] = {0.35, 0.5, 0.6, 0.75, 0.9, 1.0, 1.25, 1.5, 2.0, 3.0};
+    double best = h->target_density, best_t = 1e300;
+    for (double d : kDensities) {
+        h->target_density = d;
+        double t = 1e300;
+        for (int rep = 0; rep < 2; rep++) {   // the first compute of a size also allocates
+            int rc = vgpu_compute(h, mode);
+            if (rc != VGPU_OK) return rc;
+            t = std::min(t, (double)h->stats.step_ms);
+        }
+        if (t < best_t) {
+            best_t = t;
+            best = d;
+        }
+    }
+    h->target_density = best;
+    int rc = vgpu_compute(h, mode);   // leave the results of the chosen setting
+    if (best_density) *best_density = best;
+    if (best_ms) *best_ms = best_t;
     return rc;
 }
 

@@ -121,11 +121,6 @@ __device__ __forceinline__ double warp_sumd(double x) {
     for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFull, x, d);
     return x;
 }
-__device__ __forceinline__ double warp_maxd(double x) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x = fmax(x, __shfl_xor_sync(kFull, x, d));
-    return x;
-}
 __device__ __forceinline__ int warp_incl_scan(int x, int lane) {
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -242,40 +237,6 @@ VGPU_HELPER VertexF32 solve_vertex_f32(const float4 *pl, const float4 *pe, unsig
     const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
     o.r2 = r * r;
     return o;
-}
-
-// FP64 vertex of triangle t: one residual correction of the FP32 vertex
-// (x,y,z) against its three FP64 planes; ill-conditioned vertices are solved
-// directly in FP64.
-VGPU_HELPER double3 refine_vertex_f64(const double4 *pl64, unsigned t, float fx, float fy, float fz) {
-    const double4 A = pl64[tri_plane(t, 0)], B = pl64[tri_plane(t, 1)], Cq = pl64[tri_plane(t, 2)];
-    const double x = fx, y = fy, z = fz;
-    const double ra = A.w - fma(A.x, x, fma(A.y, y, A.z * z));
-    const double rb = B.w - fma(B.x, x, fma(B.y, y, B.z * z));
-    const double rc = Cq.w - fma(Cq.x, x, fma(Cq.y, y, Cq.z * z));
-    const float ax = (float)A.x, ay = (float)A.y, az = (float)A.z;
-    const float bx = (float)B.x, by = (float)B.y, bz = (float)B.z;
-    const float cx = (float)Cq.x, cy = (float)Cq.y, cz = (float)Cq.z;
-    const float bcx = by * cz - bz * cy, bcy = bz * cx - bx * cz, bcz = bx * cy - by * cx;
-    const float cax = cy * az - cz * ay, cay = cz * ax - cx * az, caz = cx * ay - cy * ax;
-    const float abx = ay * bz - az * by, aby = az * bx - ax * bz, abz = ax * by - ay * bx;
-    const float D = ax * bcx + ay * bcy + az * bcz;
-    const float scale = (fabsf(ax) + fabsf(ay) + fabsf(az)) * (fabsf(bx) + fabsf(by) + fabsf(bz)) *
-                        (fabsf(cx) + fabsf(cy) + fabsf(cz));
-    double3 v;
-    if (fabsf(D) > 1e-3f * scale) {
-        // well conditioned: one correction step is exact to ~1e-14
-        const float fra = (float)ra, frb = (float)rb, frc = (float)rc;
-        const float inv = 1.0f / D;
-        v.x = x + (double)((fra * bcx + frb * cax + frc * abx) * inv);
-        v.y = y + (double)((fra * bcy + frb * cay + frc * aby) * inv);
-        v.z = z + (double)((fra * bcz + frb * caz + frc * abz) * inv);
-    } else {
-        double DD;
-        float kn;
-        solve_f64(A, B, Cq, v.x, v.y, v.z, DD, kn);
-    }
-    return v;
 }
 
 // ------------------------------------------------------------------ warp sort of candidate keys
@@ -1539,8 +1500,7 @@ __global__ void sum_volumes_kernel(const double *vol, const int *flags, int n, d
 }
 
 template <int MODE, int K>
-cudaError_t launch_one(const CellParams &cp, int sms, cudaStream_t s) {
-    const int warps = 4;
+cudaError_t launch_one(const CellParams &cp, int warps, int sms, cudaStream_t s) {
     const size_t off_bytes = ((size_t)cp.noffsets * sizeof(int) + 15) & ~(size_t)15;
     const size_t smem = off_bytes + warps * sizeof(WarpShared<MODE, K>);
     cudaError_t e = cudaFuncSetAttribute(cell_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1620,12 +1580,13 @@ cudaError_t upload_box_tables() {
     return cudaMemcpyToSymbol(c_box_adj, adj, sizeof(adj));
 }
 
-cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s) {
+cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps) {
     if (cp.ncells <= 0) return cudaSuccess;
+    warps = warps < 1 ? 4 : (warps > 4 ? 4 : warps);   // the kernels are built for at most 4 warps per CTA
     if (mode == VGPU_FP64) {
-        return big ? launch_one<VGPU_FP64, 4>(cp, sms, s) : launch_one<VGPU_FP64, 2>(cp, sms, s);
+        return big ? launch_one<VGPU_FP64, 4>(cp, warps, sms, s) : launch_one<VGPU_FP64, 2>(cp, warps, sms, s);
     }
-    return big ? launch_one<VGPU_MIXED, 4>(cp, sms, s) : launch_one<VGPU_MIXED, 2>(cp, sms, s);
+    return big ? launch_one<VGPU_MIXED, 4>(cp, warps, sms, s) : launch_one<VGPU_MIXED, 2>(cp, warps, sms, s);
 }
 
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s) {

@@ -160,7 +160,7 @@ cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorde
                                    int nkept, int *dup_flag, cudaStream_t s);
 
 // vgpu_cell.cu
-cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s);
+cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps = 4);
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
 cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s);
 cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s);

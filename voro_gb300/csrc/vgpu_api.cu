@@ -141,7 +141,7 @@ struct vgpu_container {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[6];
-    double target_density = 1.5;
+    double target_density = 0.6;   // the autotuner's choice on the 4M periodic box
     int warps_per_cta = 4;
     // particles put() so far, staged on the device in put() order
     int64_t staged = 0;

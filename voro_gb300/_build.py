@@ -15,9 +15,11 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libvorogpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu", "vgpu_noalloc.cu"]
+SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu", "vgpu_clip_mixed.cu", "vgpu_clip_fp64.cu",
+           "vgpu_finish.cu", "vgpu_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "1444"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wno-deprecated-declarations",
+              "-diag-suppress", "1444"]
 
 
 def _nvcc():
@@ -62,10 +64,12 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None, out=None
         if verbose and log:
             print(log)
         if p.returncode != 0:
-            # nvcc has crashed (SIGSEGV) on aarch64 hosts under parallel load: retry
-            # serially, then once more without line tables
+            # nvcc has crashed (SIGSEGV) on aarch64 hosts, not reproducibly: retry
+            # serially, again, then without line tables, and last with a lower
+            # ptxas optimisation level
             ok = False
-            for fl in (flags, [f for f in flags if f != "-lineinfo"]):
+            nolines = [f for f in flags if f != "-lineinfo"]
+            for fl in (flags, flags, nolines, nolines + ["-Xptxas", "-O2"]):
                 cmd = [nvcc] + ARCH + fl + ["-c", os.path.join(CSRC, src), "-o", obj]
                 r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
                 if r.returncode == 0:

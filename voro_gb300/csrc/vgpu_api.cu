@@ -15,7 +15,6 @@
 #include <atomic>
 
 namespace vgpu {
-cudaError_t upload_box_tables();
 static std::atomic<long long> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
@@ -83,8 +82,6 @@ struct DevBuf {
     T *as() const { return reinterpret_cast<T *>(p); }
 };
 
-std::mutex g_dev_mutex;
-bool g_box_uploaded[64] = {false};
 
 struct OffsetTable {
     std::vector<int> codes;
@@ -253,11 +250,6 @@ int ensure_device(vgpu_container *h) {
     int dev = 0;
     VG_CUDA(cudaGetDevice(&dev));
     h->device = dev;
-    std::lock_guard<std::mutex> lock(g_dev_mutex);
-    if (dev >= 0 && dev < 64 && !g_box_uploaded[dev]) {
-        VG_CUDA(upload_box_tables());
-        g_box_uploaded[dev] = true;
-    }
     return VGPU_OK;
 }
 

@@ -1,1465 +1,10 @@
-// The per-cell engine: one warp computes one Voronoi cell.
-//
-// It replaces voro_compute::compute_cell (src/v_compute.cc:289-621) and the
-// voronoicell_base plane-cutting engine (nplane, src/cell.cc:718-870;
-// create_facet 874-1364; collapse_order2/1 1376-1464; delete_connection
-// 1472-1513; plane_intersects 2366-2409) plus the per-cell reductions
-// (volume 1584-1616, centroid 1861-1901, number_of_faces 2168-2187,
-// neighbors 2660-2678), with a different representation chosen for warps:
-//
-//  * A cell is a convex polyhedron stored by its vertices.  Every vertex is
-//    the meeting point of three planes (a,b,c), stored as a "triangle" of
-//    plane indices oriented so that det(n_a,n_b,n_c) > 0 (faces counter-
-//    clockwise seen from outside), plus the three neighbouring vertices across
-//    its three edges.  Lane l owns vertex slots l, l+32, ... in registers;
-//    an empty slot holds a NaN position, so it never tests outside a plane.
-//  * A candidate plane is tested against all vertices at once (one side test
-//    per lane and slot, then a ballot).  The common case — the plane misses —
-//    costs a handful of instructions.  A cut removes the vertices outside,
-//    stages the boundary of the removed region (a cycle of edges) in shared
-//    memory, and every free slot of rank r builds the new vertex for boundary
-//    edge r, so slot assignment needs only a population count.
-//  * Side tests run in FP32 (MIXED mode) under a forward error bound: a test
-//    is certain when |value| exceeds the bound plus the reference tolerance;
-//    otherwise it is redone in FP64 from the planes' double-precision source.
-//    A vertex still inside the reference's tolerance band (|value| <= tol,
-//    src/cell.cc:2050-2059) marks the cell MARGINAL: there the reference
-//    merges vertices and the topology depends on its insertion order.
-//  * Candidates come from the engine's own block grid, gathered shell by shell
-//    in order of the blocks' lower-bound distance and sorted by (power)
-//    distance inside a batch, with the same radius cut-off as the reference's
-//    r_ctest / r_scale_check (src/rad_option.hh:320-341,387-431).
-//  * Final vertices are rebuilt in FP64 from their three planes (one
-//    residual-correction step from the FP32 vertex); volume and centroid are
-//    accumulated in FP64 over the cell's edges, relative to one of its vertices.
-#include <cfloat>
-#include <cstdio>
+// Dispatch of the cell engine's kernels and the small kernels over its
+// results (CSR neighbour lists, volume sums).
 #include "vgpu_dev.cuh"
 
 namespace vgpu {
 
 namespace {
-
-// Initial box: eight corners as plane triangles and their neighbours.  Planes
-// 0..5 are -x,+x,-y,+y,-z,+z.  Filled from the host (see build_box_tables).
-__constant__ unsigned c_box_tri[8];
-__constant__ unsigned c_box_adj[8];
-
-// ------------------------------------------------------------------ masks
-// Slot s of lane l is bit l+32s.
-template <int K>
-struct Mask {
-    static constexpr int W = (K + 1) / 2;
-    unsigned long long w[W];
-    __device__ __forceinline__ void clear() {
-#pragma unroll
-        for (int i = 0; i < W; i++) w[i] = 0ull;
-    }
-    __device__ __forceinline__ bool test(int t) const { return (w[t >> 6] >> (t & 63)) & 1ull; }
-    __device__ __forceinline__ int popc() const {
-        int c = 0;
-#pragma unroll
-        for (int i = 0; i < W; i++) c += __popcll(w[i]);
-        return c;
-    }
-    __device__ __forceinline__ bool any() const {
-        unsigned long long o = 0;
-#pragma unroll
-        for (int i = 0; i < W; i++) o |= w[i];
-        return o != 0ull;
-    }
-    __device__ __forceinline__ bool equals(const Mask &o) const {
-        bool e = true;
-#pragma unroll
-        for (int i = 0; i < W; i++) e = e && (w[i] == o.w[i]);
-        return e;
-    }
-    // number of set bits below bit t
-    __device__ __forceinline__ int rank(int t) const {
-        int c = 0;
-        const int wi = t >> 6;
-#pragma unroll
-        for (int i = 0; i < W; i++) {
-            if (i < wi) c += __popcll(w[i]);
-            else if (i == wi) c += __popcll(w[i] & ((1ull << (t & 63)) - 1ull));
-        }
-        return c;
-    }
-    // lowest set bit, or -1
-    __device__ __forceinline__ int first() const {
-#pragma unroll
-        for (int i = 0; i < W; i++)
-            if (w[i]) return i * 64 + __ffsll((long long)w[i]) - 1;
-        return -1;
-    }
-};
-
-template <int K>
-__device__ __forceinline__ Mask<K> ballot_mask(const bool (&pred)[K]) {
-    Mask<K> m;
-    m.clear();
-#pragma unroll
-    for (int s = 0; s < K; s++) {
-        unsigned b = __ballot_sync(kFull, pred[s]);
-        m.w[s >> 1] |= (unsigned long long)b << (32 * (s & 1));
-    }
-    return m;
-}
-
-__device__ __forceinline__ unsigned long long warp_or64(unsigned long long x) {
-    unsigned lo = __reduce_or_sync(kFull, (unsigned)x);
-    unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
-    return ((unsigned long long)hi << 32) | lo;
-}
-__device__ __forceinline__ float warp_maxf(float x) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, d));
-    return x;
-}
-__device__ __forceinline__ double warp_sumd(double x) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFull, x, d);
-    return x;
-}
-__device__ __forceinline__ int warp_incl_scan(int x, int lane) {
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(kFull, x, d);
-        if (lane >= d) x += y;
-    }
-    return x;
-}
-
-// ------------------------------------------------------------------ shared memory per warp
-template <int MODE, int K>
-struct WarpShared {
-    float4 pl[kMaxPlanes];   // plane n.x, n.y, n.z, h  (n.v <= h inside)
-    float4 pe[kMaxPlanes];   // |n|, en (abs error of n), eh (abs error of h), |h|
-    // (pl and pe are contiguous: at the end of a cell they hold the FP64 planes)
-    double4 pl64x[MODE == VGPU_FP64 ? kMaxPlanes : 1];   // FP64 planes (FP64 engine, during the search)
-    int pid[kMaxPlanes];     // neighbour ID of the plane
-    int psrc[kMaxPlanes];    // engine index of the generating particle, -1 for initial faces
-    int pshift[kMaxPlanes];  // packed periodic image counts (initial faces: face index)
-    unsigned tri[32 * K];
-    unsigned adj[32 * K];
-    unsigned stage[48 * K];  // boundary edges of a cut (a | b<<8 | u<<16); final stage: edge list
-    unsigned char vmap[32 * K];   // finished cell: vertex slot -> compact index
-    unsigned char startN[kMaxPlanes];
-    unsigned char endN[kMaxPlanes];
-    union {
-        struct {
-            unsigned ck[kCandBuf];    // sort keys
-            int cj[kCandBuf];         // engine index
-            int cs[kCandBuf];         // packed periodic image counts
-            float4 cd[kCandBuf];      // plane (FP32): n, h
-            float4 ce[kCandBuf];      // en, eh, |n|, rs
-            double4 cd64[MODE == VGPU_FP64 ? kCandBuf : 1];  // plane (FP64), FP64 engine
-        } c;
-        struct {
-            double vx[32 * K], vy[32 * K], vz[32 * K];   // FP64 vertices relative to c0
-            double fx[kMaxPlanes], fy[kMaxPlanes], fz[kMaxPlanes];  // face points relative to c0
-        } f;
-    } u;
-};
-
-// ------------------------------------------------------------------ per-lane vertex registers
-template <int MODE, int K>
-struct Verts {
-    unsigned tri[K];
-    float x[K], y[K], z[K];   // FP32 position (NaN = empty slot)
-    float a[K], e[K];         // |v| and the forward error bound of the position
-    float r2[K];              // bound on |v|^2 (0 for empty)
-    double dx[K], dy[K], dz[K];   // FP64 engine positions (NaN = empty)
-};
-
-struct CellCtx {
-    double4 me64;     // particle (remapped position, radius)
-    float4 me32;      // local coords, radius
-    int bi, bj, bk;   // engine block coordinates
-    int k;            // engine index
-    float R2;         // upper bound of max |v|^2
-    float cutoff2;    // squared distance bound for candidates / blocks
-    float ri2;        // particle radius squared (poly)
-    bool deleted, overflow, marginal, repaired;
-    int fail_reason;  // why overflow was set (VGPU_FAIL_*)
-    unsigned long long freeplanes;
-    int ncand;
-    unsigned tests, repairs, ptested, pcut;
-#ifdef VGPU_PHASE_TIMING
-    unsigned long long phase[8];
-#endif
-};
-
-// ------------------------------------------------------------------ out-of-line helpers
-// The vertex solve, its FP64 refinement and the key sorts.  They are inlined by
-// default (measured faster on the 4M periodic box: 16.9M vs 15.3M cells/s);
-// -DVGPU_OUTLINE=1 keeps one out-of-line copy of each instead, which shrinks
-// the kernel's code at the price of spills around the calls.
-#ifndef VGPU_OUTLINE
-#define VGPU_OUTLINE 0
-#endif
-#if VGPU_OUTLINE
-#define VGPU_HELPER __device__ __noinline__
-#else
-#define VGPU_HELPER __device__ __forceinline__
-#endif
-struct VertexF32 {
-    float x, y, z, a, e, r2;
-    bool good;
-};
-
-// Vertex of planes (a,b,c) of triangle t in FP32, with a forward error bound e
-// covering the planes' own storage error (pe: |n|, en, eh, |h|) and the
-// rounding of this Cramer solve: |adj(A)| <= |n_b||n_c| + |n_c||n_a| + |n_a||n_b|
-// and every row's error is at most rho.
-VGPU_HELPER VertexF32 solve_vertex_f32(const float4 *pl, const float4 *pe, unsigned t) {
-    const int a = tri_plane(t, 0), b = tri_plane(t, 1), c = tri_plane(t, 2);
-    const float4 A = pl[a], B = pl[b], Cc = pl[c];
-    const float4 EA = pe[a], EB = pe[b], EC = pe[c];
-    const float bcx = B.y * Cc.z - B.z * Cc.y, bcy = B.z * Cc.x - B.x * Cc.z, bcz = B.x * Cc.y - B.y * Cc.x;
-    const float cax = Cc.y * A.z - Cc.z * A.y, cay = Cc.z * A.x - Cc.x * A.z, caz = Cc.x * A.y - Cc.y * A.x;
-    const float abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
-    const float D = A.x * bcx + A.y * bcy + A.z * bcz;
-    const float inv = 1.0f / D;
-    VertexF32 o;
-    o.x = (A.w * bcx + B.w * cax + Cc.w * abx) * inv;
-    o.y = (A.w * bcy + B.w * cay + Cc.w * aby) * inv;
-    o.z = (A.w * bcz + B.w * caz + Cc.w * abz) * inv;
-    o.a = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-    const float cof = fmaf(EB.x, EC.x, fmaf(EC.x, EA.x, EA.x * EB.x));
-    const float r8 = 8.0f * kU32;
-    const float ra = fmaf(EA.y, o.a, EA.z) + r8 * fmaf(EA.x, o.a, EA.w);
-    const float rb = fmaf(EB.y, o.a, EB.z) + r8 * fmaf(EB.x, o.a, EB.w);
-    const float rc = fmaf(EC.y, o.a, EC.z) + r8 * fmaf(EC.x, o.a, EC.w);
-    o.e = 2.0f * cof * fmaxf(ra, fmaxf(rb, rc)) / fabsf(D) + r8 * o.a;
-    o.good = D > 0.0f && isfinite(o.e) && isfinite(o.a);
-    if (!o.good) o.e = 3.0e38f;  // every test on it is repaired in FP64
-    const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
-    o.r2 = r * r;
-    return o;
-}
-
-// ------------------------------------------------------------------ warp sort of candidate keys
-VGPU_HELPER unsigned bitonic32(unsigned x, int lane) {
-#pragma unroll
-    for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            unsigned y = __shfl_xor_sync(kFull, x, j);
-            bool up = (lane & k) == 0;
-            bool lower = (lane & j) == 0;
-            x = (lower == up) ? min(x, y) : max(x, y);
-        }
-    }
-    return x;
-}
-VGPU_HELPER uint2 bitonic64(unsigned x0, unsigned x1, int lane) {
-#pragma unroll 1
-    for (int k = 2; k <= 64; k <<= 1) {
-#pragma unroll 1
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j == 32) {
-                unsigned a = min(x0, x1), b = max(x0, x1);
-                x0 = a;
-                x1 = b;
-            } else {
-                unsigned y0 = __shfl_xor_sync(kFull, x0, j);
-                unsigned y1 = __shfl_xor_sync(kFull, x1, j);
-                bool lower = (lane & j) == 0;
-                bool up0 = (lane & k) == 0;
-                bool up1 = ((lane + 32) & k) == 0;
-                x0 = (lower == up0) ? min(x0, y0) : max(x0, y0);
-                x1 = (lower == up1) ? min(x1, y1) : max(x1, y1);
-            }
-        }
-    }
-    return make_uint2(x0, x1);
-}
-
-// FP64 plane of an existing plane slot of a cell
-template <int MODE, int K>
-__device__ __forceinline__ double4 plane64_slot(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int p) {
-    const int src = S.psrc[p];
-    if (src >= 0) return plane64_from(P, me, src, S.pshift[p]);
-    return face64(P, me, S.pshift[p]);
-}
-
-// FP64 re-test of the vertices whose FP32 test against candidate cb was
-// uncertain (bit s of uncbits: slot s of this lane, vertex planes tri_s).
-// Returns the outside bits; *marginal is set for tolerance-band hits.
-template <int MODE, int K>
-__device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int cb,
-                                              unsigned uncbits, unsigned tri0, unsigned tri1, unsigned tri2,
-                                              unsigned tri3, bool *marginal) {
-    unsigned outbits = 0;
-    bool anym = false;
-    if (uncbits) {
-        const double4 Q = plane64_from(P, me, S.u.c.cj[cb], S.u.c.cs[cb]);
-        for (int s = 0; s < K; s++) {
-            if (!((uncbits >> s) & 1u)) continue;
-            const unsigned t = s == 0 ? tri0 : (s == 1 ? tri1 : (s == 2 ? tri2 : tri3));
-            const double4 A = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 0));
-            const double4 B = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 1));
-            const double4 Cq = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 2));
-            double x, y, z, D;
-            float kn;
-            solve_f64(A, B, Cq, x, y, z, D, kn);
-            const double v = fma(Q.x, x, fma(Q.y, y, fma(Q.z, z, -Q.w)));
-            const double vv = sqrt(x * x + y * y + z * z);
-            const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
-            const double verr = 16.0 * kU64 * (double)kn / fabs(D) + 64.0 * kU64 * vv;
-            const double bnd = nq * verr + 8.0 * kU64 * (nq * vv + fabs(Q.w)) + P.g.tol_h;
-            if (!(D > 0.0)) anym = true;
-            else if (v > bnd) outbits |= 1u << s;
-            else if (v >= -bnd) anym = true;
-        }
-    }
-    *marginal = anym;
-    return outbits;
-}
-
-// A vertex whose FP32 solve is ill-conditioned (error bound above
-// kVertexTrust of its distance, or the determinant's sign lost) is solved in
-// FP64 from the planes' double-precision source instead and rounded to FP32;
-// its error bound is then the FP64 solve's plus that rounding.  Only nearly
-// degenerate plane triples (as in jittered lattices) get here: FP64 runs at a
-// small fraction of the FP32 rate, so the threshold is high and the code is
-// kept out of line.  (At 1e-4 about 1 % of vertices came here and the 4M
-// periodic box ran 1.8x slower.)
-constexpr float kVertexTrust = 1e-2f;
-
-template <int MODE, int K>
-__device__ __noinline__ VertexF32 vertex_f64_fallback(const CellParams &P, const WarpShared<MODE, K> &S, double4 me,
-                                                      unsigned t) {
-    const double4 A = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 0));
-    const double4 B = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 1));
-    const double4 Cq = plane64_slot<MODE, K>(P, S, me, tri_plane(t, 2));
-    double x, y, z, D;
-    float kn;
-    solve_f64(A, B, Cq, x, y, z, D, kn);
-    VertexF32 o;
-    const double vv = sqrt(x * x + y * y + z * z);
-    o.x = (float)x;
-    o.y = (float)y;
-    o.z = (float)z;
-    o.a = (float)vv;
-    const double verr = 16.0 * kU64 * (double)kn / fabs(D) + 64.0 * kU64 * vv;
-    o.e = (float)(verr * (1.0 + 1e-6)) + 4.0f * kU32 * o.a;
-    o.good = D > 0.0 && isfinite(o.e) && isfinite(o.a);
-    if (!o.good) o.e = 3.0e38f;   // every test on it is repaired in FP64
-    const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
-    o.r2 = r * r;
-    return o;
-}
-
-// Optional per-phase clock accounting (diagnostics builds: -DVGPU_PHASE_TIMING).
-// Phases: 0 init, 1 block/candidate gather, 2 sort, 3 side tests, 4 cuts, 5 finish.
-#ifdef VGPU_PHASE_TIMING
-#define PHASE_BEGIN(v) const long long v = clock64()
-#define PHASE_END(v, ph) C.phase[ph] += (unsigned long long)(clock64() - (v))
-#else
-#define PHASE_BEGIN(v)
-#define PHASE_END(v, ph)
-#endif
-
-// ------------------------------------------------------------------ the engine
-template <int MODE, int K>
-struct Engine {
-    const CellParams &P;
-    WarpShared<MODE, K> &S;
-    const int *offsets;   // shared copy of the offset table
-    const int lane;
-    Verts<MODE, K> V;
-    Mask<K> Vm;           // valid vertex slots
-    CellCtx C;
-
-    __device__ Engine(const CellParams &p, WarpShared<MODE, K> &s, const int *off, int l)
-        : P(p), S(s), offsets(off), lane(l) {}
-
-    __device__ __forceinline__ void clear_slot(int s) {
-        V.x[s] = V.y[s] = V.z[s] = __int_as_float(0x7fffffff);
-        V.a[s] = V.e[s] = 0.0f;
-        V.r2[s] = 0.0f;
-        V.tri[s] = 0;
-        if (MODE == VGPU_FP64) V.dx[s] = V.dy[s] = V.dz[s] = __longlong_as_double(0x7ff8000000000000ll);
-    }
-
-    // ---- bound of max |v|^2 and the candidate cut-off
-    __device__ __forceinline__ void update_radius() {
-        float m = V.r2[0];
-#pragma unroll
-        for (int s = 1; s < K; s++) m = fmaxf(m, V.r2[s]);
-        C.R2 = warp_maxf(m);
-        if (P.g.poly) {
-            float R = sqrtf(C.R2);
-            float q = C.R2 + P.g.rmax32 * P.g.rmax32 - C.ri2;
-            float D = R + sqrtf(fmaxf(q, 0.0f));
-            C.cutoff2 = D * D * (1.0f + 8.0f * kU32);
-        } else {
-            C.cutoff2 = 4.0f * C.R2;
-        }
-    }
-
-    // ---- vertex of slot s from the three planes of V.tri[s]
-    __device__ __forceinline__ void compute_vertex(int s) {
-        const unsigned t = V.tri[s];
-        const int a = tri_plane(t, 0), b = tri_plane(t, 1), c = tri_plane(t, 2);
-        if (MODE == VGPU_FP64) {
-            double D;
-            float kn;
-            solve_f64(S.pl64x[a], S.pl64x[b], S.pl64x[c], V.dx[s], V.dy[s], V.dz[s], D, kn);
-            const float vv = sqrtf((float)(V.dx[s] * V.dx[s] + V.dy[s] * V.dy[s] + V.dz[s] * V.dz[s]));
-            V.e[s] = (float)(16.0 * kU64 * (double)kn / fabs(D)) + (float)(64.0 * kU64) * vv;
-            V.a[s] = vv;
-            if (!(D > 0.0)) C.marginal = true;
-            const float r = vv * (1.0f + 4.0f * kU32) + V.e[s];
-            V.r2[s] = r * r;
-            return;
-        }
-        VertexF32 o = solve_vertex_f32(S.pl, S.pe, t);
-        if (!(o.e <= kVertexTrust * o.a)) o = vertex_f64_fallback<MODE, K>(P, S, C.me64, t);
-        V.x[s] = o.x;
-        V.y[s] = o.y;
-        V.z[s] = o.z;
-        V.a[s] = o.a;
-        V.e[s] = o.e;
-        V.r2[s] = o.r2;
-    }
-
-    // ---- initial cell: container box (src/container.hh:191-203, src/cell.cc:294-318,2567-2580)
-    //      or the periodic unit cell (src/container_prd.hh:124-131)
-    __device__ void init_cell(int k) {
-        C.k = k;
-        C.me64 = P.a.p64[k];
-        C.me32 = P.a.l32[k];
-        const int b = P.a.gblock[k];
-        C.bi = b % P.g.gn[0];
-        C.bj = (b / P.g.gn[0]) % P.g.gn[1];
-        C.bk = b / (P.g.gn[0] * P.g.gn[1]);
-        C.ri2 = C.me32.w * C.me32.w;
-        C.deleted = C.overflow = C.marginal = C.repaired = false;
-        C.fail_reason = 0;
-        C.freeplanes = ~0x3full;
-        C.ncand = 0;
-        C.tests = C.repairs = C.ptested = C.pcut = 0;
-        if (lane < 6) {
-            const double4 q = face64(P, C.me64, lane);
-            if (MODE == VGPU_FP64) S.pl64x[lane] = q;
-            S.pl[lane] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
-            const float hf = fabsf((float)q.w);
-            S.pe[lane] = make_float4(1.0f, 0.0f, 2.0f * kU32 * hf, hf);
-            S.pid[lane] = P.g.unit_cell ? 0 : -(lane + 1);
-            S.psrc[lane] = -1;
-            S.pshift[lane] = lane;
-        }
-        Vm.clear();
-        Vm.w[0] = 0xffull;
-#pragma unroll
-        for (int s = 0; s < K; s++) clear_slot(s);
-        if (lane < 8) {
-            S.tri[lane] = c_box_tri[lane];
-            S.adj[lane] = c_box_adj[lane];
-            V.tri[0] = c_box_tri[lane];
-        }
-        __syncwarp();
-        if (lane < 8) compute_vertex(0);
-        update_radius();
-    }
-
-    // ---- plane slot allocation with recycling of dead planes
-    __device__ __forceinline__ int alloc_plane() {
-        if (C.freeplanes == 0ull) {
-            unsigned long long live = 0ull;
-#pragma unroll
-            for (int s = 0; s < K; s++)
-                if (Vm.test(lane + 32 * s)) {
-                    const unsigned t = V.tri[s];
-                    live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
-                }
-            C.freeplanes = ~warp_or64(live);
-            if (C.freeplanes == 0ull) return -1;
-        }
-        const int p = __ffsll((long long)C.freeplanes) - 1;
-        C.freeplanes &= ~(1ull << p);
-        return p;
-    }
-
-    // ---- test candidate (buffer slot cb) and cut the cell if it intersects.
-    __device__ __forceinline__ void test_and_cut(int cb) {
-        PHASE_BEGIN(t_test);
-        C.ptested++;
-        C.tests += (unsigned)Vm.popc();
-        bool out[K];
-        unsigned uncbits = 0;
-        if (MODE == VGPU_FP64) {
-            const double4 Q = S.u.c.cd64[cb];
-            const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
-#pragma unroll
-            for (int s = 0; s < K; s++) {
-                const double v = fma(Q.x, V.dx[s], fma(Q.y, V.dy[s], fma(Q.z, V.dz[s], -Q.w)));
-                const double bnd = nq * (double)V.e[s] + 8.0 * kU64 * (nq * (double)V.a[s] + fabs(Q.w)) + P.g.tol_h;
-                out[s] = v > bnd;
-                if (!out[s] && v >= -bnd) uncbits |= 1u << s;
-            }
-            if (__any_sync(kFull, uncbits != 0)) C.marginal = true;   // tolerance band: kept, cell flagged
-        } else {
-            const float4 Q = S.u.c.cd[cb];
-            const float4 E = S.u.c.ce[cb];
-            const float A = fmaf(3.0f * kU32, E.z, E.x);
-            const float Cq = fmaf(3.0f * kU32, fabsf(Q.w), E.y) + (float)P.g.tol_h;
-#pragma unroll
-            for (int s = 0; s < K; s++) {
-                const float v = fmaf(Q.x, V.x[s], fmaf(Q.y, V.y[s], fmaf(Q.z, V.z[s], -Q.w)));
-                const float bnd = 1.5f * fmaf(A, V.a[s], fmaf(E.z, V.e[s], Cq));
-                out[s] = v > bnd;
-                if (!(v > bnd) && v >= -bnd) uncbits |= 1u << s;
-            }
-            const unsigned ub = __ballot_sync(kFull, uncbits != 0);
-            if (ub) {
-                C.repaired = true;
-                C.repairs += __popc(ub);
-                bool m = false;
-                const unsigned ob = repair_tests<MODE, K>(P, S, C.me64, cb, uncbits, V.tri[0], K > 1 ? V.tri[K > 1 ? 1 : 0] : 0u,
-                                                          K > 2 ? V.tri[K > 2 ? 2 : 0] : 0u, K > 3 ? V.tri[K > 3 ? 3 : 0] : 0u, &m);
-                if (__any_sync(kFull, m)) C.marginal = true;
-#pragma unroll
-                for (int s = 0; s < K; s++)
-                    if ((uncbits >> s) & 1u) out[s] = (ob >> s) & 1u;
-            }
-        }
-        const Mask<K> Rm = ballot_mask<K>(out);
-        PHASE_END(t_test, 3);
-        if (!Rm.any()) return;
-        if (Rm.equals(Vm)) {
-            C.deleted = true;
-            return;
-        }
-        PHASE_BEGIN(t_cut);
-        C.pcut++;
-        const int p = alloc_plane();
-        if (p < 0) {
-            C.overflow = true;
-            C.fail_reason = VGPU_FAIL_PLANES;
-            return;
-        }
-        if (lane == 0) {
-            const float4 Q = S.u.c.cd[cb];
-            const float4 E = S.u.c.ce[cb];
-            const int j = S.u.c.cj[cb];
-            S.pl[p] = Q;
-            S.pe[p] = make_float4(E.z, E.x, E.y, fabsf(Q.w));
-            S.pid[p] = P.a.pid[j];
-            S.psrc[p] = j;
-            S.pshift[p] = S.u.c.cs[cb];
-            if (MODE == VGPU_FP64) S.pl64x[p] = S.u.c.cd64[cb];
-        }
-        cut(p, Rm);
-        PHASE_END(t_cut, 4);
-    }
-
-    // ---- remove the vertices in Rm and close the hole with the face of plane p
-    __device__ __forceinline__ void cut(int p, const Mask<K> &Rm) {
-        // Phase A: count boundary edges (edges from a removed vertex to a kept one)
-        unsigned bnd[K];
-        int nbe = 0;
-        bool broken = false;
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            bnd[s] = 0;
-            const int t = lane + 32 * s;
-            if (Rm.test(t)) {
-                const unsigned A3 = S.adj[t];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    const int u = (A3 >> (8 * e)) & 255u;
-                    if (u >= 32 * K) broken = true;
-                    else if (!Rm.test(u)) bnd[s] |= 1u << e;
-                }
-                nbe += __popc(bnd[s]);
-            }
-        }
-        const int incl = warp_incl_scan(nbe, lane);
-        const int total = __shfl_sync(kFull, incl, 31);
-        if (__any_sync(kFull, broken)) {  // inconsistent adjacency: hand the cell to the large engine
-            C.overflow = true;
-            C.fail_reason = VGPU_FAIL_ADJACENCY;
-            return;
-        }
-        if (total < 3) {  // not a closed boundary: inconsistent side decisions
-            C.marginal = true;
-            return;
-        }
-        Mask<K> Fm;
-#pragma unroll
-        for (int i = 0; i < Mask<K>::W; i++) Fm.w[i] = ~Vm.w[i] | Rm.w[i];
-        if (Fm.popc() < total) {
-            C.overflow = true;
-            C.fail_reason = VGPU_FAIL_VERTICES;
-            return;
-        }
-        // stage the boundary edges (a -> b, kept neighbour u) in lane order
-        {
-            int q = incl - nbe;
-#pragma unroll
-            for (int s = 0; s < K; s++) {
-                if (bnd[s]) {
-                    const unsigned T = V.tri[s];
-                    const unsigned A3 = S.adj[lane + 32 * s];
-#pragma unroll
-                    for (int e = 0; e < 3; e++)
-                        if ((bnd[s] >> e) & 1u) {
-                            const int a = tri_plane(T, e), b = tri_plane(T, e == 2 ? 0 : e + 1);
-                            const unsigned u = (A3 >> (8 * e)) & 255u;
-                            S.stage[q++] = (unsigned)a | ((unsigned)b << 8) | (u << 16);
-                        }
-                }
-            }
-        }
-        __syncwarp();
-        // Phase B: the free slot of rank r hosts the new vertex (a, b, p) of boundary edge r
-        bool host[K];
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            const int t = lane + 32 * s;
-            host[s] = false;
-            if (Fm.test(t)) {
-                const int r = Fm.rank(t);
-                if (r < total) {
-                    host[s] = true;
-                    const unsigned E = S.stage[r];
-                    const int a = E & 255u, b = (E >> 8) & 255u, u = (E >> 16) & 255u;
-                    const unsigned T = (unsigned)a | ((unsigned)b << 8) | ((unsigned)p << 16);
-                    V.tri[s] = T;
-                    S.tri[t] = T;
-                    S.adj[t] = (unsigned)u;
-                    S.startN[a] = (unsigned char)t;
-                    S.endN[b] = (unsigned char)t;
-                    const unsigned Tu = S.tri[u];
-#pragma unroll
-                    for (int e = 0; e < 3; e++)
-                        if (tri_plane(Tu, e) == b && tri_plane(Tu, e == 2 ? 0 : e + 1) == a)
-                            reinterpret_cast<unsigned char *>(&S.adj[u])[e] = (unsigned char)t;
-                }
-            }
-        }
-        __syncwarp();
-        // Phase C: link the new vertices around the new face; clear freed slots
-        bool bad = false;
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            if (host[s]) {
-                const int t = lane + 32 * s;
-                const unsigned T = V.tri[s];
-                const int a = T & 255u, b = (T >> 8) & 255u;
-                if (S.startN[a] != t) bad = true;
-                unsigned char *ab = reinterpret_cast<unsigned char *>(&S.adj[t]);
-                ab[1] = S.startN[b];
-                ab[2] = S.endN[a];
-            } else if (Rm.test(lane + 32 * s)) {
-                clear_slot(s);
-            }
-        }
-        if (__any_sync(kFull, bad)) C.marginal = true;
-        const Mask<K> Nm = ballot_mask<K>(host);
-#pragma unroll
-        for (int i = 0; i < Mask<K>::W; i++) Vm.w[i] = (Vm.w[i] & ~Rm.w[i]) | Nm.w[i];
-        __syncwarp();
-        // Phase D: positions of the new vertices
-#pragma unroll
-        for (int s = 0; s < K; s++)
-            if (host[s]) compute_vertex(s);
-        update_radius();
-    }
-
-    // ---- candidate buffer: sort by (power) distance and test in order
-    __device__ void flush() {
-        const int n = C.ncand;
-        if (n == 0) return;
-        PHASE_BEGIN(t_sort);
-        __syncwarp();
-        unsigned k0 = lane < n ? S.u.c.ck[lane] : 0xffffffffu;
-        unsigned k1 = lane + 32 < n ? S.u.c.ck[lane + 32] : 0xffffffffu;
-        if (n > 32) {
-            const uint2 kk = bitonic64(k0, k1, lane);
-            k0 = kk.x;
-            k1 = kk.y;
-        } else {
-            k0 = bitonic32(k0, lane);
-        }
-        PHASE_END(t_sort, 2);
-        for (int i = 0; i < n; i++) {
-            const unsigned key = __shfl_sync(kFull, i < 32 ? k0 : k1, i & 31);
-            const int cb = key & 63u;
-            const float4 E = S.u.c.ce[cb];
-            if (P.g.poly) {
-                const float rs = E.w;
-                if (!(rs <= 0.0f || rs * rs < 4.0f * C.R2 * E.z * E.z * (1.0f + 16.0f * kU32))) continue;
-            } else {
-                if (E.w >= C.cutoff2 * (1.0f + 1e-4f)) break;
-            }
-            test_and_cut(cb);
-            if (C.deleted || C.overflow) break;
-        }
-        C.ncand = 0;
-        __syncwarp();
-    }
-
-    // ---- candidates from a range of block offsets: wrap/skip, block distance,
-    //      then one lane per candidate particle
-    __device__ void gather_offsets(int e_begin, int e_end, bool from_table, int shell_r) {
-        const float l0 = C.me32.x, l1 = C.me32.y, l2 = C.me32.z;
-        for (int base = e_begin; base < e_end; base += 32) {
-            const int e = base + lane;
-            int di = 0, dj = 0, dk = 0;
-            bool ok = e < e_end;
-            if (ok) {
-                if (from_table) {
-                    const int code = offsets[e];
-                    di = (code & 31) - 16;
-                    dj = ((code >> 5) & 31) - 16;
-                    dk = ((code >> 10) & 31) - 16;
-                } else {
-                    const int w = 2 * shell_r + 1;
-                    di = e % w - shell_r;
-                    dj = (e / w) % w - shell_r;
-                    dk = e / (w * w) - shell_r;
-                    const int m = max(abs(di), max(abs(dj), abs(dk)));
-                    const int a = max(abs(di) - 1, 0), b = max(abs(dj) - 1, 0), c = max(abs(dk) - 1, 0);
-                    ok = (m == shell_r) && (a * a + b * b + c * c > kTableLb2Max);
-                }
-            }
-            int cnt = 0, st = 0, code = 0;
-            {
-                const int d[3] = {di, dj, dk};
-                const int cb[3] = {C.bi + di, C.bj + dj, C.bk + dk};
-                const float l[3] = {l0, l1, l2};
-                int wr[3], img[3];
-                float md2 = 0.0f;
-#pragma unroll
-                for (int a = 0; a < 3; a++) {
-                    const int n = P.g.gn[a];
-                    int c = cb[a];
-                    img[a] = 0;
-                    if (P.g.per[a]) {
-                        if (from_table && n > 2 * kOffsetRadius) {
-                            if (c < 0) { c += n; img[a] = -1; }
-                            else if (c >= n) { c -= n; img[a] = 1; }
-                        } else {
-                            int w = c % n;
-                            if (w < 0) w += n;
-                            img[a] = (c - w) / n;
-                            c = w;
-                        }
-                    } else if (c < 0 || c >= n) {
-                        ok = false;
-                    }
-                    wr[a] = c;
-                    const float bs = P.g.gbs32[a];
-                    float t = d[a] > 0 ? (float)d[a] * bs - l[a] : (d[a] < 0 ? l[a] - (float)(d[a] + 1) * bs : 0.0f);
-                    t = fmaxf(t, 0.0f);
-                    md2 = fmaf(t, t, md2);
-                }
-                if (ok && md2 * (1.0f - 1e-5f) >= C.cutoff2) ok = false;
-                if (ok) {
-                    const int b = wr[0] + P.g.gn[0] * (wr[1] + P.g.gn[1] * wr[2]);
-                    st = P.a.bstart[b];
-                    cnt = P.a.bstart[b + 1] - st;
-                    code = (img[0] + 128) | ((img[1] + 128) << 8) | ((img[2] + 128) << 16);
-                }
-            }
-            const int incl = warp_incl_scan(cnt, lane);
-            const int tot = __shfl_sync(kFull, incl, 31);
-            const int packed_d = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
-            for (int c0 = 0; c0 < tot; c0 += 32) {
-                if (C.ncand > kCandBuf - 32) flush();
-                if (C.deleted || C.overflow) return;
-                const int c = c0 + lane;
-                // owner lane: number of lanes whose inclusive prefix is <= c
-                int pos = 0;
-#pragma unroll
-                for (int w = 16; w >= 1; w >>= 1) {
-                    const int v = __shfl_sync(kFull, incl, pos + w - 1);
-                    if (v <= c) pos += w;
-                }
-                pos = min(pos, 31);
-                const int o_incl = __shfl_sync(kFull, incl, pos);
-                const int o_cnt = __shfl_sync(kFull, cnt, pos);
-                const int o_st = __shfl_sync(kFull, st, pos);
-                const int o_code = __shfl_sync(kFull, code, pos);
-                const int o_d = __shfl_sync(kFull, packed_d, pos);
-                bool pass = false;
-                unsigned key = 0;
-                float4 cd = make_float4(0, 0, 0, 0), ce = make_float4(0, 0, 0, 0);
-                const int j = o_st + (c - (o_incl - o_cnt));
-                if (c < tot) {
-                    const int ddi = (o_d & 31) - 16, ddj = ((o_d >> 5) & 31) - 16, ddk = ((o_d >> 10) & 31) - 16;
-                    const bool self = (j == C.k) && ddi == 0 && ddj == 0 && ddk == 0;
-                    if (!self) {
-                        const float4 lj = P.a.l32[j];
-                        const float dx = fmaf((float)ddi, P.g.gbs32[0], lj.x - l0);
-                        const float dy = fmaf((float)ddj, P.g.gbs32[1], lj.y - l1);
-                        const float dz = fmaf((float)ddk, P.g.gbs32[2], lj.z - l2);
-                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                        float rs = d2, rr = 0.0f;
-                        if (P.g.poly) {
-                            rr = C.ri2 + lj.w * lj.w;
-                            rs = d2 + (C.ri2 - lj.w * lj.w);
-                            pass = rs <= 0.0f || rs * rs < 4.0f * C.R2 * d2 * (1.0f + 16.0f * kU32);
-                        } else {
-                            pass = d2 < C.cutoff2 * (1.0f + 1e-5f);
-                        }
-                        // forward error of the FP32 plane: local coordinates and block
-                        // offsets each carry at most u*bs; the sum one more rounding
-                        const int M = max(abs(ddi), max(abs(ddj), abs(ddk)));
-                        const float dn = sqrtf(d2);
-                        const float en = kU32 * (1.75f * (float)(M + 3) * P.g.gbs_max + 1.01f * dn) + 1e-12f * P.g.gbs_max;
-                        const float eh = dn * en + 2.0f * kU32 * (d2 + rr) + 0.5f * en * en;
-                        cd = make_float4(dx, dy, dz, 0.5f * rs);
-                        ce = make_float4(en, eh, dn, rs);
-                        key = float_key(rs);
-                    }
-                }
-                const unsigned bal = __ballot_sync(kFull, pass);
-                if (pass) {
-                    const int slot = C.ncand + __popc(bal & ((1u << lane) - 1u));
-                    S.u.c.ck[slot] = (key & ~63u) | (unsigned)slot;
-                    S.u.c.cj[slot] = j;
-                    S.u.c.cs[slot] = o_code;
-                    S.u.c.cd[slot] = cd;
-                    S.u.c.ce[slot] = ce;
-                    if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C.me64, j, o_code);
-                }
-                C.ncand += __popc(bal);
-            }
-        }
-    }
-
-    // ---- the search: blocks in order of lower-bound distance (src/v_compute.cc:289-621
-    //      does the same with its 64 worklists, mrad cut-offs and the block queue).
-    //      Segments 0..ngroups-1 are the table's distance groups; after them come
-    //      Chebyshev shells r = kOffsetRadius, ... with what the table covered skipped.
-    __device__ void search() {
-        const float bmin2 = P.g.gbs_min * P.g.gbs_min;
-        const int rmax_grid = max(P.g.gn[0], max(P.g.gn[1], P.g.gn[2]));
-        const bool any_periodic = P.g.per[0] || P.g.per[1] || P.g.per[2];
-        const int rlim = min(4 * rmax_grid + 8, 40);
-        for (int seg = 0;; seg++) {
-            const bool table = seg < P.ngroups;
-            int b0 = 0, b1 = 0, r = 0;
-            float lb2;
-            if (table) {
-                lb2 = (float)P.group_lb2[seg] * bmin2;
-                b0 = P.group_start[seg];
-                b1 = P.group_start[seg + 1];
-            } else {
-                r = kOffsetRadius + (seg - P.ngroups);
-                if (r >= rlim) {
-                    C.overflow = true;  // search did not terminate
-                    C.fail_reason = VGPU_FAIL_SEARCH;
-                    return;
-                }
-                if (!any_periodic && r > rmax_grid + 1) return;
-                lb2 = (float)((r - 1) * (r - 1)) * bmin2;
-                b1 = (2 * r + 1) * (2 * r + 1) * (2 * r + 1);
-            }
-            if (lb2 >= C.cutoff2 * (1.0f + 1e-5f)) return;
-            PHASE_BEGIN(t_g);
-            gather_offsets(b0, b1, table, r);
-            PHASE_END(t_g, 1);
-            if (C.deleted || C.overflow) return;
-            flush();
-            if (C.deleted || C.overflow) return;
-        }
-    }
-
-    // ---- reductions: vertex/face counts, neighbours, FP64 volume and centroid
-    // ---- results of a cell with no polytope: deleted (compute_cell false), or
-    //      overflowed (a larger engine reruns it and overwrites this; if none
-    //      does, it stays failed)
-    __device__ __forceinline__ void write_empty() {
-        const int out = P.a.outpos[C.k];
-        if (lane == 0) {
-            P.r.vol[out] = 0.0;
-            P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-            P.r.nf[out] = 0;
-            P.r.nv[out] = 0;
-            P.r.maxr2[out] = 0.0;
-            P.r.flags[out] = C.overflow ? (VGPU_CELL_FAILED | (C.fail_reason << 8))
-                                        : ((C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0));
-        }
-    }
-
-    __device__ void run(int k) {
-#ifdef VGPU_PHASE_TIMING
-        for (int i = 0; i < 8; i++) C.phase[i] = 0;
-#endif
-        PHASE_BEGIN(t_init);
-        init_cell(k);
-        PHASE_END(t_init, 0);
-        search();
-        PHASE_BEGIN(t_fin);
-        // no reductions here: the finish kernel completes the cell from its
-        // record, which keeps the FP64 code out of this kernel's instruction
-        // stream; a full record store fails the cell
-        if (!C.overflow && !C.deleted) {
-            if (emit_record()) {
-                PHASE_END(t_fin, 5);
-                return;
-            }
-            C.overflow = true;
-            C.fail_reason = VGPU_FAIL_RECORDS;
-        }
-        write_empty();
-        PHASE_END(t_fin, 5);
-    }
-
-    // ---- the finished polytope as a compact record for the finish kernel
-    //      (layout in CellParams): valid vertices and live planes only, in
-    //      slot order, with plane and vertex indices renumbered to match;
-    //      false if the record store is full
-    __device__ bool emit_record() {
-        constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;   // words per vertex position
-        unsigned long long live = 0ull;
-#pragma unroll
-        for (int s = 0; s < K; s++)
-            if (Vm.test(lane + 32 * s)) {
-                const unsigned t = V.tri[s];
-                live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
-            }
-        live = warp_or64(live);
-        const int nf = __popcll(live);
-        const int nv = Vm.popc();
-        const unsigned words = (unsigned)(kRecHeader + (2 + VW) * nv + 3 * nf);
-        unsigned long long off = 0;
-        if (lane == 0) off = atomicAdd(P.rec_used, (unsigned long long)words);
-        off = __shfl_sync(kFull, off, 0);
-        if (off + words > P.rec_cap) return false;
-        unsigned *R = P.rec + off;
-        if (lane == 0) {
-            R[0] = (unsigned)nv;
-            R[1] = (unsigned)nf;
-            R[2] = (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
-            R[3] = 0;
-            R[4] = 0;
-        }
-        // compact indices: vertex slot -> rank among valid slots (vmap),
-        // plane slot -> rank among live planes (endN, free once the cell is done)
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            const int t = lane + 32 * s;
-            if (Vm.test(t)) S.vmap[t] = (unsigned char)Vm.rank(t);
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int q = lane + 32 * h;
-            if ((live >> q) & 1ull) S.endN[q] = (unsigned char)__popcll(live & ((1ull << q) - 1ull));
-        }
-        __syncwarp();
-        unsigned *rv = R + kRecHeader;
-#pragma unroll
-        for (int s = 0; s < K; s++) {
-            const int t = lane + 32 * s;
-            if (Vm.test(t)) {
-                const int r = S.vmap[t];
-                const unsigned T = V.tri[s];
-                const unsigned A3 = S.adj[t];
-                rv[r] = (unsigned)S.endN[tri_plane(T, 0)] | ((unsigned)S.endN[tri_plane(T, 1)] << 8) |
-                        ((unsigned)S.endN[tri_plane(T, 2)] << 16);
-                rv[nv + r] = (unsigned)S.vmap[A3 & 255u] | ((unsigned)S.vmap[(A3 >> 8) & 255u] << 8) |
-                             ((unsigned)S.vmap[(A3 >> 16) & 255u] << 16);
-                if (MODE == VGPU_FP64) {
-                    const double c[3] = {V.dx[s], V.dy[s], V.dz[s]};
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        const unsigned long long b = (unsigned long long)__double_as_longlong(c[a]);
-                        rv[(2 + 2 * a) * nv + 2 * r] = (unsigned)b;
-                        rv[(2 + 2 * a) * nv + 2 * r + 1] = (unsigned)(b >> 32);
-                    }
-                } else {
-                    rv[2 * nv + r] = __float_as_uint(V.x[s]);
-                    rv[3 * nv + r] = __float_as_uint(V.y[s]);
-                    rv[4 * nv + r] = __float_as_uint(V.z[s]);
-                }
-            }
-        }
-        unsigned *rp = rv + (2 + VW) * nv;
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int q = lane + 32 * h;
-            if ((live >> q) & 1ull) {
-                const int r = S.endN[q];
-                rp[r] = (unsigned)S.psrc[q];
-                rp[nf + r] = (unsigned)S.pshift[q];
-                rp[2 * nf + r] = (unsigned)S.pid[q];
-            }
-        }
-        if (lane == 0) P.rec_off[C.k] = (unsigned)off;
-        return true;
-    }
-};
-
-// CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot) engine;
-// it fixes the register budget (65536 / (128 * blocks)).
-#ifndef VGPU_MIN_BLOCKS
-#define VGPU_MIN_BLOCKS 4
-#endif
-template <int MODE, int K>
-constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
-
-template <int MODE, int K>
-__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int *offsets = reinterpret_cast<int *>(smem_raw);
-    const size_t off_bytes = ((size_t)P.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    WarpShared<MODE, K> *ws = reinterpret_cast<WarpShared<MODE, K> *>(smem_raw + off_bytes);
-    for (int i = threadIdx.x; i < P.noffsets; i += blockDim.x) offsets[i] = P.offsets[i];
-    __syncthreads();
-    WarpShared<MODE, K> &S = ws[wid];
-    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0;
-#ifdef VGPU_PHASE_TIMING
-    unsigned long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const long long t_kernel0 = clock64();
-#endif
-    unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
-    for (;;) {
-        int w = 0;
-        if (lane == 0) w = (int)atomicAdd(work, 1ull);
-        w = __shfl_sync(kFull, w, 0);
-        if (w >= P.ncells) break;
-        const int k = P.cell_list ? P.cell_list[w] : w;
-        Engine<MODE, K> eng(P, S, offsets, lane);
-        eng.run(k);
-        tests += eng.C.tests;
-        repairs += eng.C.repairs;
-        ptested += eng.C.ptested;
-        pcut += eng.C.pcut;
-#ifdef VGPU_PHASE_TIMING
-        for (int i = 0; i < 8; i++) ph[i] += eng.C.phase[i];
-#endif
-        if (eng.C.overflow) {
-            if (lane == 0) {
-                const unsigned long long slot = atomicAdd(&P.cnt->overflow, 1ull);
-                if (P.overflow_list) P.overflow_list[slot] = k;
-            }
-        } else {
-            deleted += eng.C.deleted ? 1 : 0;
-            marginal += eng.C.marginal ? 1 : 0;
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        atomicAdd(&P.cnt->side_tests, tests);
-        atomicAdd(&P.cnt->fp64_repairs, repairs);
-        atomicAdd(&P.cnt->planes_tested, ptested);
-        atomicAdd(&P.cnt->planes_cut, pcut);
-        atomicAdd(&P.cnt->deleted, deleted);
-        atomicAdd(&P.cnt->marginal, marginal);
-#ifdef VGPU_PHASE_TIMING
-        ph[7] = (unsigned long long)(clock64() - t_kernel0);
-        for (int i = 0; i < 8; i++) atomicAdd(&P.cnt->phase_cycles[i], ph[i]);
-#endif
-    }
-}
-
-// Many containers in one persistent launch.  A warp takes global cell indices
-// from one queue (container-major, so neighbouring warps share blocks); when
-// a cell belongs to another container than the warp's previous one, the warp
-// copies that container's parameters into its shared slot and flushes its
-// counters to the previous container's.
-template <int MODE, int K>
-__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int warps = blockDim.x >> 5;
-    int *offsets = reinterpret_cast<int *>(smem_raw);
-    const size_t off_bytes = ((size_t)B.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    constexpr size_t cp_slot = (sizeof(CellParams) + 15) & ~(size_t)15;
-    CellParams *cps = reinterpret_cast<CellParams *>(smem_raw + off_bytes);
-    WarpShared<MODE, K> *ws = reinterpret_cast<WarpShared<MODE, K> *>(smem_raw + off_bytes + cp_slot * warps);
-    for (int i = threadIdx.x; i < B.noffsets; i += blockDim.x) offsets[i] = B.offsets[i];
-    __syncthreads();
-    CellParams &P = *reinterpret_cast<CellParams *>(reinterpret_cast<unsigned char *>(cps) + cp_slot * wid);
-    WarpShared<MODE, K> &S = ws[wid];
-    int cur = -1;
-    long long cbeg = 0, cend = 0;
-    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0, ovf = 0;
-    auto flush = [&]() {
-        if (cur >= 0 && lane == 0) {
-            Counters *c = B.cps[cur].cnt;
-            atomicAdd(&c->side_tests, tests);
-            atomicAdd(&c->fp64_repairs, repairs);
-            atomicAdd(&c->planes_tested, ptested);
-            atomicAdd(&c->planes_cut, pcut);
-            atomicAdd(&c->deleted, deleted);
-            atomicAdd(&c->marginal, marginal);
-            if (ovf) atomicAdd(B.overflow_list ? &c->overflow : &c->failed, ovf);
-        }
-        tests = repairs = ptested = pcut = deleted = marginal = ovf = 0;
-    };
-    for (;;) {
-        long long w = 0;
-        if (lane == 0) w = (long long)atomicAdd(B.work, 1ull);
-        w = __shfl_sync(kFull, w, 0);
-        if (w >= B.ncells) break;
-        const long long gidx = B.cell_list ? B.cell_list[w] : w;
-        if (gidx < cbeg || gidx >= cend) {
-            flush();
-            // the container c with cell_start[c] <= gidx < cell_start[c+1]
-            int lo = 0, hi = B.ncont;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (B.cell_start[mid] <= gidx) lo = mid;
-                else hi = mid;
-            }
-            cur = lo;
-            cbeg = B.cell_start[lo];
-            cend = B.cell_start[lo + 1];
-            __syncwarp();
-            const unsigned *src = reinterpret_cast<const unsigned *>(B.cps + cur);
-            unsigned *dst = reinterpret_cast<unsigned *>(&P);
-            for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
-            __syncwarp();
-        }
-        const int k = (int)(gidx - cbeg);
-        Engine<MODE, K> eng(P, S, offsets, lane);
-        eng.run(k);
-        tests += eng.C.tests;
-        repairs += eng.C.repairs;
-        ptested += eng.C.ptested;
-        pcut += eng.C.pcut;
-        if (eng.C.overflow) {
-            ovf++;
-            if (lane == 0 && B.overflow_list) {
-                const unsigned long long slot = atomicAdd(B.overflow_count, 1ull);
-                B.overflow_list[slot] = gidx;
-            }
-        } else {
-            deleted += eng.C.deleted ? 1 : 0;
-            marginal += eng.C.marginal ? 1 : 0;
-        }
-        __syncwarp();
-    }
-    flush();
-}
-
-// ------------------------------------------------------------------ finish
-// The FP64 reductions of every cell from the compact record its clipping
-// kernel wrote (layout in CellParams).  They run as a separate kernel so that
-// the clipping loop keeps the instruction cache to itself.  Vertices: the
-// MIXED engine's FP32 vertices get one FP64 residual correction against their
-// three FP64 planes (refine_vertex_rec); the FP64 engine's are used as they
-// are.  Volume and centroid: FP64 sums over edges relative to vertex 0 with
-// each face's reference point one of its own vertices (the edge formula holds
-// for any point of the face).  Optionally the polytope itself is written out.
-constexpr int kFinMaxV = 128;   // vertices (the 128-slot engine's capacity)
-constexpr int kFinMaxE = 192;   // edges (3 * kFinMaxV / 2)
-
-struct FinishShared {
-    unsigned tri[kFinMaxV];
-    unsigned adj[kFinMaxV];
-    int psrc[kMaxPlanes], pshift[kMaxPlanes];
-    int rep[kMaxPlanes];             // per face: its lowest vertex
-    int ford[kMaxPlanes];            // per face: its vertex count
-    double4 pl64[kMaxPlanes];
-    float4 pn[kMaxPlanes];           // the FP64 plane normals rounded to FP32
-    double vx[kFinMaxV], vy[kFinMaxV], vz[kFinMaxV];   // FP64 vertices relative to c0
-    unsigned stage[kFinMaxE];        // owned edges (t < u)
-};
-
-__device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
-    const int src = F.psrc[p];
-    if (src >= 0) return plane64_from(P, me, src, F.pshift[p]);
-    return face64(P, me, F.pshift[p]);
-}
-
-// refine_vertex_f64 with the planes' FP32 normals taken from F.pn (rounded
-// once per plane rather than once per vertex and plane).
-__device__ __forceinline__ double3 refine_vertex_rec(const FinishShared &F, unsigned t, float fx, float fy, float fz) {
-    const int ia = tri_plane(t, 0), ib = tri_plane(t, 1), ic = tri_plane(t, 2);
-    const double4 A = F.pl64[ia], B = F.pl64[ib], Cq = F.pl64[ic];
-    const float4 a = F.pn[ia], b = F.pn[ib], c = F.pn[ic];
-    const double x = fx, y = fy, z = fz;
-    const double ra = A.w - fma(A.x, x, fma(A.y, y, A.z * z));
-    const double rb = B.w - fma(B.x, x, fma(B.y, y, B.z * z));
-    const double rc = Cq.w - fma(Cq.x, x, fma(Cq.y, y, Cq.z * z));
-    const float bcx = b.y * c.z - b.z * c.y, bcy = b.z * c.x - b.x * c.z, bcz = b.x * c.y - b.y * c.x;
-    const float cax = c.y * a.z - c.z * a.y, cay = c.z * a.x - c.x * a.z, caz = c.x * a.y - c.y * a.x;
-    const float abx = a.y * b.z - a.z * b.y, aby = a.z * b.x - a.x * b.z, abz = a.x * b.y - a.y * b.x;
-    const float D = a.x * bcx + a.y * bcy + a.z * bcz;
-    const float scale = (fabsf(a.x) + fabsf(a.y) + fabsf(a.z)) * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z)) *
-                        (fabsf(c.x) + fabsf(c.y) + fabsf(c.z));
-    double3 v;
-    if (fabsf(D) > 1e-3f * scale) {
-        const float fra = (float)ra, frb = (float)rb, frc = (float)rc;
-        const float inv = 1.0f / D;
-        v.x = x + (double)((fra * bcx + frb * cax + frc * abx) * inv);
-        v.y = y + (double)((fra * bcy + frb * cay + frc * aby) * inv);
-        v.z = z + (double)((fra * bcz + frb * caz + frc * abz) * inv);
-    } else {
-        double DD;
-        float kn;
-        solve_f64(A, B, Cq, v.x, v.y, v.z, DD, kn);
-    }
-    return v;
-}
-
-// Warp sums of four values with few FP64 additions (the FP64 pipe bounds the
-// finish kernel): halves of the warp first fold different pairs, then
-// quarters different singles, then each quarter folds its own; the four sums
-// end in lanes 0, 8, 16, 24 and are broadcast.  Fixed order: deterministic.
-__device__ __forceinline__ void warp_sum4(double &a, double &b, double &c, double &d, int lane) {
-    const bool lo = lane < 16;
-    double k0 = lo ? a : c, k1 = lo ? b : d;
-    const double s0 = lo ? c : a, s1 = lo ? d : b;
-    k0 += __shfl_xor_sync(kFull, s0, 16);
-    k1 += __shfl_xor_sync(kFull, s1, 16);
-    const bool lo8 = (lane & 8) == 0;
-    double k = lo8 ? k0 : k1;
-    k += __shfl_xor_sync(kFull, lo8 ? k1 : k0, 8);
-    k += __shfl_xor_sync(kFull, k, 4);
-    k += __shfl_xor_sync(kFull, k, 2);
-    k += __shfl_xor_sync(kFull, k, 1);
-    a = __shfl_sync(kFull, k, 0);
-    b = __shfl_sync(kFull, k, 8);
-    c = __shfl_sync(kFull, k, 16);
-    d = __shfl_sync(kFull, k, 24);
-}
-
-// Warp maximum of non-negative doubles by their bit patterns (ordered like
-// the values), on the integer reduction unit instead of the FP64 pipe.
-__device__ __forceinline__ double warp_max_nonneg(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned mhi = __reduce_max_sync(kFull, hi);
-    const unsigned mlo = __reduce_max_sync(kFull, hi == mhi ? lo : 0u);
-    return __longlong_as_double((long long)(((unsigned long long)mhi << 32) | mlo));
-}
-
-__device__ __forceinline__ double rec_double(const unsigned *w) {
-    return __longlong_as_double((long long)((unsigned long long)w[0] | ((unsigned long long)w[1] << 32)));
-}
-
-// The reductions of cell k (engine order) from its record, if it has one.
-template <int MODE>
-__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int lane) {
-    constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;
-    constexpr int SL = kFinMaxV / 32;
-    const unsigned off = P.rec_off[k];
-    if (off == kNoRecord) return;
-    const unsigned *R = P.rec + off;
-    const int nv = (int)R[0], nf = (int)R[1];
-    const unsigned fl = R[2];
-    const unsigned *rv = R + kRecHeader;
-    const unsigned *rp = rv + (2 + VW) * nv;
-    const double4 me = P.a.p64[k];
-    const int out = P.a.outpos[k];
-    // planes: neighbour IDs (plane order), sources, FP64 planes
-    for (int q = lane; q < nf; q += 32) {
-        F.psrc[q] = (int)rp[q];
-        F.pshift[q] = (int)rp[nf + q];
-        F.rep[q] = 0x7fffffff;
-        F.ford[q] = 0;
-        P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
-        const double4 pl = plane64_rec(P, F, me, q);
-        F.pl64[q] = pl;
-        F.pn[q] = make_float4((float)pl.x, (float)pl.y, (float)pl.z, 0.0f);
-    }
-    __syncwarp();
-    unsigned tri[SL];
-    double vx[SL], vy[SL], vz[SL];
-    double mr2 = 0.0;
-#pragma unroll
-    for (int s = 0; s < SL; s++) {
-        const int t = lane + 32 * s;
-        tri[s] = 0;
-        vx[s] = vy[s] = vz[s] = 0.0;
-        if (t < nv) {
-            tri[s] = rv[t];
-            F.tri[t] = tri[s];
-            F.adj[t] = rv[nv + t];
-            if (MODE == VGPU_FP64) {
-                vx[s] = rec_double(rv + 2 * nv + 2 * t);
-                vy[s] = rec_double(rv + 4 * nv + 2 * t);
-                vz[s] = rec_double(rv + 6 * nv + 2 * t);
-            } else {
-                const double3 r = refine_vertex_rec(F, tri[s], __uint_as_float(rv[2 * nv + t]),
-                                                    __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
-                vx[s] = r.x;
-                vy[s] = r.y;
-                vz[s] = r.z;
-            }
-            mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
-#pragma unroll
-            for (int e = 0; e < 3; e++) {
-                atomicMin(&F.rep[tri_plane(tri[s], e)], t);
-                atomicAdd(&F.ford[tri_plane(tri[s], e)], 1);
-            }
-        }
-    }
-    // origin of the sums: vertex 0
-    const double c0x = __shfl_sync(kFull, vx[0], 0);
-    const double c0y = __shfl_sync(kFull, vy[0], 0);
-    const double c0z = __shfl_sync(kFull, vz[0], 0);
-    int ne = 0;
-    unsigned own[SL];
-#pragma unroll
-    for (int s = 0; s < SL; s++) {
-        own[s] = 0;
-        const int t = lane + 32 * s;
-        if (t < nv) {
-            F.vx[t] = vx[s] - c0x;
-            F.vy[t] = vy[s] - c0y;
-            F.vz[t] = vz[s] - c0z;
-            const unsigned A3 = F.adj[t];
-#pragma unroll
-            for (int e = 0; e < 3; e++)
-                if ((int)((A3 >> (8 * e)) & 255u) > t) own[s] |= 1u << e;
-            ne += __popc(own[s]);
-        }
-    }
-    const int eincl = warp_incl_scan(ne, lane);
-    const int etot = __shfl_sync(kFull, eincl, 31);
-    {
-        int q = eincl - ne;
-#pragma unroll
-        for (int s = 0; s < SL; s++)
-#pragma unroll
-            for (int e = 0; e < 3; e++)
-                if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
-    }
-    __syncwarp();
-    // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
-    double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-    for (int i = lane; i < etot; i += 32) {
-        const unsigned E = F.stage[i];
-        const int t = E & 255u, e = E >> 8;
-        const unsigned T = F.tri[t];
-        const int u = (F.adj[t] >> (8 * e)) & 255u;
-        const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
-        const double tx = F.vx[t], ty = F.vy[t], tz = F.vz[t];
-        const double ux = F.vx[u], uy = F.vy[u], uz = F.vz[u];
-        const double wx = ty * uz - tz * uy;
-        const double wy = tz * ux - tx * uz;
-        const double wz = tx * uy - ty * ux;
-        const double ax = F.vx[rx], ay = F.vy[rx], az = F.vz[rx];
-        const double bx = F.vx[ry], by = F.vy[ry], bz = F.vz[ry];
-        const double dy = bx * wx + by * wy + bz * wz;
-        const double dx = ax * wx + ay * wy + az * wz;
-        const double dd = dy - dx;
-        vs += dd;
-        cx += dd * (tx + ux) + dy * bx - dx * ax;
-        cy += dd * (ty + uy) + dy * by - dx * ay;
-        cz += dd * (tz + uz) + dy * bz - dx * az;
-    }
-    warp_sum4(vs, cx, cy, cz, lane);
-    mr2 = warp_max_nonneg(mr2);
-    if (lane == 0) {
-        const double vol = vs / 6.0;
-        P.r.vol[out] = vol;
-        if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
-            const double f = 1.0 / (4.0 * vs);
-            P.r.cen[3 * out] = c0x + cx * f;
-            P.r.cen[3 * out + 1] = c0y + cy * f;
-            P.r.cen[3 * out + 2] = c0z + cz * f;
-        } else {
-            P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-        }
-        P.r.nf[out] = nf;
-        P.r.nv[out] = nv;
-        P.r.maxr2[out] = mr2;
-        P.r.flags[out] = VGPU_CELL_OK | (int)fl;
-    }
-    if (P.poly != nullptr) {
-        // the polytope: [nv, nf, vertices (3 nv, particle-relative), then per
-        // face (plane order): neighbour ID, vertex count, vertex loop]; each
-        // loop walks the face by the edges that start on it, which orders the
-        // vertices clockwise seen from outside, as the reference's
-        // face_vertices does (src/cell.cc:2285-2308)
-        const unsigned long long need = 2ull + 6ull * (unsigned long long)nv + 2ull * (unsigned long long)nf;
-        unsigned long long po = 0;
-        if (lane == 0) po = atomicAdd(P.poly_used, need);
-        po = __shfl_sync(kFull, po, 0);
-        if (po + need <= P.poly_cap) {
-            double *D = P.poly + po;
-            if (lane == 0) {
-                D[0] = (double)nv;
-                D[1] = (double)nf;
-            }
-#pragma unroll
-            for (int s = 0; s < SL; s++) {
-                const int t = lane + 32 * s;
-                if (t < nv) {
-                    D[2 + 3 * t] = vx[s];
-                    D[3 + 3 * t] = vy[s];
-                    D[4 + 3 * t] = vz[s];
-                }
-            }
-            double *DF = D + 2 + 3 * nv;
-            for (int q0 = 0; q0 < nf; q0 += 32) {
-                const int q = q0 + lane;
-                const int ord = q < nf ? F.ford[q] : 0;
-                // faces before q: q0 * 2 header words plus their orders
-                int before = 0;
-                for (int j = 0; j < q0; j++) before += F.ford[j];
-                const int incl = warp_incl_scan(ord, lane);
-                if (q < nf) {
-                    double *df = DF + 2 * q + before + (incl - ord);
-                    df[0] = (double)P.r.nb[(size_t)out * kMaxNb + q];
-                    df[1] = (double)ord;
-                    int t = F.rep[q];
-                    for (int j = 0; j < ord; j++) {
-                        df[2 + j] = (double)t;
-                        const unsigned T = F.tri[t];
-                        const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
-                        t = (F.adj[t] >> (8 * e)) & 255u;
-                    }
-                }
-            }
-            if (lane == 0) P.poly_off[out] = (long long)po;
-        } else if (lane == 0) {
-            P.poly_off[out] = -2;   // store full
-        }
-    }
-    __syncwarp();
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(128) finish_kernel(const __grid_constant__ CellParams P) {
-    __shared__ FinishShared fsh[4];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * 4;
-    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) finish_record<MODE>(P, fsh[wid], k, lane);
-}
-
-// The same over the cells of a batch (global numbering as cell_batch_kernel).
-template <int MODE>
-__global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant__ BatchParams B) {
-    __shared__ FinishShared fsh[4];
-    __shared__ __align__(16) unsigned char cpw[4][(sizeof(CellParams) + 15) & ~(size_t)15];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    CellParams &P = *reinterpret_cast<CellParams *>(cpw[wid]);
-    const long long nwarps = (long long)gridDim.x * 4;
-    long long cbeg = 0, cend = 0;
-    for (long long g = (long long)blockIdx.x * 4 + wid; g < B.ncells; g += nwarps) {
-        if (g < cbeg || g >= cend) {
-            int lo = 0, hi = B.ncont;
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (B.cell_start[mid] <= g) lo = mid;
-                else hi = mid;
-            }
-            cbeg = B.cell_start[lo];
-            cend = B.cell_start[lo + 1];
-            __syncwarp();
-            const unsigned *src = reinterpret_cast<const unsigned *>(B.cps + lo);
-            unsigned *dst = reinterpret_cast<unsigned *>(&P);
-            for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
-            __syncwarp();
-        }
-        finish_record<MODE>(P, fsh[wid], (int)(g - cbeg), lane);
-    }
-}
 
 __global__ void nf_to_ll_kernel(const int *nf, long long *out, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1499,47 +44,6 @@ __global__ void sum_volumes_kernel(const double *vol, const int *flags, int n, d
     }
 }
 
-template <int MODE, int K>
-cudaError_t launch_one(const CellParams &cp, int warps, int sms, cudaStream_t s) {
-    const size_t off_bytes = ((size_t)cp.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    const size_t smem = off_bytes + warps * sizeof(WarpShared<MODE, K>);
-    cudaError_t e = cudaFuncSetAttribute(cell_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_kernel<MODE, K>, warps * 32, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sms * per_sm;
-    const long long need = (cp.ncells + warps - 1) / warps;
-    int grid = (int)(want < need ? want : need);
-    if (grid < 1) grid = 1;
-    cell_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(cp);
-    note_launch();
-    return cudaGetLastError();
-}
-
-template <int MODE, int K>
-cudaError_t launch_batch_one(const BatchParams &bp, int sms, cudaStream_t s) {
-    const int warps = 4;
-    const size_t off_bytes = ((size_t)bp.noffsets * sizeof(int) + 15) & ~(size_t)15;
-    const size_t cp_slot = (sizeof(CellParams) + 15) & ~(size_t)15;
-    const size_t smem = off_bytes + warps * (cp_slot + sizeof(WarpShared<MODE, K>));
-    cudaError_t e =
-        cudaFuncSetAttribute(cell_batch_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_batch_kernel<MODE, K>, warps * 32, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sms * per_sm;
-    const long long need = (bp.ncells + warps - 1) / warps;
-    int grid = (int)(want < need ? want : need);
-    if (grid < 1) grid = 1;
-    cell_batch_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(bp);
-    note_launch();
-    return cudaGetLastError();
-}
-
 }  // namespace
 
 // Box tables: corner (sx,sy,sz) uses faces x:(sx>0), y:2+(sy>0), z:4+(sz>0),
@@ -1572,68 +76,15 @@ static void build_box_tables(unsigned tri[8], unsigned adj[8]) {
 
 void box_tables(unsigned tri[8], unsigned adj[8]) { build_box_tables(tri, adj); }
 
-cudaError_t upload_box_tables() {
-    unsigned tri[8], adj[8];
-    build_box_tables(tri, adj);
-    cudaError_t e = cudaMemcpyToSymbol(c_box_tri, tri, sizeof(tri));
-    if (e != cudaSuccess) return e;
-    return cudaMemcpyToSymbol(c_box_adj, adj, sizeof(adj));
-}
-
 cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps) {
     if (cp.ncells <= 0) return cudaSuccess;
     warps = warps < 1 ? 4 : (warps > 4 ? 4 : warps);   // the kernels are built for at most 4 warps per CTA
-    if (mode == VGPU_FP64) {
-        return big ? launch_one<VGPU_FP64, 4>(cp, warps, sms, s) : launch_one<VGPU_FP64, 2>(cp, warps, sms, s);
-    }
-    return big ? launch_one<VGPU_MIXED, 4>(cp, warps, sms, s) : launch_one<VGPU_MIXED, 2>(cp, warps, sms, s);
+    return mode == VGPU_FP64 ? launch_cells_fp64(cp, big, sms, s, warps) : launch_cells_mixed(cp, big, sms, s, warps);
 }
 
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s) {
     if (bp.ncells <= 0) return cudaSuccess;
-    if (mode == VGPU_FP64) {
-        return big ? launch_batch_one<VGPU_FP64, 4>(bp, sms, s) : launch_batch_one<VGPU_FP64, 2>(bp, sms, s);
-    }
-    return big ? launch_batch_one<VGPU_MIXED, 4>(bp, sms, s) : launch_batch_one<VGPU_MIXED, 2>(bp, sms, s);
-}
-
-template <int MODE>
-cudaError_t launch_finish_t(const CellParams &cp, int sms, cudaStream_t s) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel<MODE>, 128, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sms * per_sm;
-    const long long need = (cp.ncells + 3) / 4;
-    const int grid = (int)(want < need ? want : need);
-    finish_kernel<MODE><<<grid, 128, 0, s>>>(cp);
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s) {
-    if (cp.ncells <= 0 || cp.rec == nullptr) return cudaSuccess;
-    return mode == VGPU_FP64 ? launch_finish_t<VGPU_FP64>(cp, sms, s) : launch_finish_t<VGPU_MIXED>(cp, sms, s);
-}
-
-template <int MODE>
-cudaError_t launch_finish_batch_t(const BatchParams &bp, int sms, cudaStream_t s) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel<MODE>, 128, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long want = (long long)sms * per_sm;
-    const long long need = (bp.ncells + 3) / 4;
-    const int grid = (int)(want < need ? want : need);
-    finish_batch_kernel<MODE><<<grid, 128, 0, s>>>(bp);
-    note_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s) {
-    if (bp.ncells <= 0) return cudaSuccess;
-    return mode == VGPU_FP64 ? launch_finish_batch_t<VGPU_FP64>(bp, sms, s)
-                             : launch_finish_batch_t<VGPU_MIXED>(bp, sms, s);
+    return mode == VGPU_FP64 ? launch_cells_batch_fp64(bp, big, sms, s) : launch_cells_batch_mixed(bp, big, sms, s);
 }
 
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s) {

@@ -74,4 +74,29 @@ static __device__ __forceinline__ void solve_f64(const double4 A, const double4 
 }
 
 
+// ------------------------------------------------------------------ warp helpers
+static __device__ __forceinline__ unsigned long long warp_or64(unsigned long long x) {
+    unsigned lo = __reduce_or_sync(kFull, (unsigned)x);
+    unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
+    return ((unsigned long long)hi << 32) | lo;
+}
+static __device__ __forceinline__ float warp_maxf(float x) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, d));
+    return x;
+}
+static __device__ __forceinline__ double warp_sumd(double x) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFull, x, d);
+    return x;
+}
+static __device__ __forceinline__ int warp_incl_scan(int x, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+    }
+    return x;
+}
+
 }  // namespace vgpu

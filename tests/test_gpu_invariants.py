@@ -92,3 +92,18 @@ def test_mixed_and_fp64_agree_on_the_4m_periodic_box(gpu):
     # the FP64 fallback rate of the mixed engine
     assert sa["fp64_repairs"] <= 0.01 * sa["side_tests"]
     assert sb["marginal_cells"] == 0
+
+
+@pytest.mark.gpu
+def test_large_container_24m(gpu):
+    """A container whose polytope records pass 4G words of offsets (24M
+    cells): no cell fails, volumes still sum to the box."""
+    n = 24_000_000
+    L = 100.0 * (n / 4e6) ** (1 / 3)
+    g = int(round((n / 5.0) ** (1 / 3)))
+    w = W.periodic_cube(n=n, L=L, seed=1010, grid=(g, g, g))
+    con = vg.from_workload(w, mode="mixed")
+    con.compute_all_cells()
+    st = con.stats()
+    assert st["cells"] == n and st["failed_cells"] == 0
+    assert abs(con.sum_cell_volumes() - L ** 3) <= 1e-9 * L ** 3

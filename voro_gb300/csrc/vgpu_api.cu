@@ -565,14 +565,14 @@ int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt) {
     if (h->nkept <= 0) return VGPU_OK;
     cudaStream_t s = h->stream;
     const unsigned long long cap = std::min<unsigned long long>(
-        (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), 0xfffffff0ull);
+        (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), ~0ull >> 8);
     VG_CUDA(h->rec.ensure(cap * 4));
-    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 4));
-    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 4, s));
+    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 8));
+    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 8, s));
     cp.rec = h->rec.as<unsigned>();
     cp.rec_cap = cap;
     cp.rec_used = &cnt->rec_used;
-    cp.rec_off = h->rec_off.as<unsigned>();
+    cp.rec_off = h->rec_off.as<unsigned long long>();
     if (h->output & VGPU_OUTPUT_POLYTOPES) {
         const unsigned long long pcap = (unsigned long long)h->nkept * kPolyDoublesPerCell + (1u << 16);
         VG_CUDA(h->poly.ensure(pcap * 8));

@@ -966,15 +966,17 @@ struct Engine {
                 rp[2 * nf + r] = (unsigned)S.pid[q];
             }
         }
-        if (lane == 0) P.rec_off[C.k] = (unsigned)off;
+        if (lane == 0) P.rec_off[C.k] = off;
         return true;
     }
 };
 
 // CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot) engine;
-// it fixes the register budget (65536 / (128 * blocks)).
+// it fixes the register budget (65536 / (128 * blocks)).  Measured on the 4M
+// periodic box: 3 (168 registers, few spills, 12 warps per SM) clips in 124 ms,
+// 4 (128 registers, spills) in 154 ms, 2 in 160 ms.
 #ifndef VGPU_MIN_BLOCKS
-#define VGPU_MIN_BLOCKS 4
+#define VGPU_MIN_BLOCKS 3
 #endif
 template <int MODE, int K>
 constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }

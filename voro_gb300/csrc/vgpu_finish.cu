@@ -108,7 +108,7 @@ template <int MODE>
 __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int lane) {
     constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;
     constexpr int SL = kFinMaxV / 32;
-    const unsigned off = P.rec_off[k];
+    const unsigned long long off = P.rec_off[k];
     if (off == kNoRecord) return;
     const unsigned *R = P.rec + off;
     const int nv = (int)R[0], nf = (int)R[1];

@@ -99,7 +99,7 @@ struct CellParams {
     unsigned *rec;
     unsigned long long rec_cap;     // words
     unsigned long long *rec_used;   // bump allocator (words)
-    unsigned *rec_off;              // per engine index: record offset, kNoRecord if none
+    unsigned long long *rec_off;    // per engine index: record offset (words), kNoRecord if none
     // Optional polytope output (written by the finish kernel), NULL: none.
     // Per cell [nv, nf, vertices (3 nv), per face: neighbour, count, loop].
     double *poly;
@@ -107,7 +107,7 @@ struct CellParams {
     unsigned long long *poly_used;  // bump allocator (doubles)
     long long *poly_off;            // per loop-order cell: offset, -1 none, -2 store full
 };
-constexpr unsigned kNoRecord = 0xffffffffu;
+constexpr unsigned long long kNoRecord = ~0ull;
 constexpr int kRecHeader = 5;
 
 // Many containers in one persistent launch: cells are numbered globally,

@@ -1,5 +1,6 @@
 """Batched containers (vgpu_batch_*): many containers computed by one
-persistent launch give exactly the per-container results."""
+persistent launch give the per-container results (same topology exactly,
+volumes and centroids to the last few bits)."""
 import numpy as np
 import pytest
 
@@ -55,10 +56,16 @@ def test_batch_equals_one_container_at_a_time(gpu):
         r = c.cells()
         assert np.array_equal(r.ids, a.ids), k
         assert np.array_equal(r.flags, a.flags), k
-        assert np.array_equal(r.vol, a.vol), k
-        assert np.array_equal(r.cen, a.cen), k
+        assert np.array_equal(r.nf, a.nf), k
+        assert np.array_equal(r.nv, a.nv), k
         assert np.array_equal(r.nb_off, a.nb_off), k
         assert np.array_equal(r.nb, a.nb), k
-    # a second compute of the same batch gives the same again
+        # the finish kernel sums a cell's terms in an order that depends on
+        # which cell shares its warp, so the last bits may differ
+        assert np.allclose(r.vol, a.vol, rtol=1e-13, atol=0), k
+        scale = np.cbrt(np.maximum(a.vol, 1e-300))[:, None]
+        assert (np.abs(r.cen - a.cen) / scale).max() <= 1e-13, k
+    # a second compute of the same batch gives exactly the same again
+    first = cons[3].cells().vol.copy()
     b.compute_all_cells(mode="mixed")
-    assert np.array_equal(cons[3].cells().vol, single[3].vol)
+    assert np.array_equal(cons[3].cells().vol, first)

@@ -67,58 +67,76 @@ __device__ __forceinline__ double3 refine_vertex_rec(const FinishShared &F, unsi
     return v;
 }
 
-// Warp sums of four values with few FP64 additions (the FP64 pipe bounds the
-// finish kernel): halves of the warp first fold different pairs, then
-// quarters different singles, then each quarter folds its own; the four sums
-// end in lanes 0, 8, 16, 24 and are broadcast.  Fixed order: deterministic.
-__device__ __forceinline__ void warp_sum4(double &a, double &b, double &c, double &d, int lane) {
-    const bool lo = lane < 16;
+// Sums of four values over a group of G lanes (G = 32 or 16) with few FP64
+// additions (the FP64 pipe bounds the finish kernel): halves of the group
+// first fold different pairs, then quarters different singles, then each
+// quarter folds its own; the four sums end in the group's lanes 0, G/4, G/2,
+// 3G/4 and are broadcast.  Fixed order: deterministic.
+template <int G>
+__device__ __forceinline__ void group_sum4(double &a, double &b, double &c, double &d, int gl) {
+    const bool lo = gl < G / 2;
     double k0 = lo ? a : c, k1 = lo ? b : d;
     const double s0 = lo ? c : a, s1 = lo ? d : b;
-    k0 += __shfl_xor_sync(kFull, s0, 16);
-    k1 += __shfl_xor_sync(kFull, s1, 16);
-    const bool lo8 = (lane & 8) == 0;
-    double k = lo8 ? k0 : k1;
-    k += __shfl_xor_sync(kFull, lo8 ? k1 : k0, 8);
-    k += __shfl_xor_sync(kFull, k, 4);
-    k += __shfl_xor_sync(kFull, k, 2);
-    k += __shfl_xor_sync(kFull, k, 1);
-    a = __shfl_sync(kFull, k, 0);
-    b = __shfl_sync(kFull, k, 8);
-    c = __shfl_sync(kFull, k, 16);
-    d = __shfl_sync(kFull, k, 24);
+    k0 += __shfl_xor_sync(kFull, s0, G / 2, G);
+    k1 += __shfl_xor_sync(kFull, s1, G / 2, G);
+    const bool lo4 = (gl & (G / 4)) == 0;
+    double k = lo4 ? k0 : k1;
+    k += __shfl_xor_sync(kFull, lo4 ? k1 : k0, G / 4, G);
+#pragma unroll
+    for (int dd = G / 8; dd >= 1; dd >>= 1) k += __shfl_xor_sync(kFull, k, dd, G);
+    a = __shfl_sync(kFull, k, 0, G);
+    b = __shfl_sync(kFull, k, G / 4, G);
+    c = __shfl_sync(kFull, k, G / 2, G);
+    d = __shfl_sync(kFull, k, 3 * G / 4, G);
 }
 
-// Warp maximum of non-negative doubles by their bit patterns (ordered like
-// the values), on the integer reduction unit instead of the FP64 pipe.
-__device__ __forceinline__ double warp_max_nonneg(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned mhi = __reduce_max_sync(kFull, hi);
-    const unsigned mlo = __reduce_max_sync(kFull, hi == mhi ? lo : 0u);
-    return __longlong_as_double((long long)(((unsigned long long)mhi << 32) | mlo));
+// Maximum of non-negative doubles over a group of G lanes by their bit
+// patterns (ordered like the values), on integer units instead of the FP64 pipe.
+template <int G>
+__device__ __forceinline__ double group_max_nonneg(double x) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(x);
+#pragma unroll
+    for (int dd = G / 2; dd >= 1; dd >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(kFull, b, dd, G);
+        b = o > b ? o : b;
+    }
+    return __longlong_as_double((long long)b);
+}
+
+template <int G>
+__device__ __forceinline__ int group_incl_scan(int x, int gl) {
+#pragma unroll
+    for (int dd = 1; dd < G; dd <<= 1) {
+        const int y = __shfl_up_sync(kFull, x, dd, G);
+        if (gl >= dd) x += y;
+    }
+    return x;
 }
 
 __device__ __forceinline__ double rec_double(const unsigned *w) {
     return __longlong_as_double((long long)((unsigned long long)w[0] | ((unsigned long long)w[1] << 32)));
 }
 
-// The reductions of cell k (engine order) from its record, if it has one.
-template <int MODE>
-__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int lane) {
+// The reductions of cell k (engine order, k < 0: none) from its record, if it
+// has one, by a group of G lanes: G = 32 for any cell, G = 16 (two cells per
+// warp, one per half) for cells of at most 64 vertices.  Every collective is
+// reached by both halves of the warp whatever their cells.
+template <int MODE, int G>
+__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int gl) {
     constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;
-    constexpr int SL = kFinMaxV / 32;
-    const unsigned long long off = P.rec_off[k];
-    if (off == kNoRecord) return;
-    const unsigned *R = P.rec + off;
-    const int nv = (int)R[0], nf = (int)R[1];
-    const unsigned fl = R[2];
+    constexpr int SL = 4;   // vertex slots per lane: 128 vertices (G = 32) or 64 (G = 16)
+    static_assert(SL * 32 == kFinMaxV, "slot count");
+    const unsigned long long off = k >= 0 ? P.rec_off[k] : kNoRecord;
+    const bool have = off != kNoRecord;
+    const unsigned *R = P.rec + (have ? off : 0);
+    const int nv = have ? (int)R[0] : 0, nf = have ? (int)R[1] : 0;
+    const unsigned fl = have ? R[2] : 0u;
     const unsigned *rv = R + kRecHeader;
     const unsigned *rp = rv + (2 + VW) * nv;
-    const double4 me = P.a.p64[k];
-    const int out = P.a.outpos[k];
+    const double4 me = have ? P.a.p64[k] : make_double4(0, 0, 0, 0);
+    const int out = have ? P.a.outpos[k] : 0;
     // planes: neighbour IDs (plane order), sources, FP64 planes
-    for (int q = lane; q < nf; q += 32) {
+    for (int q = gl; q < nf; q += G) {
         F.psrc[q] = (int)rp[q];
         F.pshift[q] = (int)rp[nf + q];
         F.rep[q] = 0x7fffffff;
@@ -134,7 +152,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     double mr2 = 0.0;
 #pragma unroll
     for (int s = 0; s < SL; s++) {
-        const int t = lane + 32 * s;
+        const int t = gl + G * s;
         tri[s] = 0;
         vx[s] = vy[s] = vz[s] = 0.0;
         if (t < nv) {
@@ -161,15 +179,15 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         }
     }
     // origin of the sums: vertex 0
-    const double c0x = __shfl_sync(kFull, vx[0], 0);
-    const double c0y = __shfl_sync(kFull, vy[0], 0);
-    const double c0z = __shfl_sync(kFull, vz[0], 0);
+    const double c0x = __shfl_sync(kFull, vx[0], 0, G);
+    const double c0y = __shfl_sync(kFull, vy[0], 0, G);
+    const double c0z = __shfl_sync(kFull, vz[0], 0, G);
     int ne = 0;
     unsigned own[SL];
 #pragma unroll
     for (int s = 0; s < SL; s++) {
         own[s] = 0;
-        const int t = lane + 32 * s;
+        const int t = gl + G * s;
         if (t < nv) {
             F.vx[t] = vx[s] - c0x;
             F.vy[t] = vy[s] - c0y;
@@ -181,20 +199,20 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             ne += __popc(own[s]);
         }
     }
-    const int eincl = warp_incl_scan(ne, lane);
-    const int etot = __shfl_sync(kFull, eincl, 31);
+    const int eincl = group_incl_scan<G>(ne, gl);
+    const int etot = __shfl_sync(kFull, eincl, G - 1, G);
     {
         int q = eincl - ne;
 #pragma unroll
         for (int s = 0; s < SL; s++)
 #pragma unroll
             for (int e = 0; e < 3; e++)
-                if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(lane + 32 * s) | ((unsigned)e << 8);
+                if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(gl + G * s) | ((unsigned)e << 8);
     }
     __syncwarp();
     // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
     double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-    for (int i = lane; i < etot; i += 32) {
+    for (int i = gl; i < etot; i += G) {
         const unsigned E = F.stage[i];
         const int t = E & 255u, e = E >> 8;
         const unsigned T = F.tri[t];
@@ -215,9 +233,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         cy += dd * (ty + uy) + dy * by - dx * ay;
         cz += dd * (tz + uz) + dy * bz - dx * az;
     }
-    warp_sum4(vs, cx, cy, cz, lane);
-    mr2 = warp_max_nonneg(mr2);
-    if (lane == 0) {
+    group_sum4<G>(vs, cx, cy, cz, gl);
+    mr2 = group_max_nonneg<G>(mr2);
+    if (have && gl == 0) {
         const double vol = vs / 6.0;
         P.r.vol[out] = vol;
         if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
@@ -233,7 +251,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         P.r.maxr2[out] = mr2;
         P.r.flags[out] = VGPU_CELL_OK | (int)fl;
     }
-    if (P.poly != nullptr) {
+    if (P.poly != nullptr) {   // (uniform: P is the same for both halves of a warp)
         // the polytope: [nv, nf, vertices (3 nv, particle-relative), then per
         // face (plane order): neighbour ID, vertex count, vertex loop]; each
         // loop walks the face by the edges that start on it, which orders the
@@ -241,70 +259,106 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         // face_vertices does (src/cell.cc:2285-2308)
         const unsigned long long need = 2ull + 6ull * (unsigned long long)nv + 2ull * (unsigned long long)nf;
         unsigned long long po = 0;
-        if (lane == 0) po = atomicAdd(P.poly_used, need);
-        po = __shfl_sync(kFull, po, 0);
-        if (po + need <= P.poly_cap) {
-            double *D = P.poly + po;
-            if (lane == 0) {
+        if (have && gl == 0) po = atomicAdd(P.poly_used, need);
+        po = __shfl_sync(kFull, po, 0, G);
+        const bool fits = have && po + need <= P.poly_cap;
+        double *D = P.poly + (fits ? po : 0);
+        if (fits) {
+            if (gl == 0) {
                 D[0] = (double)nv;
                 D[1] = (double)nf;
             }
 #pragma unroll
             for (int s = 0; s < SL; s++) {
-                const int t = lane + 32 * s;
+                const int t = gl + G * s;
                 if (t < nv) {
                     D[2 + 3 * t] = vx[s];
                     D[3 + 3 * t] = vy[s];
                     D[4 + 3 * t] = vz[s];
                 }
             }
-            double *DF = D + 2 + 3 * nv;
-            for (int q0 = 0; q0 < nf; q0 += 32) {
-                const int q = q0 + lane;
-                const int ord = q < nf ? F.ford[q] : 0;
-                // faces before q: q0 * 2 header words plus their orders
-                int before = 0;
-                for (int j = 0; j < q0; j++) before += F.ford[j];
-                const int incl = warp_incl_scan(ord, lane);
-                if (q < nf) {
-                    double *df = DF + 2 * q + before + (incl - ord);
-                    df[0] = (double)P.r.nb[(size_t)out * kMaxNb + q];
-                    df[1] = (double)ord;
-                    int t = F.rep[q];
-                    for (int j = 0; j < ord; j++) {
-                        df[2 + j] = (double)t;
-                        const unsigned T = F.tri[t];
-                        const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
-                        t = (F.adj[t] >> (8 * e)) & 255u;
-                    }
+        }
+        // face loops; the loop over face chunks runs the same number of times
+        // in both halves, because it holds a group scan
+        double *DF = D + 2 + 3 * nv;
+        const int nfmax = __reduce_max_sync(kFull, fits ? nf : 0);
+        for (int q0 = 0; q0 < nfmax; q0 += G) {
+            const int q = q0 + gl;
+            const bool mine = fits && q < nf;
+            const int ord = mine ? F.ford[q] : 0;
+            // faces before q: q * 2 header words plus their orders
+            int before = 0;
+            if (fits)
+                for (int j = 0; j < q0 && j < nf; j++) before += F.ford[j];
+            const int incl = group_incl_scan<G>(ord, gl);
+            if (mine) {
+                double *df = DF + 2 * q + before + (incl - ord);
+                df[0] = (double)P.r.nb[(size_t)out * kMaxNb + q];
+                df[1] = (double)ord;
+                int t = F.rep[q];
+                for (int j = 0; j < ord; j++) {
+                    df[2 + j] = (double)t;
+                    const unsigned T = F.tri[t];
+                    const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
+                    t = (F.adj[t] >> (8 * e)) & 255u;
                 }
             }
-            if (lane == 0) P.poly_off[out] = (long long)po;
-        } else if (lane == 0) {
+        }
+        if (fits) {
+            if (gl == 0) P.poly_off[out] = (long long)po;
+        } else if (have && gl == 0) {
             P.poly_off[out] = -2;   // store full
         }
     }
     __syncwarp();
 }
 
+constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
+
+// Two cells per warp, one per 16-lane half, when both have at most 64
+// vertices (nearly always: their FP64 work then fills the lanes better);
+// otherwise the whole warp does one cell after the other.
 template <int MODE>
-__global__ void __launch_bounds__(128) finish_kernel(const __grid_constant__ CellParams P) {
-    __shared__ FinishShared fsh[4];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = gridDim.x * 4;
-    for (int k = blockIdx.x * 4 + wid; k < P.ncells; k += nwarps) finish_record<MODE>(P, fsh[wid], k, lane);
+__device__ __forceinline__ void finish_pair(const CellParams &P, FinishShared *F2, int k0, int k1, int lane) {
+    const int half = lane >> 4, gl = lane & 15;
+    const int mine = half ? k1 : k0;
+    int nv = 0;
+    if (mine >= 0) {
+        const unsigned long long off = P.rec_off[mine];
+        if (off != kNoRecord) nv = (int)P.rec[off];
+    }
+    if (!__any_sync(kFull, nv > 64)) {
+        finish_record<MODE, 16>(P, F2[half], mine, gl);
+    } else {
+        finish_record<MODE, 32>(P, F2[0], k0, lane);
+        finish_record<MODE, 32>(P, F2[0], k1, lane);
+    }
 }
 
-// The same over the cells of a batch (global numbering as cell_batch_kernel).
 template <int MODE>
-__global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant__ BatchParams B) {
-    __shared__ FinishShared fsh[4];
-    __shared__ __align__(16) unsigned char cpw[4][(sizeof(CellParams) + 15) & ~(size_t)15];
+__global__ void __launch_bounds__(32 * kFinWarps) finish_kernel(const __grid_constant__ CellParams P) {
+    __shared__ FinishShared fsh[kFinWarps][2];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int npairs = (P.ncells + 1) / 2;
+    for (int pi = blockIdx.x * kFinWarps + wid; pi < npairs; pi += gridDim.x * kFinWarps) {
+        const int i0 = 2 * pi, i1 = 2 * pi + 1;
+        const int k0 = P.cell_list ? P.cell_list[i0] : i0;
+        const int k1 = i1 < P.ncells ? (P.cell_list ? P.cell_list[i1] : i1) : -1;
+        finish_pair<MODE>(P, fsh[wid], k0, k1, lane);
+    }
+}
+
+// The same over the cells of a batch (global numbering as cell_batch_kernel);
+// a pair never straddles two containers.
+template <int MODE>
+__global__ void __launch_bounds__(32 * kFinWarps) finish_batch_kernel(const __grid_constant__ BatchParams B) {
+    __shared__ FinishShared fsh[kFinWarps][2];
+    __shared__ __align__(16) unsigned char cpw[kFinWarps][(sizeof(CellParams) + 15) & ~(size_t)15];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     CellParams &P = *reinterpret_cast<CellParams *>(cpw[wid]);
-    const long long nwarps = (long long)gridDim.x * 4;
+    const long long nwarps = (long long)gridDim.x * kFinWarps;
     long long cbeg = 0, cend = 0;
-    for (long long g = (long long)blockIdx.x * 4 + wid; g < B.ncells; g += nwarps) {
+    for (long long g = 2 * ((long long)blockIdx.x * kFinWarps + wid); g < B.ncells; g += 2 * nwarps) {
         if (g < cbeg || g >= cend) {
             int lo = 0, hi = B.ncont;
             while (hi - lo > 1) {
@@ -320,7 +374,28 @@ __global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant
             for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
             __syncwarp();
         }
-        finish_record<MODE>(P, fsh[wid], (int)(g - cbeg), lane);
+        // the pair (g, g+1); its second cell may belong to the next container
+        const int k0 = (int)(g - cbeg);
+        const int k1 = g + 1 < cend ? (int)(g + 1 - cbeg) : -1;
+        finish_pair<MODE>(P, fsh[wid], k0, k1, lane);
+        if (k1 < 0 && g + 1 < B.ncells) {
+            // g + 1 starts the next container: finish it with that container's parameters
+            const long long g1 = g + 1;
+            int lo = 0, hi = B.ncont;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (B.cell_start[mid] <= g1) lo = mid;
+                else hi = mid;
+            }
+            cbeg = B.cell_start[lo];
+            cend = B.cell_start[lo + 1];
+            __syncwarp();
+            const unsigned *src = reinterpret_cast<const unsigned *>(B.cps + lo);
+            unsigned *dst = reinterpret_cast<unsigned *>(&P);
+            for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
+            __syncwarp();
+            finish_pair<MODE>(P, fsh[wid], (int)(g1 - cbeg), -1, lane);
+        }
     }
 }
 
@@ -329,13 +404,13 @@ __global__ void __launch_bounds__(128) finish_batch_kernel(const __grid_constant
 template <int MODE>
 cudaError_t launch_finish_t(const CellParams &cp, int sms, cudaStream_t s) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel<MODE>, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_kernel<MODE>, 32 * kFinWarps, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
-    const long long need = (cp.ncells + 3) / 4;
+    const long long need = ((cp.ncells + 1) / 2 + kFinWarps - 1) / kFinWarps;
     const int grid = (int)(want < need ? want : need);
-    finish_kernel<MODE><<<grid, 128, 0, s>>>(cp);
+    finish_kernel<MODE><<<grid, 32 * kFinWarps, 0, s>>>(cp);
     note_launch();
     return cudaGetLastError();
 }
@@ -348,13 +423,13 @@ cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t 
 template <int MODE>
 cudaError_t launch_finish_batch_t(const BatchParams &bp, int sms, cudaStream_t s) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel<MODE>, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, finish_batch_kernel<MODE>, 32 * kFinWarps, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
-    const long long need = (bp.ncells + 3) / 4;
+    const long long need = ((bp.ncells + 1) / 2 + kFinWarps - 1) / kFinWarps;
     const int grid = (int)(want < need ? want : need);
-    finish_batch_kernel<MODE><<<grid, 128, 0, s>>>(bp);
+    finish_batch_kernel<MODE><<<grid, 32 * kFinWarps, 0, s>>>(bp);
     note_launch();
     return cudaGetLastError();
 }

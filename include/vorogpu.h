@@ -181,7 +181,8 @@ int vgpu_phase_cycles(vgpu_container *h, double out[8]);
 int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t **dev_nfaces);
 
 /* Engine tuning: target particles per engine block (0 = default 0.6) and warps
- * (cells in flight) per CTA of the clipping kernel, 1-4 (0 = default 4).
+ * (cells in flight) per CTA of the clipping kernel, 1-8, at most what the
+ * library was built for (0 = default 4).
  * Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
 

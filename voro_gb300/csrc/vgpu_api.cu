@@ -379,7 +379,7 @@ int vgpu_clear(vgpu_container *h) {
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
     if (particles_per_block > 0) h->target_density = particles_per_block;
-    if (warps_per_cta > 4) return fail(VGPU_ERR_ARG, "at most 4 warps per CTA (got %d)", warps_per_cta);
+    if (warps_per_cta > 8) return fail(VGPU_ERR_ARG, "at most 8 warps per CTA (got %d)", warps_per_cta);
     if (warps_per_cta > 0) h->warps_per_cta = warps_per_cta;
     return VGPU_OK;
 }

@@ -78,7 +78,7 @@ void box_tables(unsigned tri[8], unsigned adj[8]) { build_box_tables(tri, adj); 
 
 cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps) {
     if (cp.ncells <= 0) return cudaSuccess;
-    warps = warps < 1 ? 4 : (warps > 4 ? 4 : warps);   // the kernels are built for at most 4 warps per CTA
+    warps = warps < 1 ? 4 : (warps > 8 ? 8 : warps);   // the clipping translation units clamp further
     return mode == VGPU_FP64 ? launch_cells_fp64(cp, big, sms, s, warps) : launch_cells_mixed(cp, big, sms, s, warps);
 }
 

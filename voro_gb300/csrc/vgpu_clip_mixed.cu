@@ -6,6 +6,7 @@
 namespace vgpu {
 
 cudaError_t launch_cells_mixed(const CellParams &cp, int big, int sms, cudaStream_t s, int warps) {
+    if (warps > kMaxCtaWarps) warps = kMaxCtaWarps;
     return big ? launch_one<VGPU_MIXED, 4>(cp, warps, sms, s) : launch_one<VGPU_MIXED, 2>(cp, warps, sms, s);
 }
 

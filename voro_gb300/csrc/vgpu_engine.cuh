@@ -978,11 +978,17 @@ struct Engine {
 #ifndef VGPU_MIN_BLOCKS
 #define VGPU_MIN_BLOCKS 3
 #endif
+// Largest CTA the clipping kernels are built for (threads); the default
+// launch uses 4 warps.
+#ifndef VGPU_CTA_THREADS
+#define VGPU_CTA_THREADS 128
+#endif
+constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
 template <int MODE, int K>
 constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
 
 template <int MODE, int K>
-__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
+__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *offsets = reinterpret_cast<int *>(smem_raw);
@@ -1043,7 +1049,7 @@ __global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_kernel(const 
 // copies that container's parameters into its shared slot and flushes its
 // counters to the previous container's.
 template <int MODE, int K>
-__global__ void __launch_bounds__(128, min_blocks<MODE, K>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
+__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;

@@ -69,3 +69,58 @@ def test_batch_equals_one_container_at_a_time(gpu):
     first = cons[3].cells().vol.copy()
     b.compute_all_cells(mode="mixed")
     assert np.array_equal(cons[3].cells().vol, first)
+
+
+@pytest.mark.gpu
+def test_batch_edge_members(gpu):
+    """Members binned by the one-CTA path next to ones binned by the
+    multi-kernel path: an empty container, one that drops particles outside
+    its walls, one of exactly the small-path limit and one just above it."""
+    rng = np.random.default_rng(5)
+
+    def walled(n):
+        c = vg.container(0, 1, 0, 1, 0, 1, 6, 6, 6, False, False, False, mode="mixed")
+        xyz = rng.uniform(-0.2, 1.2, size=(n, 3))
+        c.put_array(np.arange(n, dtype=np.int32), xyz)
+        return c
+
+    def periodic(n):
+        c = vg.container_periodic(10, 0, 10, 0, 0, 10, 8, 8, 8, mode="mixed")
+        c.put_array(np.arange(n, dtype=np.int32), rng.uniform(0, 10, size=(n, 3)))
+        return c
+
+    makers = [lambda: walled(0), lambda: walled(3000), lambda: periodic(4096), lambda: periodic(4097),
+              lambda: walled(1)]
+    state = rng.bit_generator.state
+    single = []
+    for m in makers:
+        c = m()
+        c.compute_all_cells()
+        single.append(c.cells())
+    rng.bit_generator.state = state
+    cons = [m() for m in makers]
+    b = vg.batch(cons)
+    b.compute_all_cells(mode="mixed")
+    for k, (c, a) in enumerate(zip(cons, single)):
+        r = c.cells()
+        assert len(r) == len(a), k
+        assert np.array_equal(r.ids, a.ids), k
+        assert np.array_equal(r.pos, a.pos), k
+        assert np.array_equal(r.nf, a.nf), k
+        assert np.array_equal(r.nb, a.nb), k
+        assert np.allclose(r.vol, a.vol, rtol=1e-13, atol=0), k
+    assert len(cons[0].cells()) == 0
+    assert 0 < len(cons[1].cells()) < 3000
+
+
+@pytest.mark.gpu
+def test_batch_reports_duplicates_in_a_small_member(gpu):
+    c = vg.container_periodic(10, 0, 10, 0, 0, 10, 4, 4, 4, mode="mixed")
+    xyz = np.random.default_rng(2).uniform(0, 10, size=(50, 3))
+    xyz[17] = xyz[3]
+    c.put_array(np.arange(50, dtype=np.int32), xyz)
+    with pytest.raises(vg.VoroError):
+        c.compute_all_cells()
+    b = vg.batch([c])
+    with pytest.raises(vg.VoroError):
+        b.compute_all_cells(mode="mixed")

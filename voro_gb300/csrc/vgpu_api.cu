@@ -388,6 +388,8 @@ int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per
 
 namespace {
 
+void fill_cell_params(vgpu_container *h, CellParams &cp);
+
 // Everything of a compute before the cell kernel: remap, loop-order sort,
 // duplicate check, engine-order sort and gather; fills cp for the engine.
 // Leaves the gather queued on the handle's stream (event ev[1] after it).
@@ -528,6 +530,16 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(cudaMemcpyAsync(h->offsets.p, ot.codes.data(), ot.codes.size() * 4, cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemsetAsync(h->counters.p, 0, sizeof(Counters), s));
     VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, sizeof(Counters), s));
+    h->nkept = nkept;
+    fill_cell_params(h, cp);
+    return VGPU_OK;
+}
+
+// The cell engine's parameters for the binned container h (h->nkept set).
+void fill_cell_params(vgpu_container *h, CellParams &cp) {
+    const OffsetTable &ot = offset_table();
+    const Geometry &g = h->g;
+    const int nkept = h->nkept;
     memset(&cp, 0, sizeof(cp));
     cp.g = g;
     cp.a.p64 = h->p64.as<double4>();
@@ -553,17 +565,88 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
     box_tables(cp.box_tri, cp.box_adj);
-    h->nkept = nkept;
+}
+
+// A batch member of at most kSmallBinMax particles is binned by one CTA of
+// small_bin_kernel: its buffers are sized for every particle (the number
+// kept is known only afterwards) and its job filled here; no launch.
+int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long long *result) {
+    if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
+    const int n = (int)n64;
+    Geometry &g = h->g;
+    memset(&h->stats, 0, sizeof(h->stats));
+    h->computed = false;
+    choose_engine_grid(g, n64, h->target_density);
+    const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
+    const size_t nn = (size_t)std::max(n, 1);
+    const int32_t *d_ids = h->use_device_input ? h->dev_ids_ext : h->ids_in.as<int32_t>();
+    const double *d_xyzr = h->use_device_input ? h->dev_xyzr_ext : h->xyzr_in.as<double>();
+    if (n > 0 && (!d_ids || !d_xyzr)) return fail(VGPU_ERR_INTERNAL, "container inputs missing");
+    if ((reinterpret_cast<uintptr_t>(d_xyzr) & 15u) != 0)
+        return fail(VGPU_ERR_ARG, "device xyzr must be 16-byte aligned");
+    VG_CUDA(h->rem.ensure(nn * 32));
+    VG_CUDA(h->outpos_in.ensure(nn * 4));
+    VG_CUDA(h->counters.ensure(sizeof(Counters)));
+    VG_CUDA(h->counters2.ensure(sizeof(Counters)));
+    VG_CUDA(h->r_vol.ensure(nn * 8));
+    VG_CUDA(h->r_cen.ensure(nn * 24));
+    VG_CUDA(h->r_nf.ensure(nn * 4));
+    VG_CUDA(h->r_nv.ensure(nn * 4));
+    VG_CUDA(h->r_mr2.ensure(nn * 8));
+    VG_CUDA(h->r_flags.ensure(nn * 4));
+    VG_CUDA(h->r_nb.ensure(nn * kMaxNb * 4));
+    VG_CUDA(h->r_ids.ensure(nn * 4));
+    VG_CUDA(h->r_pos.ensure(nn * 24));
+    VG_CUDA(h->r_rad.ensure(nn * 8));
+    VG_CUDA(h->p64.ensure(nn * 32));
+    VG_CUDA(h->l32.ensure(nn * 16));
+    VG_CUDA(h->pid.ensure(nn * 4));
+    VG_CUDA(h->outpos.ensure(nn * 4));
+    VG_CUDA(h->gblock.ensure(nn * 4));
+    VG_CUDA(h->bstart.ensure(((size_t)nblocks + 2) * 4));
+    VG_CUDA(h->ovf_list.ensure(nn * 4));
+    memset(&job, 0, sizeof(job));
+    job.g = g;
+    job.n = n;
+    job.nub = g.un[0] * g.un[1] * g.un[2];
+    job.nblocks = nblocks;
+    job.ids_in = d_ids;
+    job.xyzr_in = reinterpret_cast<const double4 *>(d_xyzr);
+    job.rem = h->rem.as<double4>();
+    job.outpos_in = h->outpos_in.as<int>();
+    job.p64 = h->p64.as<double4>();
+    job.l32 = h->l32.as<float4>();
+    job.pid = h->pid.as<int>();
+    job.outpos = h->outpos.as<int>();
+    job.gblock = h->gblock.as<int>();
+    job.bstart = h->bstart.as<int>();
+    job.res_ids = h->r_ids.as<int>();
+    job.res_pos = h->r_pos.as<double>();
+    job.res_rad = h->r_rad.as<double>();
+    job.result = result;
+    h->launches0 = launch_count();
+    return VGPU_OK;
+}
+
+// After small_bin_kernel: the kept count, largest radius and duplicate flag of h.
+int finish_small(vgpu_container *h, const unsigned long long res[2]) {
+    if (res[0] >> 32) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
+    h->nkept = (int)(res[0] & 0xffffffffu);
+    double rmax = 0.0;
+    memcpy(&rmax, &res[1], 8);
+    h->g.rmax = rmax;
+    h->g.rmax32 = (float)rmax * (1.0f + 1e-6f);
     return VGPU_OK;
 }
 
 // The record store the clipping kernels write and the finish kernel reads,
-// and the optional polytope output, for the compute of h described by cp.
-int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt) {
+// and the optional polytope output, for the compute of h described by cp;
+// the offset arrays are reset on stream s.
+int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt, cudaStream_t s) {
     cp.rec = nullptr;
     cp.poly = nullptr;
     if (h->nkept <= 0) return VGPU_OK;
-    cudaStream_t s = h->stream;
     const unsigned long long cap = std::min<unsigned long long>(
         (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), ~0ull >> 8);
     VG_CUDA(h->rec.ensure(cap * 4));
@@ -622,7 +705,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     int rc = prepare_cells(h, mode, cp);
     if (rc != VGPU_OK) return rc;
     cudaStream_t s = h->stream;
-    rc = setup_records(h, mode, cp, h->counters.as<Counters>());
+    rc = setup_records(h, mode, cp, h->counters.as<Counters>(), h->stream);
     if (rc != VGPU_OK) return rc;
     // clipping (64-vertex engine, then the 128-vertex one for the cells that
     // overflowed), then the finish kernel over every record
@@ -855,7 +938,8 @@ struct vgpu_batch {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4];
-    DevBuf cps, starts, counters, work, ovf_list;
+    DevBuf cps, starts, counters, work, ovf_list, jobs, bin_res, offsets;
+    bool offsets_ready = false;
     vgpu_stats stats{};
 };
 
@@ -888,7 +972,7 @@ int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
 int vgpu_batch_destroy(vgpu_batch *b) {
     if (!b) return VGPU_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list};
+    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list, &b->jobs, &b->bin_res, &b->offsets};
     for (DevBuf *d : bufs) d->release();
     for (int i = 0; i < 4; i++) cudaEventDestroy(b->ev[i]);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -907,22 +991,70 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     cudaStream_t s = b->stream;
     VG_CUDA(b->counters.ensure((size_t)nc * sizeof(Counters)));
     VG_CUDA(cudaMemsetAsync(b->counters.p, 0, (size_t)nc * sizeof(Counters), s));
-    // binning of every container on its own stream; the batch stream waits for each gather
+    const OffsetTable &ot = offset_table();
+    if (!b->offsets_ready) {
+        VG_CUDA(b->offsets.ensure(ot.codes.size() * 4));
+        VG_CUDA(cudaMemcpyAsync(b->offsets.p, ot.codes.data(), ot.codes.size() * 4, cudaMemcpyHostToDevice, s));
+        b->offsets_ready = true;
+    }
     std::vector<CellParams> cps(nc);
     std::vector<long long> starts(nc + 1, 0);
+    // members of at most kSmallBinMax particles: binned together, one CTA each
+    std::vector<int> small;
     for (int i = 0; i < nc; i++) {
+        const vgpu_container *h = b->members[i];
+        const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
+        if (n <= kSmallBinMax) small.push_back(i);
+    }
+    const int ns = (int)small.size();
+    if (ns > 0) {
+        std::vector<SmallBinJob> jobs(ns);
+        VG_CUDA(b->bin_res.ensure((size_t)ns * 16));
+        VG_CUDA(b->jobs.ensure((size_t)ns * sizeof(SmallBinJob)));
+        for (int j = 0; j < ns; j++) {
+            int rc = prepare_small(b->members[small[j]], mode, jobs[j], b->bin_res.as<unsigned long long>() + 2 * j);
+            if (rc != VGPU_OK) return rc;
+        }
+        VG_CUDA(cudaMemcpyAsync(b->jobs.p, jobs.data(), (size_t)ns * sizeof(SmallBinJob), cudaMemcpyHostToDevice, s));
+        for (int j = 0; j < ns; j++) cudaEventRecord(b->members[small[j]]->ev[0], s);
+        VG_CUDA(launch_small_bin(b->jobs.as<SmallBinJob>(), ns, s));
+        for (int j = 0; j < ns; j++) cudaEventRecord(b->members[small[j]]->ev[1], s);
+    }
+    // the others on their own streams; the batch stream waits for each gather
+    for (int i = 0, j = 0; i < nc; i++) {
+        if (j < ns && small[j] == i) {
+            j++;
+            continue;
+        }
         vgpu_container *h = b->members[i];
-        memset(&cps[i], 0, sizeof(CellParams));
         int rc = prepare_cells(h, mode, cps[i]);
         if (rc != VGPU_OK) return rc;
         cps[i].cnt = b->counters.as<Counters>() + i;
+        rc = setup_records(h, mode, cps[i], cps[i].cnt, h->stream);
+        if (rc != VGPU_OK) return rc;
+        cudaEventRecord(h->ev[2], h->stream);   // after the gather and the record resets
+        VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
+    }
+    if (ns > 0) {
+        std::vector<unsigned long long> res((size_t)ns * 2);
+        VG_CUDA(cudaMemcpyAsync(res.data(), b->bin_res.p, (size_t)ns * 16, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        for (int j = 0; j < ns; j++) {
+            const int i = small[j];
+            vgpu_container *h = b->members[i];
+            int rc = finish_small(h, &res[2 * (size_t)j]);
+            if (rc != VGPU_OK) return rc;
+            fill_cell_params(h, cps[i]);
+            cps[i].cnt = b->counters.as<Counters>() + i;
+            rc = setup_records(h, mode, cps[i], cps[i].cnt, s);
+            if (rc != VGPU_OK) return rc;
+        }
+    }
+    for (int i = 0; i < nc; i++) {
         cps[i].cell_list = nullptr;
         cps[i].overflow_list = nullptr;
-        rc = setup_records(h, mode, cps[i], cps[i].cnt);
-        if (rc != VGPU_OK) return rc;
-        starts[i + 1] = starts[i] + h->nkept;
-        cudaEventRecord(h->ev[2], h->stream);   // after the gather and the offsets upload
-        VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
+        cps[i].offsets = b->offsets.as<int>();   // the same table for every container
+        starts[i + 1] = starts[i] + b->members[i]->nkept;
     }
     const long long total = starts[nc];
     const auto t1 = std::chrono::steady_clock::now();
@@ -930,7 +1062,6 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     VG_CUDA(b->starts.ensure((size_t)(nc + 1) * 8));
     VG_CUDA(b->work.ensure(64));
     VG_CUDA(b->ovf_list.ensure((size_t)std::max<long long>(total, 1) * 8));
-    const OffsetTable &ot = offset_table();
     VG_CUDA(cudaMemcpyAsync(b->cps.p, cps.data(), (size_t)nc * sizeof(CellParams), cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemcpyAsync(b->starts.p, starts.data(), (size_t)(nc + 1) * 8, cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemsetAsync(b->work.p, 0, 64, s));
@@ -945,7 +1076,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     unsigned long long *wk = b->work.as<unsigned long long>();
     bp.work = wk;
     bp.overflow_count = wk + 1;
-    bp.offsets = cps[0].offsets;   // the same table for every container
+    bp.offsets = b->offsets.as<int>();
     bp.noffsets = (int)ot.codes.size();
     cudaEventRecord(b->ev[0], s);
     VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));

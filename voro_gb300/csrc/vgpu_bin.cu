@@ -20,11 +20,10 @@ __device__ __forceinline__ int step_int(double a) {
 __device__ __forceinline__ int step_mod(int a, int b) { return a >= 0 ? a % b : b - 1 - (b - 1 - a) % b; }
 __device__ __forceinline__ int step_div(int a, int b) { return a >= 0 ? a / b : -1 + (a + 1) / b; }
 
-__global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsigned long long *rmax_bits) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= bp.n) return;
-    const Geometry &g = bp.g;
-    double4 q = bp.xyzr_in[i];
+// The reference's placement of one particle: remapped position c, its
+// reference block key uk (nub if put() drops it) and engine block key gk.
+__device__ __forceinline__ bool remap_one(const Geometry &g, double4 q, int nub, int nblocks, double4 &out,
+                                          unsigned &uk, unsigned &gk) {
     double c[3] = {q.x, q.y, q.z};
     int b[3];
     bool ok = true;
@@ -52,7 +51,6 @@ __global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsi
             b[a] = ijk;
         }
     }
-    unsigned uk, gk;
     if (ok) {
         uk = (unsigned)(b[0] + g.un[0] * (b[1] + g.un[1] * b[2]));
         int e[3];
@@ -62,14 +60,43 @@ __global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsi
             e[a] = v < 0 ? 0 : (v >= g.gn[a] ? g.gn[a] - 1 : v);
         }
         gk = (unsigned)(e[0] + g.gn[0] * (e[1] + g.gn[1] * e[2]));
-        atomicAdd(kept, 1);
-        // radius_poly::max_radius over stored particles (src/container.cc:108)
-        if (g.poly) atomicMax(rmax_bits, (unsigned long long)__double_as_longlong(fmax(q.w, 0.0)));
     } else {
         uk = (unsigned)nub;
         gk = (unsigned)nblocks;
     }
-    bp.rem[i] = make_double4(c[0], c[1], c[2], q.w);
+    out = make_double4(c[0], c[1], c[2], q.w);
+    return ok;
+}
+
+// The engine-order record of particle i (input order) placed at engine index k.
+__device__ __forceinline__ void gather_one(const Geometry &g, int k, int b, double4 p, int id, int outpos_i,
+                                           double4 *p64, float4 *l32, int *pid, int *outpos, int *gblock) {
+    int bx = b % g.gn[0];
+    int by = (b / g.gn[0]) % g.gn[1];
+    int bz = b / (g.gn[0] * g.gn[1]);
+    double ox = g.lo[0] + bx * g.gbs[0];
+    double oy = g.lo[1] + by * g.gbs[1];
+    double oz = g.lo[2] + bz * g.gbs[2];
+    p64[k] = p;
+    l32[k] = make_float4((float)(p.x - ox), (float)(p.y - oy), (float)(p.z - oz), (float)p.w);
+    pid[k] = id;
+    outpos[k] = outpos_i;
+    gblock[k] = b;
+}
+
+__global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsigned long long *rmax_bits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= bp.n) return;
+    const Geometry &g = bp.g;
+    const double4 q = bp.xyzr_in[i];
+    double4 r;
+    unsigned uk, gk;
+    if (remap_one(g, q, nub, nblocks, r, uk, gk)) {
+        atomicAdd(kept, 1);
+        // radius_poly::max_radius over stored particles (src/container.cc:108)
+        if (g.poly) atomicMax(rmax_bits, (unsigned long long)__double_as_longlong(fmax(q.w, 0.0)));
+    }
+    bp.rem[i] = r;
     bp.ukey[i] = uk;
     bp.gkey[i] = gk;
     bp.idx[i] = i;
@@ -96,23 +123,116 @@ __global__ void gather_kernel(Geometry g, int nkept, const int *gorder, const un
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nkept) return;
     int i = gorder[k];
-    double4 p = rem[i];
     int b = (int)gkey_sorted[k];
-    int bx = b % g.gn[0];
-    int by = (b / g.gn[0]) % g.gn[1];
-    int bz = b / (g.gn[0] * g.gn[1]);
-    double ox = g.lo[0] + bx * g.gbs[0];
-    double oy = g.lo[1] + by * g.gbs[1];
-    double oz = g.lo[2] + bz * g.gbs[2];
-    p64[k] = p;
-    l32[k] = make_float4((float)(p.x - ox), (float)(p.y - oy), (float)(p.z - oz), (float)p.w);
-    pid[k] = ids_in[i];
-    outpos[k] = outpos_by_input[i];
-    gblock[k] = b;
+    gather_one(g, k, b, rem[i], ids_in[i], outpos_by_input[i], p64, l32, pid, outpos, gblock);
     int prev = k == 0 ? -1 : (int)gkey_sorted[k - 1];
     for (int q = prev + 1; q <= b; q++) bstart[q] = k;
     if (k == nkept - 1)
         for (int q = b + 1; q <= nblocks; q++) bstart[q] = nkept;
+}
+
+// The whole of put()'s binning for one small container in one CTA: remap,
+// the stable sort into loop order (reference block, then insertion order),
+// the duplicate check, the stable sort into engine order and the gather, with
+// the keys sorted in shared memory (bitonic, over 64-bit keys whose low half
+// is the input index: stable).  A batch bins all its small members with one
+// launch of this kernel instead of a dozen launches each.
+__device__ __forceinline__ void cta_bitonic(unsigned long long *key, int n2) {
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
+                const int i = 2 * j * (t / j) + (t % j);
+                const int l = i + j;
+                const bool up = (i & k) == 0;
+                const unsigned long long a = key[i], b = key[l];
+                if ((a > b) == up) {
+                    key[i] = b;
+                    key[l] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const SmallBinJob *jobs) {
+    extern __shared__ unsigned long long sbin[];
+    __shared__ int s_kept, s_dup;
+    __shared__ unsigned long long s_rmax;
+    const SmallBinJob &J = jobs[blockIdx.x];
+    const Geometry &g = J.g;
+    const int n = J.n;
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    unsigned long long *key = sbin;                                  // n2 keys
+    unsigned *gk_in = reinterpret_cast<unsigned *>(sbin + kSmallBinMax);   // engine key per input index
+    if (threadIdx.x == 0) {
+        s_kept = 0;
+        s_dup = 0;
+        s_rmax = 0ull;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        if (i < n) {
+            const double4 q = J.xyzr_in[i];
+            double4 r;
+            unsigned uk, gk;
+            if (remap_one(g, q, J.nub, J.nblocks, r, uk, gk)) {
+                atomicAdd(&s_kept, 1);
+                if (g.poly) atomicMax(&s_rmax, (unsigned long long)__double_as_longlong(fmax(q.w, 0.0)));
+            }
+            J.rem[i] = r;
+            key[i] = ((unsigned long long)uk << 32) | (unsigned)i;
+            gk_in[i] = gk;
+        } else {
+            key[i] = ~0ull;
+        }
+    }
+    __syncthreads();
+    cta_bitonic(key, n2);
+    const int nkept = s_kept;
+    // loop order (c_loop_all): stored ids, positions, radii; input -> result slot
+    for (int m = threadIdx.x; m < nkept; m += blockDim.x) {
+        const int i = (int)(key[m] & 0xffffffffu);
+        J.outpos_in[i] = m;
+        J.res_ids[m] = J.ids_in[i];
+        const double4 p = J.rem[i];
+        J.res_pos[3 * m] = p.x;
+        J.res_pos[3 * m + 1] = p.y;
+        J.res_pos[3 * m + 2] = p.z;
+        J.res_rad[m] = p.w;
+        // check_duplicate within the reference block (src/common.cc:14-20)
+        if (g.unit_cell) {
+            const unsigned blk = (unsigned)(key[m] >> 32);
+            for (int q = m + 1; q < nkept && (unsigned)(key[q] >> 32) == blk; q++) {
+                const double4 o = J.rem[(int)(key[q] & 0xffffffffu)];
+                const double dx = o.x - p.x, dy = o.y - p.y, dz = o.z - p.z;
+                if (dx * dx + dy * dy + dz * dz < 1e-10) s_dup = 1;
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n2; i += blockDim.x)
+        key[i] = i < n ? (((unsigned long long)gk_in[i] << 32) | (unsigned)i) : ~0ull;
+    __syncthreads();
+    cta_bitonic(key, n2);
+    // engine order and the block starts
+    for (int k = threadIdx.x; k < nkept; k += blockDim.x) {
+        const int i = (int)(key[k] & 0xffffffffu);
+        const int b = (int)(key[k] >> 32);
+        gather_one(g, k, b, J.rem[i], J.ids_in[i], J.outpos_in[i], J.p64, J.l32, J.pid, J.outpos, J.gblock);
+        const int prev = k == 0 ? -1 : (int)(key[k - 1] >> 32);
+        for (int q = prev + 1; q <= b; q++) J.bstart[q] = k;
+        if (k == nkept - 1)
+            for (int q = b + 1; q <= J.nblocks; q++) J.bstart[q] = nkept;
+    }
+    if (nkept == 0)
+        for (int q = threadIdx.x; q <= J.nblocks; q += blockDim.x) J.bstart[q] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        J.result[0] = (unsigned long long)nkept | ((unsigned long long)s_dup << 32);
+        J.result[1] = s_rmax;
+    }
 }
 
 __global__ void empty_bstart_kernel(int *bstart, int nblocks) {
@@ -165,6 +285,16 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
     note_launch();
     gather_kernel<<<blocks, threads, 0, s>>>(g, nkept, gorder, gkey_sorted, rem, ids_in, outpos_by_input, p64,
                                              l32, pid, outpos, gblock, bstart, nblocks);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, cudaStream_t s) {
+    if (njobs <= 0) return cudaSuccess;
+    const size_t smem = kSmallBinMax * 8 + kSmallBinMax * 4;
+    cudaError_t e = cudaFuncSetAttribute(small_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    small_bin_kernel<<<njobs, kSmallBinThreads, smem, s>>>(jobs);
     note_launch();
     return cudaGetLastError();
 }

@@ -156,6 +156,24 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
                           int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
                           double *res_rad, cudaStream_t s);
+// One small container's binning in one CTA (batches): at most kSmallBinMax particles.
+constexpr int kSmallBinMax = 4096;
+constexpr int kSmallBinThreads = 512;
+struct SmallBinJob {
+    Geometry g;
+    int n, nub, nblocks;
+    const int *ids_in;
+    const double4 *xyzr_in;
+    double4 *rem;
+    int *outpos_in;
+    double4 *p64;
+    float4 *l32;
+    int *pid, *outpos, *gblock, *bstart;
+    int *res_ids;
+    double *res_pos, *res_rad;
+    unsigned long long *result;   // [0] kept | duplicate << 32, [1] largest radius (bits)
+};
+cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, cudaStream_t s);
 cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,
                                    int nkept, int *dup_flag, cudaStream_t s);
 

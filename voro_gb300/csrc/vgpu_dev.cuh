@@ -80,15 +80,32 @@ static __device__ __forceinline__ unsigned long long warp_or64(unsigned long lon
     unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
     return ((unsigned long long)hi << 32) | lo;
 }
-static __device__ __forceinline__ float warp_maxf(float x) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) x = fmaxf(x, __shfl_xor_sync(kFull, x, d));
-    return x;
+// Largest of the lanes' values, for values that are +0 or positive (their
+// bit patterns order like unsigned integers): one redux instead of a
+// shuffle tree.
+static __device__ __forceinline__ float warp_max_nonneg(float x) {
+    return __uint_as_float(__reduce_max_sync(kFull, __float_as_uint(x)));
 }
 static __device__ __forceinline__ double warp_sumd(double x) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFull, x, d);
     return x;
+}
+// Exclusive prefix sum and total of small non-negative lane values
+// (x < 2^BITS) from one ballot per bit: the ballots are independent, so the
+// latency is that of one ballot rather than of a chain of shuffles.
+template <int BITS>
+static __device__ __forceinline__ int warp_excl_scan_small(int x, int lane, int &total) {
+    const unsigned lt = (1u << lane) - 1u;
+    int ex = 0, tot = 0;
+#pragma unroll
+    for (int b = 0; b < BITS; b++) {
+        const unsigned m = __ballot_sync(kFull, (x >> b) & 1);
+        ex += __popc(m & lt) << b;
+        tot += __popc(m) << b;
+    }
+    total = tot;
+    return ex;
 }
 static __device__ __forceinline__ int warp_incl_scan(int x, int lane) {
 #pragma unroll

@@ -185,6 +185,11 @@ struct VertexF32 {
 // covering the planes' own storage error (pe: |n|, en, eh, |h|) and the
 // rounding of this Cramer solve: |adj(A)| <= |n_b||n_c| + |n_c||n_a| + |n_a||n_b|
 // and every row's error is at most rho.
+// The reciprocal of D and |v| use the approximate hardware operations, whose
+// documented errors (__fdividef: 2 ulp for 2^-126 <= |D| <= 2^126; rsqrtf:
+// 2 ulp) are covered by widening the bound: 4u|v| more for the reciprocal's
+// relative error in every coordinate, (1 + 8u) on 1/|D| in the first term,
+// and |v| rounded up by 8u so that it stays an upper bound of the root.
 VGPU_HELPER VertexF32 solve_vertex_f32(const float4 *pl, const float4 *pe, unsigned t) {
     const int a = tri_plane(t, 0), b = tri_plane(t, 1), c = tri_plane(t, 2);
     const float4 A = pl[a], B = pl[b], Cc = pl[c];
@@ -193,19 +198,20 @@ VGPU_HELPER VertexF32 solve_vertex_f32(const float4 *pl, const float4 *pe, unsig
     const float cax = Cc.y * A.z - Cc.z * A.y, cay = Cc.z * A.x - Cc.x * A.z, caz = Cc.x * A.y - Cc.y * A.x;
     const float abx = A.y * B.z - A.z * B.y, aby = A.z * B.x - A.x * B.z, abz = A.x * B.y - A.y * B.x;
     const float D = A.x * bcx + A.y * bcy + A.z * bcz;
-    const float inv = 1.0f / D;
+    const float inv = __fdividef(1.0f, D);
     VertexF32 o;
     o.x = (A.w * bcx + B.w * cax + Cc.w * abx) * inv;
     o.y = (A.w * bcy + B.w * cay + Cc.w * aby) * inv;
     o.z = (A.w * bcz + B.w * caz + Cc.w * abz) * inv;
-    o.a = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+    const float s2 = o.x * o.x + o.y * o.y + o.z * o.z;
+    o.a = s2 * rsqrtf(s2) * (1.0f + 8.0f * kU32);   // NaN for s2 = 0 or inf: not good
     const float cof = fmaf(EB.x, EC.x, fmaf(EC.x, EA.x, EA.x * EB.x));
     const float r8 = 8.0f * kU32;
     const float ra = fmaf(EA.y, o.a, EA.z) + r8 * fmaf(EA.x, o.a, EA.w);
     const float rb = fmaf(EB.y, o.a, EB.z) + r8 * fmaf(EB.x, o.a, EB.w);
     const float rc = fmaf(EC.y, o.a, EC.z) + r8 * fmaf(EC.x, o.a, EC.w);
-    o.e = 2.0f * cof * fmaxf(ra, fmaxf(rb, rc)) / fabsf(D) + r8 * o.a;
-    o.good = D > 0.0f && isfinite(o.e) && isfinite(o.a);
+    o.e = 2.0f * cof * fmaxf(ra, fmaxf(rb, rc)) * (fabsf(inv) * (1.0f + 8.0f * kU32)) + (12.0f * kU32) * o.a;
+    o.good = D >= FLT_MIN && D <= 8.5e37f && isfinite(o.e) && isfinite(o.a);
     if (!o.good) o.e = 3.0e38f;  // every test on it is repaired in FP64
     const float r = fminf((o.a + o.e) * (1.0f + 4.0f * kU32), 1.0e18f);
     o.r2 = r * r;
@@ -359,10 +365,10 @@ struct Engine {
 
     // ---- bound of max |v|^2 and the candidate cut-off
     __device__ __forceinline__ void update_radius() {
-        float m = V.r2[0];
+        float m = 0.0f;   // r2 >= 0; fmaxf drops a NaN
 #pragma unroll
-        for (int s = 1; s < K; s++) m = fmaxf(m, V.r2[s]);
-        C.R2 = warp_maxf(m);
+        for (int s = 0; s < K; s++) m = fmaxf(m, V.r2[s]);
+        C.R2 = warp_max_nonneg(m);
         if (P.g.poly) {
             float R = sqrtf(C.R2);
             float q = C.R2 + P.g.rmax32 * P.g.rmax32 - C.ri2;
@@ -551,8 +557,8 @@ struct Engine {
                 nbe += __popc(bnd[s]);
             }
         }
-        const int incl = warp_incl_scan(nbe, lane);
-        const int total = __shfl_sync(kFull, incl, 31);
+        int total;
+        const int excl = warp_excl_scan_small<(3 * K < 8 ? 3 : (3 * K < 16 ? 4 : 5))>(nbe, lane, total);
         if (__any_sync(kFull, broken)) {  // inconsistent adjacency: hand the cell to the large engine
             C.overflow = true;
             C.fail_reason = VGPU_FAIL_ADJACENCY;
@@ -572,7 +578,7 @@ struct Engine {
         }
         // stage the boundary edges (a -> b, kept neighbour u) in lane order
         {
-            int q = incl - nbe;
+            int q = excl;
 #pragma unroll
             for (int s = 0; s < K; s++) {
                 if (bnd[s]) {
@@ -589,14 +595,28 @@ struct Engine {
             }
         }
         __syncwarp();
-        // Phase B: the free slot of rank r hosts the new vertex (a, b, p) of boundary edge r
+        // Phase B: the free slot of rank r hosts the new vertex (a, b, p) of boundary
+        // edge r.  Ranks count within the first slot row s (lanes' s-th slots) that
+        // has room for all the new vertices, so that their solves below run in
+        // one pass; across all free slots only when no row has room.
+        unsigned fw[K];   // free lanes of each slot row
+#pragma unroll
+        for (int s = 0; s < K; s++) fw[s] = (unsigned)(Fm.w[s >> 1] >> (32 * (s & 1)));
+        int hs = -1;
+#pragma unroll
+        for (int s = K - 1; s >= 0; s--)
+            if (__popc(fw[s]) >= total) hs = s;
+        const unsigned lt = (1u << lane) - 1u;
+        int before = 0;   // free slots ranked in the rows before s
         bool host[K];
 #pragma unroll
         for (int s = 0; s < K; s++) {
             const int t = lane + 32 * s;
+            const unsigned row = (hs < 0 || hs == s) ? fw[s] : 0u;
+            const int r = before + __popc(row & lt);
+            before += __popc(row);
             host[s] = false;
-            if (Fm.test(t)) {
-                const int r = Fm.rank(t);
+            if ((row >> lane) & 1u) {
                 if (r < total) {
                     host[s] = true;
                     const unsigned E = S.stage[r];
@@ -784,7 +804,8 @@ struct Engine {
                         // forward error of the FP32 plane: local coordinates and block
                         // offsets each carry at most u*bs; the sum one more rounding
                         const int M = max(abs(ddi), max(abs(ddj), abs(ddk)));
-                        const float dn = sqrtf(d2);
+                        // |n| rounded up (rsqrtf: 2 ulp) as an upper bound of the root
+                        const float dn = d2 > 0.0f ? d2 * rsqrtf(d2) * (1.0f + 8.0f * kU32) : 0.0f;
                         const float en = kU32 * (1.75f * (float)(M + 3) * P.g.gbs_max + 1.01f * dn) + 1e-12f * P.g.gbs_max;
                         const float eh = dn * en + 2.0f * kU32 * (d2 + rr) + 0.5f * en * en;
                         cd = make_float4(dx, dy, dz, 0.5f * rs);

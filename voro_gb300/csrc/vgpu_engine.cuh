@@ -1007,6 +1007,12 @@ struct Engine {
 constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
 template <int MODE, int K>
 constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
+// Cells a warp takes from the work queue at a time.  Consecutive cells (engine
+// order: neighbouring blocks) search nearly the same blocks, so a warp that
+// runs them back to back finds their block starts and particles in its SM's L1.
+#ifndef VGPU_CELL_CHUNK
+#define VGPU_CELL_CHUNK 8
+#endif
 
 template <int MODE, int K>
 __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
@@ -1024,12 +1030,16 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
     const long long t_kernel0 = clock64();
 #endif
     unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
+    int w = 0, wend = 0;
     for (;;) {
-        int w = 0;
-        if (lane == 0) w = (int)atomicAdd(work, 1ull);
-        w = __shfl_sync(kFull, w, 0);
-        if (w >= P.ncells) break;
+        if (w == wend) {
+            if (lane == 0) w = (int)atomicAdd(work, (unsigned long long)VGPU_CELL_CHUNK);
+            w = __shfl_sync(kFull, w, 0);
+            if (w >= P.ncells) break;
+            wend = min(w + VGPU_CELL_CHUNK, P.ncells);
+        }
         const int k = P.cell_list ? P.cell_list[w] : w;
+        w++;
         Engine<MODE, K> eng(P, S, offsets, lane);
         eng.run(k);
         tests += eng.C.tests;
@@ -1099,12 +1109,16 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
         }
         tests = repairs = ptested = pcut = deleted = marginal = ovf = 0;
     };
+    long long w = 0, wend = 0;
     for (;;) {
-        long long w = 0;
-        if (lane == 0) w = (long long)atomicAdd(B.work, 1ull);
-        w = __shfl_sync(kFull, w, 0);
-        if (w >= B.ncells) break;
+        if (w == wend) {
+            if (lane == 0) w = (long long)atomicAdd(B.work, (unsigned long long)VGPU_CELL_CHUNK);
+            w = __shfl_sync(kFull, w, 0);
+            if (w >= B.ncells) break;
+            wend = min(w + (long long)VGPU_CELL_CHUNK, B.ncells);
+        }
         const long long gidx = B.cell_list ? B.cell_list[w] : w;
+        w++;
         if (gidx < cbeg || gidx >= cend) {
             flush();
             // the container c with cell_start[c] <= gidx < cell_start[c+1]

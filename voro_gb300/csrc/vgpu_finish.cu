@@ -1,5 +1,5 @@
-// The FP64 finish kernel: volume, centroid, neighbours and the optional
-// polytope of every cell from the records the clipping kernels write.
+// The finish kernel: volume, centroid, neighbours and the optional polytope
+// of every cell from the records the clipping kernels write.
 #include "vgpu_dev.cuh"
 
 namespace vgpu {
@@ -7,14 +7,16 @@ namespace vgpu {
 namespace {
 
 // ------------------------------------------------------------------ finish
-// The FP64 reductions of every cell from the compact record its clipping
-// kernel wrote (layout in CellParams).  They run as a separate kernel so that
-// the clipping loop keeps the instruction cache to itself.  Vertices: the
-// MIXED engine's FP32 vertices get one FP64 residual correction against their
-// three FP64 planes (refine_vertex_rec); the FP64 engine's are used as they
-// are.  Volume and centroid: FP64 sums over edges relative to vertex 0 with
-// each face's reference point one of its own vertices (the edge formula holds
-// for any point of the face).  Optionally the polytope itself is written out.
+// The reductions of every cell from the compact record its clipping kernel
+// wrote (layout in CellParams).  They run as a separate kernel so that the
+// clipping loop keeps the instruction cache to itself.  Planes are rebuilt
+// in FP64 from the particles (the reference's arithmetic).  Vertices: the
+// FP64 engine's are used as they are; the MIXED engine's FP32 vertices get
+// one residual correction against their three planes (refine_vertex_ff).
+// Volume and centroid: sums over edges relative to vertex 0 with each face's
+// reference point one of its own vertices (the edge formula holds for any
+// point of the face), in FP64 for the FP64 engine and in float pairs for the
+// MIXED engine.  Optionally the polytope itself is written out.
 constexpr int kFinMaxV = 128;   // vertices (the 128-slot engine's capacity)
 constexpr int kFinMaxE = 192;   // edges (3 * kFinMaxV / 2)
 
@@ -24,11 +26,68 @@ struct FinishShared {
     int psrc[kMaxPlanes], pshift[kMaxPlanes];
     int rep[kMaxPlanes];             // per face: its lowest vertex
     int ford[kMaxPlanes];            // per face: its vertex count
-    double4 pl64[kMaxPlanes];
-    float4 pn[kMaxPlanes];           // the FP64 plane normals rounded to FP32
-    double vx[kFinMaxV], vy[kFinMaxV], vz[kFinMaxV];   // FP64 vertices relative to c0
+    float4 plh[kMaxPlanes], pll[kMaxPlanes];   // the FP64 planes as float pairs (MIXED engine)
+    // vertices relative to c0: FP64 (FP64 engine) or scaled float pairs
+    // (MIXED engine: vh + vl, see the edge sums)
+    union {
+        struct {
+            double vx[kFinMaxV], vy[kFinMaxV], vz[kFinMaxV];
+        } d;
+        struct {
+            float vh[3][kFinMaxV], vl[3][kFinMaxV];
+        } f;
+    } v;
     unsigned stage[kFinMaxE];        // owned edges (t < u)
 };
+
+// ------------------------------------------------------------------ float-pair arithmetic
+// A value is the unevaluated sum h + l of two floats (|l| <= ulp(h)/2): about
+// 48 significant bits.  GB300 issues FP32 at 64 times its FP64 rate, so the
+// MIXED engine's vertex corrections and edge sums run on pairs: Knuth's
+// two-sum and the FMA two-product (exact error terms; every operation is an
+// explicitly rounded intrinsic that the compiler may neither contract nor
+// reorder).  Addition and multiplication have relative errors of a few
+// 2^-46 (of |a| + |b| for a sum), so the sums keep about 1e-13 of the cell's
+// scale: far inside the 1e-10 tolerance of the MIXED engine.
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {   // |a| >= |b| or a = 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float v = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = ff_two_sum(a.h, b.h);
+    return ff_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ FF ff_sub(FF a, FF b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_mulf(FF a, float b) {   // pair times float
+    const float p = __fmul_rn(a.h, b);
+    return ff_fast_two_sum(p, __fmaf_rn(a.l, b, __fmaf_rn(a.h, b, -p)));
+}
+__device__ __forceinline__ FF ff_scale(FF a, float pow2) { return {__fmul_rn(a.h, pow2), __fmul_rn(a.l, pow2)}; }
+__device__ __forceinline__ bool ff_less(FF a, FF b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ FF ff_from_double(double d) {
+    const float h = __double2float_rn(d);
+    return {h, __double2float_rn(d - (double)h)};
+}
+// 2^k as a float (|k| <= 126) and as a double (|k| <= 1022): exact
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+__device__ __forceinline__ double pow2d(int k) { return __hiloint2double((1023 + k) << 20, 0); }
 
 __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
     const int src = F.psrc[p];
@@ -36,42 +95,48 @@ __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const Finish
     return face64(P, me, F.pshift[p]);
 }
 
-// refine_vertex_f64 with the planes' FP32 normals taken from F.pn (rounded
-// once per plane rather than once per vertex and plane).
-__device__ __forceinline__ double3 refine_vertex_rec(const FinishShared &F, unsigned t, float fx, float fy, float fz) {
+// The FP32 vertex (fx, fy, fz) of planes t corrected by one residual step:
+// residuals r = h - n.v against the planes' float pairs (exact products of
+// the pairs and the floats, pair sums), the correction A^-1 r solved in FP32
+// with the planes' FP32 normals, and the vertex returned as the pair
+// v + correction.  A nearly singular FP32 system (|D| <= 1e-3 of the product
+// of the normals' norms) is solved in FP64 from the FP64 planes instead,
+// rebuilt for it.
+__device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FinishShared &F, double4 me, unsigned t,
+                                                 float fx, float fy, float fz, FF &vx, FF &vy, FF &vz) {
     const int ia = tri_plane(t, 0), ib = tri_plane(t, 1), ic = tri_plane(t, 2);
-    const double4 A = F.pl64[ia], B = F.pl64[ib], Cq = F.pl64[ic];
-    const float4 a = F.pn[ia], b = F.pn[ib], c = F.pn[ic];
-    const double x = fx, y = fy, z = fz;
-    const double ra = A.w - fma(A.x, x, fma(A.y, y, A.z * z));
-    const double rb = B.w - fma(B.x, x, fma(B.y, y, B.z * z));
-    const double rc = Cq.w - fma(Cq.x, x, fma(Cq.y, y, Cq.z * z));
+    const float4 a = F.plh[ia], b = F.plh[ib], c = F.plh[ic];
     const float bcx = b.y * c.z - b.z * c.y, bcy = b.z * c.x - b.x * c.z, bcz = b.x * c.y - b.y * c.x;
     const float cax = c.y * a.z - c.z * a.y, cay = c.z * a.x - c.x * a.z, caz = c.x * a.y - c.y * a.x;
     const float abx = a.y * b.z - a.z * b.y, aby = a.z * b.x - a.x * b.z, abz = a.x * b.y - a.y * b.x;
     const float D = a.x * bcx + a.y * bcy + a.z * bcz;
     const float scale = (fabsf(a.x) + fabsf(a.y) + fabsf(a.z)) * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z)) *
                         (fabsf(c.x) + fabsf(c.y) + fabsf(c.z));
-    double3 v;
     if (fabsf(D) > 1e-3f * scale) {
-        const float fra = (float)ra, frb = (float)rb, frc = (float)rc;
+        float r[3];
+        const int ip[3] = {ia, ib, ic};
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float4 h = F.plh[ip[q]], l = F.pll[ip[q]];
+            FF acc = ff_mulf({h.x, l.x}, fx);
+            acc = ff_add(acc, ff_mulf({h.y, l.y}, fy));
+            acc = ff_add(acc, ff_mulf({h.z, l.z}, fz));
+            r[q] = ff_sub({h.w, l.w}, acc).h;
+        }
         const float inv = 1.0f / D;
-        v.x = x + (double)((fra * bcx + frb * cax + frc * abx) * inv);
-        v.y = y + (double)((fra * bcy + frb * cay + frc * aby) * inv);
-        v.z = z + (double)((fra * bcz + frb * caz + frc * abz) * inv);
+        vx = ff_two_sum(fx, (r[0] * bcx + r[1] * cax + r[2] * abx) * inv);
+        vy = ff_two_sum(fy, (r[0] * bcy + r[1] * cay + r[2] * aby) * inv);
+        vz = ff_two_sum(fz, (r[0] * bcz + r[1] * caz + r[2] * abz) * inv);
     } else {
-        double DD;
+        double x, y, z, DD;
         float kn;
-        solve_f64(A, B, Cq, v.x, v.y, v.z, DD, kn);
+        solve_f64(plane64_rec(P, F, me, ia), plane64_rec(P, F, me, ib), plane64_rec(P, F, me, ic), x, y, z, DD, kn);
+        vx = ff_from_double(x);
+        vy = ff_from_double(y);
+        vz = ff_from_double(z);
     }
-    return v;
 }
 
-// Sums of four values over a group of G lanes (G = 32 or 16) with few FP64
-// additions (the FP64 pipe bounds the finish kernel): halves of the group
-// first fold different pairs, then quarters different singles, then each
-// quarter folds its own; the four sums end in the group's lanes 0, G/4, G/2,
-// 3G/4 and are broadcast.  Fixed order: deterministic.
 template <int G>
 __device__ __forceinline__ void group_sum4(double &a, double &b, double &c, double &d, int gl) {
     const bool lo = gl < G / 2;
@@ -123,7 +188,8 @@ __device__ __forceinline__ double rec_double(const unsigned *w) {
 // reached by both halves of the warp whatever their cells.
 template <int MODE, int G>
 __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int gl) {
-    constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;
+    constexpr bool kFF = MODE == VGPU_MIXED;   // float-pair vertices and sums
+    constexpr int VW = kFF ? 3 : 6;
     constexpr int SL = 4;   // vertex slots per lane: 128 vertices (G = 32) or 64 (G = 16)
     static_assert(SL * 32 == kFinMaxV, "slot count");
     const unsigned long long off = k >= 0 ? P.rec_off[k] : kNoRecord;
@@ -135,42 +201,52 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     const unsigned *rp = rv + (2 + VW) * nv;
     const double4 me = have ? P.a.p64[k] : make_double4(0, 0, 0, 0);
     const int out = have ? P.a.outpos[k] : 0;
-    // planes: neighbour IDs (plane order), sources, FP64 planes
+    // planes: neighbour IDs (plane order), sources, FP64 planes as float pairs
     for (int q = gl; q < nf; q += G) {
         F.psrc[q] = (int)rp[q];
         F.pshift[q] = (int)rp[nf + q];
         F.rep[q] = 0x7fffffff;
         F.ford[q] = 0;
         P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
-        const double4 pl = plane64_rec(P, F, me, q);
-        F.pl64[q] = pl;
-        F.pn[q] = make_float4((float)pl.x, (float)pl.y, (float)pl.z, 0.0f);
+        if (kFF) {   // (the FP64 engine's vertices need no planes)
+            const double4 pl = plane64_rec(P, F, me, q);
+            const FF x = ff_from_double(pl.x), y = ff_from_double(pl.y), z = ff_from_double(pl.z),
+                     w = ff_from_double(pl.w);
+            F.plh[q] = make_float4(x.h, y.h, z.h, w.h);
+            F.pll[q] = make_float4(x.l, y.l, z.l, w.l);
+        }
     }
     __syncwarp();
+    // vertices (particle-relative): FP64 (vd) or float pairs (vf)
     unsigned tri[SL];
-    double vx[SL], vy[SL], vz[SL];
+    double vd[SL][3];
+    FF vf[SL][3];
     double mr2 = 0.0;
+    FF mf = {0.0f, 0.0f};
 #pragma unroll
     for (int s = 0; s < SL; s++) {
         const int t = gl + G * s;
         tri[s] = 0;
-        vx[s] = vy[s] = vz[s] = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            vd[s][a] = 0.0;
+            vf[s][a] = {0.0f, 0.0f};
+        }
         if (t < nv) {
             tri[s] = rv[t];
             F.tri[t] = tri[s];
             F.adj[t] = rv[nv + t];
-            if (MODE == VGPU_FP64) {
-                vx[s] = rec_double(rv + 2 * nv + 2 * t);
-                vy[s] = rec_double(rv + 4 * nv + 2 * t);
-                vz[s] = rec_double(rv + 6 * nv + 2 * t);
+            if (kFF) {
+                refine_vertex_ff(P, F, me, tri[s], __uint_as_float(rv[2 * nv + t]), __uint_as_float(rv[3 * nv + t]),
+                                 __uint_as_float(rv[4 * nv + t]), vf[s][0], vf[s][1], vf[s][2]);
+                const FF q = ff_add(ff_add(ff_mul(vf[s][0], vf[s][0]), ff_mul(vf[s][1], vf[s][1])),
+                                    ff_mul(vf[s][2], vf[s][2]));
+                if (ff_less(mf, q)) mf = q;
             } else {
-                const double3 r = refine_vertex_rec(F, tri[s], __uint_as_float(rv[2 * nv + t]),
-                                                    __uint_as_float(rv[3 * nv + t]), __uint_as_float(rv[4 * nv + t]));
-                vx[s] = r.x;
-                vy[s] = r.y;
-                vz[s] = r.z;
+#pragma unroll
+                for (int a = 0; a < 3; a++) vd[s][a] = rec_double(rv + (2 + 2 * a) * nv + 2 * t);
+                mr2 = fmax(mr2, vd[s][0] * vd[s][0] + vd[s][1] * vd[s][1] + vd[s][2] * vd[s][2]);
             }
-            mr2 = fmax(mr2, vx[s] * vx[s] + vy[s] * vy[s] + vz[s] * vz[s]);
 #pragma unroll
             for (int e = 0; e < 3; e++) {
                 atomicMin(&F.rep[tri_plane(tri[s], e)], t);
@@ -178,10 +254,35 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             }
         }
     }
+    // the largest |v|^2 over the group and, for the pairs, the power of two
+    // 2^sc (about 2 sqrt(max |v|^2) >= |v - c0|) that scales the relative
+    // coordinates to magnitude about 1, so that their products neither
+    // underflow nor overflow
+    int sc = 0;
+    if (kFF) {
+#pragma unroll
+        for (int dd = G / 2; dd >= 1; dd >>= 1) {
+            const FF o = {__shfl_xor_sync(kFull, mf.h, dd, G), __shfl_xor_sync(kFull, mf.l, dd, G)};
+            if (ff_less(mf, o)) mf = o;
+        }
+        mr2 = ff_to_double(mf);
+        if (mf.h > 0.0f && mf.h < 3.0e38f) sc = (ilogbf(mf.h) + 2) / 2 + 1;
+    } else {
+        mr2 = group_max_nonneg<G>(mr2);
+    }
     // origin of the sums: vertex 0
-    const double c0x = __shfl_sync(kFull, vx[0], 0, G);
-    const double c0y = __shfl_sync(kFull, vy[0], 0, G);
-    const double c0z = __shfl_sync(kFull, vz[0], 0, G);
+    double c0[3];
+    FF c0f[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (kFF) {
+            c0f[a] = {__shfl_sync(kFull, vf[0][a].h, 0, G), __shfl_sync(kFull, vf[0][a].l, 0, G)};
+            c0[a] = ff_to_double(c0f[a]);
+        } else {
+            c0[a] = __shfl_sync(kFull, vd[0][a], 0, G);
+        }
+    }
+    const float down = pow2f(-sc);
     int ne = 0;
     unsigned own[SL];
 #pragma unroll
@@ -189,9 +290,16 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         own[s] = 0;
         const int t = gl + G * s;
         if (t < nv) {
-            F.vx[t] = vx[s] - c0x;
-            F.vy[t] = vy[s] - c0y;
-            F.vz[t] = vz[s] - c0z;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (kFF) {
+                    const FF q = ff_scale(ff_sub(vf[s][a], c0f[a]), down);
+                    F.v.f.vh[a][t] = q.h;
+                    F.v.f.vl[a][t] = q.l;
+                } else {
+                    (a == 0 ? F.v.d.vx : (a == 1 ? F.v.d.vy : F.v.d.vz))[t] = vd[s][a] - c0[a];
+                }
+            }
             const unsigned A3 = F.adj[t];
 #pragma unroll
             for (int e = 0; e < 3; e++)
@@ -212,37 +320,71 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     __syncwarp();
     // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
     double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-    for (int i = gl; i < etot; i += G) {
-        const unsigned E = F.stage[i];
-        const int t = E & 255u, e = E >> 8;
-        const unsigned T = F.tri[t];
-        const int u = (F.adj[t] >> (8 * e)) & 255u;
-        const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
-        const double tx = F.vx[t], ty = F.vy[t], tz = F.vz[t];
-        const double ux = F.vx[u], uy = F.vy[u], uz = F.vz[u];
-        const double wx = ty * uz - tz * uy;
-        const double wy = tz * ux - tx * uz;
-        const double wz = tx * uy - ty * ux;
-        const double ax = F.vx[rx], ay = F.vy[rx], az = F.vz[rx];
-        const double bx = F.vx[ry], by = F.vy[ry], bz = F.vz[ry];
-        const double dy = bx * wx + by * wy + bz * wz;
-        const double dx = ax * wx + ay * wy + az * wz;
-        const double dd = dy - dx;
-        vs += dd;
-        cx += dd * (tx + ux) + dy * bx - dx * ax;
-        cy += dd * (ty + uy) + dy * by - dx * ay;
-        cz += dd * (tz + uz) + dy * bz - dx * az;
+    if (kFF) {
+        FF s0 = {0.0f, 0.0f}, s1 = s0, s2 = s0, s3 = s0;
+        for (int i = gl; i < etot; i += G) {
+            const unsigned E = F.stage[i];
+            const int t = E & 255u, e = E >> 8;
+            const unsigned T = F.tri[t];
+            const int u = (F.adj[t] >> (8 * e)) & 255u;
+            const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
+            FF tv[3], uv[3], av[3], bv[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                tv[c] = {F.v.f.vh[c][t], F.v.f.vl[c][t]};
+                uv[c] = {F.v.f.vh[c][u], F.v.f.vl[c][u]};
+                av[c] = {F.v.f.vh[c][rx], F.v.f.vl[c][rx]};
+                bv[c] = {F.v.f.vh[c][ry], F.v.f.vl[c][ry]};
+            }
+            const FF w[3] = {ff_sub(ff_mul(tv[1], uv[2]), ff_mul(tv[2], uv[1])),
+                             ff_sub(ff_mul(tv[2], uv[0]), ff_mul(tv[0], uv[2])),
+                             ff_sub(ff_mul(tv[0], uv[1]), ff_mul(tv[1], uv[0]))};
+            const FF dy = ff_add(ff_add(ff_mul(bv[0], w[0]), ff_mul(bv[1], w[1])), ff_mul(bv[2], w[2]));
+            const FF dx = ff_add(ff_add(ff_mul(av[0], w[0]), ff_mul(av[1], w[1])), ff_mul(av[2], w[2]));
+            const FF dd = ff_sub(dy, dx);
+            s0 = ff_add(s0, dd);
+            s1 = ff_add(s1, ff_sub(ff_add(ff_mul(dd, ff_add(tv[0], uv[0])), ff_mul(dy, bv[0])), ff_mul(dx, av[0])));
+            s2 = ff_add(s2, ff_sub(ff_add(ff_mul(dd, ff_add(tv[1], uv[1])), ff_mul(dy, bv[1])), ff_mul(dx, av[1])));
+            s3 = ff_add(s3, ff_sub(ff_add(ff_mul(dd, ff_add(tv[2], uv[2])), ff_mul(dy, bv[2])), ff_mul(dx, av[2])));
+        }
+        // back to FP64 and to the true scale: vs by 2^(3 sc), the moments by 2^(4 sc)
+        const double up3 = pow2d(3 * sc), up4 = pow2d(4 * sc);
+        vs = ff_to_double(s0) * up3;
+        cx = ff_to_double(s1) * up4;
+        cy = ff_to_double(s2) * up4;
+        cz = ff_to_double(s3) * up4;
+    } else {
+        for (int i = gl; i < etot; i += G) {
+            const unsigned E = F.stage[i];
+            const int t = E & 255u, e = E >> 8;
+            const unsigned T = F.tri[t];
+            const int u = (F.adj[t] >> (8 * e)) & 255u;
+            const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
+            const double tx = F.v.d.vx[t], ty = F.v.d.vy[t], tz = F.v.d.vz[t];
+            const double ux = F.v.d.vx[u], uy = F.v.d.vy[u], uz = F.v.d.vz[u];
+            const double wx = ty * uz - tz * uy;
+            const double wy = tz * ux - tx * uz;
+            const double wz = tx * uy - ty * ux;
+            const double ax = F.v.d.vx[rx], ay = F.v.d.vy[rx], az = F.v.d.vz[rx];
+            const double bx = F.v.d.vx[ry], by = F.v.d.vy[ry], bz = F.v.d.vz[ry];
+            const double dy = bx * wx + by * wy + bz * wz;
+            const double dx = ax * wx + ay * wy + az * wz;
+            const double dd = dy - dx;
+            vs += dd;
+            cx += dd * (tx + ux) + dy * bx - dx * ax;
+            cy += dd * (ty + uy) + dy * by - dx * ay;
+            cz += dd * (tz + uz) + dy * bz - dx * az;
+        }
     }
     group_sum4<G>(vs, cx, cy, cz, gl);
-    mr2 = group_max_nonneg<G>(mr2);
     if (have && gl == 0) {
         const double vol = vs / 6.0;
         P.r.vol[out] = vol;
         if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
             const double f = 1.0 / (4.0 * vs);
-            P.r.cen[3 * out] = c0x + cx * f;
-            P.r.cen[3 * out + 1] = c0y + cy * f;
-            P.r.cen[3 * out + 2] = c0z + cz * f;
+            P.r.cen[3 * out] = c0[0] + cx * f;
+            P.r.cen[3 * out + 1] = c0[1] + cy * f;
+            P.r.cen[3 * out + 2] = c0[2] + cz * f;
         } else {
             P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
         }
@@ -271,11 +413,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
 #pragma unroll
             for (int s = 0; s < SL; s++) {
                 const int t = gl + G * s;
-                if (t < nv) {
-                    D[2 + 3 * t] = vx[s];
-                    D[3 + 3 * t] = vy[s];
-                    D[4 + 3 * t] = vz[s];
-                }
+                if (t < nv)
+#pragma unroll
+                    for (int a = 0; a < 3; a++) D[2 + 3 * t + a] = kFF ? ff_to_double(vf[s][a]) : vd[s][a];
             }
         }
         // face loops; the loop over face chunks runs the same number of times

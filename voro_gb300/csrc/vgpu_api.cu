@@ -150,7 +150,7 @@ struct vgpu_container {
     DevBuf ids_in, xyzr_in;
     // work buffers
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
-    DevBuf p64, l32, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
+    DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
     DevBuf rec, rec_off, poly, poly_off;
     DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
@@ -213,6 +213,7 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
     }
     double tol = 10.0 * 2.220446049250313e-16 * max_len_sq;  // src/config.hh:80, src/cell.cc:24
     g.tol_h = 0.5 * tol;
+    g.tol_h32 = std::nextafter((float)g.tol_h, 3.0e38f);
     g.tol_cu = tol * std::sqrt(tol);
     return VGPU_OK;
 }
@@ -239,6 +240,8 @@ void choose_engine_grid(Geometry &g, int64_t n, double density) {
     for (int a = 0; a < 3; a++) {
         g.gbs[a] = g.len[a] / g.gn[a];
         g.gbs32[a] = (float)g.gbs[a];
+        g.gbs_h[a] = g.gbs32[a];
+        g.gbs_l[a] = (float)(g.gbs[a] - (double)g.gbs32[a]);
         bmin = std::min(bmin, g.gbs32[a]);
         bmax = std::max(bmax, g.gbs32[a]);
     }
@@ -301,7 +304,8 @@ int vgpu_container_destroy(vgpu_container *h) {
     if (!h) return VGPU_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
     DevBuf *bufs[] = {&h->ids_in, &h->xyzr_in, &h->rem, &h->ukey, &h->gkey, &h->idx, &h->idx2, &h->keys_alt,
-                      &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64, &h->l32, &h->pid,
+                      &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64,
+                      &h->lffh, &h->lffl, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
                       &h->r_pos, &h->r_rad, &h->rec, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
@@ -488,7 +492,8 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(h->r_pos.ensure(nk * 24));
     VG_CUDA(h->r_rad.ensure(nk * 8));
     VG_CUDA(h->p64.ensure(nk * 32));
-    VG_CUDA(h->l32.ensure(nk * 16));
+    VG_CUDA(h->lffh.ensure(nk * 16));
+    VG_CUDA(h->lffl.ensure(nk * 16));
     VG_CUDA(h->pid.ensure(nk * 4));
     VG_CUDA(h->outpos.ensure(nk * 4));
     VG_CUDA(h->gblock.ensure(nk * 4));
@@ -519,7 +524,8 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
         return fail(VGPU_ERR_INTERNAL, "sort buffer aliasing");
 
     VG_CUDA(launch_gather(g, nkept, uorder, gorder, gkey_sorted, h->rem.as<double4>(), d_ids,
-                          h->outpos_in.as<int>(), h->p64.as<double4>(), h->l32.as<float4>(), h->pid.as<int>(),
+                          h->outpos_in.as<int>(), h->p64.as<double4>(), h->lffh.as<float4>(),
+                          h->lffl.as<float4>(), h->pid.as<int>(),
                           h->outpos.as<int>(), h->gblock.as<int>(), h->bstart.as<int>(), nblocks,
                           h->r_ids.as<int>(), h->r_pos.as<double>(), h->r_rad.as<double>(), s));
     cudaEventRecord(h->ev[1], s);
@@ -543,7 +549,9 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     memset(&cp, 0, sizeof(cp));
     cp.g = g;
     cp.a.p64 = h->p64.as<double4>();
-    cp.a.l32 = h->l32.as<float4>();
+    cp.a.l32 = h->lffh.as<float4>();
+    cp.a.lffh = h->lffh.as<float4>();
+    cp.a.lffl = h->lffl.as<float4>();
     cp.a.pid = h->pid.as<int>();
     cp.a.outpos = h->outpos.as<int>();
     cp.a.gblock = h->gblock.as<int>();
@@ -600,7 +608,8 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
     VG_CUDA(h->r_pos.ensure(nn * 24));
     VG_CUDA(h->r_rad.ensure(nn * 8));
     VG_CUDA(h->p64.ensure(nn * 32));
-    VG_CUDA(h->l32.ensure(nn * 16));
+    VG_CUDA(h->lffh.ensure(nn * 16));
+    VG_CUDA(h->lffl.ensure(nn * 16));
     VG_CUDA(h->pid.ensure(nn * 4));
     VG_CUDA(h->outpos.ensure(nn * 4));
     VG_CUDA(h->gblock.ensure(nn * 4));
@@ -616,7 +625,8 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
     job.rem = h->rem.as<double4>();
     job.outpos_in = h->outpos_in.as<int>();
     job.p64 = h->p64.as<double4>();
-    job.l32 = h->l32.as<float4>();
+    job.lffh = h->lffh.as<float4>();
+    job.lffl = h->lffl.as<float4>();
     job.pid = h->pid.as<int>();
     job.outpos = h->outpos.as<int>();
     job.gblock = h->gblock.as<int>();

@@ -68,9 +68,13 @@ __device__ __forceinline__ bool remap_one(const Geometry &g, double4 q, int nub,
     return ok;
 }
 
-// The engine-order record of particle i (input order) placed at engine index k.
+// The engine-order record of particle i (input order) placed at engine index k:
+// its position, and its position relative to its engine block's origin as a
+// float pair h + l (h: the clipping kernels' FP32 position; h + l: the
+// finish kernel's planes).
 __device__ __forceinline__ void gather_one(const Geometry &g, int k, int b, double4 p, int id, int outpos_i,
-                                           double4 *p64, float4 *l32, int *pid, int *outpos, int *gblock) {
+                                           double4 *p64, float4 *lffh, float4 *lffl, int *pid,
+                                           int *outpos, int *gblock) {
     int bx = b % g.gn[0];
     int by = (b / g.gn[0]) % g.gn[1];
     int bz = b / (g.gn[0] * g.gn[1]);
@@ -78,7 +82,15 @@ __device__ __forceinline__ void gather_one(const Geometry &g, int k, int b, doub
     double oy = g.lo[1] + by * g.gbs[1];
     double oz = g.lo[2] + bz * g.gbs[2];
     p64[k] = p;
-    l32[k] = make_float4((float)(p.x - ox), (float)(p.y - oy), (float)(p.z - oz), (float)p.w);
+    const double d[4] = {p.x - ox, p.y - oy, p.z - oz, p.w};
+    float h[4], l[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        h[a] = __double2float_rn(d[a]);
+        l[a] = __double2float_rn(d[a] - (double)h[a]);
+    }
+    lffh[k] = make_float4(h[0], h[1], h[2], h[3]);
+    lffl[k] = make_float4(l[0], l[1], l[2], l[3]);
     pid[k] = id;
     outpos[k] = outpos_i;
     gblock[k] = b;
@@ -118,13 +130,13 @@ __global__ void loop_order_kernel(const int *uorder, int nkept, const int *ids_i
 
 __global__ void gather_kernel(Geometry g, int nkept, const int *gorder, const unsigned *gkey_sorted,
                               const double4 *rem, const int *ids_in, const int *outpos_by_input,
-                              double4 *p64, float4 *l32, int *pid, int *outpos, int *gblock, int *bstart,
-                              int nblocks) {
+                              double4 *p64, float4 *lffh, float4 *lffl, int *pid, int *outpos,
+                              int *gblock, int *bstart, int nblocks) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nkept) return;
     int i = gorder[k];
     int b = (int)gkey_sorted[k];
-    gather_one(g, k, b, rem[i], ids_in[i], outpos_by_input[i], p64, l32, pid, outpos, gblock);
+    gather_one(g, k, b, rem[i], ids_in[i], outpos_by_input[i], p64, lffh, lffl, pid, outpos, gblock);
     int prev = k == 0 ? -1 : (int)gkey_sorted[k - 1];
     for (int q = prev + 1; q <= b; q++) bstart[q] = k;
     if (k == nkept - 1)
@@ -220,7 +232,8 @@ __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const Small
     for (int k = threadIdx.x; k < nkept; k += blockDim.x) {
         const int i = (int)(key[k] & 0xffffffffu);
         const int b = (int)(key[k] >> 32);
-        gather_one(g, k, b, J.rem[i], J.ids_in[i], J.outpos_in[i], J.p64, J.l32, J.pid, J.outpos, J.gblock);
+        gather_one(g, k, b, J.rem[i], J.ids_in[i], J.outpos_in[i], J.p64, J.lffh, J.lffl, J.pid, J.outpos,
+                   J.gblock);
         const int prev = k == 0 ? -1 : (int)(key[k - 1] >> 32);
         for (int q = prev + 1; q <= b; q++) J.bstart[q] = k;
         if (k == nkept - 1)
@@ -270,7 +283,8 @@ cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rma
 
 cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
-                          int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
+                          int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl,
+                          int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
                           double *res_rad, cudaStream_t s) {
     int threads = 256;
@@ -284,7 +298,7 @@ cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const
                                                   res_rad);
     note_launch();
     gather_kernel<<<blocks, threads, 0, s>>>(g, nkept, gorder, gkey_sorted, rem, ids_in, outpos_by_input, p64,
-                                             l32, pid, outpos, gblock, bstart, nblocks);
+                                             lffh, lffl, pid, outpos, gblock, bstart, nblocks);
     note_launch();
     return cudaGetLastError();
 }

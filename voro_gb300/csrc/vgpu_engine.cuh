@@ -485,7 +485,7 @@ struct Engine {
             const float4 Q = S.u.c.cd[cb];
             const float4 E = S.u.c.ce[cb];
             const float A = fmaf(3.0f * kU32, E.z, E.x);
-            const float Cq = fmaf(3.0f * kU32, fabsf(Q.w), E.y) + (float)P.g.tol_h;
+            const float Cq = fmaf(3.0f * kU32, fabsf(Q.w), E.y) + P.g.tol_h32;
 #pragma unroll
             for (int s = 0; s < K; s++) {
                 const float v = fmaf(Q.x, V.x[s], fmaf(Q.y, V.y[s], fmaf(Q.z, V.z[s], -Q.w)));

@@ -95,6 +95,32 @@ __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const Finish
     return face64(P, me, F.pshift[p]);
 }
 
+// The plane of candidate j (image code) of the cell of particle k as float
+// pairs, without FP64 arithmetic: the difference of the two particles is
+// their engine-block offset times the block size plus the difference of
+// their block-local positions (both stored as float pairs by the binning),
+// h = |d|^2 / 2 [+ (r_k^2 - r_j^2) / 2].  Its error is a few 2^-46 of the
+// cell's scale, against the reference's own rounding of p_j - p_k.
+struct PlaneFF {
+    FF x, y, z, w;
+};
+__device__ __forceinline__ PlaneFF plane_ff(const CellParams &P, int bk[3], float4 mh, float4 ml, int j, int code) {
+    const int b = P.a.gblock[j];
+    const int bj[3] = {b % P.g.gn[0], (b / P.g.gn[0]) % P.g.gn[1], b / (P.g.gn[0] * P.g.gn[1])};
+    const float4 qh = P.a.lffh[j], ql = P.a.lffl[j];
+    const float lq[3] = {qh.x, qh.y, qh.z}, lqe[3] = {ql.x, ql.y, ql.z};
+    const float lm[3] = {mh.x, mh.y, mh.z}, lme[3] = {ml.x, ml.y, ml.z};
+    FF d[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int db = bj[a] - bk[a] + unpack_shift(code, a) * P.g.gn[a];
+        d[a] = ff_add(ff_mulf({P.g.gbs_h[a], P.g.gbs_l[a]}, (float)db), ff_sub({lq[a], lqe[a]}, {lm[a], lme[a]}));
+    }
+    FF rs = ff_add(ff_add(ff_mul(d[0], d[0]), ff_mul(d[1], d[1])), ff_mul(d[2], d[2]));
+    if (P.g.poly) rs = ff_add(rs, ff_sub(ff_mul({mh.w, ml.w}, {mh.w, ml.w}), ff_mul({qh.w, ql.w}, {qh.w, ql.w})));
+    return {d[0], d[1], d[2], ff_scale(rs, 0.5f)};
+}
+
 // The FP32 vertex (fx, fy, fz) of planes t corrected by one residual step:
 // residuals r = h - n.v against the planes' float pairs (exact products of
 // the pairs and the floats, pair sums), the correction A^-1 r solved in FP32
@@ -201,7 +227,17 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
     const unsigned *rp = rv + (2 + VW) * nv;
     const double4 me = have ? P.a.p64[k] : make_double4(0, 0, 0, 0);
     const int out = have ? P.a.outpos[k] : 0;
-    // planes: neighbour IDs (plane order), sources, FP64 planes as float pairs
+    int bk[3] = {0, 0, 0};
+    float4 mh = make_float4(0, 0, 0, 0), ml = mh;
+    if (kFF && have) {
+        const int b = P.a.gblock[k];
+        bk[0] = b % P.g.gn[0];
+        bk[1] = (b / P.g.gn[0]) % P.g.gn[1];
+        bk[2] = b / (P.g.gn[0] * P.g.gn[1]);
+        mh = P.a.lffh[k];
+        ml = P.a.lffl[k];
+    }
+    // planes: neighbour IDs (plane order), sources, planes as float pairs
     for (int q = gl; q < nf; q += G) {
         F.psrc[q] = (int)rp[q];
         F.pshift[q] = (int)rp[nf + q];
@@ -209,11 +245,15 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         F.ford[q] = 0;
         P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
         if (kFF) {   // (the FP64 engine's vertices need no planes)
-            const double4 pl = plane64_rec(P, F, me, q);
-            const FF x = ff_from_double(pl.x), y = ff_from_double(pl.y), z = ff_from_double(pl.z),
-                     w = ff_from_double(pl.w);
-            F.plh[q] = make_float4(x.h, y.h, z.h, w.h);
-            F.pll[q] = make_float4(x.l, y.l, z.l, w.l);
+            PlaneFF pl;
+            if (F.psrc[q] >= 0) {
+                pl = plane_ff(P, bk, mh, ml, F.psrc[q], F.pshift[q]);
+            } else {   // a wall of the container (FP64, rare)
+                const double4 w = face64(P, me, F.pshift[q]);
+                pl = {ff_from_double(w.x), ff_from_double(w.y), ff_from_double(w.z), ff_from_double(w.w)};
+            }
+            F.plh[q] = make_float4(pl.x.h, pl.y.h, pl.z.h, pl.w.h);
+            F.pll[q] = make_float4(pl.x.l, pl.y.l, pl.z.l, pl.w.l);
         }
     }
     __syncwarp();

@@ -31,9 +31,11 @@ struct Geometry {
     int gn[3];
     double gbs[3];      // engine block sizes
     float gbs32[3];
+    float gbs_h[3], gbs_l[3];   // engine block sizes as float pairs (h + l)
     float gbs_min;
     float gbs_max;
     double tol_h;       // half the reference tolerance: 0.5*10*DBL_EPSILON*max_len_sq
+    float tol_h32;      // the same rounded up to FP32 (the FP32 side tests' band)
     double tol_cu;      // reference tol_cu (centroid threshold, src/cell.cc:25)
     double rmax;        // largest radius (poly kinds)
     float rmax32;
@@ -43,6 +45,8 @@ struct Geometry {
 struct EngineArrays {
     const double4 *p64;   // remapped position + radius (double)
     const float4 *l32;    // position local to its engine block + radius (float)
+    const float4 *lffh;   // the same as float pairs: high parts (the same array as l32)
+    const float4 *lffl;   // ... and low parts (finish kernel)
     const int *pid;       // particle id
     const int *outpos;    // slot of this particle in the loop-order result arrays
     const int *gblock;    // engine block index of this particle
@@ -153,7 +157,8 @@ struct BinParams {
 cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s);
 cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
-                          int *outpos_by_input, double4 *p64, float4 *l32, int *pid, int *outpos,
+                          int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl,
+                          int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
                           double *res_rad, cudaStream_t s);
 // One small container's binning in one CTA (batches): at most kSmallBinMax particles.
@@ -167,7 +172,7 @@ struct SmallBinJob {
     double4 *rem;
     int *outpos_in;
     double4 *p64;
-    float4 *l32;
+    float4 *lffh, *lffl;
     int *pid, *outpos, *gblock, *bstart;
     int *res_ids;
     double *res_pos, *res_rad;

@@ -109,12 +109,29 @@ const OffsetTable &offset_table() {
             if (x.lb2 != y.lb2) return x.lb2 < y.lb2;
             return x.r2 < y.r2;
         });
+        // one group per lower bound lb2, then a small group (at most 24
+        // offsets) joins the one before it when that saves a 32-lane pass of
+        // the gather: a group is gathered and its candidates tested (nearest
+        // first) before the next, so merging saves a pass and a sort, and its
+        // lower bound (the first group's) still ends the search correctly
+        std::vector<int> start, lb2;
         for (size_t i = 0; i < es.size(); i++) {
             if (i == 0 || es[i].lb2 != es[i - 1].lb2) {
-                o.group_start.push_back((int)i);
-                o.group_lb2.push_back(es[i].lb2);
+                start.push_back((int)i);
+                lb2.push_back(es[i].lb2);
             }
             o.codes.push_back(es[i].code);
+        }
+        start.push_back((int)es.size());
+        auto passes = [](int n) { return (n + 31) / 32; };
+        for (size_t g = 0; g + 1 < start.size(); g++) {
+            const int n = start[g + 1] - start[g];
+            if (!o.group_start.empty()) {
+                const int prev = start[g] - o.group_start.back();
+                if (n <= 24 && passes(prev + n) < passes(prev) + passes(n)) continue;   // joins the previous group
+            }
+            o.group_start.push_back(start[g]);
+            o.group_lb2.push_back(lb2[g]);
         }
         o.group_start.push_back((int)es.size());
         return o;

@@ -201,6 +201,13 @@ int vgpu_batch_compute(vgpu_batch *b, int mode);
 /* Sums over the members; kernel_ms = the batched launch(es), bin_ms = the
  * members' binning (host wall time), step_ms = the whole call (wall time). */
 int vgpu_batch_get_stats(vgpu_batch *b, vgpu_stats *out);
+/* Budget in bytes of the batch's polytope-record store (the scratch the
+ * clipping kernels write and the finish kernel reads; about 1 KB per cell),
+ * 0 = the default 8 GiB.  A batch whose records exceed it is processed in
+ * waves of cells, each clipped and finished before the next; results are the
+ * same.  *waves (vgpu_batch_waves) = the waves of the last compute. */
+int vgpu_batch_set_record_budget(vgpu_batch *b, int64_t bytes);
+int vgpu_batch_waves(vgpu_batch *b, int *waves);
 int vgpu_batch_destroy(vgpu_batch *b);
 
 /* Σ of n device-resident cell volumes (e.g. vgpu_device_results' dev_vol;

@@ -124,3 +124,30 @@ def test_batch_reports_duplicates_in_a_small_member(gpu):
     b = vg.batch([c])
     with pytest.raises(vg.VoroError):
         b.compute_all_cells(mode="mixed")
+
+
+@pytest.mark.gpu
+def test_batch_in_record_waves_matches_one_wave(gpu):
+    """A record budget far below the batch's records runs it in waves of
+    cells (each clipped and finished before the next): the same results."""
+    ws = W.batched(count=24, nmin=64, nmax=30000, seed=91)
+    one = [vg.from_workload(w, mode="mixed") for w in ws]
+    b1 = vg.batch(one)
+    b1.compute_all_cells(mode="mixed")
+    assert b1.waves() == 1
+    many = [vg.from_workload(w, mode="mixed") for w in ws]
+    b2 = vg.batch(many)
+    b2.set_record_budget(40 << 20)   # about 40k cells per wave
+    b2.compute_all_cells(mode="mixed")
+    assert b2.waves() >= 3
+    assert b2.stats()["failed_cells"] == 0
+    for k, (c, a) in enumerate(zip(many, one)):
+        r, q = c.cells(), a.cells()
+        assert np.array_equal(r.ids, q.ids), k
+        assert np.array_equal(r.flags, q.flags), k
+        assert np.array_equal(r.nf, q.nf), k
+        assert np.array_equal(r.nb, q.nb), k
+        # (a wave may pair cells differently in the finish kernel's warps)
+        assert np.allclose(r.vol, q.vol, rtol=1e-13, atol=0), k
+        scale = np.cbrt(np.maximum(q.vol, 1e-300))[:, None]
+        assert (np.abs(r.cen - q.cen) / scale).max() <= 1e-13, k

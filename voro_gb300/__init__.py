@@ -50,7 +50,8 @@ EXPORTED = [
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
-    "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_set_output", "vgpu_get_polytopes",
+    "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_batch_set_record_budget", "vgpu_batch_waves",
+    "vgpu_set_output", "vgpu_get_polytopes",
     "vgpu_autotune",
 ]
 
@@ -126,6 +127,8 @@ def load_library(build_if_missing=True):
     lib.vgpu_batch_compute.argtypes = [vp, ctypes.c_int]
     lib.vgpu_batch_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.vgpu_batch_destroy.argtypes = [vp]
+    lib.vgpu_batch_set_record_budget.argtypes = [vp, ctypes.c_int64]
+    lib.vgpu_batch_waves.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -662,6 +665,16 @@ class batch:
         st = Stats()
         _check(self._lib.vgpu_batch_get_stats(self._h, ctypes.byref(st)))
         return st.as_dict()
+
+    def set_record_budget(self, nbytes):
+        """Budget of the record store (0 = default 8 GiB); larger batches run in waves."""
+        _check(self._lib.vgpu_batch_set_record_budget(self._h, int(nbytes)))
+
+    def waves(self):
+        """Record-store waves of the last compute."""
+        w = ctypes.c_int()
+        _check(self._lib.vgpu_batch_waves(self._h, ctypes.byref(w)))
+        return w.value
 
     def __del__(self):
         try:

@@ -68,7 +68,7 @@ struct DevBuf {
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
-        size_t b = want + want / 8 + 256;
+        size_t b = want + std::min<size_t>(want / 8, (size_t)64 << 20) + 256;   // headroom for regrowth
         cudaError_t e = cudaMalloc(&p, b);
         if (e == cudaSuccess) bytes = b;
         return e;
@@ -148,6 +148,14 @@ const OffsetTable &offset_table() {
 // (about 195).
 constexpr unsigned long long kRecWordsPerCell[2] = {384, 256};   // FP64, MIXED
 constexpr unsigned long long kPolyDoublesPerCell = 256;
+// neighbour overflow store (ints) for n cells: cells with more than kNbStride
+// faces are rare (Poisson cells average 15.5); this holds a quarter of an int
+// per cell, e.g. 6 % of the cells at 36 faces
+inline size_t nb_ovf_ints(size_t n) { return std::min<size_t>(n / 4 + 4096, (size_t)1 << 30); }
+
+// default budget of a batch's record store (records are scratch between the
+// clipping and finish kernels; larger batches are processed in waves)
+constexpr unsigned long long kBatchRecordBytes = 8ull << 30;
 
 struct vgpu_container {
     Geometry g;
@@ -169,8 +177,8 @@ struct vgpu_container {
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
-    DevBuf rec, rec_off, poly, poly_off;
-    DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
+    DevBuf rec_off, poly, poly_off;
+    DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_nb_ovf, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
     int nkept = 0;              // cells of the compute in progress
     int output = 0;             // VGPU_OUTPUT_* flags
@@ -324,8 +332,8 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64,
                       &h->lffh, &h->lffl, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
-                      &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_ids,
-                      &h->r_pos, &h->r_rad, &h->rec, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+                      &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_nb_ovf, &h->r_ids,
+                      &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -504,7 +512,8 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(h->r_nv.ensure(nk * 4));
     VG_CUDA(h->r_mr2.ensure(nk * 8));
     VG_CUDA(h->r_flags.ensure(nk * 4));
-    VG_CUDA(h->r_nb.ensure(nk * kMaxNb * 4));
+    VG_CUDA(h->r_nb.ensure(nk * kNbStride * 4));
+    VG_CUDA(h->r_nb_ovf.ensure(nb_ovf_ints(nk) * 4));
     VG_CUDA(h->r_ids.ensure(nk * 4));
     VG_CUDA(h->r_pos.ensure(nk * 24));
     VG_CUDA(h->r_rad.ensure(nk * 8));
@@ -580,6 +589,8 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     cp.r.maxr2 = h->r_mr2.as<double>();
     cp.r.flags = h->r_flags.as<int>();
     cp.r.nb = h->r_nb.as<int>();
+    cp.r.nb_ovf = h->r_nb_ovf.as<int>();
+    cp.r.nb_ovf_cap = nb_ovf_ints((size_t)std::max(nkept, 1));
     cp.cnt = h->counters.as<Counters>();
     cp.ncells = nkept;
     cp.cell_list = nullptr;
@@ -620,7 +631,8 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
     VG_CUDA(h->r_nv.ensure(nn * 4));
     VG_CUDA(h->r_mr2.ensure(nn * 8));
     VG_CUDA(h->r_flags.ensure(nn * 4));
-    VG_CUDA(h->r_nb.ensure(nn * kMaxNb * 4));
+    VG_CUDA(h->r_nb.ensure(nn * kNbStride * 4));
+    VG_CUDA(h->r_nb_ovf.ensure(nb_ovf_ints(nn) * 4));
     VG_CUDA(h->r_ids.ensure(nn * 4));
     VG_CUDA(h->r_pos.ensure(nn * 24));
     VG_CUDA(h->r_rad.ensure(nn * 8));
@@ -667,21 +679,56 @@ int finish_small(vgpu_container *h, const unsigned long long res[2]) {
     return VGPU_OK;
 }
 
-// The record store the clipping kernels write and the finish kernel reads,
+// The record store: scratch between the clipping kernels and the finish
+// kernel of one compute, shared by all containers of a device so that many
+// containers hold no records between computes.  A compute holds it (mutex)
+// from before its first clipping launch until its finish kernel completed.
+struct RecordStore {
+    std::mutex m;
+    DevBuf buf;
+};
+RecordStore &record_store(int device) {
+    static RecordStore stores[64];
+    return stores[device & 63];
+}
+
+// The record store (held by the caller) as the clipping kernels' output,
 // and the optional polytope output, for the compute of h described by cp;
 // the offset arrays are reset on stream s.
-int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt, cudaStream_t s) {
+int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt, cudaStream_t s, DevBuf &store) {
     cp.rec = nullptr;
     cp.poly = nullptr;
     if (h->nkept <= 0) return VGPU_OK;
     const unsigned long long cap = std::min<unsigned long long>(
         (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), ~0ull >> 8);
-    VG_CUDA(h->rec.ensure(cap * 4));
+    VG_CUDA(store.ensure(cap * 4));
     VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 8));
     VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 8, s));
-    cp.rec = h->rec.as<unsigned>();
+    cp.rec = store.as<unsigned>();
     cp.rec_cap = cap;
     cp.rec_used = &cnt->rec_used;
+    cp.rec_off = h->rec_off.as<unsigned long long>();
+    if (h->output & VGPU_OUTPUT_POLYTOPES) {
+        const unsigned long long pcap = (unsigned long long)h->nkept * kPolyDoublesPerCell + (1u << 16);
+        VG_CUDA(h->poly.ensure(pcap * 8));
+        VG_CUDA(h->poly_off.ensure((size_t)h->nkept * 8));
+        VG_CUDA(cudaMemsetAsync(h->poly_off.p, 0xff, (size_t)h->nkept * 8, s));
+        cp.poly = h->poly.as<double>();
+        cp.poly_cap = pcap;
+        cp.poly_used = &cnt->poly_used;
+        cp.poly_off = h->poly_off.as<long long>();
+    }
+    return VGPU_OK;
+}
+
+// A batch member's record offsets (reset) and optional polytope output; its
+// records go to the batch's store (fields rec, rec_cap, rec_used set later).
+int setup_member_records(vgpu_container *h, CellParams &cp, Counters *cnt, cudaStream_t s) {
+    cp.rec = nullptr;
+    cp.poly = nullptr;
+    if (h->nkept <= 0) return VGPU_OK;
+    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 8));
+    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 8, s));
     cp.rec_off = h->rec_off.as<unsigned long long>();
     if (h->output & VGPU_OUTPUT_POLYTOPES) {
         const unsigned long long pcap = (unsigned long long)h->nkept * kPolyDoublesPerCell + (1u << 16);
@@ -710,7 +757,7 @@ int finish_compute(vgpu_container *h, const Counters &c1, const Counters &c2, fl
     h->stats.planes_tested = (int64_t)(c1.planes_tested + c2.planes_tested);
     h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
     h->stats.overflow_reruns = (int64_t)c1.overflow;
-    h->stats.failed_cells = (int64_t)(c2.overflow + c1.failed);
+    h->stats.failed_cells = (int64_t)(c2.overflow + c1.failed + c1.nb_failed);
     for (int i = 0; i < 8; i++) h->phase[i] = (double)(c1.phase_cycles[i] + c2.phase_cycles[i]);
     h->stats.kernel_ms = cell_ms;
     h->stats.bin_ms = bin_ms;
@@ -732,7 +779,9 @@ int vgpu_compute(vgpu_container *h, int mode) {
     int rc = prepare_cells(h, mode, cp);
     if (rc != VGPU_OK) return rc;
     cudaStream_t s = h->stream;
-    rc = setup_records(h, mode, cp, h->counters.as<Counters>(), h->stream);
+    RecordStore &store = record_store(h->device);
+    std::lock_guard<std::mutex> hold(store.m);
+    rc = setup_records(h, mode, cp, h->counters.as<Counters>(), h->stream, store.buf);
     if (rc != VGPU_OK) return rc;
     // clipping (64-vertex engine, then the 128-vertex one for the cells that
     // overflowed), then the finish kernel over every record
@@ -755,10 +804,11 @@ int vgpu_compute(vgpu_container *h, int mode) {
     cudaEventRecord(h->ev[4], s);
     VG_CUDA(launch_finish(cp, mode, h->sms, s));
     cudaEventRecord(h->ev[3], s);
-    unsigned long long pused = 0;
-    VG_CUDA(cudaMemcpyAsync(&pused, &h->counters.as<Counters>()->poly_used, 8, cudaMemcpyDeviceToHost, s));
+    Counters c3;   // after the finish kernel: polytope output used, neighbour store failures
+    VG_CUDA(cudaMemcpyAsync(&c3, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
-    h->poly_used = pused;
+    h->poly_used = c3.poly_used;
+    c1.nb_failed = c3.nb_failed;
     VG_CUDA(cudaGetLastError());
     float cell_ms = 0, clip_ms = 0, fin_ms = 0;
     cudaEventElapsedTime(&cell_ms, h->ev[2], h->ev[3]);
@@ -916,7 +966,8 @@ int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids) {
     if (offsets) VG_CUDA(cudaMemcpyAsync(offsets, h->nb_off.p, (n + 1) * 8, cudaMemcpyDeviceToHost, s));
     if (ids && total > 0) {
         VG_CUDA(h->nb_out.ensure((size_t)total * 4));
-        VG_CUDA(launch_compact_neighbors(h->r_nf.as<int>(), h->r_nb.as<int>(), h->nb_off.as<long long>(), (int)n,
+        VG_CUDA(launch_compact_neighbors(h->r_nf.as<int>(), h->r_nb.as<int>(), h->r_nb_ovf.as<int>(),
+                                         h->nb_off.as<long long>(), (int)n,
                                          h->nb_out.as<int>(), s));
         VG_CUDA(cudaMemcpyAsync(ids, h->nb_out.p, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
     }
@@ -965,8 +1016,10 @@ struct vgpu_batch {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4];
-    DevBuf cps, starts, counters, work, ovf_list, jobs, bin_res, offsets;
+    DevBuf cps, starts, counters, work, ovf_list, jobs, bin_res, offsets, rec;
     bool offsets_ready = false;
+    int64_t record_bytes = 0;   // record store budget (0: kBatchRecordBytes)
+    int waves = 0;              // record-store waves of the last compute
     vgpu_stats stats{};
 };
 
@@ -999,7 +1052,8 @@ int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
 int vgpu_batch_destroy(vgpu_batch *b) {
     if (!b) return VGPU_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list, &b->jobs, &b->bin_res, &b->offsets};
+    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list, &b->jobs, &b->bin_res, &b->offsets,
+                      &b->rec};
     for (DevBuf *d : bufs) d->release();
     for (int i = 0; i < 4; i++) cudaEventDestroy(b->ev[i]);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -1057,7 +1111,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         int rc = prepare_cells(h, mode, cps[i]);
         if (rc != VGPU_OK) return rc;
         cps[i].cnt = b->counters.as<Counters>() + i;
-        rc = setup_records(h, mode, cps[i], cps[i].cnt, h->stream);
+        rc = setup_member_records(h, cps[i], cps[i].cnt, h->stream);
         if (rc != VGPU_OK) return rc;
         cudaEventRecord(h->ev[2], h->stream);   // after the gather and the record resets
         VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
@@ -1073,7 +1127,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
             if (rc != VGPU_OK) return rc;
             fill_cell_params(h, cps[i]);
             cps[i].cnt = b->counters.as<Counters>() + i;
-            rc = setup_records(h, mode, cps[i], cps[i].cnt, s);
+            rc = setup_member_records(h, cps[i], cps[i].cnt, s);
             if (rc != VGPU_OK) return rc;
         }
     }
@@ -1085,49 +1139,76 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     }
     const long long total = starts[nc];
     const auto t1 = std::chrono::steady_clock::now();
+    // one record store for the whole batch, reused by waves of cells when
+    // the batch's records would not fit the budget: each wave is clipped,
+    // rerun where it overflowed, and finished before the next starts
+    const unsigned long long per_cell = kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0];
+    const unsigned long long slack = 1ull << 20;
+    const unsigned long long budget_words =
+        std::max<unsigned long long>((b->record_bytes > 0 ? (unsigned long long)b->record_bytes : kBatchRecordBytes) / 4,
+                                     slack + per_cell);
+    const unsigned long long cap = std::min<unsigned long long>((unsigned long long)total * per_cell + slack, budget_words);
+    const long long wave = std::max<long long>(1, (long long)((cap - slack) / per_cell));
+    VG_CUDA(b->rec.ensure(cap * 4));
     VG_CUDA(b->cps.ensure((size_t)nc * sizeof(CellParams)));
     VG_CUDA(b->starts.ensure((size_t)(nc + 1) * 8));
     VG_CUDA(b->work.ensure(64));
     VG_CUDA(b->ovf_list.ensure((size_t)std::max<long long>(total, 1) * 8));
+    unsigned long long *wk = b->work.as<unsigned long long>();   // work, overflows, rerun work, records used
+    for (int i = 0; i < nc; i++) {
+        cps[i].rec = b->rec.as<unsigned>();
+        cps[i].rec_cap = cap;
+        cps[i].rec_used = wk + 3;
+    }
     VG_CUDA(cudaMemcpyAsync(b->cps.p, cps.data(), (size_t)nc * sizeof(CellParams), cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemcpyAsync(b->starts.p, starts.data(), (size_t)(nc + 1) * 8, cudaMemcpyHostToDevice, s));
-    VG_CUDA(cudaMemsetAsync(b->work.p, 0, 64, s));
     BatchParams bp;
     memset(&bp, 0, sizeof(bp));
     bp.cps = b->cps.as<CellParams>();
     bp.cell_start = b->starts.as<long long>();
     bp.ncont = nc;
-    bp.ncells = total;
     bp.cell_list = nullptr;
     bp.overflow_list = b->ovf_list.as<long long>();
-    unsigned long long *wk = b->work.as<unsigned long long>();
     bp.work = wk;
     bp.overflow_count = wk + 1;
     bp.offsets = b->offsets.as<int>();
     bp.noffsets = (int)ot.codes.size();
-    cudaEventRecord(b->ev[0], s);
-    VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
-    unsigned long long novf = 0;
-    VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
-    VG_CUDA(cudaStreamSynchronize(s));
-    if (novf > 0) {
-        BatchParams bp2 = bp;
-        bp2.ncells = (long long)novf;
-        bp2.cell_list = b->ovf_list.as<long long>();
-        bp2.overflow_list = nullptr;
-        bp2.work = wk + 2;
-        VG_CUDA(launch_cells_batch(bp2, mode, 1, b->sms, s));
+    float clip_ms = 0, fin_ms = 0;
+    b->waves = 0;
+    for (long long w0 = 0; w0 < total; w0 += wave) {
+        bp.cell_begin = w0;
+        bp.ncells = std::min<long long>(wave, total - w0);
+        VG_CUDA(cudaMemsetAsync(b->work.p, 0, 64, s));
+        cudaEventRecord(b->ev[0], s);
+        VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
+        unsigned long long novf = 0;
+        VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        if (novf > 0) {
+            BatchParams bp2 = bp;
+            bp2.ncells = (long long)novf;
+            bp2.cell_list = b->ovf_list.as<long long>();
+            bp2.overflow_list = nullptr;
+            bp2.work = wk + 2;
+            VG_CUDA(launch_cells_batch(bp2, mode, 1, b->sms, s));
+        }
+        cudaEventRecord(b->ev[2], s);
+        VG_CUDA(launch_finish_batch(bp, mode, b->sms, s));
+        cudaEventRecord(b->ev[1], s);
+        VG_CUDA(cudaEventSynchronize(b->ev[1]));
+        float a = 0, f = 0;
+        cudaEventElapsedTime(&a, b->ev[0], b->ev[2]);
+        cudaEventElapsedTime(&f, b->ev[2], b->ev[1]);
+        clip_ms += a;
+        fin_ms += f;
+        b->waves++;
     }
-    cudaEventRecord(b->ev[2], s);
-    VG_CUDA(launch_finish_batch(bp, mode, b->sms, s));
-    cudaEventRecord(b->ev[1], s);
     for (int i = 0; i < nc; i++) cudaEventRecord(b->members[i]->ev[3], s);
     std::vector<Counters> cs(nc);
     VG_CUDA(cudaMemcpyAsync(cs.data(), b->counters.p, (size_t)nc * sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
     VG_CUDA(cudaGetLastError());
-    float cell_ms = 0;
-    cudaEventElapsedTime(&cell_ms, b->ev[0], b->ev[1]);
+    const float cell_ms = clip_ms + fin_ms;
     Counters zero;
     memset(&zero, 0, sizeof(zero));
     int first_err = VGPU_OK;
@@ -1149,9 +1230,6 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     }
     const auto t2 = std::chrono::steady_clock::now();
     b->stats.kernel_ms = cell_ms;
-    float clip_ms = 0, fin_ms = 0;
-    cudaEventElapsedTime(&clip_ms, b->ev[0], b->ev[2]);
-    cudaEventElapsedTime(&fin_ms, b->ev[2], b->ev[1]);
     b->stats.clip_ms = clip_ms;
     b->stats.finish_ms = fin_ms;
     b->stats.bin_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
@@ -1165,6 +1243,18 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
 int vgpu_batch_get_stats(vgpu_batch *b, vgpu_stats *out) {
     if (!b || !out) return fail(VGPU_ERR_ARG, "null argument");
     *out = b->stats;
+    return VGPU_OK;
+}
+
+int vgpu_batch_set_record_budget(vgpu_batch *b, int64_t bytes) {
+    if (!b || bytes < 0) return fail(VGPU_ERR_ARG, "bad record budget");
+    b->record_bytes = bytes;
+    return VGPU_OK;
+}
+
+int vgpu_batch_waves(vgpu_batch *b, int *waves) {
+    if (!b || !waves) return fail(VGPU_ERR_ARG, "null argument");
+    *waves = b->waves;
     return VGPU_OK;
 }
 

@@ -11,7 +11,15 @@ __global__ void nf_to_ll_kernel(const int *nf, long long *out, int n) {
     if (i < n) out[i] = nf[i];
 }
 
-__global__ void compact_nb_kernel(const int *nf, const int *nb, const long long *off, int n, int *out) {
+// neighbour q of cell i (m faces): its row, or the overflow store
+__device__ __forceinline__ int nb_get(const int *nb, const int *ovf, int i, int m, int q) {
+    const int *row = nb + (size_t)i * kNbStride;
+    if (m <= kNbStride || q < kNbStride - 1) return row[q];
+    return ovf[(size_t)row[kNbStride - 1] + (q - (kNbStride - 1))];
+}
+
+__global__ void compact_nb_kernel(const int *nf, const int *nb, const int *ovf, const long long *off, int n,
+                                  int *out) {
     int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -19,10 +27,10 @@ __global__ void compact_nb_kernel(const int *nf, const int *nb, const long long 
     long long o = off[i];
     // ascending order of neighbour IDs
     for (int q = lane; q < m; q += 32) {
-        int v = nb[(size_t)i * kMaxNb + q];
+        int v = nb_get(nb, ovf, i, m, q);
         int rank = 0;
         for (int r = 0; r < m; r++) {
-            int w = nb[(size_t)i * kMaxNb + r];
+            int w = nb_get(nb, ovf, i, m, r);
             rank += (w < v) || (w == v && r < q);
         }
         out[o + rank] = v;
@@ -94,10 +102,10 @@ cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n, int *out,
-                                     cudaStream_t s) {
+cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const int *ovf, const long long *off, int n,
+                                     int *out, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    compact_nb_kernel<<<(n + 7) / 8, 256, 0, s>>>(nf, nb, off, n, out);
+    compact_nb_kernel<<<(n + 7) / 8, 256, 0, s>>>(nf, nb, ovf, off, n, out);
     note_launch();
     return cudaGetLastError();
 }

@@ -1007,9 +1007,11 @@ struct Engine {
 constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
 template <int MODE, int K>
 constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
-// Cells a warp takes from the work queue at a time.  Consecutive cells (engine
-// order: neighbouring blocks) search nearly the same blocks, so a warp that
-// runs them back to back finds their block starts and particles in its SM's L1.
+// Cells a warp takes from the work queue at a time (at most; fewer when the
+// launch has under four chunks per warp, so that small containers still
+// spread over all warps).  Consecutive cells (engine order: neighbouring
+// blocks) search nearly the same blocks, so a warp that runs them back to
+// back finds their block starts and particles in its SM's L1.
 #ifndef VGPU_CELL_CHUNK
 #define VGPU_CELL_CHUNK 8
 #endif
@@ -1030,13 +1032,14 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
     const long long t_kernel0 = clock64();
 #endif
     unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
+    const int chunk = max(1, min(VGPU_CELL_CHUNK, P.ncells / (int)(4 * gridDim.x * (blockDim.x >> 5))));
     int w = 0, wend = 0;
     for (;;) {
         if (w == wend) {
-            if (lane == 0) w = (int)atomicAdd(work, (unsigned long long)VGPU_CELL_CHUNK);
+            if (lane == 0) w = (int)atomicAdd(work, (unsigned long long)chunk);
             w = __shfl_sync(kFull, w, 0);
             if (w >= P.ncells) break;
-            wend = min(w + VGPU_CELL_CHUNK, P.ncells);
+            wend = min(w + chunk, P.ncells);
         }
         const int k = P.cell_list ? P.cell_list[w] : w;
         w++;
@@ -1109,15 +1112,17 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
         }
         tests = repairs = ptested = pcut = deleted = marginal = ovf = 0;
     };
+    const long long chunk =
+        max(1ll, min((long long)VGPU_CELL_CHUNK, B.ncells / (long long)(4 * gridDim.x * (blockDim.x >> 5))));
     long long w = 0, wend = 0;
     for (;;) {
         if (w == wend) {
-            if (lane == 0) w = (long long)atomicAdd(B.work, (unsigned long long)VGPU_CELL_CHUNK);
+            if (lane == 0) w = (long long)atomicAdd(B.work, (unsigned long long)chunk);
             w = __shfl_sync(kFull, w, 0);
             if (w >= B.ncells) break;
-            wend = min(w + (long long)VGPU_CELL_CHUNK, B.ncells);
+            wend = min(w + chunk, B.ncells);
         }
-        const long long gidx = B.cell_list ? B.cell_list[w] : w;
+        const long long gidx = B.cell_list ? B.cell_list[w] : B.cell_begin + w;
         w++;
         if (gidx < cbeg || gidx >= cend) {
             flush();

@@ -237,13 +237,27 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         mh = P.a.lffh[k];
         ml = P.a.lffl[k];
     }
+    // neighbour IDs: the cell's row of kNbStride, or with more faces its
+    // first kNbStride-1 there and the rest in the overflow store
+    int *row = P.r.nb + (size_t)out * kNbStride;
+    long long ovf = 0;
+    if (have && nf > kNbStride && gl == 0) {
+        const unsigned long long need = (unsigned long long)(nf - (kNbStride - 1));
+        const unsigned long long o = atomicAdd(&P.cnt->nb_ovf_used, need);
+        ovf = o + need <= P.r.nb_ovf_cap ? (long long)o : -1;
+        if (ovf >= 0) row[kNbStride - 1] = (int)ovf;
+    }
+    ovf = __shfl_sync(kFull, ovf, 0, G);
+    const bool nb_full = ovf < 0;
     // planes: neighbour IDs (plane order), sources, planes as float pairs
     for (int q = gl; q < nf; q += G) {
         F.psrc[q] = (int)rp[q];
         F.pshift[q] = (int)rp[nf + q];
         F.rep[q] = 0x7fffffff;
         F.ford[q] = 0;
-        P.r.nb[(size_t)out * kMaxNb + q] = (int)rp[2 * nf + q];
+        const int id = (int)rp[2 * nf + q];
+        if (nf <= kNbStride || q < kNbStride - 1) row[q] = id;
+        else if (!nb_full) P.r.nb_ovf[ovf + q - (kNbStride - 1)] = id;
         if (kFF) {   // (the FP64 engine's vertices need no planes)
             PlaneFF pl;
             if (F.psrc[q] >= 0) {
@@ -428,10 +442,11 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
         } else {
             P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
         }
-        P.r.nf[out] = nf;
+        P.r.nf[out] = nb_full ? 0 : nf;
         P.r.nv[out] = nv;
         P.r.maxr2[out] = mr2;
-        P.r.flags[out] = VGPU_CELL_OK | (int)fl;
+        P.r.flags[out] = nb_full ? (VGPU_CELL_FAILED | (VGPU_FAIL_RECORDS << 8)) : (VGPU_CELL_OK | (int)fl);
+        if (nb_full) atomicAdd(&P.cnt->nb_failed, 1ull);
     }
     if (P.poly != nullptr) {   // (uniform: P is the same for both halves of a warp)
         // the polytope: [nv, nf, vertices (3 nv, particle-relative), then per
@@ -473,7 +488,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             const int incl = group_incl_scan<G>(ord, gl);
             if (mine) {
                 double *df = DF + 2 * q + before + (incl - ord);
-                df[0] = (double)P.r.nb[(size_t)out * kMaxNb + q];
+                df[0] = (double)(int)rp[2 * nf + q];
                 df[1] = (double)ord;
                 int t = F.rep[q];
                 for (int j = 0; j < ord; j++) {
@@ -528,8 +543,9 @@ __global__ void __launch_bounds__(32 * kFinWarps) finish_kernel(const __grid_con
     }
 }
 
-// The same over the cells of a batch (global numbering as cell_batch_kernel);
-// a pair never straddles two containers.
+// The same over the cells cell_begin .. cell_begin+ncells-1 of a batch
+// (global numbering as cell_batch_kernel); a pair never straddles two
+// containers.
 template <int MODE>
 __global__ void __launch_bounds__(32 * kFinWarps) finish_batch_kernel(const __grid_constant__ BatchParams B) {
     __shared__ FinishShared fsh[kFinWarps][2];
@@ -538,7 +554,8 @@ __global__ void __launch_bounds__(32 * kFinWarps) finish_batch_kernel(const __gr
     CellParams &P = *reinterpret_cast<CellParams *>(cpw[wid]);
     const long long nwarps = (long long)gridDim.x * kFinWarps;
     long long cbeg = 0, cend = 0;
-    for (long long g = 2 * ((long long)blockIdx.x * kFinWarps + wid); g < B.ncells; g += 2 * nwarps) {
+    const long long gend = B.cell_begin + B.ncells;
+    for (long long g = B.cell_begin + 2 * ((long long)blockIdx.x * kFinWarps + wid); g < gend; g += 2 * nwarps) {
         if (g < cbeg || g >= cend) {
             int lo = 0, hi = B.ncont;
             while (hi - lo > 1) {
@@ -556,9 +573,9 @@ __global__ void __launch_bounds__(32 * kFinWarps) finish_batch_kernel(const __gr
         }
         // the pair (g, g+1); its second cell may belong to the next container
         const int k0 = (int)(g - cbeg);
-        const int k1 = g + 1 < cend ? (int)(g + 1 - cbeg) : -1;
+        const int k1 = g + 1 < cend && g + 1 < gend ? (int)(g + 1 - cbeg) : -1;
         finish_pair<MODE>(P, fsh[wid], k0, k1, lane);
-        if (k1 < 0 && g + 1 < B.ncells) {
+        if (k1 < 0 && g + 1 < gend) {
             // g + 1 starts the next container: finish it with that container's parameters
             const long long g1 = g + 1;
             int lo = 0, hi = B.ncont;

@@ -8,7 +8,10 @@ namespace vgpu {
 constexpr int kWarp = 32;
 constexpr int kMaxPlanes = 64;     // plane slots per cell (64-bit plane masks)
 constexpr int kCandBuf = 64;       // candidate buffer entries per warp
-constexpr int kMaxNb = 64;         // neighbour slots per cell in the fixed-stride output
+// Neighbour IDs: kNbStride slots per cell in a fixed-stride array; a cell with
+// more faces keeps kNbStride-1 there and the rest in an overflow store, whose
+// offset takes the row's last slot.
+constexpr int kNbStride = 32;
 constexpr int kOffsetRadius = 4;   // engine search table covers Chebyshev radius <= 4
 constexpr int kTableLb2Max = 15;   // ... and lower-bound shells lb2 <= 15 (complete there)
 constexpr int kMaxGroups = 16;
@@ -60,7 +63,9 @@ struct Results {
     int *nv;
     double *maxr2;
     int *flags;
-    int *nb;          // kMaxNb per cell
+    int *nb;          // kNbStride per cell
+    int *nb_ovf;      // overflow store of the neighbour IDs (use: Counters::nb_ovf_used)
+    unsigned long long nb_ovf_cap;     // its capacity (ints, < 2^31)
 };
 
 struct Counters {
@@ -76,6 +81,8 @@ struct Counters {
     unsigned long long failed;     // batched launches: cells that overflowed every capacity
     unsigned long long rec_used;   // words of the polytope record store in use
     unsigned long long poly_used;  // doubles of the polytope output in use
+    unsigned long long nb_ovf_used;  // ints of the neighbour overflow store in use
+    unsigned long long nb_failed;    // finish kernel: cells whose neighbours found it full
     unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
 };
 
@@ -121,7 +128,8 @@ struct BatchParams {
     const long long *cell_start;    // ncont + 1 prefix sums of cells
     int ncont;
     long long ncells;               // cells in this pass
-    const long long *cell_list;     // NULL: global cells 0..ncells-1; else global indices
+    long long cell_begin;           // cell_list NULL: global cells cell_begin .. cell_begin+ncells-1
+    const long long *cell_list;     // else their global indices
     long long *overflow_list;       // first pass: cells that need the larger engine; NULL: rerun
     unsigned long long *overflow_count;
     unsigned long long *work;       // work-queue counter (starts at 0)
@@ -192,7 +200,7 @@ cudaError_t launch_cells_batch_fp64(const BatchParams &bp, int big, int sms, cud
 cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
 cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s);
 cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s);
-cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const long long *off, int n,
+cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const int *ovf, const long long *off, int n,
                                      int *out, cudaStream_t s);
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);
 cudaError_t exclusive_scan_ll(const long long *in, long long *out, int n, long long *tmp, cudaStream_t s);

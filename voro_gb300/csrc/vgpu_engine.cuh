@@ -124,6 +124,7 @@ struct WarpShared {
             unsigned ck[kCandBuf];    // sort keys
             int cj[kCandBuf];         // engine index
             int cs[kCandBuf];         // packed periodic image counts
+            int cpid[kCandBuf];       // neighbour ID
             float4 cd[kCandBuf];      // plane (FP32): n, h
             float4 ce[kCandBuf];      // en, eh, |n|, rs
             double4 cd64[MODE == VGPU_FP64 ? kCandBuf : 1];  // plane (FP64), FP64 engine
@@ -527,7 +528,7 @@ struct Engine {
             const int j = S.u.c.cj[cb];
             S.pl[p] = Q;
             S.pe[p] = make_float4(E.z, E.x, E.y, fabsf(Q.w));
-            S.pid[p] = P.a.pid[j];
+            S.pid[p] = S.u.c.cpid[cb];
             S.psrc[p] = j;
             S.pshift[p] = S.u.c.cs[cb];
             if (MODE == VGPU_FP64) S.pl64x[p] = S.u.c.cd64[cb];
@@ -596,9 +597,9 @@ struct Engine {
         }
         __syncwarp();
         // Phase B: the free slot of rank r hosts the new vertex (a, b, p) of boundary
-        // edge r.  Ranks count within the first slot row s (lanes' s-th slots) that
-        // has room for all the new vertices, so that their solves below run in
-        // one pass; across all free slots only when no row has room.
+        // edge r and solves its position.  Ranks count within the first slot row s
+        // (lanes' s-th slots) that has room for all the new vertices, so that their
+        // solves run in one pass; across all free slots only when no row has room.
         unsigned fw[K];   // free lanes of each slot row
 #pragma unroll
         for (int s = 0; s < K; s++) fw[s] = (unsigned)(Fm.w[s >> 1] >> (32 * (s & 1)));
@@ -632,6 +633,9 @@ struct Engine {
                     for (int e = 0; e < 3; e++)
                         if (tri_plane(Tu, e) == b && tri_plane(Tu, e == 2 ? 0 : e + 1) == a)
                             reinterpret_cast<unsigned char *>(&S.adj[u])[e] = (unsigned char)t;
+                    // its position: independent of the linking, so the solve's
+                    // arithmetic fills the shared-memory latencies around it
+                    compute_vertex(s);
                 }
             }
         }
@@ -657,10 +661,6 @@ struct Engine {
 #pragma unroll
         for (int i = 0; i < Mask<K>::W; i++) Vm.w[i] = (Vm.w[i] & ~Rm.w[i]) | Nm.w[i];
         __syncwarp();
-        // Phase D: positions of the new vertices
-#pragma unroll
-        for (int s = 0; s < K; s++)
-            if (host[s]) compute_vertex(s);
         update_radius();
     }
 
@@ -819,6 +819,7 @@ struct Engine {
                     S.u.c.ck[slot] = (key & ~63u) | (unsigned)slot;
                     S.u.c.cj[slot] = j;
                     S.u.c.cs[slot] = o_code;
+                    S.u.c.cpid[slot] = P.a.pid[j];
                     S.u.c.cd[slot] = cd;
                     S.u.c.ce[slot] = ce;
                     if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C.me64, j, o_code);

@@ -81,6 +81,18 @@ __device__ __forceinline__ FF ff_mulf(FF a, float b) {   // pair times float
 __device__ __forceinline__ FF ff_scale(FF a, float pow2) { return {__fmul_rn(a.h, pow2), __fmul_rn(a.l, pow2)}; }
 __device__ __forceinline__ bool ff_less(FF a, FF b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
 __device__ __forceinline__ double ff_to_double(FF a) { return (double)a.h + (double)a.l; }
+// a / b: the float quotient, corrected by the pair remainder (long division)
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q1 = __fdiv_rn(a.h, b.h);
+    const FF r = ff_sub(a, ff_mulf(b, q1));
+    return ff_fast_two_sum(q1, __fdiv_rn(r.h, b.h));
+}
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int d, int w) {
+    return {__shfl_xor_sync(kFull, a.h, d, w), __shfl_xor_sync(kFull, a.l, d, w)};
+}
+__device__ __forceinline__ FF ff_shfl(FF a, int src, int w) {
+    return {__shfl_sync(kFull, a.h, src, w), __shfl_sync(kFull, a.l, src, w)};
+}
 __device__ __forceinline__ FF ff_from_double(double d) {
     const float h = __double2float_rn(d);
     return {h, __double2float_rn(d - (double)h)};
@@ -183,6 +195,25 @@ __device__ __forceinline__ void group_sum4(double &a, double &b, double &c, doub
 
 // Maximum of non-negative doubles over a group of G lanes by their bit
 // patterns (ordered like the values), on integer units instead of the FP64 pipe.
+// group_sum4 on float pairs (the same transposed folding, FP32 pipe only)
+template <int G>
+__device__ __forceinline__ void group_sum4_ff(FF &a, FF &b, FF &c, FF &d, int gl) {
+    const bool lo = gl < G / 2;
+    FF k0 = lo ? a : c, k1 = lo ? b : d;
+    const FF s0 = lo ? c : a, s1 = lo ? d : b;
+    k0 = ff_add(k0, ff_shfl_xor(s0, G / 2, G));
+    k1 = ff_add(k1, ff_shfl_xor(s1, G / 2, G));
+    const bool lo4 = (gl & (G / 4)) == 0;
+    FF k = lo4 ? k0 : k1;
+    k = ff_add(k, ff_shfl_xor(lo4 ? k1 : k0, G / 4, G));
+#pragma unroll
+    for (int dd = G / 8; dd >= 1; dd >>= 1) k = ff_add(k, ff_shfl_xor(k, dd, G));
+    a = ff_shfl(k, 0, G);
+    b = ff_shfl(k, G / 4, G);
+    c = ff_shfl(k, G / 2, G);
+    d = ff_shfl(k, 3 * G / 4, G);
+}
+
 template <int G>
 __device__ __forceinline__ double group_max_nonneg(double x) {
     unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -319,7 +350,6 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             const FF o = {__shfl_xor_sync(kFull, mf.h, dd, G), __shfl_xor_sync(kFull, mf.l, dd, G)};
             if (ff_less(mf, o)) mf = o;
         }
-        mr2 = ff_to_double(mf);
         if (mf.h > 0.0f && mf.h < 3.0e38f) sc = (ilogbf(mf.h) + 2) / 2 + 1;
     } else {
         mr2 = group_max_nonneg<G>(mr2);
@@ -401,12 +431,25 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             s2 = ff_add(s2, ff_sub(ff_add(ff_mul(dd, ff_add(tv[1], uv[1])), ff_mul(dy, bv[1])), ff_mul(dx, av[1])));
             s3 = ff_add(s3, ff_sub(ff_add(ff_mul(dd, ff_add(tv[2], uv[2])), ff_mul(dy, bv[2])), ff_mul(dx, av[2])));
         }
-        // back to FP64 and to the true scale: vs by 2^(3 sc), the moments by 2^(4 sc)
-        const double up3 = pow2d(3 * sc), up4 = pow2d(4 * sc);
-        vs = ff_to_double(s0) * up3;
-        cx = ff_to_double(s1) * up4;
-        cy = ff_to_double(s2) * up4;
-        cz = ff_to_double(s3) * up4;
+        // the group's sums, then the outputs from pairs with few FP64
+        // operations: vol = s0 / 6 * 2^(3 sc); centroid = c0 + 2^sc C / (4 s0)
+        group_sum4_ff<G>(s0, s1, s2, s3, gl);
+        if (have && gl == 0) {
+            constexpr float kSixthH = (float)(1.0 / 6.0);
+            constexpr float kSixthL = (float)(1.0 / 6.0 - (double)(float)(1.0 / 6.0));
+            const double vol = ff_to_double(ff_mul(s0, {kSixthH, kSixthL})) * pow2d(3 * sc);
+            P.r.vol[out] = vol;
+            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
+                const FF inv = ff_div({1.0f, 0.0f}, ff_scale(s0, 4.0f));
+                const float up = pow2f(sc);
+                const FF sc3[3] = {s1, s2, s3};
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+                    P.r.cen[3 * out + a] = ff_to_double(ff_add(c0f[a], ff_scale(ff_mul(sc3[a], inv), up)));
+            } else {
+                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+            }
+        }
     } else {
         for (int i = gl; i < etot; i += G) {
             const unsigned E = F.stage[i];
@@ -429,22 +472,24 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             cy += dd * (ty + uy) + dy * by - dx * ay;
             cz += dd * (tz + uz) + dy * bz - dx * az;
         }
-    }
-    group_sum4<G>(vs, cx, cy, cz, gl);
-    if (have && gl == 0) {
-        const double vol = vs / 6.0;
-        P.r.vol[out] = vol;
-        if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
-            const double f = 1.0 / (4.0 * vs);
-            P.r.cen[3 * out] = c0[0] + cx * f;
-            P.r.cen[3 * out + 1] = c0[1] + cy * f;
-            P.r.cen[3 * out + 2] = c0[2] + cz * f;
-        } else {
-            P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+        group_sum4<G>(vs, cx, cy, cz, gl);
+        if (have && gl == 0) {
+            const double vol = vs / 6.0;
+            P.r.vol[out] = vol;
+            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
+                const double f = 1.0 / (4.0 * vs);
+                P.r.cen[3 * out] = c0[0] + cx * f;
+                P.r.cen[3 * out + 1] = c0[1] + cy * f;
+                P.r.cen[3 * out + 2] = c0[2] + cz * f;
+            } else {
+                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+            }
         }
+    }
+    if (have && gl == 0) {
         P.r.nf[out] = nb_full ? 0 : nf;
         P.r.nv[out] = nv;
-        P.r.maxr2[out] = mr2;
+        P.r.maxr2[out] = kFF ? ff_to_double(mf) : mr2;
         P.r.flags[out] = nb_full ? (VGPU_CELL_FAILED | (VGPU_FAIL_RECORDS << 8)) : (VGPU_CELL_OK | (int)fl);
         if (nb_full) atomicAdd(&P.cnt->nb_failed, 1ull);
     }

@@ -320,6 +320,23 @@ class container_gpu_base {
         return s;
     }
 
+    // container::find_voronoi_cell (src/container.cc:237-301,
+    // src/container_prd.cc:303-359): the particle whose Voronoi cell holds
+    // (x, y, z); false outside a non-periodic wall or with no particles.
+    bool find_voronoi_cell(double x, double y, double z, double &rx, double &ry, double &rz, int &pid) {
+        flush();
+        const double q[3] = {x, y, z};
+        double r[3] = {0, 0, 0};
+        int32_t id = -1, found = 0;
+        gpu_detail::check(vgpu_find_voronoi_cells(h_, 1, q, &id, r, &found), "find_voronoi_cell");
+        if (!found) return false;
+        rx = r[0];
+        ry = r[1];
+        rz = r[2];
+        pid = id;
+        return true;
+    }
+
     // container_base::total_particles (src/container.hh:150-155)
     int total_particles() {
         ensure();

@@ -170,6 +170,21 @@ int vgpu_get_radii(vgpu_container *h, double *radii);
  * (src/cell.cc:86-95). */
 int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
 
+/* Point location: for each of n points (xyz[3i..3i+2]) the particle whose
+ * Voronoi cell contains it (container::find_voronoi_cell,
+ * src/container.cc:237-301; container_periodic::find_voronoi_cell,
+ * src/container_prd.cc:303-359): the particle of smallest squared distance
+ * (power distance |x - p|^2 - r^2 for the radical kinds) over the periodic
+ * images.  found[i] = 0 where the reference returns false (a point outside a
+ * non-periodic wall, or no particles); else pid[i] = its ID and
+ * rxyz[3i..3i+2] = its position, the periodic image nearest the point in
+ * the point's own frame (stored position plus image counts times the box
+ * lengths, as the reference assembles it).  Exact ties may pick another of
+ * the tied particles than the reference.  Host arrays.  Bins the particles
+ * first if no compute has since the last put. */
+int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int32_t *pid, double *rxyz,
+                            int32_t *found);
+
 /* Diagnostics: per-phase SM clock totals of the last compute's cell kernel,
  * summed over warps (0 init, 1 candidate gather, 2 sort, 3 side tests,
  * 4 cuts, 5 reductions, 7 whole kernel).  All zero unless the library was

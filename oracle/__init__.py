@@ -135,6 +135,22 @@ class RefLib(_Lib):
         if f(*_args(w), fmt.encode(), str(path).encode()) != 0:
             raise ValueError("bad container kind")
 
+    def find_voronoi_cells(self, w, q):
+        """The reference's find_voronoi_cell for each row of q (n x 3):
+        (found, pid, r) with r the returned particle positions (n x 3)."""
+        f = self.lib.ref_find_voronoi_cells
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_int, _f64p,
+                      _i32p, _i32p, _f64p]
+        q = np.ascontiguousarray(q, np.float64)
+        nq = len(q)
+        found = np.zeros(nq, np.int32)
+        pid = np.zeros(nq, np.int32)
+        r = np.zeros((nq, 3), np.float64)
+        if f(*_args(w), nq, q, found, pid, r) != 0:
+            raise ValueError("bad container kind")
+        return found, pid, r
+
     def time_compute_all(self, w):
         f = self.lib.ref_time_compute_all
         f.restype = ctypes.c_double

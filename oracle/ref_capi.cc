@@ -163,6 +163,27 @@ long ref_polytopes(int kind, const double *geom, const int *grid, const int *per
     return (long)buf.size();
 }
 
+// Point location with the reference: find_voronoi_cell for each query point
+// (container::find_voronoi_cell, src/container.cc:237-263 and 275-301;
+// container_periodic::find_voronoi_cell, src/container_prd.cc:303-359).
+// found[i] = 0 where it returns false; else pid[i] and r[3i..3i+2].
+int ref_find_voronoi_cells(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
+                           const double *xyzr, int nq, const double *q, int *found, int *pid, double *r) {
+    bool ok = with_container(kind, geom, grid, periodic, n, ids, xyzr, [&](auto &con, auto &) {
+        for (int i = 0; i < nq; i++) {
+            double rx = 0, ry = 0, rz = 0;
+            int id = -1;
+            const bool f = con.find_voronoi_cell(q[3 * i], q[3 * i + 1], q[3 * i + 2], rx, ry, rz, id);
+            found[i] = f ? 1 : 0;
+            pid[i] = f ? id : -1;
+            r[3 * i] = f ? rx : 0.0;
+            r[3 * i + 1] = f ? ry : 0.0;
+            r[3 * i + 2] = f ? rz : 0.0;
+        }
+    });
+    return ok ? 0 : -2;
+}
+
 // The reference's own print_custom output for every cell, written to path
 // (container::print_custom(format, filename), src/container.cc:401-417).
 int ref_print_custom(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,

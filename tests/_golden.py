@@ -8,9 +8,21 @@ HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
-    """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly)."""
+    """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly;
+    locate_*.npz point-location answers, see load_locate)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
-                  if not os.path.basename(p).startswith("poly_"))
+                  if not os.path.basename(p).startswith(("poly_", "locate_")))
+
+
+def locate_names():
+    return sorted(os.path.basename(p)[7:-4] for p in glob.glob(os.path.join(HERE, "locate_*.npz")))
+
+
+def load_locate(name):
+    """Query points of fixture ``name`` and the reference's find_voronoi_cell
+    answers: (q, found, pid, r)."""
+    z = np.load(os.path.join(HERE, f"locate_{name}.npz"))
+    return z["q"], z["found"], z["pid"], z["r"]
 
 
 def poly_names():

@@ -93,12 +93,46 @@ def make_poly_fixtures(ref, all_cases):
         print(f"poly_{name}: {len(cells)} cells, {os.path.getsize(out)} bytes")
 
 
+# Point-location fixtures: query points and the reference's find_voronoi_cell
+# answer for each (found flag, particle ID, returned particle position): points
+# spread over the domain grown by 20% on every side (outside a non-periodic
+# wall: not found), the stored particle positions themselves, and, where an
+# axis is periodic, points several box lengths away.
+LOCATE_QUERIES = 400
+
+
+def locate_queries(w, seed):
+    rng = np.random.default_rng(seed)
+    g = np.asarray(w["geom"], float)
+    if w["kind"] in (W.KIND_PERIODIC, W.KIND_PERIODIC_POLY):
+        lo, hi = np.zeros(3), np.array([g[0], g[2], g[5]])
+    else:
+        lo, hi = g[0::2], g[1::2]
+    span = hi - lo
+    a = rng.uniform(lo - 0.2 * span, hi + 0.2 * span, size=(LOCATE_QUERIES - 100, 3))
+    b = w["xyzr"][rng.choice(len(w["ids"]), 50), :3]
+    c = rng.uniform(lo, hi, size=(50, 3)) + rng.integers(-3, 4, size=(50, 3)) * span
+    return np.concatenate([a, b, c])
+
+
+def make_locate_fixtures(ref, all_cases):
+    for i, (name, w) in enumerate(all_cases.items()):
+        q = locate_queries(w, 3000 + i)
+        found, pid, r = ref.find_voronoi_cells(w, q)
+        out = os.path.join(HERE, f"locate_{name}.npz")
+        np.savez_compressed(out, q=q, found=found, pid=pid, r=r)
+        print(f"locate_{name}: {len(q)} queries, {int(found.sum())} found, {os.path.getsize(out)} bytes")
+
+
 def main():
     if not build_ref():
         raise SystemExit("reference sources not available; cannot generate fixtures")
     ref = RefLib()
     if "--poly-only" in sys.argv:
         make_poly_fixtures(ref, cases())
+        return
+    if "--locate-only" in sys.argv:
+        make_locate_fixtures(ref, cases())
         return
     for name, w in cases().items():
         rec = ref.compute(w)
@@ -116,6 +150,7 @@ def main():
             nb=nb_flat, nb_off=nb_off)
         print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
     make_poly_fixtures(ref, cases())
+    make_locate_fixtures(ref, cases())
 
 
 if __name__ == "__main__":

@@ -51,7 +51,7 @@ EXPORTED = [
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
     "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_batch_set_record_budget", "vgpu_batch_waves",
-    "vgpu_set_output", "vgpu_get_polytopes",
+    "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells",
     "vgpu_autotune",
 ]
 
@@ -128,6 +128,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_batch_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.vgpu_batch_destroy.argtypes = [vp]
     lib.vgpu_batch_set_record_budget.argtypes = [vp, ctypes.c_int64]
+    lib.vgpu_find_voronoi_cells.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp]
     lib.vgpu_batch_waves.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
@@ -393,6 +394,26 @@ class _ContainerBase:
         out = ctypes.c_double(0)
         _check(self._lib.vgpu_sum_cell_volumes(self._h, ctypes.byref(out)))
         return out.value
+
+    # ---- find_voronoi_cell: src/container.cc:237-301, src/container_prd.cc:303-359
+    def find_voronoi_cells(self, points):
+        """Point location for many points (n, 3): (found, pid, r) with found
+        a bool array, pid the IDs and r (n, 3) the particles' positions (the
+        periodic image nearest each point), as the reference's
+        find_voronoi_cell returns them point by point."""
+        self._flush_pending()
+        q = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(q)
+        found = np.zeros(n, np.int32)
+        pid = np.zeros(n, np.int32)
+        r = np.zeros((n, 3), np.float64)
+        _check(self._lib.vgpu_find_voronoi_cells(self._h, n, _ptr(q), _ptr(pid), _ptr(r), _ptr(found)))
+        return found != 0, pid, r
+
+    def find_voronoi_cell(self, x, y, z):
+        """The reference's signature: (found, rx, ry, rz, pid)."""
+        f, pid, r = self.find_voronoi_cells([[x, y, z]])
+        return bool(f[0]), float(r[0, 0]), float(r[0, 1]), float(r[0, 2]), int(pid[0])
 
     def stats(self):
         st = Stats()

@@ -16,7 +16,7 @@ LIB = os.path.join(LIBDIR, "libvorogpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu", "vgpu_clip_mixed.cu", "vgpu_clip_fp64.cu",
-           "vgpu_finish.cu", "vgpu_noalloc.cu"]
+           "vgpu_finish.cu", "vgpu_noalloc.cu", "vgpu_locate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wno-deprecated-declarations",
               "-diag-suppress", "1444"]

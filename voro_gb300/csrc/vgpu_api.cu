@@ -178,6 +178,7 @@ struct vgpu_container {
     DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
     // results
     DevBuf rec_off, poly, poly_off;
+    DevBuf loc_q, loc_found, loc_pid, loc_r;   // point-location queries and answers
     DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_nb_ovf, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
     int nkept = 0;              // cells of the compute in progress
@@ -185,6 +186,7 @@ struct vgpu_container {
     unsigned long long poly_used = 0;   // doubles of polytope output of the last compute
     long long launches0 = 0;    // launch counter at its start
     bool computed = false;
+    bool binned = false;        // engine-order arrays match the particles (after a compute or a locate)
     vgpu_stats stats{};
     double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
@@ -333,6 +335,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->lffh, &h->lffl, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_nb_ovf, &h->r_ids,
+                      &h->loc_q, &h->loc_found, &h->loc_pid, &h->loc_r,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
@@ -378,6 +381,7 @@ int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyz
     VG_CUDA(cudaStreamSynchronize(h->stream));
     h->staged += n;
     h->computed = false;
+    h->binned = false;
     return VGPU_OK;
 }
 
@@ -390,6 +394,7 @@ int vgpu_put_device(vgpu_container *h, int64_t n, const int32_t *dev_ids, const 
     h->dev_xyzr_ext = dev_xyzr;
     h->dev_n_ext = n;
     h->computed = false;
+    h->binned = false;
     return VGPU_OK;
 }
 
@@ -401,13 +406,17 @@ int vgpu_clear(vgpu_container *h) {
     h->dev_xyzr_ext = nullptr;
     h->dev_n_ext = 0;
     h->computed = false;
+    h->binned = false;
     h->ncells = 0;
     return VGPU_OK;
 }
 
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
-    if (particles_per_block > 0) h->target_density = particles_per_block;
+    if (particles_per_block > 0 && particles_per_block != h->target_density) {
+        h->target_density = particles_per_block;
+        h->binned = false;   // the engine grid changes
+    }
     if (warps_per_cta > 8) return fail(VGPU_ERR_ARG, "at most 8 warps per CTA (got %d)", warps_per_cta);
     if (warps_per_cta > 0) h->warps_per_cta = warps_per_cta;
     return VGPU_OK;
@@ -563,6 +572,7 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(cudaMemsetAsync(h->counters.p, 0, sizeof(Counters), s));
     VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, sizeof(Counters), s));
     h->nkept = nkept;
+    h->binned = true;
     fill_cell_params(h, cp);
     return VGPU_OK;
 }
@@ -672,6 +682,7 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
 int finish_small(vgpu_container *h, const unsigned long long res[2]) {
     if (res[0] >> 32) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
     h->nkept = (int)(res[0] & 0xffffffffu);
+    h->binned = true;
     double rmax = 0.0;
     memcpy(&rmax, &res[1], 8);
     h->g.rmax = rmax;
@@ -989,6 +1000,33 @@ int vgpu_sum_cell_volumes(vgpu_container *h, double *out) {
     double t = 0.0;
     for (int i = 0; i < 64; i++) t += part[i];
     *out = t;
+    return VGPU_OK;
+}
+
+int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int32_t *pid, double *rxyz,
+                            int32_t *found) {
+    if (!h || n < 0 || (n > 0 && (!xyz || !pid || !rxyz || !found))) return fail(VGPU_ERR_ARG, "bad arguments");
+    if (n == 0) return VGPU_OK;
+    if (n > (int64_t)INT32_MAX / 4) return fail(VGPU_ERR_MEMORY, "too many query points");
+    CellParams cp;
+    if (!h->binned) {   // bin the particles as a compute would (no cells computed)
+        int rc = prepare_cells(h, VGPU_MIXED, cp);
+        if (rc != VGPU_OK) return rc;
+    } else {
+        fill_cell_params(h, cp);
+    }
+    cudaStream_t s = h->stream;
+    VG_CUDA(h->loc_q.ensure((size_t)n * 24));
+    VG_CUDA(h->loc_r.ensure((size_t)n * 24));
+    VG_CUDA(h->loc_found.ensure((size_t)n * 4));
+    VG_CUDA(h->loc_pid.ensure((size_t)n * 4));
+    VG_CUDA(cudaMemcpyAsync(h->loc_q.p, xyz, (size_t)n * 24, cudaMemcpyHostToDevice, s));
+    VG_CUDA(launch_locate(cp, (int)n, h->loc_q.as<double>(), h->loc_found.as<int>(), h->loc_pid.as<int>(),
+                          h->loc_r.as<double>(), s));
+    VG_CUDA(cudaMemcpyAsync(found, h->loc_found.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaMemcpyAsync(pid, h->loc_pid.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaMemcpyAsync(rxyz, h->loc_r.p, (size_t)n * 24, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
     return VGPU_OK;
 }
 

@@ -6,19 +6,11 @@
 //   container_periodic: put_locate_block   src/container_prd.cc:189-216
 // and computes two keys per particle: the reference block (which fixes the
 // loop order of results) and the engine block (which fixes the search grid).
-#include "vgpu_internal.cuh"
-#include "../../include/vorogpu.h"
+#include "vgpu_dev.cuh"
 
 namespace vgpu {
 
 namespace {
-
-// step_int, step_mod, step_div: src/v_base.hh:61-80
-__device__ __forceinline__ int step_int(double a) {
-    return a < 0 ? __double2int_rz(a) - 1 : __double2int_rz(a);
-}
-__device__ __forceinline__ int step_mod(int a, int b) { return a >= 0 ? a % b : b - 1 - (b - 1 - a) % b; }
-__device__ __forceinline__ int step_div(int a, int b) { return a >= 0 ? a / b : -1 + (a + 1) / b; }
 
 // The reference's placement of one particle: remapped position c, its
 // reference block key uk (nub if put() drops it) and engine block key gk.

@@ -21,6 +21,13 @@ static __device__ __forceinline__ unsigned float_key(float f) {
 
 static __device__ __forceinline__ int unpack_shift(int code, int a) { return ((code >> (8 * a)) & 255) - 128; }
 
+// step_int, step_mod, step_div: src/v_base.hh:61-80
+static __device__ __forceinline__ int step_int(double a) {
+    return a < 0 ? __double2int_rz(a) - 1 : __double2int_rz(a);
+}
+static __device__ __forceinline__ int step_mod(int a, int b) { return a >= 0 ? a % b : b - 1 - (b - 1 - a) % b; }
+static __device__ __forceinline__ int step_div(int a, int b) { return a >= 0 ? a / b : -1 + (a + 1) / b; }
+
 // FP64 plane of a candidate (engine index j, image counts) relative to the
 // particle, with the reference's own arithmetic: x1 = p_j - (x - qx)
 // (src/v_compute.cc:383-397) and rs = x1*x1+y1*y1+z1*z1 [+ r_i^2 - r_j^2]

@@ -206,6 +206,9 @@ cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s
 cudaError_t exclusive_scan_ll(const long long *in, long long *out, int n, long long *tmp, cudaStream_t s);
 cudaError_t launch_sum_volumes(const double *vol, const int *flags, int n, double *out, cudaStream_t s);
 void box_tables(unsigned tri[8], unsigned adj[8]);
+// vgpu_locate.cu
+cudaError_t launch_locate(const CellParams &cp, int n, const double *qxyz, int *found, int *pid, double *rxyz,
+                          cudaStream_t s);
 
 
 }  // namespace vgpu

@@ -335,6 +335,27 @@ class _ContainerBase:
         _check(self._lib.vgpu_put(self._h, n, _ptr(ids), _ptr(xyzr)))
         self._dirty = True
 
+    # ---- import: src/container.cc:333-376, src/container_prd.cc:400-433
+    def import_file(self, f):
+        """container::import: entries "id x y z" ("id x y z r" for the
+        radical kinds) read as whitespace-separated numbers until the end of
+        the file (a file name or an open text file); an incomplete or
+        malformed entry is the reference's "File import error"."""
+        text = open(f).read() if isinstance(f, (str, bytes, os.PathLike)) else f.read()
+        poly = self.kind in (KIND_CONTAINER_POLY, KIND_PERIODIC_POLY)
+        k = 5 if poly else 4
+        tok = text.split()
+        if len(tok) % k:
+            raise VoroError(1, "File import error")
+        try:
+            ids = np.array([int(t) for t in tok[0::k]], dtype=np.int32)
+            vals = np.array([[float(t) for t in tok[i + 1:i + k]] for i in range(0, len(tok), k)],
+                            dtype=np.float64).reshape(-1, k - 1)
+        except ValueError:
+            raise VoroError(1, "File import error") from None
+        if len(ids):
+            self.put_array(ids, vals[:, :3], vals[:, 3] if poly else None)
+
     def put_xyzr(self, ids, xyzr):
         """put() of int32 ids (n,) and float64 xyzr (n,4) without a host copy."""
         self._flush_pending()

@@ -185,6 +185,25 @@ int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
 int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int32_t *pid, double *rxyz,
                             int32_t *found);
 
+/* Ghost cells: the Voronoi cells of n ghost particles (xyzr[4i..4i+3], the
+ * radius used by the radical kinds) among the container's particles, each
+ * as if it alone were added (compute_ghost_cell, src/container.hh:487-498
+ * and 710-721; src/container_prd.hh:414-422 and 635-644): a ghost is placed
+ * like a put() (outside a non-periodic wall: no cell, flags 0), is no
+ * neighbour of any other cell or ghost, and a radius above the container's
+ * largest widens the search as the reference's max_radius does.  The
+ * container's own results are untouched.  Results (ghost order):
+ * vgpu_get_ghost_cells (as vgpu_get_cells; centroids relative to the
+ * ghost's stored position), vgpu_get_ghost_neighbors (CSR, each list
+ * ascending) and, with VGPU_OUTPUT_POLYTOPES set, vgpu_get_ghost_polytopes
+ * (as vgpu_get_polytopes).  Bins the particles first if no compute has
+ * since the last put. */
+int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const double *xyzr);
+int vgpu_get_ghost_cells(vgpu_container *h, double *vol, double *cen, int32_t *nfaces, int32_t *nverts,
+                         double *maxr2, int32_t *flags);
+int vgpu_get_ghost_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
+int vgpu_get_ghost_polytopes(vgpu_container *h, int64_t *offsets, double *data);
+
 /* Diagnostics: per-phase SM clock totals of the last compute's cell kernel,
  * summed over warps (0 init, 1 candidate gather, 2 sort, 3 side tests,
  * 4 cuts, 5 reductions, 7 whole kernel).  All zero unless the library was

@@ -151,6 +151,24 @@ class RefLib(_Lib):
             raise ValueError("bad container kind")
         return found, pid, r
 
+    def ghost_cells(self, w, gxyzr, nb_per_cell=60) -> CellRecords:
+        """The reference's compute_ghost_cell for each row of gxyzr (x, y, z,
+        r): one record per ghost (ids -1, pos = the given position)."""
+        f = self.lib.ref_ghost_cells
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_int, _f64p,
+                      _i32p, _f64p, _f64p, _i32p, _i32p, _f64p, ctypes.c_long, _i32p, _i64p]
+        g = np.ascontiguousarray(gxyzr, np.float64).reshape(-1, 4)
+        m = len(g)
+        ok = np.zeros(m, np.int32); vol = np.zeros(m); cen = np.zeros((m, 3)); nf = np.zeros(m, np.int32)
+        nv = np.zeros(m, np.int32); mrs = np.zeros(m)
+        cap = nb_per_cell * max(m, 1)
+        nb = np.zeros(cap, np.int32); nb_off = np.zeros(m + 1, np.int64)
+        if f(*_args(w), m, g, ok, vol, cen, nf, nv, mrs, cap, nb, nb_off) != 0:
+            raise ValueError("ghost cells: bad kind or neighbour capacity")
+        return CellRecords(np.full(m, -1, np.int32), g[:, :3].copy(), vol, cen, nf, nv, ok, mrs,
+                           nb[:nb_off[m]], nb_off)
+
     def time_compute_all(self, w):
         f = self.lib.ref_time_compute_all
         f.restype = ctypes.c_double

@@ -12,6 +12,7 @@
 // (src/c_loops.hh:165-210) or c_loop_all_periodic (src/c_loops.hh:325-393).
 #include <algorithm>
 #include <chrono>
+#include <type_traits>
 #include <vector>
 #include "voro++.hh"
 
@@ -105,6 +106,15 @@ bool with_container(int kind, const double *geom, const int *grid, const int *pe
     return true;
 }
 
+// compute_ghost_cell of the container's kind (radius for the radical kinds)
+template <class con_t>
+bool ghost_of(con_t &con, voronoicell_neighbor &c, const double *g) {
+    if constexpr (std::is_same<con_t, container_poly>::value || std::is_same<con_t, container_periodic_poly>::value)
+        return con.compute_ghost_cell(c, g[0], g[1], g[2], g[3]);
+    else
+        return con.compute_ghost_cell(c, g[0], g[1], g[2]);
+}
+
 }  // namespace
 
 extern "C" {
@@ -182,6 +192,49 @@ int ref_find_voronoi_cells(int kind, const double *geom, const int *grid, const 
         }
     });
     return ok ? 0 : -2;
+}
+
+// Ghost cells with the reference: compute_ghost_cell for each ghost
+// (gxyzr: x, y, z, r; r used by the radical kinds), one record per ghost as
+// ref_compute_cells writes them (ok, vol, centroid, faces, vertices,
+// max_radius_squared, neighbours in CSR).  Returns 0, or -1 if nb_cap was
+// too small.
+int ref_ghost_cells(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
+                    const double *xyzr, int ng, const double *gxyzr, int *out_ok, double *out_vol, double *out_cen,
+                    int *out_nf, int *out_nv, double *out_mrs, long nb_cap, int *out_nb, long *out_nb_off) {
+    int status = 0;
+    bool ok = with_container(kind, geom, grid, periodic, n, ids, xyzr, [&](auto &con, auto &) {
+        voronoicell_neighbor c(con);
+        std::vector<int> v;
+        long used = 0;
+        for (int i = 0; i < ng; i++) {
+            out_nb_off[i] = used;
+            const bool q = ghost_of(con, c, gxyzr + 4 * i);
+            out_ok[i] = q ? 1 : 0;
+            if (!q) {
+                out_vol[i] = 0;
+                out_cen[3 * i] = out_cen[3 * i + 1] = out_cen[3 * i + 2] = 0;
+                out_nf[i] = out_nv[i] = 0;
+                out_mrs[i] = 0;
+                continue;
+            }
+            double cx, cy, cz;
+            out_vol[i] = c.volume();
+            c.centroid(cx, cy, cz);
+            out_cen[3 * i] = cx; out_cen[3 * i + 1] = cy; out_cen[3 * i + 2] = cz;
+            out_nf[i] = c.number_of_faces();
+            out_nv[i] = c.p;
+            out_mrs[i] = c.max_radius_squared();
+            c.neighbors(v);
+            for (size_t j = 0; j < v.size(); j++) {
+                if (used >= nb_cap) { status = -1; return; }
+                out_nb[used++] = v[j];
+            }
+        }
+        out_nb_off[ng] = used;
+    });
+    if (!ok) return -2;
+    return status;
 }
 
 // The reference's own print_custom output for every cell, written to path

@@ -9,13 +9,26 @@ HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 def names():
     """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly;
-    locate_*.npz point-location answers, see load_locate)."""
+    locate_*.npz point-location answers, see load_locate; ghost_*.npz ghost
+    cells, see load_ghost)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
-                  if not os.path.basename(p).startswith(("poly_", "locate_")))
+                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_")))
 
 
 def locate_names():
     return sorted(os.path.basename(p)[7:-4] for p in glob.glob(os.path.join(HERE, "locate_*.npz")))
+
+
+def ghost_names():
+    return sorted(os.path.basename(p)[6:-4] for p in glob.glob(os.path.join(HERE, "ghost_*.npz")))
+
+
+def load_ghost(name):
+    """Ghost particles of fixture ``name`` (n x 4: x, y, z, r) and the
+    reference's compute_ghost_cell records (npz fields ok, vol, cen, nf, nv,
+    mrs, nb, nb_off)."""
+    z = np.load(os.path.join(HERE, f"ghost_{name}.npz"))
+    return z["g"], z
 
 
 def load_locate(name):

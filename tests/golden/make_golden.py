@@ -124,6 +124,45 @@ def make_locate_fixtures(ref, all_cases):
         print(f"locate_{name}: {len(q)} queries, {int(found.sum())} found, {os.path.getsize(out)} bytes")
 
 
+# Ghost-cell fixtures: ghost particles and the reference's compute_ghost_cell
+# record for each (ok, volume, centroid, faces, vertices, max_radius_squared,
+# sorted neighbours): ghosts spread over the domain grown by 10% (outside a
+# non-periodic wall: no cell) and, where periodic, some boxes away; radical
+# kinds give each ghost a radius from the particles' own range.
+GHOST_COUNT = 200
+
+
+def ghost_particles(w, seed):
+    rng = np.random.default_rng(seed)
+    g = np.asarray(w["geom"], float)
+    if w["kind"] in (W.KIND_PERIODIC, W.KIND_PERIODIC_POLY):
+        lo, hi = np.zeros(3), np.array([g[0], g[2], g[5]])
+    else:
+        lo, hi = g[0::2], g[1::2]
+    span = hi - lo
+    a = rng.uniform(lo - 0.1 * span, hi + 0.1 * span, size=(GHOST_COUNT - 40, 3))
+    c = rng.uniform(lo, hi, size=(40, 3)) + rng.integers(-2, 3, size=(40, 3)) * span
+    xyz = np.concatenate([a, c])
+    r = w["xyzr"][:, 3]
+    rad = rng.uniform(r.min(), r.max(), size=len(xyz)) if w["kind"] in (W.KIND_CONTAINER_POLY,
+                                                                          W.KIND_PERIODIC_POLY) else np.full(len(xyz), 0.5)
+    return np.concatenate([xyz, rad[:, None]], 1)
+
+
+def make_ghost_fixtures(ref, all_cases):
+    for i, (name, w) in enumerate(all_cases.items()):
+        gx = ghost_particles(w, 4000 + i)
+        rec = ref.ghost_cells(w, gx)
+        nb = [np.sort(rec.neighbors(k)) for k in range(len(rec))]
+        nb_off = np.zeros(len(rec) + 1, np.int64)
+        nb_off[1:] = np.cumsum([len(x) for x in nb])
+        nb_flat = np.concatenate(nb).astype(np.int32) if nb else np.zeros(0, np.int32)
+        out = os.path.join(HERE, f"ghost_{name}.npz")
+        np.savez_compressed(out, g=gx, ok=rec.ok, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, mrs=rec.mrs,
+                            nb=nb_flat, nb_off=nb_off)
+        print(f"ghost_{name}: {len(gx)} ghosts, {int(rec.ok.sum())} cells, {os.path.getsize(out)} bytes")
+
+
 def main():
     if not build_ref():
         raise SystemExit("reference sources not available; cannot generate fixtures")
@@ -133,6 +172,9 @@ def main():
         return
     if "--locate-only" in sys.argv:
         make_locate_fixtures(ref, cases())
+        return
+    if "--ghost-only" in sys.argv:
+        make_ghost_fixtures(ref, cases())
         return
     for name, w in cases().items():
         rec = ref.compute(w)
@@ -151,6 +193,7 @@ def main():
         print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
     make_poly_fixtures(ref, cases())
     make_locate_fixtures(ref, cases())
+    make_ghost_fixtures(ref, cases())
 
 
 if __name__ == "__main__":

@@ -51,7 +51,8 @@ EXPORTED = [
     "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
     "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_batch_set_record_budget", "vgpu_batch_waves",
-    "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells",
+    "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells", "vgpu_compute_ghost_cells",
+    "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes",
     "vgpu_autotune",
 ]
 
@@ -129,6 +130,10 @@ def load_library(build_if_missing=True):
     lib.vgpu_batch_destroy.argtypes = [vp]
     lib.vgpu_batch_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_find_voronoi_cells.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp]
+    lib.vgpu_compute_ghost_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp]
+    lib.vgpu_get_ghost_cells.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    lib.vgpu_get_ghost_neighbors.argtypes = [vp, vp, vp]
+    lib.vgpu_get_ghost_polytopes.argtypes = [vp, vp, vp]
     lib.vgpu_batch_waves.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     for name in EXPORTED:
         if name not in ("vgpu_version", "vgpu_last_error"):
@@ -430,6 +435,38 @@ class _ContainerBase:
         r = np.zeros((n, 3), np.float64)
         _check(self._lib.vgpu_find_voronoi_cells(self._h, n, _ptr(q), _ptr(pid), _ptr(r), _ptr(found)))
         return found != 0, pid, r
+
+    # ---- compute_ghost_cell: src/container.hh:487-498, 710-721; src/container_prd.hh:414-422, 635-644
+    def compute_ghost_cells(self, xyz, r=None):
+        """The cells of ghost particles at the rows of xyz (radii r for the
+        radical kinds), each as if it alone were added to the container;
+        returns a GhostResults (vol, cen, nf, nv, maxr2, flags, ok,
+        neighbors(k), and polytope(k) when set_polytopes is on)."""
+        self._flush_pending()
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = len(xyz)
+        xyzr = np.zeros((n, 4), np.float64)
+        xyzr[:, :3] = xyz
+        xyzr[:, 3] = 0.5 if r is None else r
+        _check(self._lib.vgpu_compute_ghost_cells(self._h, VGPU_FP64 if self.mode == "fp64" else VGPU_MIXED, n,
+                                                  _ptr(xyzr)))
+        vol = np.zeros(n); cen = np.zeros((n, 3)); nf = np.zeros(n, np.int32); nv = np.zeros(n, np.int32)
+        mr2 = np.zeros(n); fl = np.zeros(n, np.int32)
+        _check(self._lib.vgpu_get_ghost_cells(self._h, _ptr(vol), _ptr(cen), _ptr(nf), _ptr(nv), _ptr(mr2),
+                                              _ptr(fl)))
+        res = CellResults(np.full(n, -1, np.int32), xyz.copy(), vol, cen, nf, nv, mr2, fl)
+        off = np.zeros(n + 1, np.int64)
+        _check(self._lib.vgpu_get_ghost_neighbors(self._h, _ptr(off), None))
+        nb = np.zeros(max(int(off[-1]), 1), np.int32)
+        _check(self._lib.vgpu_get_ghost_neighbors(self._h, _ptr(off), _ptr(nb)))
+        res.nb, res.nb_off = nb[:int(off[-1])], off
+        if self._polytopes:
+            poff = np.zeros(n + 1, np.int64)
+            _check(self._lib.vgpu_get_ghost_polytopes(self._h, _ptr(poff), None))
+            data = np.zeros(max(int(poff[-1]), 1))
+            _check(self._lib.vgpu_get_ghost_polytopes(self._h, _ptr(poff), _ptr(data)))
+            res.poly_off, res.poly_data = poff, data
+        return res
 
     def find_voronoi_cell(self, x, y, z):
         """The reference's signature: (found, rx, ry, rz, pid)."""

@@ -179,6 +179,14 @@ struct vgpu_container {
     // results
     DevBuf rec_off, poly, poly_off;
     DevBuf loc_q, loc_found, loc_pid, loc_r;   // point-location queries and answers
+    // ghost cells: engine arrays (the particles, then the ghosts), their
+    // record offsets, work lists and results
+    DevBuf gh_p64, gh_lffh, gh_lffl, gh_pid, gh_gblock, gh_outpos, gh_rec_off, gh_q, gh_keep, gh_list, gh_ovf,
+        gh_cnt, gh_vol, gh_cen, gh_nf, gh_nv, gh_mr2, gh_flags, gh_nb, gh_nb_ovf, gh_nb_off, gh_nb_out, gh_poly,
+        gh_poly_off;
+    int64_t ghost_n = 0;            // ghosts of the last ghost compute
+    bool ghost_poly = false;        // their polytopes were kept
+    unsigned long long ghost_poly_used = 0;
     DevBuf r_vol, r_cen, r_nf, r_nv, r_mr2, r_flags, r_nb, r_nb_ovf, r_ids, r_pos, r_rad, nb_off, nb_out, nb_tmp, sum_tmp;
     int64_t ncells = 0;
     int nkept = 0;              // cells of the compute in progress
@@ -335,7 +343,10 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->lffh, &h->lffl, &h->pid,
                       &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_nb_ovf, &h->r_ids,
-                      &h->loc_q, &h->loc_found, &h->loc_pid, &h->loc_r,
+                      &h->loc_q, &h->loc_found, &h->loc_pid, &h->loc_r, &h->gh_p64, &h->gh_lffh, &h->gh_lffl,
+                      &h->gh_pid, &h->gh_gblock, &h->gh_outpos, &h->gh_rec_off, &h->gh_q, &h->gh_keep, &h->gh_list,
+                      &h->gh_ovf, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
+                      &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
@@ -866,20 +877,21 @@ int vgpu_set_output(vgpu_container *h, int flags) {
     return VGPU_OK;
 }
 
-int vgpu_get_polytopes(vgpu_container *h, int64_t *offsets, double *data) {
-    if (!h || !offsets) return fail(VGPU_ERR_ARG, "null argument");
-    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
-    if (!(h->output & VGPU_OUTPUT_POLYTOPES))
-        return fail(VGPU_ERR_ARG, "polytope output was not requested (vgpu_set_output) for the last compute");
-    const size_t n = (size_t)h->ncells;
+}  // extern "C"
+
+namespace {
+
+// The polytopes of n cells from a store (offsets poff, doubles used) as CSR.
+int assemble_polytopes(vgpu_container *h, size_t n, const DevBuf &poff, const DevBuf &poly, unsigned long long pused,
+                       int64_t *offsets, double *data) {
     offsets[0] = 0;
     if (n == 0) return VGPU_OK;
     cudaStream_t s = h->stream;
     std::vector<long long> off(n);
-    VG_CUDA(cudaMemcpyAsync(off.data(), h->poly_off.p, n * 8, cudaMemcpyDeviceToHost, s));
-    const unsigned long long used = std::min<unsigned long long>(h->poly_used, h->poly.bytes / 8);
+    VG_CUDA(cudaMemcpyAsync(off.data(), poff.p, n * 8, cudaMemcpyDeviceToHost, s));
+    const unsigned long long used = std::min<unsigned long long>(pused, poly.bytes / 8);
     std::vector<double> store(used);
-    if (used > 0) VG_CUDA(cudaMemcpyAsync(store.data(), h->poly.p, used * 8, cudaMemcpyDeviceToHost, s));
+    if (used > 0) VG_CUDA(cudaMemcpyAsync(store.data(), poly.p, used * 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
     for (size_t k = 0; k < n; k++) {
         if (off[k] == -2) return fail(VGPU_ERR_CAPACITY, "polytope output store full");
@@ -895,6 +907,18 @@ int vgpu_get_polytopes(vgpu_container *h, int64_t *offsets, double *data) {
         if (data && len > 0) memcpy(data + offsets[k], store.data() + off[k], (size_t)len * 8);
     }
     return VGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgpu_get_polytopes(vgpu_container *h, int64_t *offsets, double *data) {
+    if (!h || !offsets) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->computed) return fail(VGPU_ERR_NOT_COMPUTED, "vgpu_compute has not run");
+    if (!(h->output & VGPU_OUTPUT_POLYTOPES))
+        return fail(VGPU_ERR_ARG, "polytope output was not requested (vgpu_set_output) for the last compute");
+    return assemble_polytopes(h, (size_t)h->ncells, h->poly_off, h->poly, h->poly_used, offsets, data);
 }
 
 int vgpu_get_stats(vgpu_container *h, vgpu_stats *out) {
@@ -1001,6 +1025,195 @@ int vgpu_sum_cell_volumes(vgpu_container *h, double *out) {
     for (int i = 0; i < 64; i++) t += part[i];
     *out = t;
     return VGPU_OK;
+}
+
+int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const double *xyzr) {
+    if (!h || n < 0 || (n > 0 && !xyzr)) return fail(VGPU_ERR_ARG, "bad arguments");
+    if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    if (n > (int64_t)INT32_MAX / 4) return fail(VGPU_ERR_MEMORY, "too many ghosts");
+    h->ghost_n = 0;
+    if (n == 0) return VGPU_OK;
+    CellParams cp;
+    if (!h->binned) {   // bin the particles as a compute would
+        int rc = prepare_cells(h, mode, cp);
+        if (rc != VGPU_OK) return rc;
+    } else {
+        fill_cell_params(h, cp);
+    }
+    cudaStream_t s = h->stream;
+    const size_t nk = (size_t)h->nkept, ng = (size_t)n, tot = nk + ng;
+    // engine arrays: the particles (copied), then the ghosts
+    VG_CUDA(h->gh_p64.ensure(tot * 32));
+    VG_CUDA(h->gh_lffh.ensure(tot * 16));
+    VG_CUDA(h->gh_lffl.ensure(tot * 16));
+    VG_CUDA(h->gh_pid.ensure(tot * 4));
+    VG_CUDA(h->gh_gblock.ensure(tot * 4));
+    VG_CUDA(h->gh_outpos.ensure(tot * 4));
+    VG_CUDA(h->gh_rec_off.ensure(tot * 8));
+    VG_CUDA(h->gh_q.ensure(ng * 32));
+    VG_CUDA(h->gh_keep.ensure(ng * 4));
+    VG_CUDA(h->gh_list.ensure(ng * 4));
+    VG_CUDA(h->gh_ovf.ensure(ng * 4));
+    VG_CUDA(h->gh_cnt.ensure(2 * sizeof(Counters)));
+    VG_CUDA(h->gh_vol.ensure(ng * 8));
+    VG_CUDA(h->gh_cen.ensure(ng * 24));
+    VG_CUDA(h->gh_nf.ensure(ng * 4));
+    VG_CUDA(h->gh_nv.ensure(ng * 4));
+    VG_CUDA(h->gh_mr2.ensure(ng * 8));
+    VG_CUDA(h->gh_flags.ensure(ng * 4));
+    VG_CUDA(h->gh_nb.ensure(ng * kNbStride * 4));
+    VG_CUDA(h->gh_nb_ovf.ensure(nb_ovf_ints(ng) * 4));
+    if (nk > 0) {
+        VG_CUDA(cudaMemcpyAsync(h->gh_p64.p, cp.a.p64, nk * 32, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->gh_lffh.p, cp.a.lffh, nk * 16, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->gh_lffl.p, cp.a.lffl, nk * 16, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->gh_pid.p, cp.a.pid, nk * 4, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->gh_gblock.p, cp.a.gblock, nk * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    VG_CUDA(cudaMemcpyAsync(h->gh_q.p, xyzr, ng * 32, cudaMemcpyHostToDevice, s));
+    VG_CUDA(launch_ghost_setup(h->g, (int)ng, h->gh_q.as<double4>(), (int)nk, h->gh_p64.as<double4>(),
+                               h->gh_lffh.as<float4>(), h->gh_lffl.as<float4>(), h->gh_pid.as<int>(),
+                               h->gh_outpos.as<int>(), h->gh_gblock.as<int>(), h->gh_keep.as<int>(), s));
+    std::vector<int> keep(ng);
+    VG_CUDA(cudaMemcpyAsync(keep.data(), h->gh_keep.p, ng * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> list;
+    list.reserve(ng);
+    double rmax = h->g.rmax;
+    for (size_t i = 0; i < ng; i++)
+        if (keep[i]) {
+            list.push_back((int)(nk + i));
+            if (h->g.poly) rmax = std::max(rmax, xyzr[4 * i + 3]);
+        }
+    const int nl = (int)list.size();
+    // results of ghosts that are not computed (outside a wall): no cell
+    VG_CUDA(cudaMemsetAsync(h->gh_vol.p, 0, ng * 8, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_cen.p, 0, ng * 24, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_nf.p, 0, ng * 4, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_nv.p, 0, ng * 4, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_mr2.p, 0, ng * 8, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_flags.p, 0, ng * 4, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_rec_off.as<char>() + nk * 8, 0xff, ng * 8, s));
+    VG_CUDA(cudaMemsetAsync(h->gh_cnt.p, 0, 2 * sizeof(Counters), s));
+    if (nl > 0) VG_CUDA(cudaMemcpyAsync(h->gh_list.p, list.data(), (size_t)nl * 4, cudaMemcpyHostToDevice, s));
+    // the engine over the ghosts only, against the particles
+    Counters *gc = h->gh_cnt.as<Counters>();
+    cp.a.p64 = h->gh_p64.as<double4>();
+    cp.a.l32 = cp.a.lffh = h->gh_lffh.as<float4>();
+    cp.a.lffl = h->gh_lffl.as<float4>();
+    cp.a.pid = h->gh_pid.as<int>();
+    cp.a.gblock = h->gh_gblock.as<int>();
+    cp.a.outpos = h->gh_outpos.as<int>();
+    cp.r.vol = h->gh_vol.as<double>();
+    cp.r.cen = h->gh_cen.as<double>();
+    cp.r.nf = h->gh_nf.as<int>();
+    cp.r.nv = h->gh_nv.as<int>();
+    cp.r.maxr2 = h->gh_mr2.as<double>();
+    cp.r.flags = h->gh_flags.as<int>();
+    cp.r.nb = h->gh_nb.as<int>();
+    cp.r.nb_ovf = h->gh_nb_ovf.as<int>();
+    cp.r.nb_ovf_cap = nb_ovf_ints(ng);
+    cp.g.rmax = rmax;   // a larger ghost radius widens the search (compute_ghost_cell raises max_radius)
+    cp.g.rmax32 = (float)rmax * (1.0f + 1e-6f);
+    cp.cnt = gc;
+    cp.ncells = nl;
+    cp.cell_list = h->gh_list.as<int>();
+    cp.overflow_list = h->gh_ovf.as<int>();
+    h->ghost_poly = (h->output & VGPU_OUTPUT_POLYTOPES) != 0;
+    h->ghost_poly_used = 0;
+    RecordStore &store = record_store(h->device);
+    std::lock_guard<std::mutex> hold(store.m);
+    const unsigned long long cap =
+        (unsigned long long)nl * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20);
+    VG_CUDA(store.buf.ensure(cap * 4));
+    cp.rec = store.buf.as<unsigned>();
+    cp.rec_cap = cap;
+    cp.rec_used = &gc->rec_used;
+    cp.rec_off = h->gh_rec_off.as<unsigned long long>();
+    cp.poly = nullptr;
+    if (h->ghost_poly) {
+        const unsigned long long pcap = (unsigned long long)ng * kPolyDoublesPerCell + (1u << 16);
+        VG_CUDA(h->gh_poly.ensure(pcap * 8));
+        VG_CUDA(h->gh_poly_off.ensure(ng * 8));
+        VG_CUDA(cudaMemsetAsync(h->gh_poly_off.p, 0xff, ng * 8, s));
+        cp.poly = h->gh_poly.as<double>();
+        cp.poly_cap = pcap;
+        cp.poly_used = &gc->poly_used;
+        cp.poly_off = h->gh_poly_off.as<long long>();
+    }
+    Counters c1, c2, c3;
+    memset(&c2, 0, sizeof(c2));
+    if (nl > 0) {
+        VG_CUDA(launch_cells(cp, mode, 0, h->sms, s, h->warps_per_cta));
+        VG_CUDA(cudaMemcpyAsync(&c1, gc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        if (c1.overflow > 0) {
+            CellParams cp2 = cp;
+            cp2.cnt = gc + 1;
+            cp2.ncells = (int)c1.overflow;
+            cp2.cell_list = h->gh_ovf.as<int>();
+            cp2.overflow_list = nullptr;
+            VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s, h->warps_per_cta));
+            VG_CUDA(cudaMemcpyAsync(&c2, gc + 1, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        }
+        VG_CUDA(launch_finish(cp, mode, h->sms, s));
+        VG_CUDA(cudaMemcpyAsync(&c3, gc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        h->ghost_poly_used = c3.poly_used;
+        const unsigned long long failed = c2.overflow + c1.failed + c3.nb_failed;
+        h->ghost_n = n;
+        if (failed > 0) return fail(VGPU_ERR_CAPACITY, "%llu ghost cells exceeded the engine capacity", failed);
+    }
+    VG_CUDA(cudaStreamSynchronize(s));
+    VG_CUDA(cudaGetLastError());
+    h->ghost_n = n;
+    return VGPU_OK;
+}
+
+int vgpu_get_ghost_cells(vgpu_container *h, double *vol, double *cen, int32_t *nfaces, int32_t *nverts, double *maxr2,
+                         int32_t *flags) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    const size_t n = (size_t)h->ghost_n;
+    if (n == 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    if (vol) VG_CUDA(cudaMemcpyAsync(vol, h->gh_vol.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (cen) VG_CUDA(cudaMemcpyAsync(cen, h->gh_cen.p, n * 24, cudaMemcpyDeviceToHost, s));
+    if (nfaces) VG_CUDA(cudaMemcpyAsync(nfaces, h->gh_nf.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (nverts) VG_CUDA(cudaMemcpyAsync(nverts, h->gh_nv.p, n * 4, cudaMemcpyDeviceToHost, s));
+    if (maxr2) VG_CUDA(cudaMemcpyAsync(maxr2, h->gh_mr2.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (flags) VG_CUDA(cudaMemcpyAsync(flags, h->gh_flags.p, n * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    return VGPU_OK;
+}
+
+int vgpu_get_ghost_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids) {
+    if (!h || !offsets) return fail(VGPU_ERR_ARG, "null argument");
+    const size_t n = (size_t)h->ghost_n;
+    offsets[0] = 0;
+    if (n == 0) return VGPU_OK;
+    cudaStream_t s = h->stream;
+    std::vector<int32_t> nf(n);
+    VG_CUDA(cudaMemcpyAsync(nf.data(), h->gh_nf.p, n * 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    for (size_t k = 0; k < n; k++) offsets[k + 1] = offsets[k] + nf[k];
+    const int64_t total = offsets[n];
+    if (ids && total > 0) {
+        VG_CUDA(h->gh_nb_off.ensure((n + 1) * 8));
+        VG_CUDA(h->gh_nb_out.ensure((size_t)total * 4));
+        VG_CUDA(cudaMemcpyAsync(h->gh_nb_off.p, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s));
+        VG_CUDA(launch_compact_neighbors(h->gh_nf.as<int>(), h->gh_nb.as<int>(), h->gh_nb_ovf.as<int>(),
+                                         h->gh_nb_off.as<long long>(), (int)n, h->gh_nb_out.as<int>(), s));
+        VG_CUDA(cudaMemcpyAsync(ids, h->gh_nb_out.p, (size_t)total * 4, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+    }
+    return VGPU_OK;
+}
+
+int vgpu_get_ghost_polytopes(vgpu_container *h, int64_t *offsets, double *data) {
+    if (!h || !offsets) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->ghost_poly)
+        return fail(VGPU_ERR_ARG, "polytope output was not requested (vgpu_set_output) for the last ghost compute");
+    return assemble_polytopes(h, (size_t)h->ghost_n, h->gh_poly_off, h->gh_poly, h->ghost_poly_used, offsets, data);
 }
 
 int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int32_t *pid, double *rxyz,

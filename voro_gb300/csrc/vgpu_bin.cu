@@ -273,6 +273,38 @@ cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rma
     return cudaGetLastError();
 }
 
+namespace {
+
+// Ghost particles (compute_ghost_cell, src/container.hh:487-498 and 710-721,
+// src/container_prd.hh:414-422 and 635-644): each is located like a put()
+// (put_locate_block: the same remap, a point outside a non-periodic wall is
+// rejected) and written as engine entry base + i, in no block's particle
+// range, so that no cell sees it as a neighbour; its result slot is i.
+__global__ void ghost_setup_kernel(Geometry g, int n, int nub, int nblocks, const double4 *q, int base,
+                                   double4 *p64, float4 *lffh, float4 *lffl, int *pid, int *outpos, int *gblock,
+                                   int *keep) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 r;
+    unsigned uk, gk;
+    const bool ok = remap_one(g, q[i], nub, nblocks, r, uk, gk);
+    keep[i] = ok ? 1 : 0;
+    if (ok) gather_one(g, base + i, (int)gk, r, -1, i, p64, lffh, lffl, pid, outpos, gblock);
+}
+
+}  // namespace
+
+cudaError_t launch_ghost_setup(const Geometry &g, int n, const double4 *q, int base, double4 *p64, float4 *lffh,
+                               float4 *lffl, int *pid, int *outpos, int *gblock, int *keep, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    ghost_setup_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(
+        g, n, g.un[0] * g.un[1] * g.un[2], g.gn[0] * g.gn[1] * g.gn[2], q, base, p64, lffh, lffl, pid, outpos, gblock,
+        keep);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
                           int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl,

@@ -187,6 +187,8 @@ struct SmallBinJob {
     unsigned long long *result;   // [0] kept | duplicate << 32, [1] largest radius (bits)
 };
 cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, cudaStream_t s);
+cudaError_t launch_ghost_setup(const Geometry &g, int n, const double4 *q, int base, double4 *p64, float4 *lffh,
+                               float4 *lffl, int *pid, int *outpos, int *gblock, int *keep, cudaStream_t s);
 cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,
                                    int nkept, int *dup_flag, cudaStream_t s);
 

@@ -360,6 +360,17 @@ class container_gpu_base {
         return true;
     }
 
+    // compute_ghost_cell (src/container.hh:487-498 and 710-721,
+    // src/container_prd.hh:414-422 and 635-644): the cell of a ghost particle
+    // at (x, y, z) (radius r for the radical kinds) among the particles;
+    // false if it has none (outside a non-periodic wall, or cut away).
+    bool compute_ghost_cell(voronoicell &c, double x, double y, double z, double r = default_radius) {
+        return ghost(c, nullptr, x, y, z, r);
+    }
+    bool compute_ghost_cell(voronoicell_neighbor &c, double x, double y, double z, double r = default_radius) {
+        return ghost(c, &c.nb_, x, y, z, r);
+    }
+
     // container::print_custom (src/container.hh:434-451; fields
     // src/cell.cc:2485-2558)
     void print_custom(const char *format, FILE *fp = stdout) {
@@ -452,6 +463,37 @@ class container_gpu_base {
         gpu_detail::check(vgpu_get_neighbors(h_, off_.data(), nb_.data()), "neighbors");
         nb_.resize(tot);
         have_nb_ = true;
+    }
+    bool ghost(voronoicell &c, std::vector<int> *nb, double x, double y, double z, double r) {
+        flush();
+        const double g[4] = {x, y, z, r};
+        gpu_detail::check(vgpu_compute_ghost_cells(h_, mode_, 1, g), "compute_ghost_cell");
+        double vol = 0, cen[3] = {0, 0, 0}, mr2 = 0;
+        int32_t nf = 0, nv = 0, fl = 0;
+        gpu_detail::check(vgpu_get_ghost_cells(h_, &vol, cen, &nf, &nv, &mr2, &fl), "compute_ghost_cell");
+        c.has_poly_ = false;
+        c.p = nv;
+        c.vol_ = vol;
+        c.cen_[0] = cen[0];
+        c.cen_[1] = cen[1];
+        c.cen_[2] = cen[2];
+        c.nf_ = nf;
+        c.mr2_ = mr2;
+        if (!(fl & VGPU_CELL_OK)) return false;
+        if (nb) {
+            int64_t off[2] = {0, 0};
+            gpu_detail::check(vgpu_get_ghost_neighbors(h_, off, nullptr), "compute_ghost_cell");
+            nb->assign((size_t)off[1], 0);
+            gpu_detail::check(vgpu_get_ghost_neighbors(h_, off, nb->data()), "compute_ghost_cell");
+        }
+        if (poly_on_) {
+            int64_t off[2] = {0, 0};
+            gpu_detail::check(vgpu_get_ghost_polytopes(h_, off, nullptr), "compute_ghost_cell");
+            std::vector<double> d((size_t)std::max<int64_t>(off[1], 1));
+            gpu_detail::check(vgpu_get_ghost_polytopes(h_, off, d.data()), "compute_ghost_cell");
+            if (off[1] > 0) load_polytope(c, d.data());
+        }
+        return true;
     }
     bool fill(voronoicell &c, int64_t k) {
         c.has_poly_ = false;

@@ -1,8 +1,10 @@
 // A reference-style program (container + c_loop_all + voronoicell_neighbor,
 // as in the reference's examples) built against the drop-in header.
 //
-// usage: shim_cells <input> <records-out> [<print_custom format> <custom-out>]
+// usage: shim_cells <input> <records-out> [<print_custom format> <custom-out>
+//                   [<queries> <queries-out>]]
 // input: "kind ax bx ay by az bz nx ny nz xp yp zp n" then n lines "id x y z r"
+// queries: lines "x y z r": find_voronoi_cell and compute_ghost_cell of each
 #include <cstdio>
 #include <vector>
 
@@ -40,6 +42,35 @@ static void put_one(container_periodic_poly &con, int id, double x, double y, do
 }
 
 template <class C>
+static int queries(C &con, const char *qpath, const char *opath) {
+    FILE *q = fopen(qpath, "r");
+    FILE *out = fopen(opath, "w");
+    if (!q || !out) return 4;
+    double x, y, z, r, rx, ry, rz, cx, cy, cz;
+    int pid;
+    voronoicell_neighbor c(con);
+    std::vector<int> neigh;
+    while (fscanf(q, "%lg %lg %lg %lg", &x, &y, &z, &r) == 4) {
+        const bool f = con.find_voronoi_cell(x, y, z, rx, ry, rz, pid);
+        fprintf(out, "find %d %d %.17g %.17g %.17g\n", f ? 1 : 0, f ? pid : -1, f ? rx : 0.0, f ? ry : 0.0,
+                f ? rz : 0.0);
+        const bool g = con.compute_ghost_cell(c, x, y, z, r);
+        if (g) {
+            c.centroid(cx, cy, cz);
+            c.neighbors(neigh);
+            fprintf(out, "ghost 1 %.17g %.17g %.17g %.17g %d %d", c.volume(), cx, cy, cz, c.number_of_faces(), c.p);
+            for (int v : neigh) fprintf(out, " %d", v);
+            fputc('\n', out);
+        } else {
+            fprintf(out, "ghost 0\n");
+        }
+    }
+    fclose(q);
+    fclose(out);
+    return 0;
+}
+
+template <class C>
 static int run(C &con, FILE *in, int n, int argc, char **argv) {
     for (int k = 0; k < n; k++) {
         int id;
@@ -52,6 +83,7 @@ static int run(C &con, FILE *in, int n, int argc, char **argv) {
     dump(con, out);
     fclose(out);
     if (argc > 4) con.print_custom(argv[3], argv[4]);
+    if (argc > 6) return queries(con, argv[5], argv[6]);
     return 0;
 }
 

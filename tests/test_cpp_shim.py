@@ -145,3 +145,40 @@ def test_shim_polytope_fields(gpu, tmp_path, name):
         else:
             errs = G.compare_custom_text(got, ref)
         assert not errs, "\n".join(errs[:10])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["unit_cube_1000", "periodic_poly_800"])
+def test_shim_point_location_and_ghost_cells(gpu, tmp_path, name):
+    """find_voronoi_cell and compute_ghost_cell through the C++ header give
+    the reference's answers stored in the fixtures."""
+    exe = _compile(tmp_path)
+    w, _ = G.load(name)
+    g, z = G.load_ghost(name)
+    inp = tmp_path / "in.txt"
+    _write_input(inp, w)
+    qf = tmp_path / "q.txt"
+    with open(qf, "w") as f:
+        for x, y, zz, r in g[:60]:
+            f.write(f"{float(x)!r} {float(y)!r} {float(zz)!r} {float(r)!r}\n")
+    out = tmp_path / "q_out.txt"
+    r = subprocess.run([exe, str(inp), str(tmp_path / "o.txt"), "%i", str(tmp_path / "c.txt"), str(qf), str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = open(out).read().splitlines()
+    finds = [l.split() for l in lines if l.startswith("find")]
+    ghosts = [l.split() for l in lines if l.startswith("ghost")]
+    assert len(finds) == len(ghosts) == 60
+    con = vg.from_workload(w, mode="mixed")
+    f, pid, rr = con.find_voronoi_cells(g[:60, :3])
+    for k, t in enumerate(finds):
+        assert int(t[1]) == int(f[k])
+        if f[k]:
+            assert int(t[2]) == pid[k] and [float(v) for v in t[3:6]] == list(rr[k])
+    for k, t in enumerate(ghosts):
+        assert int(t[1]) == int(z["ok"][k]), k
+        if z["ok"][k]:
+            assert abs(float(t[2]) - z["vol"][k]) <= 1e-10 * z["vol"][k]
+            assert int(t[6]) == z["nf"][k]
+            nb = np.sort(np.array([int(v) for v in t[8:]], np.int32))
+            assert np.array_equal(nb, z["nb"][z["nb_off"][k]:z["nb_off"][k + 1]])

@@ -150,6 +150,22 @@ int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *bes
  * print_custom fields %p %P %o %g %E %e %F %A %a %f %t %l, src/cell.cc:
  * 2485-2558).  Applies from the next compute. */
 #define VGPU_OUTPUT_POLYTOPES 1
+
+/* Walls (src/wall.hh:25-130; container_base only: not for the
+ * container_periodic kinds, VGPU_ERR_UNSUPPORTED).  Each cuts every cell
+ * after its initial box, in the order added, with one plane computed from
+ * the particle's position as the reference's cut_cell does (src/wall.cc);
+ * its faces carry the wall's ID as neighbour.  params (7 doubles):
+ *   VGPU_WALL_SPHERE   xc yc zc rc            (wall_sphere)
+ *   VGPU_WALL_PLANE    xc yc zc ac            (wall_plane: x.c < ac inside)
+ *   VGPU_WALL_CYLINDER xc yc zc xa ya za rc   (wall_cylinder)
+ *   VGPU_WALL_CONE     xc yc zc xa ya za ang  (wall_cone)
+ * Applies from the next compute.  point_inside_walls
+ * (src/container.hh:75-78) is vgpu_point_inside_walls. */
+#define VGPU_WALL_SPHERE 0
+#define VGPU_WALL_PLANE 1
+#define VGPU_WALL_CYLINDER 2
+#define VGPU_WALL_CONE 3
 int vgpu_set_output(vgpu_container *h, int flags);
 /* The polytopes of the last compute in loop order, CSR: offsets[n+1] (int64,
  * in doubles) and data.  Cell k is data[offsets[k] .. offsets[k+1]):
@@ -169,6 +185,10 @@ int vgpu_get_radii(vgpu_container *h, double *radii);
  * (src/cell.cc:2567-2580); unit-cell faces of periodic kinds are 0
  * (src/cell.cc:86-95). */
 int vgpu_get_neighbors(vgpu_container *h, int64_t *offsets, int32_t *ids);
+
+int vgpu_add_wall(vgpu_container *h, int type, const double params[7], int id);
+int vgpu_clear_walls(vgpu_container *h);
+int vgpu_point_inside_walls(vgpu_container *h, double x, double y, double z, int *inside);
 
 /* Point location: for each of n points (xyz[3i..3i+2]) the particle whose
  * Voronoi cell contains it (container::find_voronoi_cell,

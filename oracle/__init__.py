@@ -113,8 +113,13 @@ class _Lib:
 class RefLib(_Lib):
     path = REF_SO
 
+    def compute(self, w, nb_per_cell=40) -> CellRecords:
+        _walls(self.lib, w)
+        return super().compute(w, nb_per_cell)
+
     def polytopes(self, w):
         """The reference's polytope of every cell (parse_polytopes format)."""
+        _walls(self.lib, w)
         f = self.lib.ref_polytopes
         f.restype = ctypes.c_long
         f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_long, _f64p]
@@ -128,6 +133,7 @@ class RefLib(_Lib):
 
     def print_custom(self, w, fmt, path):
         """The reference's container::print_custom(fmt, path) output."""
+        _walls(self.lib, w)
         f = self.lib.ref_print_custom
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_char_p,
@@ -138,6 +144,7 @@ class RefLib(_Lib):
     def find_voronoi_cells(self, w, q):
         """The reference's find_voronoi_cell for each row of q (n x 3):
         (found, pid, r) with r the returned particle positions (n x 3)."""
+        _walls(self.lib, w)
         f = self.lib.ref_find_voronoi_cells
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_int, _f64p,
@@ -154,6 +161,7 @@ class RefLib(_Lib):
     def ghost_cells(self, w, gxyzr, nb_per_cell=60) -> CellRecords:
         """The reference's compute_ghost_cell for each row of gxyzr (x, y, z,
         r): one record per ghost (ids -1, pos = the given position)."""
+        _walls(self.lib, w)
         f = self.lib.ref_ghost_cells
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_int, _f64p, _i32p, _i32p, ctypes.c_int, _i32p, _f64p, ctypes.c_int, _f64p,
@@ -204,6 +212,21 @@ def parse_polytopes(flat):
             i += order
         cells.append({"ok": bool(ok), "verts": verts, "sa": float(sa), "ted": float(ted), "faces": faces})
     return cells
+
+
+def _walls(lib, w):
+    """Hands the workload's walls (list of (type, params, id)) to the
+    reference driver; they apply to kind 0/1 containers."""
+    f = lib.ref_set_walls
+    f.restype = None
+    f.argtypes = [ctypes.c_int, _i32p, _f64p, _i32p]
+    walls = w.get("walls") or []
+    t = np.array([x[0] for x in walls], np.int32)
+    p = np.zeros((len(walls), 7), np.float64)
+    for i, x in enumerate(walls):
+        p[i, :len(x[1])] = x[1]
+    ids = np.array([x[2] for x in walls], np.int32)
+    f(len(walls), t, np.ascontiguousarray(p), ids)
 
 
 def _args(w):

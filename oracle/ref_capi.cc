@@ -71,20 +71,45 @@ void run_cells(con_t &con, loop_t &vl, rec_sink &s) {
     if (s.nb_off) s.nb_off[s.n] = s.nb_used;
 }
 
+// Walls to add to the next containers of kinds 0 and 1 (ref_set_walls): type
+// (0 sphere, 1 plane, 2 cylinder, 3 cone), 7 parameters, ID.
+struct wall_rec {
+    int type, id;
+    double p[7];
+};
+std::vector<wall_rec> g_walls;
+
+template <class con_t>
+void add_walls(con_t &con, std::vector<wall *> &owned) {
+    for (const wall_rec &w : g_walls) {
+        wall *o = nullptr;
+        const double *p = w.p;
+        if (w.type == 0) o = new wall_sphere(p[0], p[1], p[2], p[3], w.id);
+        else if (w.type == 1) o = new wall_plane(p[0], p[1], p[2], p[3], w.id);
+        else if (w.type == 2) o = new wall_cylinder(p[0], p[1], p[2], p[3], p[4], p[5], p[6], w.id);
+        else o = new wall_cone(p[0], p[1], p[2], p[3], p[4], p[5], p[6], w.id);
+        owned.push_back(o);
+        con.add_wall(o);
+    }
+}
+
 // Builds the container of the given kind, puts the particles, and calls
 // f(con, loop).  Returns false on an unknown kind.
 template <class F>
 bool with_container(int kind, const double *geom, const int *grid, const int *periodic, int n, const int *ids,
                     const double *xyzr, F f) {
+    std::vector<wall *> owned;
     if (kind == 0) {
         container con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
                       periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
+        add_walls(con, owned);
         for (int i = 0; i < n; i++) con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2]);
         c_loop_all vl(con);
         f(con, vl);
     } else if (kind == 1) {
         container_poly con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
                            periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
+        add_walls(con, owned);
         for (int i = 0; i < n; i++)
             con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2], xyzr[4 * i + 3]);
         c_loop_all vl(con);
@@ -103,6 +128,7 @@ bool with_container(int kind, const double *geom, const int *grid, const int *pe
     } else {
         return false;
     }
+    for (wall *w : owned) delete w;
     return true;
 }
 
@@ -118,6 +144,18 @@ bool ghost_of(con_t &con, voronoicell_neighbor &c, const double *g) {
 }  // namespace
 
 extern "C" {
+
+// The walls later calls add to kind 0/1 containers (n = 0: none).
+void ref_set_walls(int n, const int *type, const double *params, const int *id) {
+    g_walls.clear();
+    for (int i = 0; i < n; i++) {
+        wall_rec w;
+        w.type = type[i];
+        w.id = id[i];
+        for (int a = 0; a < 7; a++) w.p[a] = params[7 * i + a];
+        g_walls.push_back(w);
+    }
+}
 
 // The polytope of every cell in loop order, flattened into doubles:
 //   ok, nv, nf, surface_area, total_edge_distance, vertices (3 nv, particle-
@@ -255,33 +293,9 @@ int ref_compute_cells(int kind, const double *geom, const int *grid, const int *
                       long nb_cap, int *out_nb, long *out_nb_off) {
     rec_sink s{cap, 0, out_id, out_pos, out_vol, out_cen, out_mrs, out_nf, out_nv, out_ok,
                out_nb, nb_cap, 0, out_nb_off, 0};
-    if (kind == 0) {
-        container con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
-                      periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
-        for (int i = 0; i < n; i++) con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2]);
-        c_loop_all vl(con);
-        run_cells(con, vl, s);
-    } else if (kind == 1) {
-        container_poly con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2],
-                           periodic[0] != 0, periodic[1] != 0, periodic[2] != 0, 8);
-        for (int i = 0; i < n; i++)
-            con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2], xyzr[4 * i + 3]);
-        c_loop_all vl(con);
-        run_cells(con, vl, s);
-    } else if (kind == 2) {
-        container_periodic con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2], 8);
-        for (int i = 0; i < n; i++) con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2]);
-        c_loop_all_periodic vl(con);
-        run_cells(con, vl, s);
-    } else if (kind == 3) {
-        container_periodic_poly con(geom[0], geom[1], geom[2], geom[3], geom[4], geom[5], grid[0], grid[1], grid[2], 8);
-        for (int i = 0; i < n; i++)
-            con.put(ids[i], xyzr[4 * i], xyzr[4 * i + 1], xyzr[4 * i + 2], xyzr[4 * i + 3]);
-        c_loop_all_periodic vl(con);
-        run_cells(con, vl, s);
-    } else {
+    if (!with_container(kind, geom, grid, periodic, n, ids, xyzr,
+                        [&](auto &con, auto &vl) { run_cells(con, vl, s); }))
         return -2;
-    }
     return s.overflow ? -1 : s.n;
 }
 

@@ -12,7 +12,12 @@ def names():
     locate_*.npz point-location answers, see load_locate; ghost_*.npz ghost
     cells, see load_ghost)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
-                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_")))
+                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_", "wall_")))
+
+
+def wall_names():
+    """Fixtures of containers with walls (the same records; load() adds the walls)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "wall_*.npz")))
 
 
 def locate_names():
@@ -114,6 +119,9 @@ def load(name):
         "ids": z["in_ids"],
         "xyzr": z["in_xyzr"],
     }
+    if "wall_type" in z:
+        w["walls"] = [(int(t), [float(v) for v in p], int(i))
+                      for t, p, i in zip(z["wall_type"], z["wall_params"], z["wall_id"])]
     return w, z
 
 

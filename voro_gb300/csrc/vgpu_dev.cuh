@@ -46,6 +46,49 @@ static __device__ __noinline__ double4 plane64_from(const CellParams &P, double4
     return make_double4(x1, y1, z1, 0.5 * rs);
 }
 
+// FP64 plane (n, h: n.v <= h inside, v relative to the particle) of wall W for
+// the particle me, with the reference's arithmetic (cut_cell_base,
+// src/wall.cc:29-120; its nplane(x, y, z, rsq) is n = (x, y, z), h = rsq/2).
+// h = NaN: the reference adds no plane (a curved wall through the particle).
+static __device__ __forceinline__ double4 wall64(const WallSpec &W, double4 me) {
+    const double x = me.x, y = me.y, z = me.z;
+    if (W.type == VGPU_WALL_PLANE) {
+        const double dq = __dmul_rn(2.0, __dsub_rn(__dsub_rn(__dsub_rn(W.r, __dmul_rn(x, W.c[0])), __dmul_rn(y, W.c[1])),
+                                                   __dmul_rn(z, W.c[2])));
+        return make_double4(W.c[0], W.c[1], W.c[2], 0.5 * dq);
+    }
+    double xd = __dsub_rn(x, W.c[0]), yd = __dsub_rn(y, W.c[1]), zd = __dsub_rn(z, W.c[2]);
+    if (W.type == VGPU_WALL_SPHERE) {
+        double dq = __dadd_rn(__dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd)), __dmul_rn(zd, zd));
+        if (!(dq > 1e-5)) return make_double4(0, 0, 0, __longlong_as_double(0x7ff8000000000000ll));
+        dq = __dmul_rn(2.0, __dsub_rn(__dmul_rn(__dsqrt_rn(dq), W.r), dq));
+        return make_double4(xd, yd, zd, 0.5 * dq);
+    }
+    double pa = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(xd, W.a[0]), __dmul_rn(yd, W.a[1])), __dmul_rn(zd, W.a[2])), W.asi);
+    xd = __dsub_rn(xd, __dmul_rn(W.a[0], pa));
+    yd = __dsub_rn(yd, __dmul_rn(W.a[1], pa));
+    zd = __dsub_rn(zd, __dmul_rn(W.a[2], pa));
+    pa = __dadd_rn(__dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd)), __dmul_rn(zd, zd));
+    if (!(pa > 1e-5)) return make_double4(0, 0, 0, __longlong_as_double(0x7ff8000000000000ll));
+    if (W.type == VGPU_WALL_CYLINDER) {
+        pa = __dmul_rn(2.0, __dsub_rn(__dmul_rn(__dsqrt_rn(pa), W.r), pa));
+        return make_double4(xd, yd, zd, 0.5 * pa);
+    }
+    // cone
+    pa = __ddiv_rn(1.0, __dsqrt_rn(pa));
+    const double q = __dsqrt_rn(W.asi);
+    const double sq = __dmul_rn(W.sang, q), cp = __dmul_rn(W.cang, pa);
+    const double xf = __dadd_rn(__dmul_rn(-sq, W.a[0]), __dmul_rn(cp, xd));
+    const double yf = __dadd_rn(__dmul_rn(-sq, W.a[1]), __dmul_rn(cp, yd));
+    const double zf = __dadd_rn(__dmul_rn(-sq, W.a[2]), __dmul_rn(cp, zd));
+    pa = __dmul_rn(2.0, __dadd_rn(__dadd_rn(__dmul_rn(xf, __dsub_rn(W.c[0], x)), __dmul_rn(yf, __dsub_rn(W.c[1], y))),
+                                  __dmul_rn(zf, __dsub_rn(W.c[2], z))));
+    return make_double4(xf, yf, zf, 0.5 * pa);
+}
+
+// wall64 out of line, for code that runs once per cell
+static __device__ __noinline__ double4 wall64_call(const WallSpec &W, double4 me) { return wall64(W, me); }
+
 // FP64 plane of an initial face (f = 2*axis + side) of the particle's cell
 static __device__ __forceinline__ double4 face64(const CellParams &P, double4 me, int f) {
     const int ax = f >> 1;
@@ -56,6 +99,12 @@ static __device__ __forceinline__ double4 face64(const CellParams &P, double4 me
     else h = hiside ? __dsub_rn(P.g.hi[ax], xa) : -__dsub_rn(P.g.lo[ax], xa);
     const double n = hiside ? 1.0 : -1.0;
     return make_double4(ax == 0 ? n : 0.0, ax == 1 ? n : 0.0, ax == 2 ? n : 0.0, h);
+}
+
+// FP64 plane of a plane slot without a source particle: initial face f < 6,
+// or wall f - 6
+static __device__ __forceinline__ double4 initial64(const CellParams &P, double4 me, int f) {
+    return f < 6 ? face64(P, me, f) : wall64(P.walls[f - 6], me);
 }
 
 // Vertex of three FP64 planes by Cramer's rule; kn = sum over rows of

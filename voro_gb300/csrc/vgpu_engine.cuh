@@ -261,7 +261,7 @@ template <int MODE, int K>
 __device__ __forceinline__ double4 plane64_slot(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int p) {
     const int src = S.psrc[p];
     if (src >= 0) return plane64_from(P, me, src, S.pshift[p]);
-    return face64(P, me, S.pshift[p]);
+    return initial64(P, me, S.pshift[p]);
 }
 
 // FP64 re-test of the vertices whose FP32 test against candidate cb was
@@ -274,7 +274,8 @@ __device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpSha
     unsigned outbits = 0;
     bool anym = false;
     if (uncbits) {
-        const double4 Q = plane64_from(P, me, S.u.c.cj[cb], S.u.c.cs[cb]);
+        const int cj = S.u.c.cj[cb];   // (a wall: -1, with its face index in cs)
+        const double4 Q = cj >= 0 ? plane64_from(P, me, cj, S.u.c.cs[cb]) : initial64(P, me, S.u.c.cs[cb]);
         for (int s = 0; s < K; s++) {
             if (!((uncbits >> s) & 1u)) continue;
             const unsigned t = s == 0 ? tri0 : (s == 1 ? tri1 : (s == 2 ? tri2 : tri3));
@@ -444,6 +445,44 @@ struct Engine {
         __syncwarp();
         if (lane < 8) compute_vertex(0);
         update_radius();
+        apply_walls();
+    }
+
+    // ---- the walls cut the initial cell in order (apply_walls,
+    //      src/container.hh:86-89): lane w builds wall w's plane and adds it
+    //      to the candidate buffer with distance 0 as source -1, face index
+    //      6 + w; the search's first flush, which sorts them ahead of every
+    //      particle candidate and in wall order, cuts with them through the
+    //      one copy of the cutting code.  A wall that cuts the whole cell
+    //      deletes it (compute_cell false).
+    __device__ void apply_walls() {
+        if (P.nwalls == 0) return;
+        bool valid = false;
+        float4 cd = make_float4(0, 0, 0, 0), ce = make_float4(0, 0, 0, 0);
+        double4 q = make_double4(0, 0, 0, 0);
+        if (lane < P.nwalls) {
+            q = wall64_call(P.walls[lane], C.me64);
+            valid = !isnan(q.w);   // NaN: no plane for this particle
+            // the FP32 plane and its rounding: each component and h within
+            // one unit in the last place
+            const float nx = (float)q.x, ny = (float)q.y, nz = (float)q.z, h = (float)q.w;
+            const float an = fabsf(nx) + fabsf(ny) + fabsf(nz);
+            cd = make_float4(nx, ny, nz, h);
+            ce = make_float4(2.0f * kU32 * an, 2.0f * kU32 * fabsf(h),
+                             sqrtf(nx * nx + ny * ny + nz * nz) * (1.0f + 8.0f * kU32) + 2.0f * kU32 * an, 0.0f);
+        }
+        const unsigned bal = __ballot_sync(kFull, valid);
+        if (valid) {
+            const int slot = __popc(bal & ((1u << lane) - 1u));
+            S.u.c.ck[slot] = (float_key(0.0f) & ~63u) | (unsigned)slot;
+            S.u.c.cj[slot] = -1;
+            S.u.c.cs[slot] = 6 + lane;
+            S.u.c.cpid[slot] = P.walls[lane].id;
+            S.u.c.cd[slot] = cd;
+            S.u.c.ce[slot] = ce;
+            if (MODE == VGPU_FP64) S.u.c.cd64[slot] = q;
+        }
+        C.ncand = __popc(bal);
     }
 
     // ---- plane slot allocation with recycling of dead planes

@@ -104,7 +104,7 @@ __device__ __forceinline__ double pow2d(int k) { return __hiloint2double((1023 +
 __device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
     const int src = F.psrc[p];
     if (src >= 0) return plane64_from(P, me, src, F.pshift[p]);
-    return face64(P, me, F.pshift[p]);
+    return initial64(P, me, F.pshift[p]);
 }
 
 // The plane of candidate j (image code) of the cell of particle k as float
@@ -294,7 +294,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
             if (F.psrc[q] >= 0) {
                 pl = plane_ff(P, bk, mh, ml, F.psrc[q], F.pshift[q]);
             } else {   // a wall of the container (FP64, rare)
-                const double4 w = face64(P, me, F.pshift[q]);
+                const double4 w = initial64(P, me, F.pshift[q]);
                 pl = {ff_from_double(w.x), ff_from_double(w.y), ff_from_double(w.z), ff_from_double(w.w)};
             }
             F.plh[q] = make_float4(pl.x.h, pl.y.h, pl.z.h, pl.w.h);

@@ -86,6 +86,19 @@ struct Counters {
     unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
 };
 
+// A wall (src/wall.hh:25-130): the parameters as the reference's classes hold
+// them, including its precomputed asi = 1/|a|^2 and the cone's tan, sin and
+// cos of the angle.  Type: VGPU_WALL_* (include/vorogpu.h).
+struct WallSpec {
+    int type;
+    int id;                 // neighbour ID of the wall's faces
+    double c[3];            // centre / normal (plane: xc, yc, zc)
+    double a[3];            // axis (cylinder, cone)
+    double r;               // radius (sphere, cylinder), ac (plane)
+    double asi, gra, sang, cang;
+};
+constexpr int kMaxWalls = 32;   // one lane each when they are applied
+
 struct CellParams {
     Geometry g;
     EngineArrays a;
@@ -117,8 +130,14 @@ struct CellParams {
     unsigned long long poly_cap;    // doubles
     unsigned long long *poly_used;  // bump allocator (doubles)
     long long *poly_off;            // per loop-order cell: offset, -1 none, -2 store full
+    // Walls cut every cell after its initial box, in order (apply_walls,
+    // src/container.hh:86-89); as planes their slots have source -1 and
+    // shift 6 + wall index.
+    const WallSpec *walls;
+    int nwalls;
 };
 constexpr unsigned long long kNoRecord = ~0ull;
+
 constexpr int kRecHeader = 5;
 
 // Many containers in one persistent launch: cells are numbered globally,

@@ -36,6 +36,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <initializer_list>
 #include <vector>
 
 #include "vorogpu.h"
@@ -81,6 +82,43 @@ inline void check(int rc, const char *what) {
 }  // namespace gpu_detail
 
 class container_gpu_base;
+
+// Walls (src/wall.hh:25-130): the reference's constructors; the container
+// hands their parameters to the engine (vgpu_add_wall), which cuts every
+// cell with them as the reference's cut_cell does.
+class wall {
+  public:
+    virtual ~wall() {}
+    int type_ = 0, w_id_ = -99;
+    double p_[7] = {0, 0, 0, 0, 0, 0, 0};
+
+  protected:
+    wall(int type, int id, std::initializer_list<double> p) : type_(type), w_id_(id) {
+        int i = 0;
+        for (double v : p) p_[i++] = v;
+    }
+};
+class wall_sphere : public wall {
+  public:
+    wall_sphere(double xc_, double yc_, double zc_, double rc_, int w_id_ = -99)
+        : wall(VGPU_WALL_SPHERE, w_id_, {xc_, yc_, zc_, rc_}) {}
+};
+class wall_plane : public wall {
+  public:
+    wall_plane(double xc_, double yc_, double zc_, double ac_, int w_id_ = -99)
+        : wall(VGPU_WALL_PLANE, w_id_, {xc_, yc_, zc_, ac_}) {}
+};
+class wall_cylinder : public wall {
+  public:
+    wall_cylinder(double xc_, double yc_, double zc_, double xa_, double ya_, double za_, double rc_,
+                  int w_id_ = -99)
+        : wall(VGPU_WALL_CYLINDER, w_id_, {xc_, yc_, zc_, xa_, ya_, za_, rc_}) {}
+};
+class wall_cone : public wall {
+  public:
+    wall_cone(double xc_, double yc_, double zc_, double xa_, double ya_, double za_, double ang, int w_id_ = -99)
+        : wall(VGPU_WALL_CONE, w_id_, {xc_, yc_, zc_, xa_, ya_, za_, ang}) {}
+};
 
 // Per-cell results of one compute_cell call (voronoicell, src/cell.hh:93-350).
 class voronoicell {
@@ -318,6 +356,18 @@ class container_gpu_base {
         double s = 0;
         gpu_detail::check(vgpu_sum_cell_volumes(h_, &s), "sum_cell_volumes");
         return s;
+    }
+
+    // wall_list::add_wall (src/container.hh:62-69) and point_inside_walls (75-78)
+    void add_wall(wall &w) {
+        gpu_detail::check(vgpu_add_wall(h_, w.type_, w.p_, w.w_id_), "add_wall");
+        dirty_ = true;
+    }
+    void add_wall(wall *w) { add_wall(*w); }
+    bool point_inside_walls(double x, double y, double z) {
+        int in = 0;
+        gpu_detail::check(vgpu_point_inside_walls(h_, x, y, z, &in), "point_inside_walls");
+        return in != 0;
     }
 
     // container::find_voronoi_cell (src/container.cc:237-301,

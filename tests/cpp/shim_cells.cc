@@ -3,9 +3,12 @@
 //
 // usage: shim_cells <input> <records-out> [<print_custom format> <custom-out>
 //                   [<queries> <queries-out>]]
-// input: "kind ax bx ay by az bz nx ny nz xp yp zp n" then n lines "id x y z r"
+// input: "kind ax bx ay by az bz nx ny nz xp yp zp n", optionally "walls k" and k
+// lines "type id p0 .. p6" (0 sphere, 1 plane, 2 cylinder, 3 cone), then n
+// lines "id x y z r"
 // queries: lines "x y z r": find_voronoi_cell and compute_ghost_cell of each
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "voro_gb300.hh"
@@ -70,6 +73,30 @@ static int queries(C &con, const char *qpath, const char *opath) {
     return 0;
 }
 
+// the optional wall lines, added with the reference's wall classes
+template <class C>
+static void read_walls(C &con, FILE *in, std::vector<wall *> &owned) {
+    const long at = ftell(in);
+    char tag[16];
+    int k = 0;
+    if (fscanf(in, "%15s", tag) != 1 || strcmp(tag, "walls") != 0 || fscanf(in, "%d", &k) != 1) {
+        fseek(in, at, SEEK_SET);
+        return;
+    }
+    for (int i = 0; i < k; i++) {
+        int t, id;
+        double p[7];
+        if (fscanf(in, "%d %d %lg %lg %lg %lg %lg %lg %lg", &t, &id, p, p + 1, p + 2, p + 3, p + 4, p + 5, p + 6) != 9)
+            return;
+        wall *w = t == 0   ? (wall *)new wall_sphere(p[0], p[1], p[2], p[3], id)
+                  : t == 1 ? (wall *)new wall_plane(p[0], p[1], p[2], p[3], id)
+                  : t == 2 ? (wall *)new wall_cylinder(p[0], p[1], p[2], p[3], p[4], p[5], p[6], id)
+                           : (wall *)new wall_cone(p[0], p[1], p[2], p[3], p[4], p[5], p[6], id);
+        owned.push_back(w);
+        con.add_wall(w);
+    }
+}
+
 template <class C>
 static int run(C &con, FILE *in, int n, int argc, char **argv) {
     for (int k = 0; k < n; k++) {
@@ -97,11 +124,14 @@ int main(int argc, char **argv) {
                &ny, &nz, &xp, &yp, &zp, &n) != 14)
         return 1;
     int rc = 1;
+    std::vector<wall *> owned;
     if (kind == 0) {
         container con(g[0], g[1], g[2], g[3], g[4], g[5], nx, ny, nz, xp, yp, zp, 8);
+        read_walls(con, in, owned);
         rc = run(con, in, n, argc, argv);
     } else if (kind == 1) {
         container_poly con(g[0], g[1], g[2], g[3], g[4], g[5], nx, ny, nz, xp, yp, zp, 8);
+        read_walls(con, in, owned);
         rc = run(con, in, n, argc, argv);
     } else if (kind == 2) {
         container_periodic con(g[0], g[1], g[2], g[3], g[4], g[5], nx, ny, nz, 8);
@@ -110,6 +140,7 @@ int main(int argc, char **argv) {
         container_periodic_poly con(g[0], g[1], g[2], g[3], g[4], g[5], nx, ny, nz, 8);
         rc = run(con, in, n, argc, argv);
     }
+    for (wall *w : owned) delete w;
     fclose(in);
     return rc;
 }

@@ -35,6 +35,12 @@ def _write_input(path, w):
     with open(path, "w") as f:
         f.write(f"{w['kind']} " + " ".join(repr(float(v)) for v in g) + " " + " ".join(str(v) for v in gr) + " " +
                 " ".join(str(int(p)) for p in per) + f" {len(w['ids'])}\n")
+        walls = w.get("walls") or []
+        if walls:
+            f.write(f"walls {len(walls)}\n")
+            for t, p, wid in walls:
+                pp = list(p) + [0.0] * (7 - len(p))
+                f.write(f"{t} {wid} " + " ".join(repr(float(v)) for v in pp) + "\n")
         for i, (x, y, z, r) in zip(w["ids"], w["xyzr"]):
             f.write(f"{int(i)} {float(x)!r} {float(y)!r} {float(z)!r} {float(r)!r}\n")
 
@@ -145,6 +151,22 @@ def test_shim_polytope_fields(gpu, tmp_path, name):
         else:
             errs = G.compare_custom_text(got, ref)
         assert not errs, "\n".join(errs[:10])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", G.wall_names())
+def test_shim_walls_match_reference(gpu, tmp_path, name):
+    """Walls added through the header's wall classes reproduce the reference's
+    records for containers with walls."""
+    exe = _compile(tmp_path)
+    w, z = G.load(name)
+    inp = tmp_path / "in.txt"
+    _write_input(inp, w)
+    out = tmp_path / "out.txt"
+    r = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    errs = G.compare_cells(_Parsed(out), z, 1e-10, 1e-10, label=f"shim/{name}")
+    assert not errs, "\n".join(errs)
 
 
 @pytest.mark.gpu

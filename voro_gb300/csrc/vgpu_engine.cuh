@@ -155,6 +155,7 @@ struct CellCtx {
     float cutoff2;    // squared distance bound for candidates / blocks
     float ri2;        // particle radius squared (poly)
     bool deleted, overflow, marginal, repaired;
+    bool needs_fp64;  // this lane's vertex solve was ill-conditioned (first pass: the cell is rerun)
     int fail_reason;  // why overflow was set (VGPU_FAIL_*)
     unsigned long long freeplanes;
     int ncand;
@@ -346,6 +347,12 @@ __device__ __noinline__ VertexF32 vertex_f64_fallback(const CellParams &P, const
 // ------------------------------------------------------------------ the engine
 template <int MODE, int K>
 struct Engine {
+    // The mixed engine's first pass (64 slots) carries no FP64 code: a cell
+    // that needs an FP64 repair or vertex goes, like one that outgrows the
+    // slots, to the 128-slot rerun, which has both.  Without the two FP64
+    // calls the kernel needs about 110 registers instead of 168 (4 CTAs per
+    // SM instead of 3).
+    static constexpr bool kLean = MODE == VGPU_MIXED && K == 2;
     const CellParams &P;
     WarpShared<MODE, K> &S;
     const int *offsets;   // shared copy of the offset table
@@ -398,7 +405,10 @@ struct Engine {
             return;
         }
         VertexF32 o = solve_vertex_f32(S.pl, S.pe, t);
-        if (!(o.e <= kVertexTrust * o.a)) o = vertex_f64_fallback<MODE, K>(P, S, C.me64, t);
+        if (!(o.e <= kVertexTrust * o.a)) {
+            if (kLean) C.needs_fp64 = true;   // the first pass hands the cell to the rerun
+            else o = vertex_f64_fallback<MODE, K>(P, S, C.me64, t);
+        }
         V.x[s] = o.x;
         V.y[s] = o.y;
         V.z[s] = o.z;
@@ -418,7 +428,7 @@ struct Engine {
         C.bj = (b / P.g.gn[0]) % P.g.gn[1];
         C.bk = b / (P.g.gn[0] * P.g.gn[1]);
         C.ri2 = C.me32.w * C.me32.w;
-        C.deleted = C.overflow = C.marginal = C.repaired = false;
+        C.deleted = C.overflow = C.marginal = C.repaired = C.needs_fp64 = false;
         C.fail_reason = 0;
         C.freeplanes = ~0x3full;
         C.ncand = 0;
@@ -444,6 +454,11 @@ struct Engine {
         }
         __syncwarp();
         if (lane < 8) compute_vertex(0);
+        if (kLean && __any_sync(kFull, C.needs_fp64)) {
+            C.overflow = true;
+            C.fail_reason = 0;
+            return;
+        }
         update_radius();
         apply_walls();
     }
@@ -535,6 +550,11 @@ struct Engine {
             }
             const unsigned ub = __ballot_sync(kFull, uncbits != 0);
             if (ub) {
+                if (kLean) {   // the first pass hands the cell to the rerun, which repairs in FP64
+                    C.overflow = true;
+                    C.fail_reason = 0;
+                    return;
+                }
                 C.repaired = true;
                 C.repairs += __popc(ub);
                 bool m = false;
@@ -679,6 +699,11 @@ struct Engine {
             }
         }
         __syncwarp();
+        if (kLean && __any_sync(kFull, C.needs_fp64)) {
+            C.overflow = true;
+            C.fail_reason = 0;
+            return;
+        }
         // Phase C: link the new vertices around the new face; clear freed slots
         bool bad = false;
 #pragma unroll
@@ -1032,12 +1057,14 @@ struct Engine {
     }
 };
 
-// CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot) engine;
-// it fixes the register budget (65536 / (128 * blocks)).  Measured on the 4M
-// periodic box: 3 (168 registers, few spills, 12 warps per SM) clips in 124 ms,
-// 4 (128 registers, spills) in 154 ms, 2 in 160 ms.
+// CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot, FP64-free)
+// engine; it fixes the register budget (65536 / (128 * blocks)).  Measured on
+// the 4M periodic box (both clipping passes): 6 (80 registers, 24 warps per
+// SM) 82.2 ms, 5 (96) 83.5 ms, 7 (72) 84.2 ms, 4 (103, no spills) 88.9 ms,
+// 3 (118) 86.8 ms.  (With the FP64 repair and vertex calls in this engine it
+// needed 224 registers: 3 CTAs at 168 registers, 102 ms.)
 #ifndef VGPU_MIN_BLOCKS
-#define VGPU_MIN_BLOCKS 3
+#define VGPU_MIN_BLOCKS 6
 #endif
 // Largest CTA the clipping kernels are built for (threads); the default
 // launch uses 4 warps.

@@ -175,13 +175,13 @@ struct vgpu_container {
     DevBuf ids_in, xyzr_in;
     // work buffers
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
-    DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, counters, counters2;
+    DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, ovf_list2, counters, counters2;
     // results
     DevBuf rec_off, poly, poly_off;
     DevBuf loc_q, loc_found, loc_pid, loc_r;   // point-location queries and answers
     // ghost cells: engine arrays (the particles, then the ghosts), their
     // record offsets, work lists and results
-    DevBuf gh_p64, gh_lffh, gh_lffl, gh_pid, gh_gblock, gh_outpos, gh_rec_off, gh_q, gh_keep, gh_list, gh_ovf,
+    DevBuf gh_p64, gh_lffh, gh_lffl, gh_pid, gh_gblock, gh_outpos, gh_rec_off, gh_q, gh_keep, gh_list, gh_ovf, gh_ovf2,
         gh_cnt, gh_vol, gh_cen, gh_nf, gh_nv, gh_mr2, gh_flags, gh_nb, gh_nb_ovf, gh_nb_off, gh_nb_out, gh_poly,
         gh_poly_off;
     std::vector<WallSpec> walls;    // walls, in the order added
@@ -344,11 +344,11 @@ int vgpu_container_destroy(vgpu_container *h) {
     DevBuf *bufs[] = {&h->ids_in, &h->xyzr_in, &h->rem, &h->ukey, &h->gkey, &h->idx, &h->idx2, &h->keys_alt,
                       &h->vals_alt, &h->hist, &h->scan_tmp, &h->outpos_in, &h->kept, &h->p64,
                       &h->lffh, &h->lffl, &h->pid,
-                      &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->counters, &h->counters2,
+                      &h->outpos, &h->gblock, &h->bstart, &h->offsets, &h->ovf_list, &h->ovf_list2, &h->counters, &h->counters2,
                       &h->r_vol, &h->r_cen, &h->r_nf, &h->r_nv, &h->r_mr2, &h->r_flags, &h->r_nb, &h->r_nb_ovf, &h->r_ids,
                       &h->loc_q, &h->loc_found, &h->loc_pid, &h->loc_r, &h->gh_p64, &h->gh_lffh, &h->gh_lffl,
                       &h->gh_pid, &h->gh_gblock, &h->gh_outpos, &h->gh_rec_off, &h->gh_q, &h->gh_keep, &h->gh_list,
-                      &h->gh_ovf, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
+                      &h->gh_ovf, &h->gh_ovf2, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
                       &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
                       &h->walls_dev,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
@@ -570,7 +570,7 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(h->outpos_in.ensure(nn * 4));
     VG_CUDA(h->kept.ensure(64));
     VG_CUDA(h->counters.ensure(sizeof(Counters)));
-    VG_CUDA(h->counters2.ensure(sizeof(Counters)));
+    VG_CUDA(h->counters2.ensure(2 * sizeof(Counters)));
 
     h->launches0 = launch_count();
     cudaEventRecord(h->ev[0], s);
@@ -668,7 +668,7 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(h->offsets.ensure(ot.codes.size() * 4));
     VG_CUDA(cudaMemcpyAsync(h->offsets.p, ot.codes.data(), ot.codes.size() * 4, cudaMemcpyHostToDevice, s));
     VG_CUDA(cudaMemsetAsync(h->counters.p, 0, sizeof(Counters), s));
-    VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, sizeof(Counters), s));
+    VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, 2 * sizeof(Counters), s));
     h->nkept = nkept;
     h->binned = true;
     fill_cell_params(h, cp);
@@ -735,7 +735,7 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
     VG_CUDA(h->rem.ensure(nn * 32));
     VG_CUDA(h->outpos_in.ensure(nn * 4));
     VG_CUDA(h->counters.ensure(sizeof(Counters)));
-    VG_CUDA(h->counters2.ensure(sizeof(Counters)));
+    VG_CUDA(h->counters2.ensure(2 * sizeof(Counters)));
     VG_CUDA(h->r_vol.ensure(nn * 8));
     VG_CUDA(h->r_cen.ensure(nn * 24));
     VG_CUDA(h->r_nf.ensure(nn * 4));
@@ -856,21 +856,79 @@ int setup_member_records(vgpu_container *h, CellParams &cp, Counters *cnt, cudaS
 }
 
 // Counters of the last compute into the handle's stats; marks it computed.
-int finish_compute(vgpu_container *h, const Counters &c1, const Counters &c2, float cell_ms) {
+// The clipping passes over cp's cells (cp.cnt, cp.overflow_list: the first
+// pass's counters and hand-on list).  MIXED: the FP64-free first pass, the
+// full 64-slot engine on the cells it handed on (counters cnt1, hand-on
+// list list2), then the 128-slot engine on what that handed on (cnt2).
+// FP64: 64 slots, then 128 slots (cnt2).  sum: the passes' counters added,
+// overflow = cells the first pass handed on, failed = cells the last pass
+// run could not complete.
+int clip_passes(cudaStream_t s, int sms, int warps, int mode, const CellParams &cp, Counters *cnt1, Counters *cnt2,
+                int *list2, Counters &sum) {
+    Counters c[3];
+    memset(c, 0, sizeof(c));
+    VG_CUDA(launch_cells(cp, mode, 0, sms, s, warps));
+    VG_CUDA(cudaMemcpyAsync(&c[0], cp.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaStreamSynchronize(s));
+    unsigned long long pending = c[0].overflow;
+    const int *list = cp.overflow_list;
+    if (pending > 0 && mode == VGPU_MIXED) {
+        CellParams p1 = cp;
+        p1.cnt = cnt1;
+        p1.ncells = (int)pending;
+        p1.cell_list = list;
+        p1.overflow_list = list2;
+        VG_CUDA(launch_cells(p1, mode, 1, sms, s, warps));
+        VG_CUDA(cudaMemcpyAsync(&c[1], cnt1, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        pending = c[1].overflow;
+        list = list2;
+    }
+    unsigned long long last_failed = 0;
+    if (pending > 0) {
+        CellParams p2 = cp;
+        p2.cnt = cnt2;
+        p2.ncells = (int)pending;
+        p2.cell_list = list;
+        p2.overflow_list = nullptr;
+        VG_CUDA(launch_cells(p2, mode, 2, sms, s, warps));
+        VG_CUDA(cudaMemcpyAsync(&c[2], cnt2, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        last_failed = c[2].overflow;
+    }
+    sum = c[0];
+    for (int k = 1; k < 3; k++) {
+        sum.side_tests += c[k].side_tests;
+        sum.fp64_repairs += c[k].fp64_repairs;
+        sum.planes_tested += c[k].planes_tested;
+        sum.planes_cut += c[k].planes_cut;
+        sum.deleted += c[k].deleted;
+        sum.marginal += c[k].marginal;
+        sum.failed += c[k].failed;
+        for (int i = 0; i < 8; i++) sum.phase_cycles[i] += c[k].phase_cycles[i];
+    }
+    sum.overflow = c[0].overflow;
+    sum.failed += last_failed;
+    return VGPU_OK;
+}
+
+// c: the compute's counters summed over its clipping passes, overflow = the
+// cells the first pass handed on, failed = the cells no pass completed.
+int finish_compute(vgpu_container *h, const Counters &c, float cell_ms) {
     float bin_ms = 0, step_ms = 0;
     cudaEventElapsedTime(&bin_ms, h->ev[0], h->ev[1]);
     cudaEventElapsedTime(&step_ms, h->ev[0], h->ev[3]);
     h->ncells = h->nkept;
     h->stats.cells = h->nkept;
-    h->stats.deleted = (int64_t)(c1.deleted + c2.deleted);
-    h->stats.marginal_cells = (int64_t)(c1.marginal + c2.marginal);
-    h->stats.side_tests = (int64_t)(c1.side_tests + c2.side_tests);
-    h->stats.fp64_repairs = (int64_t)(c1.fp64_repairs + c2.fp64_repairs);
-    h->stats.planes_tested = (int64_t)(c1.planes_tested + c2.planes_tested);
-    h->stats.planes_cut = (int64_t)(c1.planes_cut + c2.planes_cut);
-    h->stats.overflow_reruns = (int64_t)c1.overflow;
-    h->stats.failed_cells = (int64_t)(c2.overflow + c1.failed + c1.nb_failed);
-    for (int i = 0; i < 8; i++) h->phase[i] = (double)(c1.phase_cycles[i] + c2.phase_cycles[i]);
+    h->stats.deleted = (int64_t)c.deleted;
+    h->stats.marginal_cells = (int64_t)c.marginal;
+    h->stats.side_tests = (int64_t)c.side_tests;
+    h->stats.fp64_repairs = (int64_t)c.fp64_repairs;
+    h->stats.planes_tested = (int64_t)c.planes_tested;
+    h->stats.planes_cut = (int64_t)c.planes_cut;
+    h->stats.overflow_reruns = (int64_t)c.overflow;
+    h->stats.failed_cells = (int64_t)(c.failed + c.nb_failed);
+    for (int i = 0; i < 8; i++) h->phase[i] = (double)c.phase_cycles[i];
     h->stats.kernel_ms = cell_ms;
     h->stats.bin_ms = bin_ms;
     h->stats.step_ms = step_ms;
@@ -895,24 +953,14 @@ int vgpu_compute(vgpu_container *h, int mode) {
     std::lock_guard<std::mutex> hold(store.m);
     rc = setup_records(h, mode, cp, h->counters.as<Counters>(), h->stream, store.buf);
     if (rc != VGPU_OK) return rc;
-    // clipping (64-vertex engine, then the 128-vertex one for the cells that
-    // overflowed), then the finish kernel over every record
+    // clipping (the passes of clip_passes), then the finish kernel over every record
     cudaEventRecord(h->ev[2], s);
-    VG_CUDA(launch_cells(cp, mode, 0, h->sms, s, h->warps_per_cta));
+    VG_CUDA(h->ovf_list2.ensure((size_t)std::max(h->nkept, 1) * 4));
+    VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, 2 * sizeof(Counters), s));
     Counters c1;
-    VG_CUDA(cudaMemcpyAsync(&c1, h->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-    VG_CUDA(cudaStreamSynchronize(s));
-    Counters c2;
-    memset(&c2, 0, sizeof(c2));
-    if (c1.overflow > 0) {
-        CellParams cp2 = cp;
-        cp2.cnt = h->counters2.as<Counters>();
-        cp2.ncells = (int)c1.overflow;
-        cp2.cell_list = h->ovf_list.as<int>();
-        cp2.overflow_list = nullptr;
-        VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s, h->warps_per_cta));
-        VG_CUDA(cudaMemcpyAsync(&c2, h->counters2.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-    }
+    rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, h->counters2.as<Counters>(),
+                     h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1);
+    if (rc != VGPU_OK) return rc;
     cudaEventRecord(h->ev[4], s);
     VG_CUDA(launch_finish(cp, mode, h->sms, s));
     cudaEventRecord(h->ev[3], s);
@@ -926,7 +974,7 @@ int vgpu_compute(vgpu_container *h, int mode) {
     cudaEventElapsedTime(&cell_ms, h->ev[2], h->ev[3]);
     cudaEventElapsedTime(&clip_ms, h->ev[2], h->ev[4]);
     cudaEventElapsedTime(&fin_ms, h->ev[4], h->ev[3]);
-    rc = finish_compute(h, c1, c2, cell_ms);
+    rc = finish_compute(h, c1, cell_ms);
     h->stats.clip_ms = clip_ms;
     h->stats.finish_ms = fin_ms;
     return rc;
@@ -1144,7 +1192,8 @@ int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const doubl
     VG_CUDA(h->gh_keep.ensure(ng * 4));
     VG_CUDA(h->gh_list.ensure(ng * 4));
     VG_CUDA(h->gh_ovf.ensure(ng * 4));
-    VG_CUDA(h->gh_cnt.ensure(2 * sizeof(Counters)));
+    VG_CUDA(h->gh_ovf2.ensure(ng * 4));
+    VG_CUDA(h->gh_cnt.ensure(3 * sizeof(Counters)));
     VG_CUDA(h->gh_vol.ensure(ng * 8));
     VG_CUDA(h->gh_cen.ensure(ng * 24));
     VG_CUDA(h->gh_nf.ensure(ng * 4));
@@ -1184,7 +1233,7 @@ int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const doubl
     VG_CUDA(cudaMemsetAsync(h->gh_mr2.p, 0, ng * 8, s));
     VG_CUDA(cudaMemsetAsync(h->gh_flags.p, 0, ng * 4, s));
     VG_CUDA(cudaMemsetAsync(h->gh_rec_off.as<char>() + nk * 8, 0xff, ng * 8, s));
-    VG_CUDA(cudaMemsetAsync(h->gh_cnt.p, 0, 2 * sizeof(Counters), s));
+    VG_CUDA(cudaMemsetAsync(h->gh_cnt.p, 0, 3 * sizeof(Counters), s));
     if (nl > 0) VG_CUDA(cudaMemcpyAsync(h->gh_list.p, list.data(), (size_t)nl * 4, cudaMemcpyHostToDevice, s));
     // the engine over the ghosts only, against the particles
     Counters *gc = h->gh_cnt.as<Counters>();
@@ -1231,26 +1280,15 @@ int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const doubl
         cp.poly_used = &gc->poly_used;
         cp.poly_off = h->gh_poly_off.as<long long>();
     }
-    Counters c1, c2, c3;
-    memset(&c2, 0, sizeof(c2));
+    Counters c1, c3;
     if (nl > 0) {
-        VG_CUDA(launch_cells(cp, mode, 0, h->sms, s, h->warps_per_cta));
-        VG_CUDA(cudaMemcpyAsync(&c1, gc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-        VG_CUDA(cudaStreamSynchronize(s));
-        if (c1.overflow > 0) {
-            CellParams cp2 = cp;
-            cp2.cnt = gc + 1;
-            cp2.ncells = (int)c1.overflow;
-            cp2.cell_list = h->gh_ovf.as<int>();
-            cp2.overflow_list = nullptr;
-            VG_CUDA(launch_cells(cp2, mode, 1, h->sms, s, h->warps_per_cta));
-            VG_CUDA(cudaMemcpyAsync(&c2, gc + 1, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-        }
+        int rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, gc + 1, gc + 2, h->gh_ovf2.as<int>(), c1);
+        if (rc != VGPU_OK) return rc;
         VG_CUDA(launch_finish(cp, mode, h->sms, s));
         VG_CUDA(cudaMemcpyAsync(&c3, gc, sizeof(Counters), cudaMemcpyDeviceToHost, s));
         VG_CUDA(cudaStreamSynchronize(s));
         h->ghost_poly_used = c3.poly_used;
-        const unsigned long long failed = c2.overflow + c1.failed + c3.nb_failed;
+        const unsigned long long failed = c1.failed + c3.nb_failed;
         h->ghost_n = n;
         if (failed > 0) return fail(VGPU_ERR_CAPACITY, "%llu ghost cells exceeded the engine capacity", failed);
     }
@@ -1357,7 +1395,7 @@ struct vgpu_batch {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4];
-    DevBuf cps, starts, counters, work, ovf_list, jobs, bin_res, offsets, rec;
+    DevBuf cps, starts, counters, work, ovf_list, ovf_list2, jobs, bin_res, offsets, rec;
     bool offsets_ready = false;
     int64_t record_bytes = 0;   // record store budget (0: kBatchRecordBytes)
     int waves = 0;              // record-store waves of the last compute
@@ -1393,7 +1431,8 @@ int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
 int vgpu_batch_destroy(vgpu_batch *b) {
     if (!b) return VGPU_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
-    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list, &b->jobs, &b->bin_res, &b->offsets,
+    DevBuf *bufs[] = {&b->cps, &b->starts, &b->counters, &b->work, &b->ovf_list, &b->ovf_list2, &b->jobs, &b->bin_res,
+                      &b->offsets,
                       &b->rec};
     for (DevBuf *d : bufs) d->release();
     for (int i = 0; i < 4; i++) cudaEventDestroy(b->ev[i]);
@@ -1495,7 +1534,9 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     VG_CUDA(b->starts.ensure((size_t)(nc + 1) * 8));
     VG_CUDA(b->work.ensure(64));
     VG_CUDA(b->ovf_list.ensure((size_t)std::max<long long>(total, 1) * 8));
-    unsigned long long *wk = b->work.as<unsigned long long>();   // work, overflows, rerun work, records used
+    VG_CUDA(b->ovf_list2.ensure((size_t)std::max<long long>(total, 1) * 8));
+    // work, hand-ons, second pass work, records used, third pass work, second hand-ons
+    unsigned long long *wk = b->work.as<unsigned long long>();
     for (int i = 0; i < nc; i++) {
         cps[i].rec = b->rec.as<unsigned>();
         cps[i].rec_cap = cap;
@@ -1521,17 +1562,32 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         bp.ncells = std::min<long long>(wave, total - w0);
         VG_CUDA(cudaMemsetAsync(b->work.p, 0, 64, s));
         cudaEventRecord(b->ev[0], s);
+        // the passes of clip_passes: first pass, (MIXED) the full 64-slot
+        // engine on the cells it handed on, the 128-slot engine on the rest
         VG_CUDA(launch_cells_batch(bp, mode, 0, b->sms, s));
         unsigned long long novf = 0;
         VG_CUDA(cudaMemcpyAsync(&novf, wk + 1, 8, cudaMemcpyDeviceToHost, s));
         VG_CUDA(cudaStreamSynchronize(s));
+        const long long *pending = b->ovf_list.as<long long>();
+        if (novf > 0 && mode == VGPU_MIXED) {
+            BatchParams bp1 = bp;
+            bp1.ncells = (long long)novf;
+            bp1.cell_list = pending;
+            bp1.overflow_list = b->ovf_list2.as<long long>();
+            bp1.overflow_count = wk + 5;
+            bp1.work = wk + 2;
+            VG_CUDA(launch_cells_batch(bp1, mode, 1, b->sms, s));
+            VG_CUDA(cudaMemcpyAsync(&novf, wk + 5, 8, cudaMemcpyDeviceToHost, s));
+            VG_CUDA(cudaStreamSynchronize(s));
+            pending = b->ovf_list2.as<long long>();
+        }
         if (novf > 0) {
             BatchParams bp2 = bp;
             bp2.ncells = (long long)novf;
-            bp2.cell_list = b->ovf_list.as<long long>();
+            bp2.cell_list = pending;
             bp2.overflow_list = nullptr;
-            bp2.work = wk + 2;
-            VG_CUDA(launch_cells_batch(bp2, mode, 1, b->sms, s));
+            bp2.work = wk + 4;
+            VG_CUDA(launch_cells_batch(bp2, mode, 2, b->sms, s));
         }
         cudaEventRecord(b->ev[2], s);
         VG_CUDA(launch_finish_batch(bp, mode, b->sms, s));
@@ -1550,13 +1606,11 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     VG_CUDA(cudaStreamSynchronize(s));
     VG_CUDA(cudaGetLastError());
     const float cell_ms = clip_ms + fin_ms;
-    Counters zero;
-    memset(&zero, 0, sizeof(zero));
     int first_err = VGPU_OK;
     for (int i = 0; i < nc; i++) {
         vgpu_container *h = b->members[i];
         h->poly_used = cs[i].poly_used;
-        int rc = finish_compute(h, cs[i], zero, cell_ms);
+        int rc = finish_compute(h, cs[i], cell_ms);
         if (rc != VGPU_OK && first_err == VGPU_OK) first_err = rc;
         vgpu_stats &t = b->stats;
         t.cells += h->stats.cells;

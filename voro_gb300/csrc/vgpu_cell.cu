@@ -84,15 +84,15 @@ static void build_box_tables(unsigned tri[8], unsigned adj[8]) {
 
 void box_tables(unsigned tri[8], unsigned adj[8]) { build_box_tables(tri, adj); }
 
-cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps) {
+cudaError_t launch_cells(const CellParams &cp, int mode, int pass, int sms, cudaStream_t s, int warps) {
     if (cp.ncells <= 0) return cudaSuccess;
     warps = warps < 1 ? 4 : (warps > 8 ? 8 : warps);   // the clipping translation units clamp further
-    return mode == VGPU_FP64 ? launch_cells_fp64(cp, big, sms, s, warps) : launch_cells_mixed(cp, big, sms, s, warps);
+    return mode == VGPU_FP64 ? launch_cells_fp64(cp, pass, sms, s, warps) : launch_cells_mixed(cp, pass, sms, s, warps);
 }
 
-cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s) {
+cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int pass, int sms, cudaStream_t s) {
     if (bp.ncells <= 0) return cudaSuccess;
-    return mode == VGPU_FP64 ? launch_cells_batch_fp64(bp, big, sms, s) : launch_cells_batch_mixed(bp, big, sms, s);
+    return mode == VGPU_FP64 ? launch_cells_batch_fp64(bp, pass, sms, s) : launch_cells_batch_mixed(bp, pass, sms, s);
 }
 
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s) {

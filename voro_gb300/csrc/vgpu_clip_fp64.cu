@@ -5,13 +5,14 @@
 
 namespace vgpu {
 
-cudaError_t launch_cells_fp64(const CellParams &cp, int big, int sms, cudaStream_t s, int warps) {
+cudaError_t launch_cells_fp64(const CellParams &cp, int pass, int sms, cudaStream_t s, int warps) {
     if (warps > kMaxCtaWarps) warps = kMaxCtaWarps;
-    return big ? launch_one<VGPU_FP64, 4>(cp, warps, sms, s) : launch_one<VGPU_FP64, 2>(cp, warps, sms, s);
+    // pass 0: 64 slots; later passes: 128 slots
+    return pass ? launch_one<VGPU_FP64, 4, false>(cp, warps, sms, s) : launch_one<VGPU_FP64, 2, false>(cp, warps, sms, s);
 }
 
-cudaError_t launch_cells_batch_fp64(const BatchParams &bp, int big, int sms, cudaStream_t s) {
-    return big ? launch_batch_one<VGPU_FP64, 4>(bp, sms, s) : launch_batch_one<VGPU_FP64, 2>(bp, sms, s);
+cudaError_t launch_cells_batch_fp64(const BatchParams &bp, int pass, int sms, cudaStream_t s) {
+    return pass ? launch_batch_one<VGPU_FP64, 4, false>(bp, sms, s) : launch_batch_one<VGPU_FP64, 2, false>(bp, sms, s);
 }
 
 }  // namespace vgpu

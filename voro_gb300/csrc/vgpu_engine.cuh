@@ -345,14 +345,14 @@ __device__ __noinline__ VertexF32 vertex_f64_fallback(const CellParams &P, const
 #endif
 
 // ------------------------------------------------------------------ the engine
-template <int MODE, int K>
+template <int MODE, int K, bool LEAN = false>
 struct Engine {
-    // The mixed engine's first pass (64 slots) carries no FP64 code: a cell
-    // that needs an FP64 repair or vertex goes, like one that outgrows the
-    // slots, to the 128-slot rerun, which has both.  Without the two FP64
-    // calls the kernel needs about 110 registers instead of 168 (4 CTAs per
-    // SM instead of 3).
-    static constexpr bool kLean = MODE == VGPU_MIXED && K == 2;
+    // LEAN (the mixed engine's first pass) carries no FP64 code: a cell that
+    // needs an FP64 repair or vertex goes, like one that outgrows the slots,
+    // to the rerun (the full 64-slot engine, then the 128-slot one).  Without
+    // the two FP64 calls the kernel needs 80 registers instead of 168 (6 CTAs
+    // per SM instead of 3).
+    static constexpr bool kLean = LEAN && MODE == VGPU_MIXED;
     const CellParams &P;
     WarpShared<MODE, K> &S;
     const int *offsets;   // shared copy of the offset table
@@ -1072,8 +1072,12 @@ struct Engine {
 #define VGPU_CTA_THREADS 128
 #endif
 constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
-template <int MODE, int K>
-constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BLOCKS : 2; }
+// CTAs per SM of the other engines: the full mixed 64-slot engine keeps 3
+// (168 registers), the 128-slot and FP64 engines 2.
+template <int MODE, int K, bool LEAN>
+constexpr int min_blocks() {
+    return (MODE == VGPU_MIXED && K == 2) ? (LEAN ? VGPU_MIN_BLOCKS : 3) : 2;
+}
 // Cells a warp takes from the work queue at a time (at most; fewer when the
 // launch has under four chunks per warp, so that small containers still
 // spread over all warps).  Consecutive cells (engine order: neighbouring
@@ -1083,8 +1087,8 @@ constexpr int min_blocks() { return (MODE == VGPU_MIXED && K == 2) ? VGPU_MIN_BL
 #define VGPU_CELL_CHUNK 8
 #endif
 
-template <int MODE, int K>
-__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_kernel(const __grid_constant__ CellParams P) {
+template <int MODE, int K, bool LEAN>
+__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>()) cell_kernel(const __grid_constant__ CellParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *offsets = reinterpret_cast<int *>(smem_raw);
@@ -1110,7 +1114,7 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
         }
         const int k = P.cell_list ? P.cell_list[w] : w;
         w++;
-        Engine<MODE, K> eng(P, S, offsets, lane);
+        Engine<MODE, K, LEAN> eng(P, S, offsets, lane);
         eng.run(k);
         tests += eng.C.tests;
         repairs += eng.C.repairs;
@@ -1149,8 +1153,8 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
 // a cell belongs to another container than the warp's previous one, the warp
 // copies that container's parameters into its shared slot and flushes its
 // counters to the previous container's.
-template <int MODE, int K>
-__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
+template <int MODE, int K, bool LEAN>
+__global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>()) cell_batch_kernel(const __grid_constant__ BatchParams B) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warps = blockDim.x >> 5;
@@ -1210,7 +1214,7 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
             __syncwarp();
         }
         const int k = (int)(gidx - cbeg);
-        Engine<MODE, K> eng(P, S, offsets, lane);
+        Engine<MODE, K, LEAN> eng(P, S, offsets, lane);
         eng.run(k);
         tests += eng.C.tests;
         repairs += eng.C.repairs;
@@ -1231,43 +1235,43 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K>()) cell_
     flush();
 }
 
-template <int MODE, int K>
+template <int MODE, int K, bool LEAN>
 cudaError_t launch_one(const CellParams &cp, int warps, int sms, cudaStream_t s) {
     const size_t off_bytes = ((size_t)cp.noffsets * sizeof(int) + 15) & ~(size_t)15;
     const size_t smem = off_bytes + warps * sizeof(WarpShared<MODE, K>);
-    cudaError_t e = cudaFuncSetAttribute(cell_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(cell_kernel<MODE, K, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_kernel<MODE, K>, warps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_kernel<MODE, K, LEAN>, warps * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
     const long long need = (cp.ncells + warps - 1) / warps;
     int grid = (int)(want < need ? want : need);
     if (grid < 1) grid = 1;
-    cell_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(cp);
+    cell_kernel<MODE, K, LEAN><<<grid, warps * 32, smem, s>>>(cp);
     note_launch();
     return cudaGetLastError();
 }
 
-template <int MODE, int K>
+template <int MODE, int K, bool LEAN>
 cudaError_t launch_batch_one(const BatchParams &bp, int sms, cudaStream_t s) {
     const int warps = 4;
     const size_t off_bytes = ((size_t)bp.noffsets * sizeof(int) + 15) & ~(size_t)15;
     const size_t cp_slot = (sizeof(CellParams) + 15) & ~(size_t)15;
     const size_t smem = off_bytes + warps * (cp_slot + sizeof(WarpShared<MODE, K>));
     cudaError_t e =
-        cudaFuncSetAttribute(cell_batch_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(cell_batch_kernel<MODE, K, LEAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_batch_kernel<MODE, K>, warps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_batch_kernel<MODE, K, LEAN>, warps * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)sms * per_sm;
     const long long need = (bp.ncells + warps - 1) / warps;
     int grid = (int)(want < need ? want : need);
     if (grid < 1) grid = 1;
-    cell_batch_kernel<MODE, K><<<grid, warps * 32, smem, s>>>(bp);
+    cell_batch_kernel<MODE, K, LEAN><<<grid, warps * 32, smem, s>>>(bp);
     note_launch();
     return cudaGetLastError();
 }

@@ -212,13 +212,13 @@ cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorde
                                    int nkept, int *dup_flag, cudaStream_t s);
 
 // vgpu_cell.cu, vgpu_finish.cu
-cudaError_t launch_cells(const CellParams &cp, int mode, int big, int sms, cudaStream_t s, int warps = 4);
+cudaError_t launch_cells(const CellParams &cp, int mode, int pass, int sms, cudaStream_t s, int warps = 4);
 // vgpu_clip_mixed.cu, vgpu_clip_fp64.cu
-cudaError_t launch_cells_mixed(const CellParams &cp, int big, int sms, cudaStream_t s, int warps);
-cudaError_t launch_cells_fp64(const CellParams &cp, int big, int sms, cudaStream_t s, int warps);
-cudaError_t launch_cells_batch_mixed(const BatchParams &bp, int big, int sms, cudaStream_t s);
-cudaError_t launch_cells_batch_fp64(const BatchParams &bp, int big, int sms, cudaStream_t s);
-cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int big, int sms, cudaStream_t s);
+cudaError_t launch_cells_mixed(const CellParams &cp, int pass, int sms, cudaStream_t s, int warps);
+cudaError_t launch_cells_fp64(const CellParams &cp, int pass, int sms, cudaStream_t s, int warps);
+cudaError_t launch_cells_batch_mixed(const BatchParams &bp, int pass, int sms, cudaStream_t s);
+cudaError_t launch_cells_batch_fp64(const BatchParams &bp, int pass, int sms, cudaStream_t s);
+cudaError_t launch_cells_batch(const BatchParams &bp, int mode, int pass, int sms, cudaStream_t s);
 cudaError_t launch_finish(const CellParams &cp, int mode, int sms, cudaStream_t s);
 cudaError_t launch_finish_batch(const BatchParams &bp, int mode, int sms, cudaStream_t s);
 cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const int *ovf, const long long *off, int n,

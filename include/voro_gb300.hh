@@ -709,8 +709,8 @@ class container_poly : public container_gpu_base {
     void import(const char *filename) { import_file(filename, true); }
 };
 
-// container_periodic (src/container_prd.hh:213-216); rectangular boxes only
-// (bxy = bxz = byz = 0), anything else is VGPU_ERR_UNSUPPORTED.
+// container_periodic (src/container_prd.hh:213-216): the periodic
+// parallelepiped of lattice vectors (bx,0,0), (bxy,by,0), (bxz,byz,bz).
 class container_periodic : public container_gpu_base {
   public:
     container_periodic(double bx_, double bxy_, double by_, double bxz_, double byz_, double bz_, int nx_, int ny_,

@@ -23,7 +23,7 @@ extern "C" {
 #define VGPU_ERR_INTERNAL 3      /* VOROPP_INTERNAL_ERROR */
 #define VGPU_ERR_ARG 16          /* bad argument / handle */
 #define VGPU_ERR_CUDA 17         /* CUDA runtime error (see vgpu_last_error) */
-#define VGPU_ERR_UNSUPPORTED 18  /* geometry not supported (e.g. sheared periodic box) */
+#define VGPU_ERR_UNSUPPORTED 18  /* not supported (walls on a periodic box; a sheared box in a batch) */
 #define VGPU_ERR_DUPLICATE 19    /* container_periodic put of a duplicate point
                                     (src/common.cc:14-20 exits; we return this) */
 #define VGPU_ERR_NOT_COMPUTED 20 /* results requested before vgpu_compute */
@@ -86,7 +86,9 @@ const char *vgpu_last_error(void);
  * init_mem) (src/container.hh:290-291), container_poly(...) (src/container.hh:512-513),
  * container_periodic(bx,bxy,by,bxz,byz,bz,nx,ny,nz,init_mem) (src/container_prd.hh:215-216)
  * and container_periodic_poly (src/container_prd.hh:436-437).
- * geom: container kinds (ax,bx,ay,by,az,bz); periodic kinds (bx,bxy,by,bxz,byz,bz).
+ * geom: container kinds (ax,bx,ay,by,az,bz); periodic kinds (bx,bxy,by,bxz,byz,bz),
+ * rectangular or sheared (the unit cell, src/unitcell.cc:26-79, is built
+ * here; VGPU_ERR_MEMORY if it is not bounded within ten shells of images).
  * grid: (nx,ny,nz) as given to the reference (it fixes the loop order of results).
  * periodic: three flags, container kinds only (ignored for periodic kinds). */
 int vgpu_container_create(vgpu_container **out, int kind, const double geom[6],
@@ -247,7 +249,8 @@ int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per
  * cell engine with a single device work queue, so thousands of small and
  * large containers share the GPU.  Results land in each member container and
  * are read with the usual getters.  Containers stay owned by the caller and
- * must outlive the batch's computes. */
+ * must outlive the batch's computes.  A sheared container_periodic is
+ * computed on its own (vgpu_batch_add: VGPU_ERR_UNSUPPORTED). */
 typedef struct vgpu_batch vgpu_batch;
 int vgpu_batch_create(vgpu_batch **out);
 int vgpu_batch_add(vgpu_batch *b, vgpu_container *h);

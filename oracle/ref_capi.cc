@@ -132,6 +132,18 @@ bool with_container(int kind, const double *geom, const int *grid, const int *pe
     return true;
 }
 
+// Every periodic image block of a container_periodic(_poly), built before any
+// ghost: the reference builds them lazily, and a block first built while a
+// ghost sits in its primary block keeps a copy of the ghost (which that
+// ghost, and any later one, then sees); built first, a ghost cell depends on
+// the particles alone.
+template <class con_t>
+void images_first(con_t &con) {
+    if constexpr (std::is_same<con_t, container_periodic>::value ||
+                  std::is_same<con_t, container_periodic_poly>::value)
+        con.create_all_images();
+}
+
 // compute_ghost_cell of the container's kind (radius for the radical kinds)
 template <class con_t>
 bool ghost_of(con_t &con, voronoicell_neighbor &c, const double *g) {
@@ -245,6 +257,7 @@ int ref_ghost_cells(int kind, const double *geom, const int *grid, const int *pe
         voronoicell_neighbor c(con);
         std::vector<int> v;
         long used = 0;
+        images_first(con);
         for (int i = 0; i < ng; i++) {
             out_nb_off[i] = used;
             const bool q = ghost_of(con, c, gxyzr + 4 * i);

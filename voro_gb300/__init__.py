@@ -719,7 +719,8 @@ class container_poly(_ContainerBase):
 
 class container_periodic(_ContainerBase):
     """container_periodic(bx,bxy,by,bxz,byz,bz,nx,ny,nz,init_mem)
-    (src/container_prd.hh:213-216); rectangular boxes (bxy=bxz=byz=0)."""
+    (src/container_prd.hh:213-216): the periodic parallelepiped of lattice
+    vectors (bx,0,0), (bxy,by,0), (bxz,byz,bz); rectangular or sheared."""
 
     def __init__(self, bx, bxy, by, bxz, byz, bz, nx, ny, nz, init_mem=8, mode="mixed"):
         super().__init__(KIND_PERIODIC, (bx, bxy, by, bxz, byz, bz), (nx, ny, nz), (True, True, True), mode)

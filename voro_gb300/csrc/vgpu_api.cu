@@ -1,5 +1,6 @@
 // C ABI of the engine (declared in include/vorogpu.h).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -184,6 +185,9 @@ struct vgpu_container {
     DevBuf gh_p64, gh_lffh, gh_lffl, gh_pid, gh_gblock, gh_outpos, gh_rec_off, gh_q, gh_keep, gh_list, gh_ovf, gh_ovf2,
         gh_cnt, gh_vol, gh_cen, gh_nf, gh_nv, gh_mr2, gh_flags, gh_nb, gh_nb_ovf, gh_nb_off, gh_nb_out, gh_poly,
         gh_poly_off;
+    std::vector<WallSpec> lattice;  // sheared periodic boxes: the unit cell's face planes (after the walls)
+    int nengine = 0;                // engine entries of the last binning: the particles, then any images
+    DevBuf x_rem, x_gkey, x_idx, x_kalt, x_valt, img_cnt, img_off, img_src, cell_list;   // images (sheared boxes)
     std::vector<WallSpec> walls;    // walls, in the order added
     DevBuf walls_dev;               // their device copy (uploaded when changed)
     bool walls_dirty = false;
@@ -204,6 +208,122 @@ struct vgpu_container {
 
 namespace {
 
+// The Voronoi cell about the origin of the lattice of a sheared periodic box
+// (unitcell::unitcell, src/unitcell.cc:26-79): a large box (max_unit_voro_shells
+// box lengths, src/config.hh:93) is cut by the bisecting planes of the lattice
+// vectors i*a + j*b + k*c shell by shell (Chebyshev index l = 1, 2, ...) until
+// no vector of a shell cuts it.  Kept as its vertices, each with the planes
+// it lies on: a cut keeps the vertices inside and adds a vertex on each edge
+// (two vertices sharing two planes) that crosses the plane.
+struct UnitCell {
+    std::vector<std::array<double, 3>> v;       // vertices
+    std::vector<std::array<double, 4>> faces;   // lattice vectors (x, y, z, |d|^2) whose bisectors are faces
+};
+
+bool build_unit_cell(const double B[6], UnitCell &U) {
+    const double bx = B[0], bxy = B[1], by = B[2], bxz = B[3], byz = B[4], bz = B[5];
+    constexpr int kShells = 10;
+    struct Vert {
+        std::array<double, 3> x;
+        std::vector<int> pl;
+    };
+    std::vector<std::array<double, 4>> planes;   // n.x <= h
+    const double uc[3] = {kShells * bx, kShells * by, kShells * bz};
+    for (int a = 0; a < 3; a++)
+        for (int sgn = -1; sgn <= 1; sgn += 2) {
+            std::array<double, 4> q = {0, 0, 0, uc[a]};
+            q[a] = sgn;
+            planes.push_back(q);
+        }
+    std::vector<Vert> V;
+    for (int c = 0; c < 8; c++) {
+        Vert w;
+        for (int a = 0; a < 3; a++) {
+            const int hi = (c >> a) & 1;
+            w.x[a] = hi ? uc[a] : -uc[a];
+            w.pl.push_back(2 * a + hi);
+        }
+        V.push_back(w);
+    }
+    const double scale = std::fabs(bx) + std::fabs(bxy) + std::fabs(by) + std::fabs(bxz) + std::fabs(byz) + std::fabs(bz);
+    const double eps = 1e-11 * scale;
+    auto side = [](const Vert &w, const std::array<double, 4> &q) {
+        return q[0] * w.x[0] + q[1] * w.x[1] + q[2] * w.x[2] - q[3];
+    };
+    auto cut = [&](const std::array<double, 4> &q) {
+        const double e = eps * (1.0 + std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
+        std::vector<double> sv(V.size());
+        bool any = false;
+        for (size_t i = 0; i < V.size(); i++) {
+            sv[i] = side(V[i], q);
+            any |= sv[i] > e;
+        }
+        if (!any) return;
+        const int idx = (int)planes.size();
+        planes.push_back(q);
+        std::vector<Vert> out;
+        for (size_t i = 0; i < V.size(); i++)
+            if (sv[i] <= e) {
+                out.push_back(V[i]);
+                if (sv[i] >= -e) out.back().pl.push_back(idx);
+            }
+        for (size_t i = 0; i < V.size(); i++) {
+            if (!(sv[i] < -e)) continue;
+            for (size_t j = 0; j < V.size(); j++) {
+                if (!(sv[j] > e)) continue;
+                std::vector<int> common;
+                for (int p : V[i].pl)
+                    if (std::find(V[j].pl.begin(), V[j].pl.end(), p) != V[j].pl.end()) common.push_back(p);
+                if (common.size() < 2) continue;
+                const double t = sv[i] / (sv[i] - sv[j]);
+                Vert w;
+                for (int a = 0; a < 3; a++) w.x[a] = V[i].x[a] + t * (V[j].x[a] - V[i].x[a]);
+                w.pl = common;
+                w.pl.push_back(idx);
+                out.push_back(w);
+            }
+        }
+        V.swap(out);
+    };
+    for (int l = 1; l < 2 * kShells; l++) {
+        std::vector<std::array<double, 4>> shell;
+        for (int k = -l; k <= l; k++)
+            for (int j = -l; j <= l; j++)
+                for (int i = -l; i <= l; i++) {
+                    if (std::max(std::abs(i), std::max(std::abs(j), std::abs(k))) != l) continue;
+                    const double x = i * bx + j * bxy + k * bxz, y = j * by + k * byz, z = k * bz;
+                    shell.push_back({x, y, z, 0.5 * (x * x + y * y + z * z)});
+                }
+        bool cuts = false;
+        for (const auto &q : shell) {
+            const double e = eps * (1.0 + std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]));
+            for (const Vert &w : V)
+                if (side(w, q) > e) {
+                    cuts = true;
+                    break;
+                }
+            if (cuts) break;
+        }
+        if (!cuts) {
+            U.v.clear();
+            for (const Vert &w : V) {
+                for (int p : w.pl)
+                    if (p < 6) return false;   // the box still bounds the cell
+                U.v.push_back(w.x);
+            }
+            U.faces.clear();
+            for (size_t p = 6; p < planes.size(); p++) {
+                int on = 0;
+                for (const Vert &w : V) on += std::find(w.pl.begin(), w.pl.end(), (int)p) != w.pl.end();
+                if (on >= 3) U.faces.push_back({planes[p][0], planes[p][1], planes[p][2], 2.0 * planes[p][3]});
+            }
+            return !U.v.empty() && U.faces.size() <= (size_t)kMaxWalls;
+        }
+        for (const auto &q : shell) cut(q);
+    }
+    return false;   // src/unitcell.cc:76-79: VOROPP_MEMORY_ERROR
+}
+
 int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int grid[3], const int periodic[3]) {
     Geometry &g = h->g;
     memset(&g, 0, sizeof(g));
@@ -222,6 +342,7 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
             g.len[a] = g.hi[a] - g.lo[a];
             if (!(g.len[a] > 0)) return fail(VGPU_ERR_ARG, "empty container extent on axis %d", a);
             g.per[a] = periodic ? (periodic[a] != 0) : 0;
+            g.ext[a] = g.len[a];
             g.ubox[a] = g.len[a] / g.un[a];   // src/container.cc:31
             g.usp[a] = 1 / g.ubox[a];          // src/v_base.cc:26
         }
@@ -230,22 +351,65 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
                      g.len[2] * g.len[2] * (g.per[2] ? 0.25 : 1);
     } else if (kind == VGPU_CONTAINER_PERIODIC || kind == VGPU_CONTAINER_PERIODIC_POLY) {
         // geom = (bx, bxy, by, bxz, byz, bz)
-        if (geom[1] != 0.0 || geom[3] != 0.0 || geom[4] != 0.0)
-            return fail(VGPU_ERR_UNSUPPORTED, "sheared periodic boxes (bxy, bxz, byz != 0) are not supported yet");
         g.unit_cell = 1;
         double L[3] = {geom[0], geom[2], geom[5]};
+        g.shear[0] = geom[1];
+        g.shear[1] = geom[3];
+        g.shear[2] = geom[4];
         for (int a = 0; a < 3; a++) {
             if (!(L[a] > 0)) return fail(VGPU_ERR_ARG, "periodic length on axis %d must be > 0", a);
+            if (!std::isfinite(g.shear[a])) return fail(VGPU_ERR_ARG, "shear terms must be finite");
             g.lo[a] = 0;
             g.len[a] = L[a];
             g.hi[a] = L[a];
+            g.ext[a] = L[a];
             g.per[a] = 1;
+            g.half[a] = 0.5 * L[a];
             g.ubox[a] = L[a] / g.un[a];        // src/container_prd.cc:31
             g.usp[a] = 1 / g.ubox[a];
         }
-        // unit_voro.max_radius_squared() of the rectangular unit cell
-        // (src/container_prd.cc:32), in the reference's doubled coordinates
-        max_len_sq = L[0] * L[0] + L[1] * L[1] + L[2] * L[2];
+        h->lattice.clear();
+        if (g.shear[0] != 0.0 || g.shear[1] != 0.0 || g.shear[2] != 0.0) {
+            UnitCell U;
+            if (!build_unit_cell(geom, U)) return fail(VGPU_ERR_MEMORY, "periodic cell computation failed");
+            // max_len_sq = unit_voro.max_radius_squared() (doubled
+            // coordinates); ghost layers ey, ez from the largest y and z a
+            // cutting particle can have (src/unitcell.cc:60-70,
+            // src/container_prd.cc:31-33)
+            double mr = 0, muy = 0, muz = 0, mab[3] = {0, 0, 0};
+            for (const auto &v : U.v) {
+                const double r = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                mr = std::max(mr, 4.0 * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+                muy = std::max(muy, v[1] + r);
+                muz = std::max(muz, v[2] + r);
+                for (int a = 0; a < 3; a++) mab[a] = std::max(mab[a], std::fabs(v[a]));
+            }
+            max_len_sq = mr;
+            const int ey = (int)(muy * g.usp[1] + 1), ez = (int)(muz * g.usp[2] + 1);
+            g.tric = 1;
+            g.per[1] = g.per[2] = 0;
+            g.lo[1] = -(ey * g.ubox[1]);
+            g.lo[2] = -(ez * g.ubox[2]);
+            g.ext[1] = (g.un[1] + 2 * ey) * g.ubox[1];
+            g.ext[2] = (g.un[2] + 2 * ez) * g.ubox[2];
+            // the initial box: the unit cell with room to spare (its own
+            // face planes cut it to the unit cell)
+            for (int a = 0; a < 3; a++) g.half[a] = 1.25 * mab[a];
+            for (const auto &f : U.faces) {
+                WallSpec w;
+                memset(&w, 0, sizeof(w));
+                w.type = kWallLattice;
+                w.id = 0;   // the unit cell's faces carry neighbour 0 (src/cell.cc:86-94)
+                for (int a = 0; a < 3; a++) w.c[a] = f[a];
+                w.r = f[3];
+                h->lattice.push_back(w);
+            }
+            h->walls_dirty = true;
+        } else {
+            // unit_voro.max_radius_squared() of the rectangular unit cell
+            // (src/container_prd.cc:32), in the reference's doubled coordinates
+            max_len_sq = L[0] * L[0] + L[1] * L[1] + L[2] * L[2];
+        }
     } else {
         return fail(VGPU_ERR_ARG, "unknown container kind %d", kind);
     }
@@ -256,13 +420,15 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
     return VGPU_OK;
 }
 
+// n particles in the domain; the engine region (ghost layers included)
+// holds them at the same density.
 void choose_engine_grid(Geometry &g, int64_t n, double density) {
     double vol = g.len[0] * g.len[1] * g.len[2];
     double nn = (double)std::max<int64_t>(n, 1);
     double bs = std::cbrt(vol * density / nn);
     long long total = 1;
     for (int a = 0; a < 3; a++) {
-        int m = (int)std::floor(g.len[a] / bs + 0.5);
+        int m = (int)std::floor(g.ext[a] / bs + 0.5);
         m = std::max(1, std::min(m, 1 << 10));
         g.gn[a] = m;
         total *= m;
@@ -276,7 +442,7 @@ void choose_engine_grid(Geometry &g, int64_t n, double density) {
     }
     float bmin = 3.4e38f, bmax = 0.0f;
     for (int a = 0; a < 3; a++) {
-        g.gbs[a] = g.len[a] / g.gn[a];
+        g.gbs[a] = g.ext[a] / g.gn[a];
         g.gbs32[a] = (float)g.gbs[a];
         g.gbs_h[a] = g.gbs32[a];
         g.gbs_l[a] = (float)(g.gbs[a] - (double)g.gbs32[a]);
@@ -518,10 +684,13 @@ void fill_cell_params(vgpu_container *h, CellParams &cp);
 // The walls' device copy, when they changed since the last upload.
 int upload_walls(vgpu_container *h) {
     if (!h->walls_dirty) return VGPU_OK;
-    if (!h->walls.empty()) {
-        VG_CUDA(h->walls_dev.ensure(h->walls.size() * sizeof(WallSpec)));
-        VG_CUDA(cudaMemcpyAsync(h->walls_dev.p, h->walls.data(), h->walls.size() * sizeof(WallSpec),
-                                cudaMemcpyHostToDevice, h->stream));
+    std::vector<WallSpec> all(h->walls);
+    all.insert(all.end(), h->lattice.begin(), h->lattice.end());
+    if ((int)all.size() > kMaxWalls) return fail(VGPU_ERR_ARG, "at most %d walls", kMaxWalls);
+    if (!all.empty()) {
+        VG_CUDA(h->walls_dev.ensure(all.size() * sizeof(WallSpec)));
+        VG_CUDA(cudaMemcpyAsync(h->walls_dev.p, all.data(), all.size() * sizeof(WallSpec), cudaMemcpyHostToDevice,
+                                h->stream));
         VG_CUDA(cudaStreamSynchronize(h->stream));
     }
     h->walls_dirty = false;
@@ -611,8 +780,29 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     const unsigned *ukey_sorted = alt ? h->keys_alt.as<unsigned>() : h->ukey.as<unsigned>();
     const int *uorder = alt ? h->vals_alt.as<int>() : h->idx.as<int>();
 
+    // sheared periodic boxes: the images in the ghost layers, counted per
+    // particle (every particle is kept), then written after the particles
+    int nengine = nkept;
+    if (g.tric && n > 0) {
+        VG_CUDA(h->img_cnt.ensure(nn * 4));
+        VG_CUDA(h->img_off.ensure(nn * 4));
+        VG_CUDA(h->scan_tmp.ensure((scan_tmp_ints(n) + 64) * 8));
+        VG_CUDA(launch_image_count(g, n, h->rem.as<double4>(), h->img_cnt.as<int>(), s));
+        VG_CUDA(exclusive_scan_int(h->img_cnt.as<int>(), h->img_off.as<int>(), n, h->scan_tmp.as<int>(),
+                                   h->scan_tmp.bytes / 4, s));
+        int last[2] = {0, 0};
+        VG_CUDA(cudaMemcpyAsync(&last[0], h->img_cnt.as<int>() + (n - 1), 4, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaMemcpyAsync(&last[1], h->img_off.as<int>() + (n - 1), 4, cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        const long long total = (long long)n + last[0] + last[1];
+        if (total > (long long)INT32_MAX / 2) return fail(VGPU_ERR_MEMORY, "too many periodic images");
+        nengine = (int)total;
+    }
+    h->nengine = nengine;
+
     // results arrays
     const size_t nk = (size_t)std::max(nkept, 1);
+    const size_t ne = (size_t)std::max(nengine, 1);
     VG_CUDA(h->r_vol.ensure(nk * 8));
     VG_CUDA(h->r_cen.ensure(nk * 24));
     VG_CUDA(h->r_nf.ensure(nk * 4));
@@ -624,12 +814,12 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     VG_CUDA(h->r_ids.ensure(nk * 4));
     VG_CUDA(h->r_pos.ensure(nk * 24));
     VG_CUDA(h->r_rad.ensure(nk * 8));
-    VG_CUDA(h->p64.ensure(nk * 32));
-    VG_CUDA(h->lffh.ensure(nk * 16));
-    VG_CUDA(h->lffl.ensure(nk * 16));
-    VG_CUDA(h->pid.ensure(nk * 4));
-    VG_CUDA(h->outpos.ensure(nk * 4));
-    VG_CUDA(h->gblock.ensure(nk * 4));
+    VG_CUDA(h->p64.ensure(ne * 32));
+    VG_CUDA(h->lffh.ensure(ne * 16));
+    VG_CUDA(h->lffl.ensure(ne * 16));
+    VG_CUDA(h->pid.ensure(ne * 4));
+    VG_CUDA(h->outpos.ensure(ne * 4));
+    VG_CUDA(h->gblock.ensure(ne * 4));
     VG_CUDA(h->bstart.ensure(((size_t)nblocks + 2) * 4));
     VG_CUDA(h->ovf_list.ensure(nk * 4));
 
@@ -645,22 +835,56 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
 
     // engine order: the u-sort consumed idx, so sort (gkey, idx2)
     bool galt = false;
-    unsigned *gk_alt = alt ? h->ukey.as<unsigned>() : h->keys_alt.as<unsigned>();
-    int *gv_alt = alt ? h->idx.as<int>() : h->vals_alt.as<int>();
-    // keep uorder intact: the g-sort ping-pongs between gkey/idx2 and the buffers not holding uorder
-    VG_CUDA(radix_sort_pairs(h->gkey.as<unsigned>(), h->idx2.as<int>(), gk_alt, gv_alt, n, gbits,
-                             h->hist.as<int>(), h->hist.bytes / 4, h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4, s,
-                             &galt));
-    const unsigned *gkey_sorted = galt ? gk_alt : h->gkey.as<unsigned>();
-    const int *gorder = galt ? gv_alt : h->idx2.as<int>();
-    if (galt && (gk_alt == (const unsigned *)ukey_sorted || gv_alt == uorder))
-        return fail(VGPU_ERR_INTERNAL, "sort buffer aliasing");
+    const unsigned *gkey_sorted;
+    const int *gorder;
+    const double4 *erem = h->rem.as<double4>();
+    const int *img_src = nullptr;
+    if (g.tric && n > 0) {
+        // the particles and their images, in buffers of their own
+        const size_t nx = (size_t)nengine;
+        VG_CUDA(h->x_rem.ensure(nx * 32));
+        VG_CUDA(h->x_gkey.ensure(nx * 4));
+        VG_CUDA(h->x_idx.ensure(nx * 4));
+        VG_CUDA(h->x_kalt.ensure(nx * 4));
+        VG_CUDA(h->x_valt.ensure(nx * 4));
+        VG_CUDA(h->img_src.ensure(std::max<size_t>(nx - (size_t)n, 1) * 4));
+        VG_CUDA(h->hist.ensure(radix_hist_ints(nengine) * 4));
+        const size_t xscan = scan_tmp_ints(std::max<int>((int)radix_hist_ints(nengine), nblocks + 1)) + 64;
+        VG_CUDA(h->scan_tmp.ensure(xscan * 8));
+        VG_CUDA(cudaMemcpyAsync(h->x_rem.p, h->rem.p, (size_t)n * 32, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->x_gkey.p, h->gkey.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(cudaMemcpyAsync(h->x_idx.p, h->idx2.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        VG_CUDA(launch_image_write(g, n, h->rem.as<double4>(), h->img_off.as<int>(), n, h->x_rem.as<double4>(),
+                                   h->x_gkey.as<unsigned>(), h->x_idx.as<int>(), h->img_src.as<int>(), s));
+        VG_CUDA(radix_sort_pairs(h->x_gkey.as<unsigned>(), h->x_idx.as<int>(), h->x_kalt.as<unsigned>(),
+                                 h->x_valt.as<int>(), nengine, gbits, h->hist.as<int>(), h->hist.bytes / 4,
+                                 h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4, s, &galt));
+        gkey_sorted = galt ? h->x_kalt.as<unsigned>() : h->x_gkey.as<unsigned>();
+        gorder = galt ? h->x_valt.as<int>() : h->x_idx.as<int>();
+        erem = h->x_rem.as<double4>();
+        img_src = h->img_src.as<int>();
+    } else {
+        unsigned *gk_alt = alt ? h->ukey.as<unsigned>() : h->keys_alt.as<unsigned>();
+        int *gv_alt = alt ? h->idx.as<int>() : h->vals_alt.as<int>();
+        // keep uorder intact: the g-sort ping-pongs between gkey/idx2 and the buffers not holding uorder
+        VG_CUDA(radix_sort_pairs(h->gkey.as<unsigned>(), h->idx2.as<int>(), gk_alt, gv_alt, n, gbits,
+                                 h->hist.as<int>(), h->hist.bytes / 4, h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4,
+                                 s, &galt));
+        gkey_sorted = galt ? gk_alt : h->gkey.as<unsigned>();
+        gorder = galt ? gv_alt : h->idx2.as<int>();
+        if (galt && (gk_alt == (const unsigned *)ukey_sorted || gv_alt == uorder))
+            return fail(VGPU_ERR_INTERNAL, "sort buffer aliasing");
+    }
 
-    VG_CUDA(launch_gather(g, nkept, uorder, gorder, gkey_sorted, h->rem.as<double4>(), d_ids,
+    VG_CUDA(launch_gather(g, nkept, nengine, n, img_src, uorder, gorder, gkey_sorted, erem, d_ids,
                           h->outpos_in.as<int>(), h->p64.as<double4>(), h->lffh.as<float4>(),
                           h->lffl.as<float4>(), h->pid.as<int>(),
                           h->outpos.as<int>(), h->gblock.as<int>(), h->bstart.as<int>(), nblocks,
                           h->r_ids.as<int>(), h->r_pos.as<double>(), h->r_rad.as<double>(), s));
+    if (g.tric) {   // the cells to compute: the particles, not their images
+        VG_CUDA(h->cell_list.ensure(nk * 4));
+        VG_CUDA(launch_cell_list(h->outpos.as<int>(), nengine, h->cell_list.as<int>(), s));
+    }
     cudaEventRecord(h->ev[1], s);
 
     // cell engine parameters
@@ -701,7 +925,7 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     cp.r.nb_ovf_cap = nb_ovf_ints((size_t)std::max(nkept, 1));
     cp.cnt = h->counters.as<Counters>();
     cp.ncells = nkept;
-    cp.cell_list = nullptr;
+    cp.cell_list = g.tric ? h->cell_list.as<int>() : nullptr;
     cp.overflow_list = h->ovf_list.as<int>();
     cp.offsets = h->offsets.as<int>();
     cp.noffsets = (int)ot.codes.size();
@@ -709,8 +933,8 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
     box_tables(cp.box_tri, cp.box_adj);
-    cp.walls = h->walls.empty() ? nullptr : h->walls_dev.as<WallSpec>();
-    cp.nwalls = (int)h->walls.size();
+    cp.nwalls = (int)(h->walls.size() + h->lattice.size());
+    cp.walls = cp.nwalls == 0 ? nullptr : h->walls_dev.as<WallSpec>();
 }
 
 // A batch member of at most kSmallBinMax particles is binned by one CTA of
@@ -783,6 +1007,7 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
 int finish_small(vgpu_container *h, const unsigned long long res[2]) {
     if (res[0] >> 32) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
     h->nkept = (int)(res[0] & 0xffffffffu);
+    h->nengine = h->nkept;
     h->binned = true;
     double rmax = 0.0;
     memcpy(&rmax, &res[1], 8);
@@ -814,8 +1039,8 @@ int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt, cu
     const unsigned long long cap = std::min<unsigned long long>(
         (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), ~0ull >> 8);
     VG_CUDA(store.ensure(cap * 4));
-    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 8));
-    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 8, s));
+    VG_CUDA(h->rec_off.ensure((size_t)h->nengine * 8));
+    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nengine * 8, s));
     cp.rec = store.as<unsigned>();
     cp.rec_cap = cap;
     cp.rec_used = &cnt->rec_used;
@@ -1179,8 +1404,8 @@ int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const doubl
         fill_cell_params(h, cp);
     }
     cudaStream_t s = h->stream;
-    const size_t nk = (size_t)h->nkept, ng = (size_t)n, tot = nk + ng;
-    // engine arrays: the particles (copied), then the ghosts
+    const size_t nk = (size_t)h->nengine, ng = (size_t)n, tot = nk + ng;
+    // engine arrays: the particles and any images (copied), then the ghosts
     VG_CUDA(h->gh_p64.ensure(tot * 32));
     VG_CUDA(h->gh_lffh.ensure(tot * 16));
     VG_CUDA(h->gh_lffl.ensure(tot * 16));
@@ -1424,6 +1649,7 @@ int vgpu_batch_create(vgpu_batch **out) {
 int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
     if (!b || !h) return fail(VGPU_ERR_ARG, "null argument");
     if (h->device != b->device) return fail(VGPU_ERR_ARG, "container and batch are on different devices");
+    if (h->g.tric) return fail(VGPU_ERR_UNSUPPORTED, "sheared periodic boxes are computed one at a time");
     b->members.push_back(h);
     return VGPU_OK;
 }

@@ -12,6 +12,17 @@ namespace vgpu {
 
 namespace {
 
+// The engine block of position c (clamped into the grid).
+__device__ __forceinline__ unsigned engine_key(const Geometry &g, const double c[3]) {
+    int e[3];
+    for (int a = 0; a < 3; a++) {
+        double t = (c[a] - g.lo[a]) / g.gbs[a];
+        int v = (int)floor(t);
+        e[a] = v < 0 ? 0 : (v >= g.gn[a] ? g.gn[a] - 1 : v);
+    }
+    return (unsigned)(e[0] + g.gn[0] * (e[1] + g.gn[1] * e[2]));
+}
+
 // The reference's placement of one particle: remapped position c, its
 // reference block key uk (nub if put() drops it) and engine block key gk.
 __device__ __forceinline__ bool remap_one(const Geometry &g, double4 q, int nub, int nblocks, double4 &out,
@@ -32,26 +43,36 @@ __device__ __forceinline__ bool remap_one(const Geometry &g, double4 q, int nub,
             b[a] = ijk;
         }
     } else {
-        // rectangular periodic box: z, then y, then x (shear terms are zero)
-        for (int a = 2; a >= 0; a--) {
-            int ijk = step_int(__dmul_rn(c[a], g.usp[a]));
-            if (ijk < 0 || ijk >= g.un[a]) {
-                int ak = step_div(ijk, g.un[a]);
-                c[a] = __dsub_rn(c[a], __dmul_rn((double)ak, g.len[a]));
-                ijk -= ak * g.un[a];
-            }
-            b[a] = ijk;
+        // container_periodic: z, then y, then x, each remapped along its
+        // lattice vector (c = (bxz, byz, bz), b = (bxy, by, 0), a = (bx, 0, 0))
+        int k = step_int(__dmul_rn(c[2], g.usp[2]));
+        if (k < 0 || k >= g.un[2]) {
+            const int ak = step_div(k, g.un[2]);
+            c[2] = __dsub_rn(c[2], __dmul_rn((double)ak, g.len[2]));
+            c[1] = __dsub_rn(c[1], __dmul_rn((double)ak, g.shear[2]));
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)ak, g.shear[1]));
+            k -= ak * g.un[2];
         }
+        int j = step_int(__dmul_rn(c[1], g.usp[1]));
+        if (j < 0 || j >= g.un[1]) {
+            const int aj = step_div(j, g.un[1]);
+            c[1] = __dsub_rn(c[1], __dmul_rn((double)aj, g.len[1]));
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)aj, g.shear[0]));
+            j -= aj * g.un[1];
+        }
+        int i = step_int(__dmul_rn(c[0], g.usp[0]));
+        if (i < 0 || i >= g.un[0]) {
+            const int ai = step_div(i, g.un[0]);
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)ai, g.len[0]));
+            i -= ai * g.un[0];
+        }
+        b[0] = i;
+        b[1] = j;
+        b[2] = k;
     }
     if (ok) {
         uk = (unsigned)(b[0] + g.un[0] * (b[1] + g.un[1] * b[2]));
-        int e[3];
-        for (int a = 0; a < 3; a++) {
-            double t = (c[a] - g.lo[a]) / g.gbs[a];
-            int v = (int)floor(t);
-            e[a] = v < 0 ? 0 : (v >= g.gn[a] ? g.gn[a] - 1 : v);
-        }
-        gk = (unsigned)(e[0] + g.gn[0] * (e[1] + g.gn[1] * e[2]));
+        gk = engine_key(g, c);
     } else {
         uk = (unsigned)nub;
         gk = (unsigned)nblocks;
@@ -120,19 +141,96 @@ __global__ void loop_order_kernel(const int *uorder, int nkept, const int *ids_i
     res_rad[m] = p.w;
 }
 
-__global__ void gather_kernel(Geometry g, int nkept, const int *gorder, const unsigned *gkey_sorted,
-                              const double4 *rem, const int *ids_in, const int *outpos_by_input,
-                              double4 *p64, float4 *lffh, float4 *lffl, int *pid, int *outpos,
-                              int *gblock, int *bstart, int nblocks) {
+// Engine entry k: input particle i = gorder[k] (i < nin), or the image
+// i - nin of particle img_src[i - nin], which has no result slot (-1).
+__global__ void gather_kernel(Geometry g, int nengine, int nin, const int *img_src, const int *gorder,
+                              const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
+                              const int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl, int *pid,
+                              int *outpos, int *gblock, int *bstart, int nblocks) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nkept) return;
+    if (k >= nengine) return;
     int i = gorder[k];
     int b = (int)gkey_sorted[k];
-    gather_one(g, k, b, rem[i], ids_in[i], outpos_by_input[i], p64, lffh, lffl, pid, outpos, gblock);
+    const bool particle = i < nin;
+    const int id = particle ? ids_in[i] : ids_in[img_src[i - nin]];
+    gather_one(g, k, b, rem[i], id, particle ? outpos_by_input[i] : -1, p64, lffh, lffl, pid, outpos, gblock);
     int prev = k == 0 ? -1 : (int)gkey_sorted[k - 1];
     for (int q = prev + 1; q <= b; q++) bstart[q] = k;
-    if (k == nkept - 1)
-        for (int q = b + 1; q <= nblocks; q++) bstart[q] = nkept;
+    if (k == nengine - 1)
+        for (int q = b + 1; q <= nblocks; q++) bstart[q] = nengine;
+}
+
+// The images of particle p (remapped into the primary domain) in the ghost
+// layers of a sheared periodic box: p + ic*c + ib*b + ia*a for every
+// (ib, ic) != (0, 0) whose y and z lie in the engine region, ia taking x into
+// the primary range as put_locate_block would.  Displacements as the
+// reference's image blocks build them (create_side_image and
+// create_vertical_image, src/container_prd.cc:583-758; put_image, 766-774):
+// x ic*bxz + ib*bxy + ia*bx, y ic*byz + ib*by, z ic*bz, each added to p.
+// WRITE: stored from slot nin + base on; returns the count.
+template <bool WRITE>
+__device__ int images_of(const Geometry &g, double4 p, int src, int nin, int base, double4 *rem_out,
+                         unsigned *gkey_out, int *idx_out, int *img_src) {
+    const double zlo = g.lo[2], zhi = g.lo[2] + g.ext[2];
+    const double ylo = g.lo[1], yhi = g.lo[1] + g.ext[1];
+    // a remapped particle lies in the primary domain, so its image counts
+    // span a few box lengths; the bounds also keep a non-finite input from
+    // looping
+    if (!(fabs(p.x) < 1e300 && fabs(p.y) < 1e300 && fabs(p.z) < 1e300)) return 0;
+    const double fz = floor((zlo - p.z) / g.len[2]);
+    if (!(fabs(fz) < 1e6)) return 0;
+    const int c0 = (int)fz - 1;
+    const int c1 = min((int)ceil((zhi - p.z) / g.len[2]) + 1, c0 + 64);
+    int cnt = 0;
+    for (int ic = c0; ic <= c1; ic++) {
+        const double z = __dadd_rn(p.z, __dmul_rn((double)ic, g.len[2]));
+        if (!(z >= zlo && z < zhi)) continue;
+        const double yc = p.y + (double)ic * g.shear[2];
+        const double fy = floor((ylo - yc) / g.len[1]);
+        if (!(fabs(fy) < 1e6)) continue;
+        const int b0 = (int)fy - 1;
+        const int b1 = min((int)ceil((yhi - yc) / g.len[1]) + 1, b0 + 64);
+        for (int ib = b0; ib <= b1; ib++) {
+            if (ib == 0 && ic == 0) continue;
+            const double dy = __dadd_rn(__dmul_rn((double)ic, g.shear[2]), __dmul_rn((double)ib, g.len[1]));
+            const double y = __dadd_rn(p.y, dy);
+            if (!(y >= ylo && y < yhi)) continue;
+            if (WRITE) {
+                const double dx0 = __dadd_rn(__dmul_rn((double)ic, g.shear[1]), __dmul_rn((double)ib, g.shear[0]));
+                const int i = step_int(__dmul_rn(__dadd_rn(p.x, dx0), g.usp[0]));
+                const int ia = (i < 0 || i >= g.un[0]) ? -step_div(i, g.un[0]) : 0;
+                const double dx = __dadd_rn(dx0, __dmul_rn((double)ia, g.len[0]));
+                const double c[3] = {__dadd_rn(p.x, dx), y, z};
+                const int t = nin + base + cnt;
+                rem_out[t] = make_double4(c[0], c[1], c[2], p.w);
+                gkey_out[t] = engine_key(g, c);
+                idx_out[t] = t;
+                img_src[base + cnt] = src;
+            }
+            cnt++;
+        }
+    }
+    return cnt;
+}
+
+__global__ void image_count_kernel(Geometry g, int n, const double4 *rem, int *count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    count[i] = images_of<false>(g, rem[i], i, 0, 0, nullptr, nullptr, nullptr, nullptr);
+}
+
+__global__ void image_write_kernel(Geometry g, int n, const double4 *rem, const int *offset, int nin,
+                                   double4 *rem_out, unsigned *gkey_out, int *idx_out, int *img_src) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    images_of<true>(g, rem[i], i, nin, offset[i], rem_out, gkey_out, idx_out, img_src);
+}
+
+__global__ void cell_list_kernel(const int *outpos, int nengine, int *list) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nengine) return;
+    const int o = outpos[k];
+    if (o >= 0) list[o] = k;
 }
 
 // The whole of put()'s binning for one small container in one CTA: remap,
@@ -305,24 +403,55 @@ cudaError_t launch_ghost_setup(const Geometry &g, int n, const double4 *q, int b
     return cudaGetLastError();
 }
 
-cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
+cudaError_t launch_gather(const Geometry &g, int nkept, int nengine, int nin, const int *img_src,
+                          const int *uorder, const int *gorder,
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
                           int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl,
                           int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
                           double *res_rad, cudaStream_t s) {
     int threads = 256;
-    if (nkept == 0) {
+    if (nengine == 0) {
         empty_bstart_kernel<<<(nblocks + 1 + threads - 1) / threads, threads, 0, s>>>(bstart, nblocks);
         note_launch();
         return cudaGetLastError();
     }
-    int blocks = (nkept + threads - 1) / threads;
-    loop_order_kernel<<<blocks, threads, 0, s>>>(uorder, nkept, ids_in, rem, outpos_by_input, res_ids, res_pos,
-                                                  res_rad);
+    if (nkept > 0) {
+        loop_order_kernel<<<(nkept + threads - 1) / threads, threads, 0, s>>>(uorder, nkept, ids_in, rem,
+                                                                              outpos_by_input, res_ids, res_pos,
+                                                                              res_rad);
+        note_launch();
+    }
+    gather_kernel<<<(nengine + threads - 1) / threads, threads, 0, s>>>(g, nengine, nin, img_src, gorder,
+                                                                        gkey_sorted, rem, ids_in, outpos_by_input,
+                                                                        p64, lffh, lffl, pid, outpos, gblock,
+                                                                        bstart, nblocks);
     note_launch();
-    gather_kernel<<<blocks, threads, 0, s>>>(g, nkept, gorder, gkey_sorted, rem, ids_in, outpos_by_input, p64,
-                                             lffh, lffl, pid, outpos, gblock, bstart, nblocks);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_image_count(const Geometry &g, int n, const double4 *rem, int *count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    image_count_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(g, n, rem, count);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_image_write(const Geometry &g, int n, const double4 *rem, const int *offset, int nin,
+                               double4 *rem_out, unsigned *gkey_out, int *idx_out, int *img_src, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    image_write_kernel<<<(n + threads - 1) / threads, threads, 0, s>>>(g, n, rem, offset, nin, rem_out, gkey_out,
+                                                                       idx_out, img_src);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, cudaStream_t s) {
+    if (nengine <= 0) return cudaSuccess;
+    const int threads = 256;
+    cell_list_kernel<<<(nengine + threads - 1) / threads, threads, 0, s>>>(outpos, nengine, list);
     note_launch();
     return cudaGetLastError();
 }

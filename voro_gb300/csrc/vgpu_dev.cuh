@@ -51,6 +51,9 @@ static __device__ __noinline__ double4 plane64_from(const CellParams &P, double4
 // src/wall.cc:29-120; its nplane(x, y, z, rsq) is n = (x, y, z), h = rsq/2).
 // h = NaN: the reference adds no plane (a curved wall through the particle).
 static __device__ __forceinline__ double4 wall64(const WallSpec &W, double4 me) {
+    // a unit-cell face plane: the bisector of a lattice vector, the same for
+    // every particle (unitcell::unit_voro_apply, src/unitcell.cc:90-94)
+    if (W.type == kWallLattice) return make_double4(W.c[0], W.c[1], W.c[2], 0.5 * W.r);
     const double x = me.x, y = me.y, z = me.z;
     if (W.type == VGPU_WALL_PLANE) {
         const double dq = __dmul_rn(2.0, __dsub_rn(__dsub_rn(__dsub_rn(W.r, __dmul_rn(x, W.c[0])), __dmul_rn(y, W.c[1])),
@@ -95,7 +98,8 @@ static __device__ __forceinline__ double4 face64(const CellParams &P, double4 me
     const bool hiside = f & 1;
     const double xa = ax == 0 ? me.x : (ax == 1 ? me.y : me.z);
     double h;
-    if (P.g.unit_cell || P.g.per[ax]) h = 0.5 * P.g.len[ax];
+    if (P.g.unit_cell) h = P.g.half[ax];
+    else if (P.g.per[ax]) h = 0.5 * P.g.len[ax];
     else h = hiside ? __dsub_rn(P.g.hi[ax], xa) : -__dsub_rn(P.g.lo[ax], xa);
     const double n = hiside ? 1.0 : -1.0;
     return make_double4(ax == 0 ? n : 0.0, ax == 1 ? n : 0.0, ax == 2 ? n : 0.0, h);

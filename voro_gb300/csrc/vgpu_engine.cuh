@@ -489,7 +489,12 @@ struct Engine {
         const unsigned bal = __ballot_sync(kFull, valid);
         if (valid) {
             const int slot = __popc(bal & ((1u << lane) - 1u));
-            S.u.c.ck[slot] = (float_key(0.0f) & ~63u) | (unsigned)slot;
+            // walls first; a unit-cell face plane among the neighbours at its
+            // lattice vector's distance, just ahead of the particle's own
+            // image there (whose plane is the same: the face keeps ID 0, as
+            // the unit cell's faces do in the reference)
+            const float dist = P.walls[lane].type == kWallLattice ? 0.999f * (float)P.walls[lane].r : 0.0f;
+            S.u.c.ck[slot] = (float_key(dist) & ~63u) | (unsigned)slot;
             S.u.c.cj[slot] = -1;
             S.u.c.cs[slot] = 6 + lane;
             S.u.c.cpid[slot] = P.walls[lane].id;

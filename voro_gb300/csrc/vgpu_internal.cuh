@@ -22,10 +22,19 @@ struct Geometry {
     int kind;           // VGPU_CONTAINER .. VGPU_CONTAINER_PERIODIC_POLY
     int poly;           // radical (power) tessellation
     int unit_cell;      // periodic kinds: initial cell is the unit Voronoi cell
-    int per[3];         // periodic flags per axis
-    double lo[3];       // domain lower corner (container: ax,ay,az; periodic kinds: 0)
-    double len[3];      // domain lengths (bx-ax, ...)
+    // Sheared container_periodic (bxy, bxz or byz != 0): the y and z images
+    // are stored as particles of ghost layers below and above the primary
+    // domain (as container_periodic_base keeps them), so the engine grid
+    // is periodic in x only and open in y and z; the initial cell is the
+    // box of half extents half[] cut by the unit cell's face planes.
+    int tric;
+    int per[3];         // periodic flags per axis (of the engine grid)
+    double lo[3];       // engine region lower corner (container: ax,ay,az; periodic kinds: 0, or the ghost layers' lower corner)
+    double len[3];      // domain lengths (bx-ax, ...); periodic kinds: bx, by, bz
     double hi[3];       // domain upper corner as given (bx, by, bz)
+    double ext[3];      // engine region extents from lo (len, or with the ghost layers)
+    double shear[3];    // bxy, bxz, byz (periodic kinds)
+    double half[3];     // unit_cell kinds: half extents of the initial box
     // reference block grid: loop order and put_remap semantics
     int un[3];          // nx, ny, nz
     double ubox[3];     // boxx = (bx-ax)/nx  (src/container.cc:31)
@@ -98,6 +107,10 @@ struct WallSpec {
     double asi, gra, sang, cang;
 };
 constexpr int kMaxWalls = 32;   // one lane each when they are applied
+// Internal wall type: a face plane of the unit Voronoi cell of a sheared
+// periodic box, n = c (the lattice vector), h = r/2 (r = |c|^2), relative to
+// the particle; staged with the neighbour candidates at distance r.
+constexpr int kWallLattice = 100;
 
 struct CellParams {
     Geometry g;
@@ -182,12 +195,24 @@ struct BinParams {
     int *idx;            // identity 0..n-1
 };
 cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s);
-cudaError_t launch_gather(const Geometry &g, int nkept, const int *uorder, const int *gorder,
+// nkept particles in loop order (uorder) and nengine engine entries in engine
+// order (gorder; an index i >= nin is image i - nin of particle img_src[i - nin])
+cudaError_t launch_gather(const Geometry &g, int nkept, int nengine, int nin, const int *img_src,
+                          const int *uorder, const int *gorder,
                           const unsigned *gkey_sorted, const double4 *rem, const int *ids_in,
                           int *outpos_by_input, double4 *p64, float4 *lffh, float4 *lffl,
                           int *pid, int *outpos,
                           int *gblock, int *bstart, int nblocks, int *res_ids, double *res_pos,
                           double *res_rad, cudaStream_t s);
+// Sheared periodic boxes: the images of the n particles (remapped positions
+// rem) that lie in the ghost layers; count per particle, then written from
+// their offsets (exclusive scan of the counts) to rem_out/gkey_out/idx_out at
+// nin + offset, with their source particle in img_src.
+cudaError_t launch_image_count(const Geometry &g, int n, const double4 *rem, int *count, cudaStream_t s);
+cudaError_t launch_image_write(const Geometry &g, int n, const double4 *rem, const int *offset, int nin,
+                               double4 *rem_out, unsigned *gkey_out, int *idx_out, int *img_src, cudaStream_t s);
+// The engine indices of the particles (not images), by loop-order slot.
+cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, cudaStream_t s);
 // One small container's binning in one CTA (batches): at most kSmallBinMax particles.
 constexpr int kSmallBinMax = 4096;
 constexpr int kSmallBinThreads = 512;

@@ -18,9 +18,12 @@
 // images as stored particles of its ghost blocks (put_image,
 // src/container_prd.cc:766-774: p + image * length), so along y and z the
 // distance and the returned position start from that image position; x is
-// wrapped by shifting the point, as for the flag-periodic container.  Exact
-// ties keep the first value found in this search order, which may differ
-// from the reference's.
+// wrapped by shifting the point, as for the flag-periodic container.  A
+// sheared box stores its y and z images as engine entries (the ghost layers),
+// so only x wraps; the answer is the stored image plus the point's image
+// displacement ak*c + aj*b + ai*a in the reference's order.  Exact ties keep
+// the first value found in this search order, which may differ from the
+// reference's.
 #include "vgpu_dev.cuh"
 
 namespace vgpu {
@@ -65,7 +68,7 @@ __device__ __forceinline__ void scan_block(const CellParams &P, const int eb[3],
     const int s0 = P.a.bstart[b], s1 = P.a.bstart[b + 1];
     // the point shifted by the image (or, for container_periodic's y and z,
     // the particle's image built as the reference stores it)
-    const bool ghost = g.kind == VGPU_CONTAINER_PERIODIC || g.kind == VGPU_CONTAINER_PERIODIC_POLY;
+    const bool ghost = (g.kind == VGPU_CONTAINER_PERIODIC || g.kind == VGPU_CONTAINER_PERIODIC_POLY) && !g.tric;
     double q[3], sh[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -110,13 +113,24 @@ __global__ void locate_kernel(const __grid_constant__ CellParams P, int n, const
                 }
             }
         }
-    } else {   // rectangular container_periodic: z, then y, then x
-        for (int ax = 2; ax >= 0; ax--) {
-            const int ci = step_int(__dmul_rn(c[ax], g.usp[ax]));
-            if (ci < 0 || ci >= g.un[ax]) {
-                a[ax] = step_div(ci, g.un[ax]);
-                c[ax] = __dsub_rn(c[ax], __dmul_rn((double)a[ax], g.len[ax]));
-            }
+    } else {   // container_periodic: z, then y, then x, along the lattice vectors
+        int ci = step_int(__dmul_rn(c[2], g.usp[2]));
+        if (ci < 0 || ci >= g.un[2]) {
+            a[2] = step_div(ci, g.un[2]);
+            c[2] = __dsub_rn(c[2], __dmul_rn((double)a[2], g.len[2]));
+            c[1] = __dsub_rn(c[1], __dmul_rn((double)a[2], g.shear[2]));
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)a[2], g.shear[1]));
+        }
+        ci = step_int(__dmul_rn(c[1], g.usp[1]));
+        if (ci < 0 || ci >= g.un[1]) {
+            a[1] = step_div(ci, g.un[1]);
+            c[1] = __dsub_rn(c[1], __dmul_rn((double)a[1], g.len[1]));
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)a[1], g.shear[0]));
+        }
+        ci = step_int(__dmul_rn(c[0], g.usp[0]));
+        if (ci < 0 || ci >= g.un[0]) {
+            a[0] = step_div(ci, g.un[0]);
+            c[0] = __dsub_rn(c[0], __dmul_rn((double)a[0], g.len[0]));
         }
     }
     Best B;
@@ -174,6 +188,15 @@ __global__ void locate_kernel(const __grid_constant__ CellParams P, int n, const
     const double pv[3] = {p.x, p.y, p.z};
     found[i] = 1;
     pid[i] = P.a.pid[B.j];
+    if (g.tric) {   // a stored image, x wrapped by the block search; then the point's images
+        rxyz[3 * i] = __dadd_rn(__dadd_rn(__dadd_rn(p.x, __dmul_rn((double)a[2], g.shear[1])),
+                                          __dmul_rn((double)a[1], g.shear[0])),
+                                __dmul_rn((double)(a[0] + B.img[0]), g.len[0]));
+        rxyz[3 * i + 1] = __dadd_rn(__dadd_rn(p.y, __dmul_rn((double)a[2], g.shear[2])),
+                                    __dmul_rn((double)a[1], g.len[1]));
+        rxyz[3 * i + 2] = __dadd_rn(p.z, __dmul_rn((double)a[2], g.len[2]));
+        return;
+    }
     const bool ghost = g.kind == VGPU_CONTAINER_PERIODIC || g.kind == VGPU_CONTAINER_PERIODIC_POLY;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {

@@ -44,6 +44,32 @@ def port():
 
 
 @pytest.mark.gpu
+def test_sheared_box_full_size_invariants(gpu):
+    """A 1M-particle sheared periodic box (images stored in ghost layers):
+    volumes tile the box, Euler's relation, a symmetric neighbour relation,
+    and the MIXED and FP64 engines agree on every cell's topology."""
+    w = W.sheared_periodic(n=1_000_000, L=100.0 * (1 / 4) ** (1 / 3))
+    res = {}
+    for mode in ("mixed", "fp64"):
+        con = vg.from_workload(w, mode=mode)
+        con.compute_all_cells()
+        st = con.stats()
+        assert st["failed_cells"] == 0 and st["marginal_cells"] == 0
+        r = con.cells()
+        vbox = G.box_volume(w)
+        assert abs(con.sum_cell_volumes() - vbox) <= 1e-9 * vbox
+        assert np.all(r.ok)
+        assert np.array_equal(r.nv, 2 * r.nf - 4), "Euler relation V = 2F - 4"
+        assert _symmetric(r), "neighbour relation not symmetric"
+        res[mode] = r
+    a, b = res["mixed"], res["fp64"]
+    assert np.array_equal(a.ids, b.ids) and np.array_equal(a.pos, b.pos)
+    assert np.array_equal(a.nf, b.nf) and np.array_equal(a.nv, b.nv)
+    assert np.array_equal(a.nb_off, b.nb_off) and np.array_equal(a.nb, b.nb)
+    assert (np.abs(a.vol - b.vol) / b.vol).max() <= 1e-10
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", list(CASES))
 def test_full_size_invariants_and_sample_parity(gpu, port, name):
     make, mode = CASES[name]

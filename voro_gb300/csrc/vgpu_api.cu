@@ -186,6 +186,8 @@ struct vgpu_container {
         gh_cnt, gh_vol, gh_cen, gh_nf, gh_nv, gh_mr2, gh_flags, gh_nb, gh_nb_ovf, gh_nb_off, gh_nb_out, gh_poly,
         gh_poly_off;
     std::vector<WallSpec> lattice;  // sheared periodic boxes: the unit cell's face planes (after the walls)
+    double full_lo[3] = {0, 0, 0}, full_ext[3] = {0, 0, 0};   // ... their ghost layers at the reference's depth
+    bool tric_thin = false;         // the last binning stored thinner ghost layers
     int nengine = 0;                // engine entries of the last binning: the particles, then any images
     DevBuf x_rem, x_gkey, x_idx, x_kalt, x_valt, img_cnt, img_off, img_src, cell_list;   // images (sheared boxes)
     std::vector<WallSpec> walls;    // walls, in the order added
@@ -405,6 +407,10 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
                 h->lattice.push_back(w);
             }
             h->walls_dirty = true;
+            for (int a = 0; a < 3; a++) {
+                h->full_lo[a] = g.lo[a];
+                h->full_ext[a] = g.ext[a];
+            }
         } else {
             // unit_voro.max_radius_squared() of the rectangular unit cell
             // (src/container_prd.cc:32), in the reference's doubled coordinates
@@ -697,7 +703,12 @@ int upload_walls(vgpu_container *h) {
     return VGPU_OK;
 }
 
-int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
+// thin: a sheared periodic box may store its images only kThinLayers mean
+// particle spacings deep (a compute checks afterwards that every cell's reach
+// stayed inside; see reach_check); else at the reference's depth.
+constexpr double kThinLayers = 8.0;
+
+int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
     if (int rc = upload_walls(h)) return rc;
     cudaStream_t s = h->stream;
@@ -706,6 +717,20 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp) {
     Geometry &g = h->g;
     memset(&h->stats, 0, sizeof(h->stats));
     h->computed = false;
+    if (g.tric) {
+        h->tric_thin = false;
+        const double sp = std::cbrt(g.len[0] * g.len[1] * g.len[2] / (double)std::max<int64_t>(n64, 1));
+        for (int a = 1; a < 3; a++) {
+            g.lo[a] = h->full_lo[a];
+            g.ext[a] = h->full_ext[a];
+            const double d = kThinLayers * sp;
+            if (thin && d < -h->full_lo[a]) {
+                g.lo[a] = -d;
+                g.ext[a] = g.len[a] + 2.0 * d;
+                h->tric_thin = true;
+            }
+        }
+    }
     choose_engine_grid(g, n64, h->target_density);
     const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
     const int nub = g.un[0] * g.un[1] * g.un[2];
@@ -1164,14 +1189,39 @@ int finish_compute(vgpu_container *h, const Counters &c, float cell_ms) {
     return VGPU_OK;
 }
 
+int compute_cells(vgpu_container *h, int mode, bool thin);
+
 }  // namespace
 
 extern "C" {
 
 int vgpu_compute(vgpu_container *h, int mode) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    int rc = compute_cells(h, mode, true);
+    if (h->g.tric && h->tric_thin && (rc == VGPU_OK || rc == VGPU_ERR_CAPACITY)) {
+        // thin ghost layers: every cell's reach must lie inside them, else
+        // again at the reference's depth
+        int *flag = h->kept.as<int>() + 12;
+        VG_CUDA(cudaMemsetAsync(flag, 0, 4, h->stream));
+        VG_CUDA(launch_reach_check(h->g, h->nkept, h->r_pos.as<double>(), h->r_mr2.as<double>(),
+                                   h->r_flags.as<int>(), flag, h->stream));
+        int out = 0;
+        VG_CUDA(cudaMemcpyAsync(&out, flag, 4, cudaMemcpyDeviceToHost, h->stream));
+        VG_CUDA(cudaStreamSynchronize(h->stream));
+        if (out) rc = compute_cells(h, mode, false);
+    }
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+
+// One compute: binning (thin: a sheared box may store thin ghost layers),
+// the clipping passes and the finish kernel.
+int compute_cells(vgpu_container *h, int mode, bool thin) {
     CellParams cp;
-    int rc = prepare_cells(h, mode, cp);
+    int rc = prepare_cells(h, mode, cp, thin);
     if (rc != VGPU_OK) return rc;
     cudaStream_t s = h->stream;
     RecordStore &store = record_store(h->device);
@@ -1204,6 +1254,10 @@ int vgpu_compute(vgpu_container *h, int mode) {
     h->stats.finish_ms = fin_ms;
     return rc;
 }
+
+}  // namespace
+
+extern "C" {
 
 int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
@@ -1397,6 +1451,7 @@ int vgpu_compute_ghost_cells(vgpu_container *h, int mode, int64_t n, const doubl
     h->ghost_n = 0;
     if (n == 0) return VGPU_OK;
     CellParams cp;
+    if (h->g.tric && h->tric_thin) h->binned = false;   // images at the reference's depth
     if (!h->binned) {   // bin the particles as a compute would
         int rc = prepare_cells(h, mode, cp);
         if (rc != VGPU_OK) return rc;
@@ -1575,6 +1630,7 @@ int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int
     if (n == 0) return VGPU_OK;
     if (n > (int64_t)INT32_MAX / 4) return fail(VGPU_ERR_MEMORY, "too many query points");
     CellParams cp;
+    if (h->g.tric && h->tric_thin) h->binned = false;   // images at the reference's depth
     if (!h->binned) {   // bin the particles as a compute would (no cells computed)
         int rc = prepare_cells(h, VGPU_MIXED, cp);
         if (rc != VGPU_OK) return rc;

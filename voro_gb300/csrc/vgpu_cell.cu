@@ -110,6 +110,37 @@ cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const int *ov
     return cudaGetLastError();
 }
 
+namespace {
+
+// A cell of max vertex distance R can be cut only by particles within its
+// reach, 2R (R + sqrt(R^2 + rmax^2) for radical cells: a cutting particle j
+// has |v - q_j|^2 < R^2 + r_j^2 at some vertex v); all of those are stored
+// when the reach stays inside the ghost layers along y and z (x wraps).
+__global__ void reach_check_kernel(Geometry g, int n, const double *pos, const double *mr2, const int *flags,
+                                   int *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !(flags[i] & VGPU_CELL_OK)) return;
+    const double R = sqrt(mr2[i]);
+    const double reach = (g.poly ? R + sqrt(R * R + g.rmax * g.rmax) : 2.0 * R) * (1.0 + 1e-9) +
+                         1e-12 * (g.len[1] + g.len[2]);
+    bool inside = true;
+    for (int a = 1; a < 3; a++) {
+        const double p = pos[3 * i + a];
+        inside = inside && p - reach >= g.lo[a] && p + reach <= g.lo[a] + g.ext[a];
+    }
+    if (!inside) atomicExch(out, 1);
+}
+
+}  // namespace
+
+cudaError_t launch_reach_check(const Geometry &g, int n, const double *pos, const double *mr2, const int *flags,
+                               int *out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    reach_check_kernel<<<(n + 255) / 256, 256, 0, s>>>(g, n, pos, mr2, flags, out);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_sum_volumes(const double *vol, const int *flags, int n, double *out, cudaStream_t s) {
     sum_volumes_kernel<<<64, 256, 0, s>>>(vol, flags, n, out);
     note_launch();

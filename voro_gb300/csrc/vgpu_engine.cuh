@@ -483,8 +483,12 @@ struct Engine {
             const float nx = (float)q.x, ny = (float)q.y, nz = (float)q.z, h = (float)q.w;
             const float an = fabsf(nx) + fabsf(ny) + fabsf(nz);
             cd = make_float4(nx, ny, nz, h);
+            // rs (w): 0 for a wall, which every flush tests; a unit-cell face
+            // plane's |d|^2 (rounded down), so that a flush stops at it once
+            // the cell no longer reaches it, as at a particle
+            const float rs = P.walls[lane].type == kWallLattice ? 0.999f * (float)P.walls[lane].r : 0.0f;
             ce = make_float4(2.0f * kU32 * an, 2.0f * kU32 * fabsf(h),
-                             sqrtf(nx * nx + ny * ny + nz * nz) * (1.0f + 8.0f * kU32) + 2.0f * kU32 * an, 0.0f);
+                             sqrtf(nx * nx + ny * ny + nz * nz) * (1.0f + 8.0f * kU32) + 2.0f * kU32 * an, rs);
         }
         const unsigned bal = __ballot_sync(kFull, valid);
         if (valid) {
@@ -493,8 +497,7 @@ struct Engine {
             // lattice vector's distance, just ahead of the particle's own
             // image there (whose plane is the same: the face keeps ID 0, as
             // the unit cell's faces do in the reference)
-            const float dist = P.walls[lane].type == kWallLattice ? 0.999f * (float)P.walls[lane].r : 0.0f;
-            S.u.c.ck[slot] = (float_key(dist) & ~63u) | (unsigned)slot;
+            S.u.c.ck[slot] = (float_key(ce.w) & ~63u) | (unsigned)slot;
             S.u.c.cj[slot] = -1;
             S.u.c.cs[slot] = 6 + lane;
             S.u.c.cpid[slot] = P.walls[lane].id;

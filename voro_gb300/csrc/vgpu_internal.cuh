@@ -251,6 +251,10 @@ cudaError_t launch_compact_neighbors(const int *nf, const int *nb, const int *ov
 cudaError_t launch_nf_to_ll(const int *nf, long long *out, int n, cudaStream_t s);
 cudaError_t exclusive_scan_ll(const long long *in, long long *out, int n, long long *tmp, cudaStream_t s);
 cudaError_t launch_sum_volumes(const double *vol, const int *flags, int n, double *out, cudaStream_t s);
+// Sheared boxes with thin ghost layers: *out = 1 if some kept cell (loop order:
+// stored position pos, max_radius_squared mr2 in real units) reaches past them.
+cudaError_t launch_reach_check(const Geometry &g, int n, const double *pos, const double *mr2, const int *flags,
+                               int *out, cudaStream_t s);
 void box_tables(unsigned tri[8], unsigned adj[8]);
 // vgpu_locate.cu
 cudaError_t launch_locate(const CellParams &cp, int n, const double *qxyz, int *found, int *pid, double *rxyz,

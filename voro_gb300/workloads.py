@@ -64,6 +64,19 @@ def periodic_cube(n=4_000_000, L=100.0, seed=1002, grid=None, kind=KIND_PERIODIC
     return _pack(KIND_CONTAINER, (0, L, 0, L, 0, L), grid, (True,) * 3, xyz)
 
 
+def sheared_periodic(n=4_000_000, L=100.0, shear=(0.3, 0.2, -0.25), seed=1006, grid=None):
+    """container_periodic of lattice vectors (L,0,0), (sxy L, L, 0),
+    (sxz L, syz L, L) (shear = (sxy, sxz, syz)), positions uniform over the
+    box [0, L)^3 (a fundamental domain of the lattice)."""
+    rng = np.random.default_rng(seed)
+    xyz = rng.random((n, 3)) * L
+    if grid is None:
+        g = max(1, int(round((n / 5.0) ** (1.0 / 3.0))))
+        grid = (g, g, g)
+    sxy, sxz, syz = shear
+    return _pack(KIND_PERIODIC, (L, sxy * L, L, sxz * L, syz * L, L), grid, (True,) * 3, xyz)
+
+
 def radical_box(n=2_000_000, L=200.0, seed=1003, grid=None):
     """container_poly on [0,L]^3 with log-normal radii (median 0.5, sigma 0.3)
     clipped to [0.1, 1.5]."""

@@ -394,9 +394,10 @@ int setup_geometry(vgpu_container *h, int kind, const double geom[6], const int 
             g.lo[2] = -(ez * g.ubox[2]);
             g.ext[1] = (g.un[1] + 2 * ey) * g.ubox[1];
             g.ext[2] = (g.un[2] + 2 * ez) * g.ubox[2];
-            // the initial box: the unit cell with room to spare (its own
-            // face planes cut it to the unit cell)
-            for (int a = 0; a < 3; a++) g.half[a] = 1.25 * mab[a];
+            // the initial box: just larger than the unit cell (its own face
+            // planes cut it to the unit cell); the FP32 side tests' error
+            // bounds grow with the vertices' distance, so no larger
+            for (int a = 0; a < 3; a++) g.half[a] = 1.02 * mab[a];
             for (const auto &f : U.faces) {
                 WallSpec w;
                 memset(&w, 0, sizeof(w));
@@ -906,9 +907,12 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
                           h->lffl.as<float4>(), h->pid.as<int>(),
                           h->outpos.as<int>(), h->gblock.as<int>(), h->bstart.as<int>(), nblocks,
                           h->r_ids.as<int>(), h->r_pos.as<double>(), h->r_rad.as<double>(), s));
-    if (g.tric) {   // the cells to compute: the particles, not their images
+    if (g.tric) {   // the cells to compute: the particles, not their images, in engine order
         VG_CUDA(h->cell_list.ensure(nk * 4));
-        VG_CUDA(launch_cell_list(h->outpos.as<int>(), nengine, h->cell_list.as<int>(), s));
+        VG_CUDA(h->scan_tmp.ensure((scan_tmp_ints(nengine) + 64) * 8));
+        // (the sort buffers x_idx and x_gkey are free once the gather has run)
+        VG_CUDA(launch_cell_list(h->outpos.as<int>(), nengine, h->cell_list.as<int>(), h->x_idx.as<int>(),
+                                 h->x_gkey.as<int>(), h->scan_tmp.as<int>(), h->scan_tmp.bytes / 4, s));
     }
     cudaEventRecord(h->ev[1], s);
 
@@ -958,7 +962,12 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     for (int i = 0; i <= cp.ngroups; i++) cp.group_start[i] = ot.group_start[i];
     for (int i = 0; i < cp.ngroups; i++) cp.group_lb2[i] = ot.group_lb2[i];
     box_tables(cp.box_tri, cp.box_adj);
-    cp.nwalls = (int)(h->walls.size() + h->lattice.size());
+    // A sheared box binned with thin ghost layers leaves out the unit cell's
+    // face planes: a cell they could cut reaches half a lattice vector, past
+    // the layers, and the reach check reruns the compute at full depth (with
+    // them); a lattice vector shorter than the layers' depth has its image
+    // stored, whose plane is the same.
+    cp.nwalls = (int)(h->walls.size() + (h->g.tric && h->tric_thin ? 0 : h->lattice.size()));
     cp.walls = cp.nwalls == 0 ? nullptr : h->walls_dev.as<WallSpec>();
 }
 

@@ -226,11 +226,14 @@ __global__ void image_write_kernel(Geometry g, int n, const double4 *rem, const 
     images_of<true>(g, rem[i], i, nin, offset[i], rem_out, gkey_out, idx_out, img_src);
 }
 
-__global__ void cell_list_kernel(const int *outpos, int nengine, int *list) {
+__global__ void particle_flag_kernel(const int *outpos, int nengine, int *flag) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nengine) return;
-    const int o = outpos[k];
-    if (o >= 0) list[o] = k;
+    if (k < nengine) flag[k] = outpos[k] >= 0 ? 1 : 0;
+}
+
+__global__ void cell_list_kernel(const int *outpos, const int *slot, int nengine, int *list) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nengine && outpos[k] >= 0) list[slot[k]] = k;
 }
 
 // The whole of put()'s binning for one small container in one CTA: remap,
@@ -448,10 +451,15 @@ cudaError_t launch_image_write(const Geometry &g, int n, const double4 *rem, con
     return cudaGetLastError();
 }
 
-cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, cudaStream_t s) {
+cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, int *flag, int *slot, int *scan_tmp,
+                             size_t scan_tmp_ints_avail, cudaStream_t s) {
     if (nengine <= 0) return cudaSuccess;
-    const int threads = 256;
-    cell_list_kernel<<<(nengine + threads - 1) / threads, threads, 0, s>>>(outpos, nengine, list);
+    const int threads = 256, blocks = (nengine + threads - 1) / threads;
+    particle_flag_kernel<<<blocks, threads, 0, s>>>(outpos, nengine, flag);
+    note_launch();
+    cudaError_t e = exclusive_scan_int(flag, slot, nengine, scan_tmp, scan_tmp_ints_avail, s);
+    if (e != cudaSuccess) return e;
+    cell_list_kernel<<<blocks, threads, 0, s>>>(outpos, slot, nengine, list);
     note_launch();
     return cudaGetLastError();
 }

@@ -211,8 +211,10 @@ cudaError_t launch_gather(const Geometry &g, int nkept, int nengine, int nin, co
 cudaError_t launch_image_count(const Geometry &g, int n, const double4 *rem, int *count, cudaStream_t s);
 cudaError_t launch_image_write(const Geometry &g, int n, const double4 *rem, const int *offset, int nin,
                                double4 *rem_out, unsigned *gkey_out, int *idx_out, int *img_src, cudaStream_t s);
-// The engine indices of the particles (not images), by loop-order slot.
-cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, cudaStream_t s);
+// The engine indices of the particles (not images), in engine order (flag and
+// slot: nengine ints of scratch each; scan_tmp: scratch of exclusive_scan_int).
+cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, int *flag, int *slot, int *scan_tmp,
+                             size_t scan_tmp_ints_avail, cudaStream_t s);
 // One small container's binning in one CTA (batches): at most kSmallBinMax particles.
 constexpr int kSmallBinMax = 4096;
 constexpr int kSmallBinThreads = 512;

@@ -242,6 +242,13 @@ int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t
  * Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
 
+/* Sheared container_periodic: depth of the ghost layers of images a compute
+ * stores first, in mean particle spacings (0 = default 8; < 0: always the
+ * reference's depth).  A compute whose cells reach past them is redone at the
+ * reference's depth, so the results never depend on it; deeper layers cost
+ * memory and binning time, shallower ones make the rerun likelier. */
+int vgpu_set_ghost_depth(vgpu_container *h, double spacings);
+
 /* ---- batches: many containers computed by one persistent launch ----
  * The reference computes containers one at a time (compute_all_cells per
  * container, src/container.cc:438-453).  A batch bins every member container

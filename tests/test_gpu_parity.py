@@ -61,3 +61,19 @@ def test_autotune_keeps_results(gpu):
     assert 0.3 <= d <= 3.0 and ms > 0
     errs = G.compare_cells(con.cells(), z, *TOL["mixed"], label="autotuned")
     assert not errs, "\n".join(errs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("spacings", [0.5, -1.0])
+@pytest.mark.parametrize("name", ["tric_dyadic_1500", "tric_poly_1000", "tric_skew_800"])
+def test_sheared_ghost_depth_never_changes_cells(gpu, name, spacings):
+    """Image layers half a spacing deep (so most boundary cells reach past
+    them and the compute is redone at the reference's depth), and always the
+    reference's depth: the same cells as the reference either way."""
+    w, z = G.load(name)
+    con = vg.from_workload(w, mode="mixed")
+    con.set_ghost_depth(spacings)
+    con.compute_all_cells()
+    errs = G.compare_cells(con.cells(), z, *TOL["mixed"], label=f"{name}/depth {spacings}")
+    assert not errs, "\n".join(errs)
+    assert con.stats()["failed_cells"] == 0

@@ -48,7 +48,7 @@ EXPORTED = [
     "vgpu_version", "vgpu_device_count", "vgpu_last_error", "vgpu_container_create", "vgpu_container_destroy",
     "vgpu_put", "vgpu_put_device", "vgpu_clear", "vgpu_compute", "vgpu_sum_cell_volumes", "vgpu_get_stats",
     "vgpu_num_cells", "vgpu_num_neighbors", "vgpu_get_cells", "vgpu_get_neighbors", "vgpu_device_results",
-    "vgpu_set_tuning", "vgpu_phase_cycles", "vgpu_get_radii",
+    "vgpu_set_tuning", "vgpu_set_ghost_depth", "vgpu_phase_cycles", "vgpu_get_radii",
     "vgpu_sum_volumes_noalloc", "vgpu_batch_create", "vgpu_batch_add", "vgpu_batch_compute",
     "vgpu_batch_get_stats", "vgpu_batch_destroy", "vgpu_batch_set_record_budget", "vgpu_batch_waves",
     "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells", "vgpu_compute_ghost_cells",
@@ -118,6 +118,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_get_neighbors.argtypes = [vp, vp, vp]
     lib.vgpu_device_results.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
+    lib.vgpu_set_ghost_depth.argtypes = [vp, ctypes.c_double]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
     lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
@@ -421,6 +422,13 @@ class _ContainerBase:
 
     def set_tuning(self, particles_per_block=0.0, warps_per_cta=0):
         _check(self._lib.vgpu_set_tuning(self._h, float(particles_per_block), int(warps_per_cta)))
+        self._dirty = True
+
+    def set_ghost_depth(self, spacings=0.0):
+        """Sheared periodic boxes: depth of the image layers a compute stores
+        first, in mean particle spacings (0: default 8; negative: always the
+        reference's depth).  Results never depend on it."""
+        _check(self._lib.vgpu_set_ghost_depth(self._h, float(spacings)))
         self._dirty = True
 
     def _mode_code(self, mode):

@@ -188,6 +188,7 @@ struct vgpu_container {
     std::vector<WallSpec> lattice;  // sheared periodic boxes: the unit cell's face planes (after the walls)
     double full_lo[3] = {0, 0, 0}, full_ext[3] = {0, 0, 0};   // ... their ghost layers at the reference's depth
     bool tric_thin = false;         // the last binning stored thinner ghost layers
+    double ghost_spacings = 8.0;    // their depth in mean particle spacings (< 0: never thin)
     int nengine = 0;                // engine entries of the last binning: the particles, then any images
     DevBuf x_rem, x_gkey, x_idx, x_kalt, x_valt, img_cnt, img_off, img_src, cell_list;   // images (sheared boxes)
     std::vector<WallSpec> walls;    // walls, in the order added
@@ -668,6 +669,17 @@ int vgpu_point_inside_walls(vgpu_container *h, double x, double y, double z, int
     return VGPU_OK;
 }
 
+int vgpu_set_ghost_depth(vgpu_container *h, double spacings) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (!std::isfinite(spacings)) return fail(VGPU_ERR_ARG, "ghost depth must be finite");
+    const double v = spacings == 0 ? 8.0 : spacings;
+    if (v != h->ghost_spacings) {
+        h->ghost_spacings = v;
+        h->binned = false;
+    }
+    return VGPU_OK;
+}
+
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta) {
     if (!h) return fail(VGPU_ERR_ARG, "null handle");
     if (particles_per_block > 0 && particles_per_block != h->target_density) {
@@ -704,11 +716,9 @@ int upload_walls(vgpu_container *h) {
     return VGPU_OK;
 }
 
-// thin: a sheared periodic box may store its images only kThinLayers mean
+// thin: a sheared periodic box may store its images only ghost_spacings mean
 // particle spacings deep (a compute checks afterwards that every cell's reach
-// stayed inside; see reach_check); else at the reference's depth.
-constexpr double kThinLayers = 8.0;
-
+// stayed inside; see reach_check_kernel); else at the reference's depth.
 int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
     if (int rc = upload_walls(h)) return rc;
@@ -724,8 +734,8 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
         for (int a = 1; a < 3; a++) {
             g.lo[a] = h->full_lo[a];
             g.ext[a] = h->full_ext[a];
-            const double d = kThinLayers * sp;
-            if (thin && d < -h->full_lo[a]) {
+            const double d = h->ghost_spacings * sp;
+            if (thin && h->ghost_spacings >= 0 && d < -h->full_lo[a]) {
                 g.lo[a] = -d;
                 g.ext[a] = g.len[a] + 2.0 * d;
                 h->tric_thin = true;

@@ -452,7 +452,17 @@ class container_gpu_base {
     container_gpu_base(int kind, const double geom[6], const int grid[3], const int per[3])
         : poly_(kind == VGPU_CONTAINER_POLY || kind == VGPU_CONTAINER_PERIODIC_POLY) {
         gpu_detail::check(vgpu_container_create(&h_, kind, geom, grid, per), "container");
+        for (int i = 0; i < 6; i++) geom_[i] = geom[i];
     }
+
+    // container_base::point_inside (src/container.cc:484-487): inside the
+    // box (every axis, periodic or not) and inside every wall
+    bool point_inside_box_and_walls(double x, double y, double z) {
+        if (x < geom_[0] || x > geom_[1] || y < geom_[2] || y > geom_[3] || z < geom_[4] || z > geom_[5])
+            return false;
+        return point_inside_walls(x, y, z);
+    }
+    double geom_[6];
 
     void stage(int n, double x, double y, double z, double r) {
         ids_in_.push_back(n);
@@ -695,6 +705,7 @@ class container : public container_gpu_base {
     void put(int n, double x, double y, double z) { stage(n, x, y, z, default_radius); }
     void import(FILE *fp = stdin) { import_stream(fp, false); }
     void import(const char *filename) { import_file(filename, false); }
+    bool point_inside(double x, double y, double z) { return point_inside_box_and_walls(x, y, z); }
 };
 
 // container_poly (src/container.hh:511-513)
@@ -707,6 +718,7 @@ class container_poly : public container_gpu_base {
     void put(int n, double x, double y, double z, double r) { stage(n, x, y, z, r); }
     void import(FILE *fp = stdin) { import_stream(fp, true); }
     void import(const char *filename) { import_file(filename, true); }
+    bool point_inside(double x, double y, double z) { return point_inside_box_and_walls(x, y, z); }
 };
 
 // container_periodic (src/container_prd.hh:213-216): the periodic

@@ -47,3 +47,19 @@ def test_point_inside_walls(gpu):
     expect = (pa >= 0) & (rad2 < pa * pa) & (p[:, 2] < 1.8)
     got = np.array([con.point_inside_walls(*q) for q in p])
     assert np.array_equal(got, expect)
+
+
+@pytest.mark.gpu
+def test_point_inside_box_and_walls(gpu):
+    """container_base::point_inside (src/container.cc:484-487): the box
+    first, then the walls."""
+    w, z = G.load("wall_cone_2000")
+    con = vg.from_workload(w, mode="mixed")
+    g = w["geom"]
+    rng = np.random.default_rng(5)
+    q = rng.uniform([g[0] - 0.5, g[2] - 0.5, g[4] - 0.5], [g[1] + 0.5, g[3] + 0.5, g[5] + 0.5], size=(400, 3))
+    in_box = np.all((q >= [g[0], g[2], g[4]]) & (q <= [g[1], g[3], g[5]]), axis=1)
+    walls = np.array([con.point_inside_walls(*p) for p in q])
+    got = np.array([con.point_inside(*p) for p in q])
+    assert np.array_equal(got, in_box & walls)
+    assert in_box.any() and (~in_box).any() and (in_box & walls).any()

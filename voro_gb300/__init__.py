@@ -364,6 +364,17 @@ class _ContainerBase:
         _check(self._lib.vgpu_point_inside_walls(self._h, float(x), float(y), float(z), ctypes.byref(out)))
         return bool(out.value)
 
+    def point_inside(self, x, y, z):
+        """container_base::point_inside (src/container.cc:484-487): inside
+        the box on every axis, periodic or not, and inside every wall
+        (container and container_poly)."""
+        if self.kind not in (KIND_CONTAINER, KIND_CONTAINER_POLY):
+            raise AttributeError("point_inside belongs to container and container_poly")
+        g = self.geom
+        if x < g[0] or x > g[1] or y < g[2] or y > g[3] or z < g[4] or z > g[5]:
+            return False
+        return self.point_inside_walls(x, y, z)
+
     # ---- import: src/container.cc:333-376, src/container_prd.cc:400-433
     def import_file(self, f):
         """container::import: entries "id x y z" ("id x y z r" for the

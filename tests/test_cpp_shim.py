@@ -102,7 +102,7 @@ def test_shim_reports_errors_like_the_reference(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["unit_cube_1000", "periodic_2000", "radical_1200", "periodic_poly_800",
-                                  "sparse_dropped_40"])
+                                  "sparse_dropped_40", "tric_dyadic_1500", "tric_poly_1000"])
 def test_shim_matches_reference_records(gpu, tmp_path, name):
     exe = _compile(tmp_path)
     w, z = G.load(name)

@@ -18,11 +18,15 @@ namespace {
 // point of the face), in FP64 for the FP64 engine and in float pairs for the
 // MIXED engine.  Optionally the polytope itself is written out.
 constexpr int kFinMaxV = 128;   // vertices (the 128-slot engine's capacity)
-constexpr int kFinMaxE = 192;   // edges (3 * kFinMaxV / 2)
 
+// One cell's shared arrays for cells of at most NV vertices (a whole warp:
+// 128; a 16-lane half: 64).  Planes: at most 64 either way (the record's
+// planes are numbered compactly, and a cell of 64 vertices has 34 faces).
+template <int NV>
 struct FinishShared {
-    unsigned tri[kFinMaxV];
-    unsigned adj[kFinMaxV];
+    static constexpr int kNV = NV;
+    unsigned tri[NV];
+    unsigned adj[NV];
     int psrc[kMaxPlanes], pshift[kMaxPlanes];
     int rep[kMaxPlanes];             // per face: its lowest vertex
     int ford[kMaxPlanes];            // per face: its vertex count
@@ -31,13 +35,20 @@ struct FinishShared {
     // (MIXED engine: vh + vl, see the edge sums)
     union {
         struct {
-            double vx[kFinMaxV], vy[kFinMaxV], vz[kFinMaxV];
+            double vx[NV], vy[NV], vz[NV];
         } d;
         struct {
-            float vh[3][kFinMaxV], vl[3][kFinMaxV];
+            float vh[3][NV], vl[3][NV];
         } f;
     } v;
-    unsigned stage[kFinMaxE];        // owned edges (t < u)
+    unsigned stage[3 * NV / 2];      // owned edges (t < u)
+};
+
+// A warp's shared arrays: one cell of up to 128 vertices, or two of up to 64
+// (one per 16-lane half) in the same space.
+union FinishWarp {
+    FinishShared<128> whole;
+    FinishShared<64> half[2];
 };
 
 // ------------------------------------------------------------------ float-pair arithmetic
@@ -101,7 +112,8 @@ __device__ __forceinline__ FF ff_from_double(double d) {
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 __device__ __forceinline__ double pow2d(int k) { return __hiloint2double((1023 + k) << 20, 0); }
 
-__device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FinishShared &F, double4 me, int p) {
+template <class FS>
+__device__ __forceinline__ double4 plane64_rec(const CellParams &P, const FS &F, double4 me, int p) {
     const int src = F.psrc[p];
     if (src >= 0) return plane64_from(P, me, src, F.pshift[p]);
     return initial64(P, me, F.pshift[p]);
@@ -140,7 +152,8 @@ __device__ __forceinline__ PlaneFF plane_ff(const CellParams &P, int bk[3], floa
 // v + correction.  A nearly singular FP32 system (|D| <= 1e-3 of the product
 // of the normals' norms) is solved in FP64 from the FP64 planes instead,
 // rebuilt for it.
-__device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FinishShared &F, double4 me, unsigned t,
+template <class FS>
+__device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FS &F, double4 me, unsigned t,
                                                  float fx, float fy, float fz, FF &vx, FF &vy, FF &vz) {
     const int ia = tri_plane(t, 0), ib = tri_plane(t, 1), ic = tri_plane(t, 2);
     const float4 a = F.plh[ia], b = F.plh[ib], c = F.plh[ic];
@@ -244,7 +257,7 @@ __device__ __forceinline__ double rec_double(const unsigned *w) {
 // warp, one per half) for cells of at most 64 vertices.  Every collective is
 // reached by both halves of the warp whatever their cells.
 template <int MODE, int G>
-__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared &F, int k, int gl) {
+__device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<4 * G> &F, int k, int gl) {
     constexpr bool kFF = MODE == VGPU_MIXED;   // float-pair vertices and sums
     constexpr int VW = kFF ? 3 : 6;
     constexpr int SL = 4;   // vertex slots per lane: 128 vertices (G = 32) or 64 (G = 16)
@@ -554,12 +567,21 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared 
 }
 
 constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
+// CTAs kept resident per SM (the register bound of the launch): with 22 KB
+// of shared memory per CTA (a warp's two 16-lane cells share the space of
+// one 128-vertex cell) the 124 registers the kernel wants decide, 8 CTAs.
+// Measured on the 4M periodic box, finish kernel: 7 (no cap) 11.0 ms, 8
+// 11.3 ms, 9 (96 registers, spills) 12.5 ms; 12.3 ms with two full-size
+// cells per warp (31.7 KB per CTA, 7 CTAs).
+#ifndef VGPU_FIN_MIN_BLOCKS
+#define VGPU_FIN_MIN_BLOCKS 7
+#endif
 
 // Two cells per warp, one per 16-lane half, when both have at most 64
 // vertices (nearly always: their FP64 work then fills the lanes better);
 // otherwise the whole warp does one cell after the other.
 template <int MODE>
-__device__ __forceinline__ void finish_pair(const CellParams &P, FinishShared *F2, int k0, int k1, int lane) {
+__device__ __forceinline__ void finish_pair(const CellParams &P, FinishWarp &W, int k0, int k1, int lane) {
     const int half = lane >> 4, gl = lane & 15;
     const int mine = half ? k1 : k0;
     int nv = 0;
@@ -568,16 +590,16 @@ __device__ __forceinline__ void finish_pair(const CellParams &P, FinishShared *F
         if (off != kNoRecord) nv = (int)P.rec[off];
     }
     if (!__any_sync(kFull, nv > 64)) {
-        finish_record<MODE, 16>(P, F2[half], mine, gl);
+        finish_record<MODE, 16>(P, W.half[half], mine, gl);
     } else {
-        finish_record<MODE, 32>(P, F2[0], k0, lane);
-        finish_record<MODE, 32>(P, F2[0], k1, lane);
+        finish_record<MODE, 32>(P, W.whole, k0, lane);
+        finish_record<MODE, 32>(P, W.whole, k1, lane);
     }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(32 * kFinWarps) finish_kernel(const __grid_constant__ CellParams P) {
-    __shared__ FinishShared fsh[kFinWarps][2];
+__global__ void __launch_bounds__(32 * kFinWarps, VGPU_FIN_MIN_BLOCKS) finish_kernel(const __grid_constant__ CellParams P) {
+    __shared__ FinishWarp fsh[kFinWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int npairs = (P.ncells + 1) / 2;
     for (int pi = blockIdx.x * kFinWarps + wid; pi < npairs; pi += gridDim.x * kFinWarps) {
@@ -592,8 +614,8 @@ __global__ void __launch_bounds__(32 * kFinWarps) finish_kernel(const __grid_con
 // (global numbering as cell_batch_kernel); a pair never straddles two
 // containers.
 template <int MODE>
-__global__ void __launch_bounds__(32 * kFinWarps) finish_batch_kernel(const __grid_constant__ BatchParams B) {
-    __shared__ FinishShared fsh[kFinWarps][2];
+__global__ void __launch_bounds__(32 * kFinWarps, VGPU_FIN_MIN_BLOCKS) finish_batch_kernel(const __grid_constant__ BatchParams B) {
+    __shared__ FinishWarp fsh[kFinWarps];
     __shared__ __align__(16) unsigned char cpw[kFinWarps][(sizeof(CellParams) + 15) & ~(size_t)15];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     CellParams &P = *reinterpret_cast<CellParams *>(cpw[wid]);

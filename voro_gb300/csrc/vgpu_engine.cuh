@@ -1080,11 +1080,14 @@ struct Engine {
 #define VGPU_CTA_THREADS 128
 #endif
 constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
-// CTAs per SM of the other engines: the full mixed 64-slot engine keeps 3
-// (168 registers), the 128-slot and FP64 engines 2.
+// CTAs per SM of the other engines: the full mixed 64-slot engine keeps
+// VGPU_FULL_MIN_BLOCKS (3: 168 registers), the 128-slot and FP64 engines 2.
+#ifndef VGPU_FULL_MIN_BLOCKS
+#define VGPU_FULL_MIN_BLOCKS 3
+#endif
 template <int MODE, int K, bool LEAN>
 constexpr int min_blocks() {
-    return (MODE == VGPU_MIXED && K == 2) ? (LEAN ? VGPU_MIN_BLOCKS : 3) : 2;
+    return (MODE == VGPU_MIXED && K == 2) ? (LEAN ? VGPU_MIN_BLOCKS : VGPU_FULL_MIN_BLOCKS) : 2;
 }
 // Cells a warp takes from the work queue at a time (at most; fewer when the
 // launch has under four chunks per warp, so that small containers still

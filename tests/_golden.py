@@ -32,7 +32,8 @@ def load_ghost(name):
     """Ghost particles of fixture ``name`` (n x 4: x, y, z, r) and the
     reference's compute_ghost_cell records (npz fields ok, vol, cen, nf, nv,
     mrs, nb, nb_off)."""
-    z = np.load(os.path.join(HERE, f"ghost_{name}.npz"))
+    with np.load(os.path.join(HERE, f"ghost_{name}.npz")) as f:
+        z = {k: f[k] for k in f.files}
     return z["g"], z
 
 
@@ -110,7 +111,9 @@ def compare_custom_text(got, ref, rtol=2e-6, atol=1e-12):
 
 
 def load(name):
-    z = np.load(os.path.join(HERE, name + ".npz"))
+    # every array read once (an NpzFile decompresses on each access)
+    with np.load(os.path.join(HERE, name + ".npz")) as f:
+        z = {k: f[k] for k in f.files}
     w = {
         "kind": int(z["kind"]),
         "geom": tuple(float(v) for v in z["geom"]),

@@ -271,6 +271,9 @@ def main():
     if "--tric-only" in sys.argv:
         make_tric_fixtures(ref)
         return
+    if "--tric-large-only" in sys.argv:
+        make_tric_large_fixture(ref)
+        return
     for name, w in cases().items():
         make_cell_fixture(ref, name, w)
     make_poly_fixtures(ref, cases())
@@ -278,6 +281,16 @@ def main():
     make_ghost_fixtures(ref, cases())
     make_wall_fixtures(ref)
     make_tric_fixtures(ref)
+    make_tric_large_fixture(ref)
+
+
+# A larger sheared box (cells only): 20,000 particles, so that the first
+# compute's thin image layers hold (no rerun at the reference's depth).
+def make_tric_large_fixture(ref):
+    rng = np.random.default_rng(2207)
+    geom = (20.0, -6.3, 18.5, 7.1, 4.9, 17.2)
+    xyz = rng.uniform(-0.5, 1.5, size=(20000, 3)) * np.array([geom[0], geom[2], geom[5]])
+    make_cell_fixture(ref, "tric_large_20000", W._pack(W.KIND_PERIODIC, geom, (9, 9, 8), (True,) * 3, xyz))
 
 
 def make_tric_fixtures(ref):

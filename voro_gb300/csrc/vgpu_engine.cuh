@@ -469,7 +469,9 @@ struct Engine {
     //      6 + w; the search's first flush, which sorts them ahead of every
     //      particle candidate and in wall order, cuts with them through the
     //      one copy of the cutting code.  A wall that cuts the whole cell
-    //      deletes it (compute_cell false).
+    //      deletes it (compute_cell false).  A sheared periodic box binned
+    //      at the reference's depth adds the unit cell's face planes here
+    //      (type kWallLattice), sorted among the particle candidates.
     __device__ void apply_walls() {
         if (P.nwalls == 0) return;
         bool valid = false;

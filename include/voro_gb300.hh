@@ -308,6 +308,14 @@ class container_gpu_base {
         dirty_ = true;
     }
 
+    // Sheared container_periodic: depth of the image layers a compute stores
+    // first, in mean particle spacings (0: default; < 0: the reference's
+    // depth from the start); the cells never depend on it.
+    void set_ghost_depth(double spacings) {
+        gpu_detail::check(vgpu_set_ghost_depth(h_, spacings), "set_ghost_depth");
+        dirty_ = true;
+    }
+
     // container::clear (src/container.cc:385-387)
     void clear() {
         ids_in_.clear();

@@ -1095,7 +1095,9 @@ constexpr int min_blocks() {
 // launch has under four chunks per warp, so that small containers still
 // spread over all warps).  Consecutive cells (engine order: neighbouring
 // blocks) search nearly the same blocks, so a warp that runs them back to
-// back finds their block starts and particles in its SM's L1.
+// back finds their block starts and particles in its SM's L1.  On the 4M
+// periodic box the clipping passes take 77.9 / 78.1 / 78.4 ms with chunks
+// of 4 / 8 / 16: within the run-to-run spread.
 #ifndef VGPU_CELL_CHUNK
 #define VGPU_CELL_CHUNK 8
 #endif

@@ -55,6 +55,12 @@ def parse():
                     help="periodic: the 4M periodic box (the headline); batched: many containers")
     ap.add_argument("--count", type=int, default=4096, help="batched: number of containers")
     ap.add_argument("--nmax", type=int, default=100_000, help="batched: largest container")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 engine on the same box")
+    ap.add_argument("--no-c4", action="store_true", help="skip the jittered-FCC (near-degenerate) leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-containers leg")
+    ap.add_argument("--batch-count", type=int, default=1024, help="containers of the batched leg")
+    ap.add_argument("--batch-nmax", type=int, default=100_000, help="largest container of the batched leg")
+    ap.add_argument("--cpu-one-core-seconds", type=float, default=8.0)
     return ap.parse_args()
 
 
@@ -63,6 +69,13 @@ def workload(n):
     L = 100.0 * (n / 4_000_000) ** (1.0 / 3.0)
     g = max(1, int(round((n / 5.0) ** (1.0 / 3.0))))
     return W.periodic_cube(n=n, L=L, seed=1002, grid=(g, g, g))
+
+
+def workload_name(w):
+    """The workload as both arms name it (GPU and reference: same input)."""
+    n = len(w["ids"])
+    return (f"container_periodic L={w['geom'][0]:.4g}, {n} particles uniform (seed 1002), "
+            f"blocks {w['grid'][0]}^3")
 
 
 def dist_env():
@@ -186,6 +199,132 @@ def cpu_baseline(w, seconds, threads=None):
                       f"{threads} threads, {t:.2f} s"}, None
 
 
+def cpu_one_core(w, seconds):
+    """The same CPU port on one thread (bounded sample of the same container)."""
+    try:
+        from oracle import PortLib, build_port
+        build_port()
+        port = PortLib()
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unavailable": f"port unavailable: {e}"}
+    n_total = len(w["ids"])
+    t, m = port.time_cells(w, first=0, count=min(5000, n_total), threads=1)
+    count = int(min(n_total, max(m, m / max(t, 1e-9) * seconds)))
+    t, m = port.time_cells(w, first=0, count=count, threads=1)
+    return {"value": m / t, "unit": "cells/s", "cores": 1, "kind": "port",
+            "sample": f"first {m} cells (loop order) of the {n_total}-particle container, 1 thread, {t:.2f} s"}
+
+
+def fp64_leg(con, n, flush, mixed):
+    """The plain FP64 engine (every side test, vertex and reduction in FP64)
+    on the same container, device-timed like the headline; its topology is
+    compared with the mixed engine's (``mixed``: that compute's results)."""
+    import torch
+    con.compute_all_cells(mode="fp64")   # warm-up (sizes the FP64 record store)
+    ms, clip, fin = [], [], []
+    for _ in range(2):
+        flush.zero_()
+        torch.cuda.synchronize()
+        con.compute_all_cells(mode="fp64")
+        st = con.stats()
+        ms.append(st["step_ms"])
+        clip.append(st["clip_ms"])
+        fin.append(st["finish_ms"])
+    f = con.cells()
+    topo = (np.array_equal(f.nf, mixed.nf) and np.array_equal(f.nv, mixed.nv)
+            and np.array_equal(f.nb_off, mixed.nb_off) and np.array_equal(f.nb, mixed.nb))
+    ok = f.vol > 0
+    rel = np.abs(mixed.vol[ok] - f.vol[ok]) / f.vol[ok]
+    t = statistics.mean(ms)
+    return {"value": n / (t / 1000.0), "unit": "cells/s", "ms_per_step": t, "clip_ms": statistics.mean(clip),
+            "finish_ms": statistics.mean(fin), "topology_equal_to_mixed": bool(topo),
+            "max_rel_volume_diff_mixed_vs_fp64": float(rel.max()) if len(rel) else 0.0}
+
+
+def c4_leg():
+    """Near-degenerate lattice: 64^3 FCC (a = 1, periodic), every coordinate
+    jittered by N(0, (1e-7)^2).  One mixed and one FP64 compute; the rate at
+    which FP32 side tests fall back to FP64 and the topology agreement."""
+    import voro_gb300 as vg
+    from voro_gb300 import workloads as W
+    w = W.fcc_jitter(cells=64, sigma=1e-7, seed=1004)
+    n = len(w["ids"])
+    con = vg.from_workload(w, mode="mixed")
+    con.compute_all_cells()              # warm-up
+    con.compute_all_cells()
+    st = con.stats()
+    m = con.cells()
+    con.compute_all_cells(mode="fp64")
+    st64 = con.stats()
+    f = con.cells()
+    topo = (np.array_equal(f.nf, m.nf) and np.array_equal(f.nv, m.nv) and np.array_equal(f.nb_off, m.nb_off)
+            and np.array_equal(f.nb, m.nb))
+    rel = np.abs(m.vol - f.vol) / f.vol
+    return {"workload": f"FCC 64^3 (a = 1, periodic cube L = 64), {n} particles, jitter sigma 1e-7 (seed 1004)",
+            "cells_per_s": n / (st["step_ms"] / 1000.0), "fp64_engine_cells_per_s": n / (st64["step_ms"] / 1000.0),
+            "side_tests": int(st["side_tests"]), "fp64_repairs": int(st["fp64_repairs"]),
+            "fp64_repairs_per_test": st["fp64_repairs"] / max(st["side_tests"], 1),
+            "cells_rerun_with_fp64": int(st["overflow_reruns"]),
+            "cells_rerun_fraction": st["overflow_reruns"] / n,
+            "marginal_cells": int(st["marginal_cells"]), "failed_cells": int(st["failed_cells"]),
+            "topology_equal_to_fp64": bool(topo), "max_rel_volume_diff_vs_fp64": float(rel.max())}
+
+
+def batched_leg(count, nmax, steps, warmup, mode="mixed"):
+    """Many containers (log-uniform sizes, mixed kinds): one vgpu_batch_compute
+    (binning per container + one persistent launch for every cell) against a
+    loop of per-container computes on the same containers.  Host wall clock."""
+    import torch
+    import voro_gb300 as vg
+    from voro_gb300 import workloads as W
+    ws = W.batched(count=count, nmin=64, nmax=nmax, seed=1005)
+    total = sum(len(w["ids"]) for w in ws)
+    cons = [vg.from_workload(w, mode=mode) for w in ws]
+    b = vg.batch(cons)
+    for _ in range(warmup):
+        b.compute_all_cells(mode=mode)
+    wall, kern, binms = [], [], []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.compute_all_cells(mode=mode)
+        wall.append(time.perf_counter() - t0)
+        st = b.stats()
+        kern.append(st["kernel_ms"])
+        binms.append(st["bin_ms"])
+    st = b.stats()
+    loop = []
+    for it in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in cons:
+            c.compute_all_cells(mode=mode)
+        torch.cuda.synchronize()
+        if it >= warmup:
+            loop.append(time.perf_counter() - t0)
+
+    def box_volume(w):
+        g = w["geom"]
+        return (g[1] - g[0]) * (g[3] - g[2]) * (g[5] - g[4]) if w["kind"] < 2 else g[0] * g[2] * g[5]
+
+    vol_ok = all(abs(c.sum_cell_volumes() - box_volume(w)) <= 1e-9 * box_volume(w) for c, w in zip(cons, ws))
+    wt = statistics.mean(wall)
+    return {
+        "workload": f"{count} containers, N log-uniform [64, {nmax}] (seed 1005), half container_periodic, "
+                    f"a quarter radical; {total} particles",
+        "value": total / wt, "unit": "cells/s", "ms_per_step": 1000.0 * wt,
+        "timing": "host wall clock around vgpu_batch_compute (binning + one persistent launch per pass)",
+        "kernel_only_cells_per_s": total / (statistics.mean(kern) / 1000.0),
+        "batched_kernel_ms": statistics.mean(kern), "batched_bin_ms": statistics.mean(binms),
+        "per_container_loop": {"value": total / statistics.mean(loop), "unit": "cells/s",
+                               "ms_per_step": 1000.0 * statistics.mean(loop)},
+        "speedup_vs_loop": statistics.mean(loop) / wt,
+        "gpu_launches": int(st["kernel_launches"]),
+        "engine": {"cells": st["cells"], "failed_cells": st["failed_cells"], "overflow_reruns": st["overflow_reruns"],
+                   "marginal_cells": st["marginal_cells"], "sum_volume_ok": bool(vol_ok)},
+    }
+
+
 def reference_tests_per_cell(w, cells=20000):
     """T_cell of the flop model: the reference algorithm's vertex-plane side
     tests (m_calc calls, src/cell.cc:2050-2059) per cell, counted by the CPU
@@ -230,8 +369,7 @@ def run_reference(args):
         "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"container_periodic L={w['geom'][0]:.4g}, {n_total} particles uniform, "
-                               f"blocks {w['grid'][0]}^3", "cells_per_step": per_step},
+        "config": {"workload": workload_name(w), "cells_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": threads, "kind": "port",
                          "sample": f"first {per_step} cells of {n_total} per step, {threads} threads"},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -349,16 +487,18 @@ def run_ours(args):
         traffic = traffic * n   # per launch: the capture's per-cell DRAM bytes times the cells of one launch
     side_tests_per_cell = st["side_tests"] / max(st["cells"], 1)
     t_ref, t_cells = reference_tests_per_cell(w)
-    v_mean = float(np.mean(con.cells(neighbors=False).nv))
+    mixed_cells = con.cells()
+    v_mean = float(np.mean(mixed_cells.nv))
     flops_cell = 6.0 * (t_ref if t_ref is not None else side_tests_per_cell) + 40.0 * v_mean
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clocks.get("sm_max_mhz") or 2070.0
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12   # FMA lanes per SM: 128
     line = {
         "metric": "cells/s (Voronoi cells computed per second)",
         "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.mode == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": f"container_periodic L={w['geom'][0]:.4g}, {n} particles uniform (seed 1002), "
-                               f"blocks {w['grid'][0]}^3, {args.mode} engine",
+        "config": {"workload": workload_name(w), "engine": args.mode,
                    "cells_per_step": n, "l2": "flushed between steps (512 MiB write)",
                    "engine_density": tuned[0] if tuned else (args.density if args.density > 0 else "default"),
                    "parallelism": f"{ws} independent replicas" if ws > 1 else "1 GPU"},
@@ -369,7 +509,8 @@ def run_ours(args):
                              "(36 in, 100 out); traffic from the ncu capture in profiles/, scaled by cells",
                      "finish_kernel_ms": fms, "cell_stage_ms": kms,
                      "pipe": {"unit": "TFLOP/s", "achieved": flops_cell * n / (kms / 1000.0) / 1e12,
-                              "peak": fp32_peak, "peak_kind": "nominal FP32",
+                              "peak": fp32_peak, "peak_kind": f"nominal FP32 ({props.multi_processor_count} SMs "
+                                                               f"x 128 lanes x 2 x {sm_mhz:.0f} MHz)",
                               "flops_per_cell": flops_cell,
                               "model": "F_cell = 6 T_cell + 40 V_cell; T_cell = reference side tests per cell "
                                        f"({t_ref if t_ref is not None else float('nan'):.1f}, CPU port on "
@@ -384,9 +525,19 @@ def run_ours(args):
                    "planes_cut_per_cell": st["planes_cut"] / max(st["cells"], 1),
                    "sum_volume_ok": bool(vol_ok)},
     }
+    if ws == 1 and args.mode == "mixed" and not args.no_fp64:
+        line["fp64"] = fp64_leg(con, n, flush, mixed_cells)
+        line["mixed_over_fp64"] = value / line["fp64"]["value"]
+    del mixed_cells, con
+    if ws == 1 and not args.no_c4:
+        line["c4"] = c4_leg()
+    if ws == 1 and not args.no_batched:
+        line["batched"] = batched_leg(args.batch_count, args.batch_nmax, steps=2, warmup=1, mode=args.mode)
     if ws == 1 and not args.no_cpu:
         cb, err = cpu_baseline(w, args.cpu_seconds)
         line["cpu_baseline"] = cb if cb else {"value": None, "unavailable": err}
+        if cb:
+            cb["one_core"] = cpu_one_core(w, args.cpu_one_core_seconds)
     print(json.dumps(line))
     if ws > 1:
         import torch.distributed as dist
@@ -395,64 +546,20 @@ def run_ours(args):
 
 
 def run_batched(args):
-    """Many containers (log-uniform sizes, mixed kinds): one vgpu_batch_compute
-    (binning per container + one persistent launch for every cell) against a
-    loop of per-container computes on the same containers."""
+    """The batched workload alone as the headline line (--workload batched)."""
     import torch
     torch.cuda.set_device(0)
-    import voro_gb300 as vg
-    from voro_gb300 import workloads as W
-    ws = W.batched(count=args.count, nmin=64, nmax=args.nmax, seed=1005)
-    total = sum(len(w["ids"]) for w in ws)
-    cons = [vg.from_workload(w, mode=args.mode) for w in ws]
-    b = vg.batch(cons)
-    for _ in range(args.warmup):
-        b.compute_all_cells(mode=args.mode)
-    wall, kern, binms = [], [], []
     with Clocks(0) as clk:
-        for _ in range(args.steps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            b.compute_all_cells(mode=args.mode)
-            wall.append(time.perf_counter() - t0)
-            st = b.stats()
-            kern.append(st["kernel_ms"])
-            binms.append(st["bin_ms"])
-    st = b.stats()
-    # the same containers one compute at a time
-    loop = []
-    for it in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for c in cons:
-            c.compute_all_cells(mode=args.mode)
-        torch.cuda.synchronize()
-        if it >= args.warmup:
-            loop.append(time.perf_counter() - t0)
-    def box_volume(w):
-        g = w["geom"]
-        return (g[1] - g[0]) * (g[3] - g[2]) * (g[5] - g[4]) if w["kind"] < 2 else g[0] * g[2] * g[5]
-
-    vol_ok = all(abs(c.sum_cell_volumes() - box_volume(w)) <= 1e-9 * box_volume(w) for c, w in zip(cons, ws))
-    wt = statistics.mean(wall)
+        b = batched_leg(args.count, args.nmax, args.steps, args.warmup, mode=args.mode)
     line = {
         "metric": "cells/s (Voronoi cells computed per second), batched containers",
-        "value": total / wt, "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * wt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "value": b.pop("value"), "unit": "cells/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": b.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if args.mode == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": f"{args.count} containers, N log-uniform [64, {args.nmax}] (seed 1005), half "
-                               f"container_periodic, a quarter radical; {total} particles",
-                   "timing": "host wall clock around vgpu_batch_compute (binning + one persistent launch)"},
-        "kernel_only_cells_per_s": total / (statistics.mean(kern) / 1000.0),
-        "batched_kernel_ms": statistics.mean(kern), "batched_bin_ms": statistics.mean(binms),
-        "per_container_loop": {"value": total / statistics.mean(loop), "unit": "cells/s",
-                               "ms_per_step": 1000.0 * statistics.mean(loop)},
-        "speedup_vs_loop": statistics.mean(loop) / wt,
-        "gpu_launches": int(st["kernel_launches"]),
+        "config": {"workload": b.pop("workload"), "timing": b.pop("timing")},
         "clocks": clk.summary(),
-        "engine": {"cells": st["cells"], "failed_cells": st["failed_cells"], "overflow_reruns": st["overflow_reruns"],
-                   "marginal_cells": st["marginal_cells"], "sum_volume_ok": bool(vol_ok)},
     }
+    line.update(b)
     print(json.dumps(line))
     return 0
 

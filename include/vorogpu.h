@@ -101,10 +101,16 @@ int vgpu_container_destroy(vgpu_container *h);
  * appends ids[i] with xyzr[4i..4i+3] = (x,y,z,r) to the container's device
  * staging area; the copy completes before return, so the caller may reuse its
  * arrays (r ignored for mono kinds).  Out-of-range points in non-periodic directions
- * are dropped at compute time exactly as put_remap (src/container.cc:174-191). */
+ * are dropped at compute time exactly as put_remap (src/container.cc:174-191).
+ * A non-finite x, y or z (or r, radical kinds) fails the whole call with
+ * VGPU_ERR_ARG and stages none of its particles (the reference has no check;
+ * its remap would turn such a value into an arbitrary block index). */
 int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyzr);
 /* Same, from device memory already resident on the container's device; the
- * next vgpu_compute reads it in place (no host staging, no copy). */
+ * next vgpu_compute reads it in place (no host staging, no copy).  The input
+ * is checked during the compute's binning instead: a non-finite x, y or z (or
+ * r, radical kinds) makes vgpu_compute return VGPU_ERR_ARG before any cell
+ * is computed. */
 int vgpu_put_device(vgpu_container *h, int64_t n, const int32_t *dev_ids, const double *dev_xyzr);
 /* Replaces container::clear() (src/container.cc:385-387). */
 int vgpu_clear(vgpu_container *h);
@@ -228,9 +234,15 @@ int vgpu_get_ghost_polytopes(vgpu_container *h, int64_t *offsets, double *data);
 
 /* Diagnostics: per-phase SM clock totals of the last compute's cell kernel,
  * summed over warps (0 init, 1 candidate gather, 2 sort, 3 side tests,
- * 4 cuts, 5 reductions, 7 whole kernel).  All zero unless the library was
- * built with -DVGPU_PHASE_TIMING. */
+ * 4 cuts, 5 record output, 6 the part of 1 spent in flushes the gather
+ * starts when its candidate buffer fills, 7 whole kernel).  All zero unless
+ * the library was built with -DVGPU_PHASE_TIMING. */
 int vgpu_phase_cycles(vgpu_container *h, double out[8]);
+/* Diagnostics, same build: event counts of the last compute's cell kernel
+ * (0 candidate flushes, 1 of them sorting 64 keys, 2 block passes of the
+ * gather, 3 candidate passes, 4 candidates kept, 5 vertices created by cuts,
+ * 6 search segments, 7 cells run). */
+int vgpu_phase_counts(vgpu_container *h, double out[8]);
 
 /* Device-resident views of the results (valid until the next compute/destroy):
  * volumes (double[n]) and face counts (int32[n]). */
@@ -248,6 +260,16 @@ int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per
  * reference's depth, so the results never depend on it; deeper layers cost
  * memory and binning time, shallower ones make the rerun likelier. */
 int vgpu_set_ghost_depth(vgpu_container *h, double spacings);
+
+/* Budget in bytes of the polytope-record store one compute of this container
+ * may use (the scratch the clipping kernels write and the finish kernel reads;
+ * about 0.75 KB per cell with the mixed engine), 0 = the default of 1 KB per
+ * cell.  Where the reference meets an allocation limit it exits with
+ * VOROPP_MEMORY_ERROR (max_vertices etc., src/config.hh:44-56;
+ * src/cell.cc:130-288); here the cells whose records do not fit are flagged
+ * VGPU_CELL_FAILED with reason VGPU_FAIL_RECORDS, the others complete, and
+ * vgpu_compute returns VGPU_ERR_CAPACITY.  Applies from the next compute. */
+int vgpu_set_record_budget(vgpu_container *h, int64_t bytes);
 
 /* ---- batches: many containers computed by one persistent launch ----
  * The reference computes containers one at a time (compute_all_cells per

@@ -31,12 +31,19 @@ _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 
+def ref_src() -> str:
+    """The reference's src/ directory: $VORO_REF_SRC when set, else a checkout
+    named "reference" beside this repository (the reference tree is absent on
+    hosts that only run the tests)."""
+    return os.environ.get("VORO_REF_SRC") or os.path.abspath(os.path.join(HERE, "..", "..", "reference", "src"))
+
+
 def build_ref(quiet=True) -> bool:
     """Builds the reference library if its sources are present."""
-    ref_src = os.environ.get("VORO_REF_SRC", "/root/reference/src")
-    if not os.path.isfile(os.path.join(ref_src, "voro++.cc")):
+    ref_src_dir = ref_src()
+    if not os.path.isfile(os.path.join(ref_src_dir, "voro++.cc")):
         return False
-    subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True,
+    subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={ref_src_dir}"], check=True,
                    stdout=subprocess.DEVNULL if quiet else None)
     return os.path.isfile(REF_SO)
 

@@ -54,13 +54,12 @@ def test_port_threads_give_same_work(port):
     assert port.last_side_tests == s1
 
 
-REF_WL = "/root/reference/src/v_base_wl.cc"
-
-
 def test_worklists_match_reference_table(port):
-    if not os.path.exists(REF_WL):
+    from oracle import ref_src
+    ref_wl = os.path.join(ref_src(), "v_base_wl.cc")
+    if not os.path.exists(ref_wl):
         pytest.skip("reference tree not present")
-    txt = open(REF_WL).read()
+    txt = open(ref_wl).read()
     body = txt[txt.index("{") + 1:txt.rindex("}")]
     vals = np.array([int(t, 0) for t in re.findall(r"0x[0-9a-f]+|\b\d+\b", body)], dtype=np.uint32)
     assert np.array_equal(vals, port.worklists())

@@ -29,7 +29,10 @@ VGPU_CELL_OK = 1
 VGPU_CELL_MARGINAL = 2
 VGPU_CELL_REPAIRED = 4
 VGPU_OUTPUT_POLYTOPES = 1
-VGPU_CELL_FAILED = 8   # bits 8-11: reason (1 planes, 2 adjacency, 3 vertices, 4 search)
+VGPU_CELL_FAILED = 8   # bits 8-11: reason (1 planes, 2 adjacency, 3 vertices, 4 search, 5 records)
+VGPU_FAIL_RECORDS = 5
+VGPU_ERR_ARG = 16
+VGPU_ERR_CAPACITY = 21
 
 KIND_CONTAINER = 0
 KIND_CONTAINER_POLY = 1
@@ -54,7 +57,7 @@ EXPORTED = [
     "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells", "vgpu_compute_ghost_cells",
     "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes", "vgpu_add_wall",
     "vgpu_clear_walls", "vgpu_point_inside_walls",
-    "vgpu_autotune",
+    "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts",
 ]
 
 
@@ -119,7 +122,9 @@ def load_library(build_if_missing=True):
     lib.vgpu_device_results.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     lib.vgpu_set_ghost_depth.argtypes = [vp, ctypes.c_double]
+    lib.vgpu_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
+    lib.vgpu_phase_counts.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
     lib.vgpu_sum_volumes_noalloc.argtypes = [vp, i64, vp, vp]
     lib.vgpu_set_output.argtypes = [vp, ctypes.c_int]
@@ -449,8 +454,19 @@ class _ContainerBase:
     # ---- compute_all_cells: src/container.cc:438-453
     def compute_all_cells(self, mode=None):
         self._flush_pending()
-        _check(self._lib.vgpu_compute(self._h, self._mode_code(mode)))
-        self._dirty = False
+        rc = self._lib.vgpu_compute(self._h, self._mode_code(mode))
+        if rc in (VGPU_OK, VGPU_ERR_CAPACITY):
+            # a capacity failure still leaves results: the cells that failed
+            # carry VGPU_CELL_FAILED and a reason, the others are complete
+            self._dirty = False
+        _check(rc)
+
+    def set_record_budget(self, nbytes=0):
+        """Record-store budget of one compute in bytes (0: the default).  Cells
+        whose records do not fit fail with VGPU_FAIL_RECORDS and the compute
+        raises VGPU_ERR_CAPACITY; the rest are complete."""
+        _check(self._lib.vgpu_set_record_budget(self._h, int(nbytes)))
+        self._dirty = True
 
     def _ensure(self):
         if self._dirty:
@@ -524,7 +540,15 @@ class _ContainerBase:
         """Per-phase clock totals (diagnostics builds only; zeros otherwise)."""
         out = (ctypes.c_double * 8)()
         _check(self._lib.vgpu_phase_cycles(self._h, out))
-        names = ["init", "gather", "sort", "test", "cut", "finish", "-", "kernel"]
+        names = ["init", "gather", "sort", "test", "cut", "finish", "gather_flush", "kernel"]
+        return dict(zip(names, list(out)))
+
+    def phase_counts(self):
+        """Per-compute event counts of the cell kernel (diagnostics builds only)."""
+        out = (ctypes.c_double * 8)()
+        _check(self._lib.vgpu_phase_counts(self._h, out))
+        names = ["flushes", "sorts64", "block_passes", "cand_passes", "cands_kept", "new_vertices",
+                 "segments", "cells_run"]
         return dict(zip(names, list(out)))
 
     def total_particles(self):

@@ -206,7 +206,8 @@ struct vgpu_container {
     bool computed = false;
     bool binned = false;        // engine-order arrays match the particles (after a compute or a locate)
     vgpu_stats stats{};
-    double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double phase[16] = {};
+    int64_t record_bytes = 0;   // record-store budget of one compute (0: kRecWordsPerCell per cell)
 };
 
 namespace {
@@ -533,6 +534,36 @@ int vgpu_container_destroy(vgpu_container *h) {
     return VGPU_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Index of the first particle whose x, y or z (or r, in a radical container)
+// is an infinity or a NaN; -1 if there is none.  Branch-free over the bit
+// patterns (an all-ones exponent) so that it runs at memory speed.
+int64_t first_nonfinite(const double *xyzr, int64_t n, bool poly) {
+    constexpr uint64_t kExp = 0x7ff0000000000000ull;
+    const uint64_t rmask = poly ? kExp : 0ull;
+    uint64_t bad = 0;
+    for (int64_t i = 0; i < n; i++) {
+        uint64_t b[4];
+        memcpy(b, xyzr + 4 * i, 32);
+        bad |= (uint64_t)((b[0] & kExp) == kExp) | (uint64_t)((b[1] & kExp) == kExp) |
+               (uint64_t)((b[2] & kExp) == kExp) | (uint64_t)(rmask != 0 && (b[3] & rmask) == rmask);
+    }
+    if (!bad) return -1;
+    for (int64_t i = 0; i < n; i++) {
+        const double *q = xyzr + 4 * i;
+        if (!(std::isfinite(q[0]) && std::isfinite(q[1]) && std::isfinite(q[2]) && (!poly || std::isfinite(q[3]))))
+            return i;
+    }
+    return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
 int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyzr) {
     if (!h || n < 0 || (n > 0 && (!ids || !xyzr))) return fail(VGPU_ERR_ARG, "bad put arguments");
     if (h->use_device_input) {
@@ -567,7 +598,14 @@ int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyz
                             h->stream));
     VG_CUDA(cudaMemcpyAsync(h->xyzr_in.as<double>() + 4 * h->staged, xyzr, (size_t)n * 32,
                             cudaMemcpyHostToDevice, h->stream));
+    // non-finite input is rejected here, while the copies run (from pinned
+    // memory they are asynchronous); the staged count does not advance, so
+    // nothing of this call is kept
+    const int64_t bad = first_nonfinite(xyzr, n, h->g.poly);
     VG_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad >= 0)
+        return fail(VGPU_ERR_ARG, "particle %lld (id %d) has a non-finite position or radius", (long long)bad,
+                    (int)ids[bad]);
     h->staged += n;
     h->computed = false;
     h->binned = false;
@@ -677,6 +715,12 @@ int vgpu_set_ghost_depth(vgpu_container *h, double spacings) {
         h->ghost_spacings = v;
         h->binned = false;
     }
+    return VGPU_OK;
+}
+
+int vgpu_set_record_budget(vgpu_container *h, int64_t bytes) {
+    if (!h || bytes < 0) return fail(VGPU_ERR_ARG, "bad record budget");
+    h->record_bytes = bytes;
     return VGPU_OK;
 }
 
@@ -792,13 +836,16 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
     int *d_kept = h->kept.as<int>();
     unsigned long long *d_rmax = reinterpret_cast<unsigned long long *>(h->kept.as<char>() + 16);
     VG_CUDA(launch_remap(bp, d_kept, d_rmax, s));
-    int nkept = 0;
+    int kept2[2] = {0, 0};   // kept particles, particles with a non-finite position or radius
     unsigned long long rmax_bits = 0;
-    VG_CUDA(cudaMemcpyAsync(&nkept, d_kept, 4, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaMemcpyAsync(kept2, d_kept, 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaMemcpyAsync(&rmax_bits, d_rmax, 8, cudaMemcpyDeviceToHost, s));
     // identity copy for the second sort
     if (n > 0) VG_CUDA(cudaMemcpyAsync(h->idx2.p, h->idx.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     VG_CUDA(cudaStreamSynchronize(s));
+    if (kept2[1] > 0)
+        return fail(VGPU_ERR_ARG, "%d particles have a non-finite position or radius", kept2[1]);
+    const int nkept = kept2[0];
     double rmax = 0.0;
     memcpy(&rmax, &rmax_bits, 8);
     g.rmax = rmax;
@@ -1049,7 +1096,8 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
 
 // After small_bin_kernel: the kept count, largest radius and duplicate flag of h.
 int finish_small(vgpu_container *h, const unsigned long long res[2]) {
-    if (res[0] >> 32) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
+    if ((res[0] >> 33) & 1ull) return fail(VGPU_ERR_ARG, "a particle has a non-finite position or radius");
+    if ((res[0] >> 32) & 1ull) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
     h->nkept = (int)(res[0] & 0xffffffffu);
     h->nengine = h->nkept;
     h->binned = true;
@@ -1080,8 +1128,9 @@ int setup_records(vgpu_container *h, int mode, CellParams &cp, Counters *cnt, cu
     cp.rec = nullptr;
     cp.poly = nullptr;
     if (h->nkept <= 0) return VGPU_OK;
-    const unsigned long long cap = std::min<unsigned long long>(
+    unsigned long long cap = std::min<unsigned long long>(
         (unsigned long long)h->nkept * kRecWordsPerCell[mode == VGPU_MIXED ? 1 : 0] + (1u << 20), ~0ull >> 8);
+    if (h->record_bytes > 0) cap = std::min<unsigned long long>(cap, (unsigned long long)h->record_bytes / 4);
     VG_CUDA(store.ensure(cap * 4));
     VG_CUDA(h->rec_off.ensure((size_t)h->nengine * 8));
     VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nengine * 8, s));
@@ -1174,7 +1223,7 @@ int clip_passes(cudaStream_t s, int sms, int warps, int mode, const CellParams &
         sum.deleted += c[k].deleted;
         sum.marginal += c[k].marginal;
         sum.failed += c[k].failed;
-        for (int i = 0; i < 8; i++) sum.phase_cycles[i] += c[k].phase_cycles[i];
+        for (int i = 0; i < 16; i++) sum.phase_cycles[i] += c[k].phase_cycles[i];
     }
     sum.overflow = c[0].overflow;
     sum.failed += last_failed;
@@ -1197,7 +1246,7 @@ int finish_compute(vgpu_container *h, const Counters &c, float cell_ms) {
     h->stats.planes_cut = (int64_t)c.planes_cut;
     h->stats.overflow_reruns = (int64_t)c.overflow;
     h->stats.failed_cells = (int64_t)(c.failed + c.nb_failed);
-    for (int i = 0; i < 8; i++) h->phase[i] = (double)c.phase_cycles[i];
+    for (int i = 0; i < 16; i++) h->phase[i] = (double)c.phase_cycles[i];
     h->stats.kernel_ms = cell_ms;
     h->stats.bin_ms = bin_ms;
     h->stats.step_ms = step_ms;
@@ -1674,6 +1723,12 @@ int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int
 int vgpu_phase_cycles(vgpu_container *h, double out[8]) {
     if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
     for (int i = 0; i < 8; i++) out[i] = h->phase[i];
+    return VGPU_OK;
+}
+
+int vgpu_phase_counts(vgpu_container *h, double out[8]) {
+    if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
+    for (int i = 0; i < 8; i++) out[i] = h->phase[8 + i];
     return VGPU_OK;
 }
 

@@ -23,6 +23,14 @@ __device__ __forceinline__ unsigned engine_key(const Geometry &g, const double c
     return (unsigned)(e[0] + g.gn[0] * (e[1] + g.gn[1] * e[2]));
 }
 
+// A particle whose position (or, in a radical container, radius) is not
+// finite cannot be placed: the remap would turn it into a block index it has
+// no business in.  Both binning paths count such particles and the host
+// fails the compute with VGPU_ERR_ARG before any cell is computed.
+__device__ __forceinline__ bool finite_input(const Geometry &g, double4 q) {
+    return isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && (!g.poly || isfinite(q.w));
+}
+
 // The reference's placement of one particle: remapped position c, its
 // reference block key uk (nub if put() drops it) and engine block key gk.
 __device__ __forceinline__ bool remap_one(const Geometry &g, double4 q, int nub, int nblocks, double4 &out,
@@ -114,6 +122,7 @@ __global__ void remap_kernel(BinParams bp, int nub, int nblocks, int *kept, unsi
     if (i >= bp.n) return;
     const Geometry &g = bp.g;
     const double4 q = bp.xyzr_in[i];
+    if (!finite_input(g, q)) atomicAdd(kept + 1, 1);   // counted; the host rejects the compute
     double4 r;
     unsigned uk, gk;
     if (remap_one(g, q, nub, nblocks, r, uk, gk)) {
@@ -262,7 +271,7 @@ __device__ __forceinline__ void cta_bitonic(unsigned long long *key, int n2) {
 
 __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const SmallBinJob *jobs) {
     extern __shared__ unsigned long long sbin[];
-    __shared__ int s_kept, s_dup;
+    __shared__ int s_kept, s_dup, s_bad;
     __shared__ unsigned long long s_rmax;
     const SmallBinJob &J = jobs[blockIdx.x];
     const Geometry &g = J.g;
@@ -274,12 +283,14 @@ __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const Small
     if (threadIdx.x == 0) {
         s_kept = 0;
         s_dup = 0;
+        s_bad = 0;
         s_rmax = 0ull;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n2; i += blockDim.x) {
         if (i < n) {
             const double4 q = J.xyzr_in[i];
+            if (!finite_input(g, q)) s_bad = 1;
             double4 r;
             unsigned uk, gk;
             if (remap_one(g, q, J.nub, J.nblocks, r, uk, gk)) {
@@ -336,7 +347,8 @@ __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const Small
         for (int q = threadIdx.x; q <= J.nblocks; q += blockDim.x) J.bstart[q] = 0;
     __syncthreads();
     if (threadIdx.x == 0) {
-        J.result[0] = (unsigned long long)nkept | ((unsigned long long)s_dup << 32);
+        J.result[0] = (unsigned long long)nkept | ((unsigned long long)s_dup << 32) |
+                      ((unsigned long long)s_bad << 33);
         J.result[1] = s_rmax;
     }
 }

@@ -161,7 +161,7 @@ struct CellCtx {
     int ncand;
     unsigned tests, repairs, ptested, pcut;
 #ifdef VGPU_PHASE_TIMING
-    unsigned long long phase[8];
+    unsigned long long phase[16];   // 8 clock totals, 8 event counts
 #endif
 };
 
@@ -339,9 +339,11 @@ __device__ __noinline__ VertexF32 vertex_f64_fallback(const CellParams &P, const
 #ifdef VGPU_PHASE_TIMING
 #define PHASE_BEGIN(v) const long long v = clock64()
 #define PHASE_END(v, ph) C.phase[ph] += (unsigned long long)(clock64() - (v))
+#define PHASE_COUNT(i, n) C.phase[8 + (i)] += (unsigned long long)(n)
 #else
 #define PHASE_BEGIN(v)
 #define PHASE_END(v, ph)
+#define PHASE_COUNT(i, n)
 #endif
 
 // ------------------------------------------------------------------ the engine
@@ -638,6 +640,7 @@ struct Engine {
             C.marginal = true;
             return;
         }
+        PHASE_COUNT(5, total);
         Mask<K> Fm;
 #pragma unroll
         for (int i = 0; i < Mask<K>::W; i++) Fm.w[i] = ~Vm.w[i] | Rm.w[i];
@@ -742,6 +745,8 @@ struct Engine {
     __device__ void flush() {
         const int n = C.ncand;
         if (n == 0) return;
+        PHASE_COUNT(0, 1);
+        PHASE_COUNT(1, n > 32 ? 1 : 0);
         PHASE_BEGIN(t_sort);
         __syncwarp();
         unsigned k0 = lane < n ? S.u.c.ck[lane] : 0xffffffffu;
@@ -776,6 +781,7 @@ struct Engine {
     __device__ void gather_offsets(int e_begin, int e_end, bool from_table, int shell_r) {
         const float l0 = C.me32.x, l1 = C.me32.y, l2 = C.me32.z;
         for (int base = e_begin; base < e_end; base += 32) {
+            PHASE_COUNT(2, 1);
             const int e = base + lane;
             int di = 0, dj = 0, dk = 0;
             bool ok = e < e_end;
@@ -838,7 +844,12 @@ struct Engine {
             const int tot = __shfl_sync(kFull, incl, 31);
             const int packed_d = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
             for (int c0 = 0; c0 < tot; c0 += 32) {
-                if (C.ncand > kCandBuf - 32) flush();
+                PHASE_COUNT(3, 1);
+                if (C.ncand > kCandBuf - 32) {
+                    PHASE_BEGIN(t_nested);
+                    flush();
+                    PHASE_END(t_nested, 6);
+                }
                 if (C.deleted || C.overflow) return;
                 const int c = c0 + lane;
                 // owner lane: number of lanes whose inclusive prefix is <= c
@@ -899,6 +910,7 @@ struct Engine {
                     if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C.me64, j, o_code);
                 }
                 C.ncand += __popc(bal);
+                PHASE_COUNT(4, __popc(bal));
             }
         }
     }
@@ -932,6 +944,7 @@ struct Engine {
                 b1 = (2 * r + 1) * (2 * r + 1) * (2 * r + 1);
             }
             if (lb2 >= C.cutoff2 * (1.0f + 1e-5f)) return;
+            PHASE_COUNT(6, 1);
             PHASE_BEGIN(t_g);
             gather_offsets(b0, b1, table, r);
             PHASE_END(t_g, 1);
@@ -960,7 +973,8 @@ struct Engine {
 
     __device__ void run(int k) {
 #ifdef VGPU_PHASE_TIMING
-        for (int i = 0; i < 8; i++) C.phase[i] = 0;
+        for (int i = 0; i < 16; i++) C.phase[i] = 0;
+        PHASE_COUNT(7, 1);
 #endif
         PHASE_BEGIN(t_init);
         init_cell(k);
@@ -1114,7 +1128,7 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
     WarpShared<MODE, K> &S = ws[wid];
     unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0;
 #ifdef VGPU_PHASE_TIMING
-    unsigned long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long ph[16] = {};
     const long long t_kernel0 = clock64();
 #endif
     unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
@@ -1136,7 +1150,7 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
         ptested += eng.C.ptested;
         pcut += eng.C.pcut;
 #ifdef VGPU_PHASE_TIMING
-        for (int i = 0; i < 8; i++) ph[i] += eng.C.phase[i];
+        for (int i = 0; i < 16; i++) ph[i] += eng.C.phase[i];
 #endif
         if (eng.C.overflow) {
             if (lane == 0) {
@@ -1158,7 +1172,7 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
         atomicAdd(&P.cnt->marginal, marginal);
 #ifdef VGPU_PHASE_TIMING
         ph[7] = (unsigned long long)(clock64() - t_kernel0);
-        for (int i = 0; i < 8; i++) atomicAdd(&P.cnt->phase_cycles[i], ph[i]);
+        for (int i = 0; i < 16; i++) atomicAdd(&P.cnt->phase_cycles[i], ph[i]);
 #endif
     }
 }

@@ -92,7 +92,7 @@ struct Counters {
     unsigned long long poly_used;  // doubles of the polytope output in use
     unsigned long long nb_ovf_used;  // ints of the neighbour overflow store in use
     unsigned long long nb_failed;    // finish kernel: cells whose neighbours found it full
-    unsigned long long phase_cycles[8];  // diagnostics build only (VGPU_PHASE_TIMING)
+    unsigned long long phase_cycles[16];  // diagnostics build only (VGPU_PHASE_TIMING): 8 clocks, 8 counts
 };
 
 // A wall (src/wall.hh:25-130): the parameters as the reference's classes hold

@@ -134,8 +134,10 @@ class voronoicell {
         cz = cen_[2];
     }
     int number_of_faces() const { return nf_; }
-    // every vertex the engine produces has order 3 (E = 3p/2)
-    int number_of_edges() const { return 3 * p / 2; }
+    // Euler's relation for a convex polyhedron, V - E + F = 2: it holds with
+    // vertices of any order, as the reference's edge count does
+    // (src/cell.cc:2469)
+    int number_of_edges() const { return p + nf_ - 2; }
     // in the reference's doubled coordinates (src/cell.cc:1907-1917)
     double max_radius_squared() const { return 4.0 * mr2_; }
 
@@ -216,10 +218,11 @@ class voronoicell {
         return 0.5 * s;   // every edge bounds two faces
     }
     void vertex_orders(std::vector<int> &v) const {
-        if (!has_poly_) {
-            v.assign(p, 3);   // every vertex the engine produces has order 3
+        if (!has_poly_ && p == 2 * nf_ - 4) {
+            v.assign(p, 3);   // V = 2F - 4: every vertex has order 3
             return;
         }
+        need_poly();
         v.assign(p, 0);
         for (int x : floops_) v[x]++;
     }
@@ -601,7 +604,7 @@ class container_gpu_base {
     static bool needs_polytope(const char *format) {
         for (const char *f = format; *f; f++)
             if (f[0] == '%' && f[1]) {
-                if (strchr("pPEeFAaftl", f[1])) return true;
+                if (strchr("pPoEeFAaftl", f[1])) return true;
                 f++;
             }
         return false;
@@ -673,15 +676,9 @@ class container_gpu_base {
                 case 'q': fprintf(fp, "%g %g %g", x, y, z); break;
                 case 'r': fprintf(fp, "%g", radius_at(k)); break;
                 case 'w': fprintf(fp, "%d", nv_[k]); break;
-                case 'o':
-                    if (poly_on_ && !poff_.empty()) {
-                        poly_field('o', k, x, y, z, fp);
-                    } else {   // every vertex the engine produces has order 3
-                        for (int v = 0; v < nv_[k]; v++) fputs(v ? " 3" : "3", fp);
-                    }
-                    break;
+                case 'o': poly_field('o', k, x, y, z, fp); break;
                 case 'm': fprintf(fp, "%g", mr2_[k]); break;
-                case 'g': fprintf(fp, "%d", 3 * nv_[k] / 2); break;
+                case 'g': fprintf(fp, "%d", nv_[k] + nf_[k] - 2); break;   // Euler: E = V + F - 2
                 case 's': fprintf(fp, "%d", nf_[k]); break;
                 case 'n':
                     for (int64_t q = off_[k]; q < off_[k + 1]; q++)

@@ -39,8 +39,16 @@ extern "C" {
 /* ---- precision modes ---------------------------------------------------- */
 #define VGPU_FP64 0  /* every side test, vertex and reduction in FP64 */
 #define VGPU_MIXED 1 /* FP32 side tests under a forward error filter; filter-band
-                        hits redone in FP64; final vertices rebuilt in FP64 from
-                        their three planes; volume/centroid accumulated in FP64 */
+                        hits redone in FP64 (topology as in FP64).  Final
+                        vertices: the FP32 vertex corrected against its three
+                        planes by residual steps in float pairs (about 48
+                        bits; ill-conditioned triples, cells that met the
+                        tolerance band and cells below 1e-4 of the cube of
+                        their radius solved in FP64); volume and centroid
+                        summed in float pairs.  Per-cell volume and centroid
+                        within 1e-10 of the FP64 engine's.  Large containers
+                        whose FP32 filter band is saturated run on the FP64
+                        engine (vgpu_set_fp64_fallback) */
 
 /* ---- per-cell flag bits (vgpu_get_cells, out_flags) -------------------- */
 #define VGPU_CELL_OK 1        /* compute_cell returned true (cell not deleted) */
@@ -74,6 +82,8 @@ typedef struct vgpu_stats {
     int64_t kernel_launches;  /* engine kernels launched by the last compute */
     double clip_ms;           /* of kernel_ms: the main clipping kernel alone */
     double finish_ms;         /* of kernel_ms: the FP64 finish kernel (mixed engine) */
+    int64_t fp64_engine_cells; /* mixed compute: cells the FP64 engine computed because a
+                                  sample showed the FP32 filter band saturated (0 or all) */
 } vgpu_stats;
 
 /* Library / device. */
@@ -270,6 +280,16 @@ int vgpu_set_ghost_depth(vgpu_container *h, double spacings);
  * VGPU_CELL_FAILED with reason VGPU_FAIL_RECORDS, the others complete, and
  * vgpu_compute returns VGPU_ERR_CAPACITY.  Applies from the next compute. */
 int vgpu_set_record_budget(vgpu_container *h, int64_t bytes);
+
+/* Mixed computes of large containers (at least 262,144 cells) first run the
+ * FP32 engine's first pass on 1/64 of the cells.  If more than this fraction
+ * of them need FP64 (tests inside the filter band or ill-conditioned
+ * vertices, as in jittered lattices where three near-coplanar bisectors meet),
+ * the whole container is computed by the FP64 engine instead, which is faster
+ * there and gives the same topology; vgpu_stats.fp64_engine_cells reports it.
+ * Default 0.25; a value >= 1 never switches.  No counterpart in the reference
+ * (it computes in FP64 throughout). */
+int vgpu_set_fp64_fallback(vgpu_container *h, double fraction);
 
 /* ---- batches: many containers computed by one persistent launch ----
  * The reference computes containers one at a time (compute_all_cells per

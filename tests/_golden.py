@@ -12,7 +12,7 @@ def names():
     locate_*.npz point-location answers, see load_locate; ghost_*.npz ghost
     cells, see load_ghost)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
-                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_", "wall_")))
+                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_", "wall_", "cli_")))
 
 
 def wall_names():
@@ -135,14 +135,9 @@ def box_volume(w):
     return g[0] * g[2] * g[5]
 
 
-def compare_cells(got, ref, vol_rtol, cen_rtol, label="", own_as_unit=False):
+def compare_cells(got, ref, vol_rtol, cen_rtol, label=""):
     """got: object with ids,pos,vol,cen,nf,nv,ok and neighbors(k) sorted;
-    ref: the fixture arrays.  Returns a list of human-readable mismatches.
-    own_as_unit: a face labelled with the cell's own ID counts as a face of
-    the unit cell (ID 0) -- a periodic box so sparse that the unit cell's
-    faces survive, where the reference relabels such a face when its search
-    meets the particle's own image, whose bisector the face lies on (a
-    plane through a face: the tolerance band)."""
+    ref: the fixture arrays.  Returns a list of human-readable mismatches."""
     errs = []
     n = len(ref["ids"])
     if len(got.ids) != n:
@@ -166,9 +161,6 @@ def compare_cells(got, ref, vol_rtol, cen_rtol, label="", own_as_unit=False):
     for k in np.nonzero(m)[0]:
         a = np.asarray(got.neighbors(k))
         b = ref["nb"][ref["nb_off"][k]:ref["nb_off"][k + 1]]
-        if own_as_unit:
-            a = np.where(a == ref["ids"][k], 0, a)
-            b = np.sort(np.where(b == ref["ids"][k], 0, b))
         if len(a) != len(b) or not np.array_equal(np.sort(a), b):
             nbad += 1
     if nbad:

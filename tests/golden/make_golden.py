@@ -59,6 +59,24 @@ def cases():
     X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
     xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
     out["degenerate_cubic_216"] = W._pack(W.KIND_CONTAINER, (0, 6, 0, 6, 0, 6), (3, 3, 3), (False,) * 3, xyz)
+    out.update(degenerate_cases())
+    return out
+
+
+# Exactly degenerate lattices whose cells have vertices of order 4: the FCC
+# lattice (every cell a rhombic dodecahedron, six of its fourteen vertices of
+# order 4), periodic and in a walled box.
+def degenerate_cases():
+    out = {}
+    out["degenerate_fcc_256"] = W.fcc_jitter(cells=4, sigma=0.0, seed=2010)
+    w = W.fcc_jitter(cells=4, sigma=0.0, seed=2011, kind=W.KIND_CONTAINER)
+    w["periodic"] = (False, False, False)
+    # shifted so that no wall of the box passes through a lattice vertex; the
+    # walls still meet the lattice's degenerate edges
+    w["xyzr"][:, :3] += 0.3
+    w["geom"] = (0.0, 4.5, 0.0, 4.5, 0.0, 4.5)
+    w["grid"] = (3, 3, 3)
+    out["degenerate_fcc_walled_256"] = w
     return out
 
 
@@ -156,14 +174,15 @@ def make_wall_fixtures(ref):
 # normal and vertex loop; surface area; total edge distance) and its
 # print_custom output for every cell over the fields that do not depend on
 # vertex or face numbering.
-POLY_NAMES = ["unit_cube_1000", "radical_1200", "periodic_poly_800", "sparse_dropped_40", "degenerate_cubic_216"]
+POLY_NAMES = ["unit_cube_1000", "radical_1200", "periodic_poly_800", "sparse_dropped_40", "degenerate_cubic_216",
+              "degenerate_fcc_256", "degenerate_fcc_walled_256"]
 POLY_CELLS = 200
 CUSTOM_FORMAT = "%i %q %r %w %s %v %c %C %m %g %F %E %A %o"
 
 
-def make_poly_fixtures(ref, all_cases):
+def make_poly_fixtures(ref, all_cases, names=None):
     import tempfile
-    for name in POLY_NAMES:
+    for name in names or POLY_NAMES:
         w = all_cases[name]
         cells = ref.polytopes(w)[:POLY_CELLS]
         flat = []
@@ -270,6 +289,12 @@ def main():
         return
     if "--tric-only" in sys.argv:
         make_tric_fixtures(ref)
+        return
+    if "--degenerate-only" in sys.argv:
+        dc = degenerate_cases()
+        for name, w in dc.items():
+            make_cell_fixture(ref, name, w)
+        make_poly_fixtures(ref, dc, names=list(dc))
         return
     if "--tric-large-only" in sys.argv:
         make_tric_large_fixture(ref)

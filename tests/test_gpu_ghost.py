@@ -22,14 +22,10 @@ def test_ghost_cells_match_reference(gpu, name, mode):
     ok = z["ok"] != 0
     assert np.array_equal(res.ok, ok)
     assert np.array_equal(res.nf[ok], z["nf"][ok])
-    # vertex counts exactly, except in cells the engine flags marginal: there
-    # (exactly degenerate vertices, as a ghost among lattice points has) the
-    # reference merges vertices into ones of order 4 or more, the engine keeps
-    # order 3
-    marginal = (res.flags & vg.VGPU_CELL_MARGINAL) != 0
-    exact = ok & ~marginal
-    assert np.array_equal(res.nv[exact], z["nv"][exact])
-    assert np.all(res.nv[ok] >= z["nv"][ok])
+    # vertex counts exactly, also in cells with vertices of order 4 or more (a
+    # ghost among exactly degenerate lattice points: the engine merges the
+    # coincident vertices of its cuts as the reference does)
+    assert np.array_equal(res.nv[ok], z["nv"][ok])
     for k in np.nonzero(ok)[0]:
         ref = z["nb"][z["nb_off"][k]:z["nb_off"][k + 1]]
         assert np.array_equal(np.sort(res.neighbors(k)), ref), k

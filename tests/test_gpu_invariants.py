@@ -6,7 +6,8 @@ properties, plus bit-exact topology against the CPU port on a seeded sample:
   lists j — periodic images included);
 * Euler's relation for simple polyhedra, V = 2F − 4 (every vertex the engine
   produces has order 3);
-* MIXED and FP64 engines give the same topology (4M periodic box);
+* MIXED and FP64 engines give the same topology on every cell, volumes and
+  centroids within 1e-10;
 * a seeded sample of cells matches the CPU port (which is bit-exact with the
   reference) in face count, vertex count and neighbour multiset, with volume
   and centroid within the engine's tolerance."""
@@ -59,7 +60,8 @@ def test_sheared_box_full_size_invariants(gpu):
         vbox = G.box_volume(w)
         assert abs(con.sum_cell_volumes() - vbox) <= 1e-9 * vbox
         assert np.all(r.ok)
-        assert np.array_equal(r.nv, 2 * r.nf - 4), "Euler relation V = 2F - 4"
+        simple = (r.flags & vg.VGPU_CELL_MARGINAL) == 0   # (merged vertices: V < 2F - 4)
+        assert np.array_equal(r.nv[simple], 2 * r.nf[simple] - 4), "Euler relation V = 2F - 4"
         assert _symmetric(r), "neighbour relation not symmetric"
         res[mode] = r
     a, b = res["mixed"], res["fp64"]
@@ -82,7 +84,11 @@ def test_full_size_invariants_and_sample_parity(gpu, port, name):
     ok = res.ok
     vbox = G.box_volume(w)
     assert abs(con.sum_cell_volumes() - vbox) <= 1e-9 * vbox
-    assert np.array_equal(res.nv[ok], 2 * res.nf[ok] - 4), "Euler relation V = 2F - 4"
+    # Euler's relation: V = 2F - 4 where every vertex has order 3, V < 2F - 4
+    # where the tolerance band merged vertices into ones of higher order
+    simple = ok & ((res.flags & vg.VGPU_CELL_MARGINAL) == 0)
+    assert np.array_equal(res.nv[simple], 2 * res.nf[simple] - 4), "Euler relation V = 2F - 4"
+    assert np.all(res.nv[ok] <= 2 * res.nf[ok] - 4)
     assert _symmetric(res), "neighbour relation not symmetric"
 
     rng = np.random.default_rng(7)
@@ -104,20 +110,55 @@ def test_full_size_invariants_and_sample_parity(gpu, port, name):
 
 
 @pytest.mark.gpu
-def test_mixed_and_fp64_agree_on_the_4m_periodic_box(gpu):
-    w = W.periodic_cube()
+@pytest.mark.parametrize("name", ["periodic_4m", "radical_2m", "fcc_jitter_1m", "unit_cube_100k"])
+def test_mixed_and_fp64_agree_on_every_cell(gpu, name):
+    """The mixed engine against the plain FP64 engine on every cell of the
+    full-size workloads: identical deleted flags, face and vertex counts and
+    neighbour lists; volume within 1e-10 relative and centroid within 1e-10
+    of the cell size."""
+    w = CASES[name][0]()
     a = vg.from_workload(w, mode="mixed")
+    a.set_fp64_fallback(1.0)   # the FP32 engine on every cell, even where its filter band is saturated
     b = vg.from_workload(w, mode="fp64")
     ra, rb = a.cells(), b.cells()
+    assert a.stats()["fp64_engine_cells"] == 0
+    assert np.array_equal(ra.ok, rb.ok)
     assert np.array_equal(ra.nf, rb.nf)
     assert np.array_equal(ra.nv, rb.nv)
     assert np.array_equal(ra.nb_off, rb.nb_off)
     assert np.array_equal(ra.nb, rb.nb)
-    assert (np.abs(ra.vol - rb.vol) / rb.vol).max() <= 1e-10
+    ok = rb.ok
+    assert (np.abs(ra.vol[ok] - rb.vol[ok]) / rb.vol[ok]).max() <= 1e-10
+    scale = np.cbrt(rb.vol[ok])[:, None]
+    assert (np.abs(ra.cen[ok] - rb.cen[ok]) / scale).max() <= 1e-10
     sa, sb = a.stats(), b.stats()
-    # the FP64 fallback rate of the mixed engine
-    assert sa["fp64_repairs"] <= 0.01 * sa["side_tests"]
-    assert sb["marginal_cells"] == 0
+    assert sa["failed_cells"] == 0 and sb["failed_cells"] == 0
+    if name != "fcc_jitter_1m":
+        # generic input: few FP64 repairs, and even the FP64 engine's own
+        # rounding band is never met (the jittered lattice meets both on purpose)
+        assert sa["fp64_repairs"] <= 0.01 * sa["side_tests"]
+        assert sb["marginal_cells"] == 0
+
+
+@pytest.mark.gpu
+def test_saturated_filter_band_switches_to_the_fp64_engine(gpu):
+    """A mixed compute samples its FP32 first pass; on the jittered FCC lattice
+    (every cell meets the filter band) the whole container runs on the FP64
+    engine, with the same topology as the FP32 engine forced through; on
+    uniform input nothing switches."""
+    w = W.fcc_jitter()
+    a = vg.from_workload(w, mode="mixed")
+    ra = a.cells()
+    assert a.stats()["fp64_engine_cells"] == len(ra)
+    f = vg.from_workload(w, mode="mixed")
+    f.set_fp64_fallback(1.0)
+    rf = f.cells()
+    assert np.array_equal(ra.nf, rf.nf) and np.array_equal(ra.nv, rf.nv)
+    assert np.array_equal(ra.nb_off, rf.nb_off) and np.array_equal(ra.nb, rf.nb)
+    assert (np.abs(ra.vol - rf.vol) / ra.vol).max() <= 1e-10
+    u = vg.from_workload(W.periodic_cube(n=500_000, L=50.0, grid=(46, 46, 46)), mode="mixed")
+    u.compute_all_cells()
+    assert u.stats()["fp64_engine_cells"] == 0
 
 
 @pytest.mark.gpu

@@ -22,7 +22,7 @@ def test_fixture_parity(gpu, name, mode):
     con.compute_all_cells()
     got = con.cells()
     st = con.stats()
-    errs = G.compare_cells(got, z, *TOL[mode], label=f"{name}/{mode}", own_as_unit="tric_small" in name)
+    errs = G.compare_cells(got, z, *TOL[mode], label=f"{name}/{mode}")
     assert not errs, "\n".join(errs) + f"\nstats {st}"
     if not name.startswith("degenerate"):
         # generic inputs never touch the reference's tolerance band

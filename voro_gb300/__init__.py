@@ -57,7 +57,7 @@ EXPORTED = [
     "vgpu_set_output", "vgpu_get_polytopes", "vgpu_find_voronoi_cells", "vgpu_compute_ghost_cells",
     "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes", "vgpu_add_wall",
     "vgpu_clear_walls", "vgpu_point_inside_walls",
-    "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts",
+    "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts", "vgpu_set_fp64_fallback",
 ]
 
 
@@ -74,7 +74,7 @@ class Stats(ctypes.Structure):
                 ("overflow_reruns", ctypes.c_int64), ("failed_cells", ctypes.c_int64),
                 ("kernel_ms", ctypes.c_double), ("bin_ms", ctypes.c_double), ("step_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("clip_ms", ctypes.c_double),
-                ("finish_ms", ctypes.c_double)]
+                ("finish_ms", ctypes.c_double), ("fp64_engine_cells", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -123,6 +123,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_set_tuning.argtypes = [vp, ctypes.c_double, ctypes.c_int]
     lib.vgpu_set_ghost_depth.argtypes = [vp, ctypes.c_double]
     lib.vgpu_set_record_budget.argtypes = [vp, ctypes.c_int64]
+    lib.vgpu_set_fp64_fallback.argtypes = [vp, ctypes.c_double]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_phase_counts.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
@@ -461,6 +462,13 @@ class _ContainerBase:
             self._dirty = False
         _check(rc)
 
+    def set_fp64_fallback(self, fraction=0.25):
+        """Mixed computes of large containers: the fraction of a sample of
+        cells needing FP64 above which the whole container runs on the FP64
+        engine (>= 1: never)."""
+        _check(self._lib.vgpu_set_fp64_fallback(self._h, float(fraction)))
+        self._dirty = True
+
     def set_record_budget(self, nbytes=0):
         """Record-store budget of one compute in bytes (0: the default).  Cells
         whose records do not fit fail with VGPU_FAIL_RECORDS and the compute
@@ -634,7 +642,7 @@ def _needs_polytope(fmt):
     i = 0
     while i < len(fmt) - 1:
         if fmt[i] == "%":
-            if fmt[i + 1] in _POLY_FIELDS and fmt[i + 1] != "o":
+            if fmt[i + 1] in _POLY_FIELDS:
                 return True
             i += 2
         else:
@@ -708,14 +716,11 @@ def _format_custom(fmt, res, k, radius):
         elif f == "w":
             out.append("%d" % res.nv[k])
         elif f == "o":
-            if res.poly_off is not None:
-                out.append(_poly_field("o", res.polytope(k), x, y, z))
-            else:   # every vertex the engine produces has order 3
-                out.append(" ".join(["3"] * int(res.nv[k])))
+            out.append(_poly_field("o", res.polytope(k), x, y, z))
         elif f == "m":
             out.append("%g" % res.maxr2[k])
-        elif f == "g":
-            out.append("%d" % (3 * int(res.nv[k]) // 2))
+        elif f == "g":   # Euler's relation: E = V + F - 2 for vertices of any order
+            out.append("%d" % (int(res.nv[k]) + int(res.nf[k]) - 2))
         elif f == "s":
             out.append("%d" % res.nf[k])
         elif f == "n":

@@ -208,6 +208,8 @@ struct vgpu_container {
     vgpu_stats stats{};
     double phase[16] = {};
     int64_t record_bytes = 0;   // record-store budget of one compute (0: kRecWordsPerCell per cell)
+    double fp64_fallback = 0.25;   // hand-on fraction of the sample above which a mixed compute runs FP64
+    int cell_chunk = 0;            // cells per work-queue grab (0: built-in default)
 };
 
 namespace {
@@ -718,6 +720,12 @@ int vgpu_set_ghost_depth(vgpu_container *h, double spacings) {
     return VGPU_OK;
 }
 
+int vgpu_set_fp64_fallback(vgpu_container *h, double fraction) {
+    if (!h || !(fraction >= 0.0)) return fail(VGPU_ERR_ARG, "bad fallback fraction");
+    h->fp64_fallback = fraction;
+    return VGPU_OK;
+}
+
 int vgpu_set_record_budget(vgpu_container *h, int64_t bytes) {
     if (!h || bytes < 0) return fail(VGPU_ERR_ARG, "bad record budget");
     h->record_bytes = bytes;
@@ -991,6 +999,7 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     const Geometry &g = h->g;
     const int nkept = h->nkept;
     memset(&cp, 0, sizeof(cp));
+    cp.cell_chunk = h->cell_chunk;
     cp.g = g;
     cp.a.p64 = h->p64.as<double4>();
     cp.a.l32 = h->lffh.as<float4>();
@@ -1181,11 +1190,19 @@ int setup_member_records(vgpu_container *h, CellParams &cp, Counters *cnt, cudaS
 // FP64: 64 slots, then 128 slots (cnt2).  sum: the passes' counters added,
 // overflow = cells the first pass handed on, failed = cells the last pass
 // run could not complete.
+// first: cells at the start of cp's range whose first pass has already run
+// (with the same counters, whose work counters the caller has reset).
 int clip_passes(cudaStream_t s, int sms, int warps, int mode, const CellParams &cp, Counters *cnt1, Counters *cnt2,
-                int *list2, Counters &sum) {
+                int *list2, Counters &sum, int first = 0) {
     Counters c[3];
     memset(c, 0, sizeof(c));
-    VG_CUDA(launch_cells(cp, mode, 0, sms, s, warps));
+    CellParams p0 = cp;
+    if (first > 0) {
+        if (cp.cell_list) p0.cell_list = cp.cell_list + first;
+        else p0.cell_begin = cp.cell_begin + first;
+        p0.ncells = cp.ncells - first;
+    }
+    VG_CUDA(launch_cells(p0, mode, 0, sms, s, warps));
     VG_CUDA(cudaMemcpyAsync(&c[0], cp.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
     unsigned long long pending = c[0].overflow;
@@ -1287,6 +1304,14 @@ namespace {
 
 // One compute: binning (thin: a sheared box may store thin ghost layers),
 // the clipping passes and the finish kernel.
+// Mixed computes of containers of at least kSampleMinCells cells sample the
+// FP64-free first pass on their first cells (engine order: a compact region);
+// measured on the jittered 64^3 FCC lattice (1M cells), where every cell meets
+// the FP32 filter band, the mixed engine ran at 6.9M cells/s and the FP64
+// engine at 10.0M, while on uniform input 2.3 % of the cells are handed on.
+constexpr int kSampleMinCells = 1 << 18;
+constexpr int kSampleFraction = 64;
+
 int compute_cells(vgpu_container *h, int mode, bool thin) {
     CellParams cp;
     int rc = prepare_cells(h, mode, cp, thin);
@@ -1300,9 +1325,33 @@ int compute_cells(vgpu_container *h, int mode, bool thin) {
     cudaEventRecord(h->ev[2], s);
     VG_CUDA(h->ovf_list2.ensure((size_t)std::max(h->nkept, 1) * 4));
     VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, 2 * sizeof(Counters), s));
+    int first = 0;
+    bool switched = false;
+    if (mode == VGPU_MIXED && h->fp64_fallback < 1.0 && cp.ncells >= kSampleMinCells) {
+        CellParams ps = cp;
+        ps.ncells = cp.ncells / kSampleFraction;
+        VG_CUDA(launch_cells(ps, mode, 0, h->sms, s, h->warps_per_cta));
+        Counters c0;
+        VG_CUDA(cudaMemcpyAsync(&c0, cp.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+        VG_CUDA(cudaStreamSynchronize(s));
+        if ((double)c0.overflow > h->fp64_fallback * ps.ncells) {
+            // the filter band is saturated: the whole container on the FP64 engine
+            mode = VGPU_FP64;
+            switched = true;
+            VG_CUDA(cudaMemsetAsync(cp.cnt, 0, sizeof(Counters), s));
+            rc = setup_records(h, mode, cp, cp.cnt, s, store.buf);
+            if (rc != VGPU_OK) return rc;
+        } else {
+            first = ps.ncells;   // the first pass continues after the sample
+            // (a launch over a cell list, as a sheared box's, takes its work
+            // from the second queue counter)
+            VG_CUDA(cudaMemsetAsync(&cp.cnt->work, 0, sizeof(unsigned long long), s));
+            VG_CUDA(cudaMemsetAsync(&cp.cnt->overflow_work, 0, sizeof(unsigned long long), s));
+        }
+    }
     Counters c1;
     rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, h->counters2.as<Counters>(),
-                     h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1);
+                     h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1, first);
     if (rc != VGPU_OK) return rc;
     cudaEventRecord(h->ev[4], s);
     VG_CUDA(launch_finish(cp, mode, h->sms, s));
@@ -1320,6 +1369,7 @@ int compute_cells(vgpu_container *h, int mode, bool thin) {
     rc = finish_compute(h, c1, cell_ms);
     h->stats.clip_ms = clip_ms;
     h->stats.finish_ms = fin_ms;
+    h->stats.fp64_engine_cells = switched ? h->nkept : 0;
     return rc;
 }
 
@@ -1384,7 +1434,15 @@ int assemble_polytopes(vgpu_container *h, size_t n, const DevBuf &poff, const De
         if (off[k] >= 0) {
             if ((unsigned long long)off[k] + 2 > used)
                 return fail(VGPU_ERR_INTERNAL, "polytope offset %lld beyond the store (%llu)", off[k], used);
-            len = 2 + 6 * (int64_t)store[off[k]] + 2 * (int64_t)store[off[k] + 1];
+            // [nv, nf, 3 nv coordinates, then per face: neighbour, order, loop]
+            // (the orders sum to 3 nv unless the cell has merged vertices)
+            const int64_t nvk = (int64_t)store[off[k]], nfk = (int64_t)store[off[k] + 1];
+            len = 2 + 3 * nvk;
+            for (int64_t f = 0; f < nfk; f++) {
+                if ((unsigned long long)(off[k] + len + 2) > used)
+                    return fail(VGPU_ERR_INTERNAL, "polytope of cell %zu runs beyond the store", k);
+                len += 2 + (int64_t)store[off[k] + len + 1];
+            }
             if ((unsigned long long)(off[k] + len) > used)
                 return fail(VGPU_ERR_INTERNAL, "polytope of cell %zu runs beyond the store", k);
         }

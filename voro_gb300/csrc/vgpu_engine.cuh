@@ -119,6 +119,10 @@ struct WarpShared {
     unsigned char vmap[32 * K];   // finished cell: vertex slot -> compact index
     unsigned char startN[kMaxPlanes];
     unsigned char endN[kMaxPlanes];
+    // the warp's counters over its cells (side tests, repairs, planes tested,
+    // planes cut, deleted, marginal): kept here rather than in registers,
+    // which the clipping loop needs more
+    unsigned long long stat[6];
     union {
         struct {
             unsigned ck[kCandBuf];    // sort keys
@@ -271,9 +275,8 @@ __device__ __forceinline__ double4 plane64_slot(const CellParams &P, const WarpS
 template <int MODE, int K>
 __device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpShared<MODE, K> &S, double4 me, int cb,
                                               unsigned uncbits, unsigned tri0, unsigned tri1, unsigned tri2,
-                                              unsigned tri3, bool *marginal) {
-    unsigned outbits = 0;
-    bool anym = false;
+                                              unsigned tri3, unsigned *bandbits) {
+    unsigned outbits = 0, band = 0;
     if (uncbits) {
         const int cj = S.u.c.cj[cb];   // (a wall: -1, with its face index in cs)
         const double4 Q = cj >= 0 ? plane64_from(P, me, cj, S.u.c.cs[cb]) : initial64(P, me, S.u.c.cs[cb]);
@@ -291,12 +294,12 @@ __device__ __noinline__ unsigned repair_tests(const CellParams &P, const WarpSha
             const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
             const double verr = 16.0 * kU64 * (double)kn / fabs(D) + 64.0 * kU64 * vv;
             const double bnd = nq * verr + 8.0 * kU64 * (nq * vv + fabs(Q.w)) + P.g.tol_h;
-            if (!(D > 0.0)) anym = true;
+            if (!(D > 0.0)) band |= 1u << s;
             else if (v > bnd) outbits |= 1u << s;
-            else if (v >= -bnd) anym = true;
+            else if (v >= -bnd) band |= 1u << s;
         }
     }
-    *marginal = anym;
+    *bandbits = band;
     return outbits;
 }
 
@@ -530,13 +533,39 @@ struct Engine {
         return p;
     }
 
+    // ---- a candidate plane that cuts nothing but holds every vertex of a
+    //      face within the tolerance band is that face's plane (a periodic
+    //      box so sparse that a unit-cell face survives until the bisector of
+    //      the particle's own image, the same plane, is tested): the face
+    //      takes the candidate's ID, as the reference's facet construction
+    //      through vertices on the plane relabels it (src/cell.cc:1166-1355).
+    //      band: this lane's slots in the band.
+    __device__ void relabel_coplanar(int cb, unsigned band) {
+        unsigned long long on = 0ull, off = 0ull;
+#pragma unroll
+        for (int s = 0; s < K; s++)
+            if (Vm.test(lane + 32 * s)) {
+                const unsigned t = V.tri[s];
+                const unsigned long long f =
+                    (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+                if ((band >> s) & 1u) on |= f;
+                else off |= f;
+            }
+        const unsigned long long faces = warp_or64(on) & ~warp_or64(off);
+        if (lane == 0 && faces) {
+            const int id = S.u.c.cpid[cb];
+            for (unsigned long long m = faces; m; m &= m - 1ull) S.pid[__ffsll((long long)m) - 1] = id;
+        }
+        __syncwarp();
+    }
+
     // ---- test candidate (buffer slot cb) and cut the cell if it intersects.
     __device__ __forceinline__ void test_and_cut(int cb) {
         PHASE_BEGIN(t_test);
         C.ptested++;
         C.tests += (unsigned)Vm.popc();
         bool out[K];
-        unsigned uncbits = 0;
+        unsigned uncbits = 0, band = 0;
         if (MODE == VGPU_FP64) {
             const double4 Q = S.u.c.cd64[cb];
             const double nq = fabs(Q.x) + fabs(Q.y) + fabs(Q.z);
@@ -547,7 +576,8 @@ struct Engine {
                 out[s] = v > bnd;
                 if (!out[s] && v >= -bnd) uncbits |= 1u << s;
             }
-            if (__any_sync(kFull, uncbits != 0)) C.marginal = true;   // tolerance band: kept, cell flagged
+            band = uncbits;   // tolerance band: kept, cell flagged
+            if (__any_sync(kFull, uncbits != 0)) C.marginal = true;
         } else {
             const float4 Q = S.u.c.cd[cb];
             const float4 E = S.u.c.ce[cb];
@@ -569,10 +599,9 @@ struct Engine {
                 }
                 C.repaired = true;
                 C.repairs += __popc(ub);
-                bool m = false;
                 const unsigned ob = repair_tests<MODE, K>(P, S, C.me64, cb, uncbits, V.tri[0], K > 1 ? V.tri[K > 1 ? 1 : 0] : 0u,
-                                                          K > 2 ? V.tri[K > 2 ? 2 : 0] : 0u, K > 3 ? V.tri[K > 3 ? 3 : 0] : 0u, &m);
-                if (__any_sync(kFull, m)) C.marginal = true;
+                                                          K > 2 ? V.tri[K > 2 ? 2 : 0] : 0u, K > 3 ? V.tri[K > 3 ? 3 : 0] : 0u, &band);
+                if (__any_sync(kFull, band != 0)) C.marginal = true;
 #pragma unroll
                 for (int s = 0; s < K; s++)
                     if ((uncbits >> s) & 1u) out[s] = (ob >> s) & 1u;
@@ -580,7 +609,10 @@ struct Engine {
         }
         const Mask<K> Rm = ballot_mask<K>(out);
         PHASE_END(t_test, 3);
-        if (!Rm.any()) return;
+        if (!Rm.any()) {
+            if (!kLean && __any_sync(kFull, band != 0)) relabel_coplanar(cb, band);
+            return;
+        }
         if (Rm.equals(Vm)) {
             C.deleted = true;
             return;
@@ -604,22 +636,24 @@ struct Engine {
             S.pshift[p] = S.u.c.cs[cb];
             if (MODE == VGPU_FP64) S.pl64x[p] = S.u.c.cd64[cb];
         }
-        cut(p, Rm);
+        cut(p, Rm, out);
         PHASE_END(t_cut, 4);
     }
 
     // ---- remove the vertices in Rm and close the hole with the face of plane p
-    __device__ __forceinline__ void cut(int p, const Mask<K> &Rm) {
+    // (out: this lane's slots in Rm, the side test's own predicates)
+    __device__ __forceinline__ void cut(int p, const Mask<K> &Rm, const bool (&out)[K]) {
         // Phase A: count boundary edges (edges from a removed vertex to a kept one)
-        unsigned bnd[K];
+        unsigned bnd[K], adj3[K];
         int nbe = 0;
         bool broken = false;
 #pragma unroll
         for (int s = 0; s < K; s++) {
             bnd[s] = 0;
-            const int t = lane + 32 * s;
-            if (Rm.test(t)) {
-                const unsigned A3 = S.adj[t];
+            adj3[s] = 0;
+            if (out[s]) {
+                const unsigned A3 = S.adj[lane + 32 * s];
+                adj3[s] = A3;
 #pragma unroll
                 for (int e = 0; e < 3; e++) {
                     const int u = (A3 >> (8 * e)) & 255u;
@@ -656,7 +690,7 @@ struct Engine {
             for (int s = 0; s < K; s++) {
                 if (bnd[s]) {
                     const unsigned T = V.tri[s];
-                    const unsigned A3 = S.adj[lane + 32 * s];
+                    const unsigned A3 = adj3[s];
 #pragma unroll
                     for (int e = 0; e < 3; e++)
                         if ((bnd[s] >> e) & 1u) {
@@ -1090,12 +1124,9 @@ struct Engine {
 #ifndef VGPU_MIN_BLOCKS
 #define VGPU_MIN_BLOCKS 6
 #endif
-// Largest CTA the clipping kernels are built for (threads); the default
-// launch uses 4 warps.
-#ifndef VGPU_CTA_THREADS
-#define VGPU_CTA_THREADS 128
-#endif
-constexpr int kMaxCtaWarps = VGPU_CTA_THREADS / 32;
+// Largest CTA the clipping kernels are built for (VGPU_CTA_THREADS, in
+// vgpu_internal.cuh); the default launch uses 4 warps.
+constexpr int kMaxCtaWarps = kBuiltCtaWarps;
 // CTAs per SM of the other engines: the full mixed 64-slot engine keeps
 // VGPU_FULL_MIN_BLOCKS (3: 168 registers), the 128-slot and FP64 engines 2.
 #ifndef VGPU_FULL_MIN_BLOCKS
@@ -1111,10 +1142,8 @@ constexpr int min_blocks() {
 // blocks) search nearly the same blocks, so a warp that runs them back to
 // back finds their block starts and particles in its SM's L1.  On the 4M
 // periodic box the clipping passes take 77.9 / 78.1 / 78.4 ms with chunks
-// of 4 / 8 / 16: within the run-to-run spread.
-#ifndef VGPU_CELL_CHUNK
-#define VGPU_CELL_CHUNK 8
-#endif
+// of 4 / 8 / 16: within the run-to-run spread.  (VGPU_CELL_CHUNK, in
+// vgpu_internal.cuh; per container: vgpu_tuning.cells_per_chunk.)
 
 template <int MODE, int K, bool LEAN>
 __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>()) cell_kernel(const __grid_constant__ CellParams P) {
@@ -1126,13 +1155,14 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
     for (int i = threadIdx.x; i < P.noffsets; i += blockDim.x) offsets[i] = P.offsets[i];
     __syncthreads();
     WarpShared<MODE, K> &S = ws[wid];
-    unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0;
+    if (lane < 6) S.stat[lane] = 0ull;
 #ifdef VGPU_PHASE_TIMING
     unsigned long long ph[16] = {};
     const long long t_kernel0 = clock64();
 #endif
     unsigned long long *work = P.cell_list ? &P.cnt->overflow_work : &P.cnt->work;
-    const int chunk = max(1, min(VGPU_CELL_CHUNK, P.ncells / (int)(4 * gridDim.x * (blockDim.x >> 5))));
+    const int chunk = max(1, min(P.cell_chunk > 0 ? P.cell_chunk : VGPU_CELL_CHUNK,
+                                 P.ncells / (int)(4 * gridDim.x * (blockDim.x >> 5))));
     int w = 0, wend = 0;
     for (;;) {
         if (w == wend) {
@@ -1141,35 +1171,35 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
             if (w >= P.ncells) break;
             wend = min(w + chunk, P.ncells);
         }
-        const int k = P.cell_list ? P.cell_list[w] : w;
+        const int k = P.cell_list ? P.cell_list[w] : P.cell_begin + w;
         w++;
         Engine<MODE, K, LEAN> eng(P, S, offsets, lane);
         eng.run(k);
-        tests += eng.C.tests;
-        repairs += eng.C.repairs;
-        ptested += eng.C.ptested;
-        pcut += eng.C.pcut;
 #ifdef VGPU_PHASE_TIMING
         for (int i = 0; i < 16; i++) ph[i] += eng.C.phase[i];
 #endif
-        if (eng.C.overflow) {
-            if (lane == 0) {
+        if (lane == 0) {
+            S.stat[0] += eng.C.tests;
+            S.stat[1] += eng.C.repairs;
+            S.stat[2] += eng.C.ptested;
+            S.stat[3] += eng.C.pcut;
+            if (eng.C.overflow) {
                 const unsigned long long slot = atomicAdd(&P.cnt->overflow, 1ull);
                 if (P.overflow_list) P.overflow_list[slot] = k;
+            } else {
+                S.stat[4] += eng.C.deleted ? 1 : 0;
+                S.stat[5] += eng.C.marginal ? 1 : 0;
             }
-        } else {
-            deleted += eng.C.deleted ? 1 : 0;
-            marginal += eng.C.marginal ? 1 : 0;
         }
         __syncwarp();
     }
     if (lane == 0) {
-        atomicAdd(&P.cnt->side_tests, tests);
-        atomicAdd(&P.cnt->fp64_repairs, repairs);
-        atomicAdd(&P.cnt->planes_tested, ptested);
-        atomicAdd(&P.cnt->planes_cut, pcut);
-        atomicAdd(&P.cnt->deleted, deleted);
-        atomicAdd(&P.cnt->marginal, marginal);
+        atomicAdd(&P.cnt->side_tests, S.stat[0]);
+        atomicAdd(&P.cnt->fp64_repairs, S.stat[1]);
+        atomicAdd(&P.cnt->planes_tested, S.stat[2]);
+        atomicAdd(&P.cnt->planes_cut, S.stat[3]);
+        atomicAdd(&P.cnt->deleted, S.stat[4]);
+        atomicAdd(&P.cnt->marginal, S.stat[5]);
 #ifdef VGPU_PHASE_TIMING
         ph[7] = (unsigned long long)(clock64() - t_kernel0);
         for (int i = 0; i < 16; i++) atomicAdd(&P.cnt->phase_cycles[i], ph[i]);

@@ -145,16 +145,27 @@ __device__ __forceinline__ PlaneFF plane_ff(const CellParams &P, int bk[3], floa
     return {d[0], d[1], d[2], ff_scale(rs, 0.5f)};
 }
 
-// The FP32 vertex (fx, fy, fz) of planes t corrected by one residual step:
-// residuals r = h - n.v against the planes' float pairs (exact products of
-// the pairs and the floats, pair sums), the correction A^-1 r solved in FP32
-// with the planes' FP32 normals, and the vertex returned as the pair
-// v + correction.  A nearly singular FP32 system (|D| <= 1e-3 of the product
-// of the normals' norms) is solved in FP64 from the FP64 planes instead,
-// rebuilt for it.
+// The FP32 vertex (fx, fy, fz) of planes t corrected by residual steps:
+// residuals r = h - n.v against the planes' float pairs (pair products and
+// sums), the correction A^-1 r solved in FP32 with the planes' FP32 normals,
+// and the vertex returned as the pair v + correction.  Each step multiplies
+// the vertex's error by about kappa u (kappa = |A| |A^-1|, u = 2^-24), and the
+// FP32 vertex starts with an error of about kappa u |v|, so one step leaves
+// (kappa u)^2 |v|: enough for kappa up to about 1 / kOneStepDet (the volume
+// then agrees with the FP64 engine's to ~1e-12); up to 1 / kFp64Det a second
+// step starts from the pair vertex.  A nearly singular FP32 system (|D| <=
+// kFp64Det of the product of the normals' norms), or force64, is solved in
+// FP64 from the FP64 planes instead, rebuilt for it.  (With one step up to
+// kappa = 1000 a cell of the 2M radical box differed from the FP64 engine by
+// 6.5e-9.)
+constexpr float kFp64Det = 1e-3f;
+constexpr float kOneStepDet = 3e-2f;
+// cells smaller than this fraction of R^3 (R: largest vertex distance from
+// the particle) get FP64 vertices (finish_record)
+constexpr double kTinyRel = 1e-4;
 template <class FS>
 __device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FS &F, double4 me, unsigned t,
-                                                 float fx, float fy, float fz, FF &vx, FF &vy, FF &vz) {
+                                                 float fx, float fy, float fz, bool force64, FF &vx, FF &vy, FF &vz) {
     const int ia = tri_plane(t, 0), ib = tri_plane(t, 1), ic = tri_plane(t, 2);
     const float4 a = F.plh[ia], b = F.plh[ib], c = F.plh[ic];
     const float bcx = b.y * c.z - b.z * c.y, bcy = b.z * c.x - b.x * c.z, bcz = b.x * c.y - b.y * c.x;
@@ -163,7 +174,7 @@ __device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FS &
     const float D = a.x * bcx + a.y * bcy + a.z * bcz;
     const float scale = (fabsf(a.x) + fabsf(a.y) + fabsf(a.z)) * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z)) *
                         (fabsf(c.x) + fabsf(c.y) + fabsf(c.z));
-    if (fabsf(D) > 1e-3f * scale) {
+    if (!force64 && fabsf(D) > kFp64Det * scale) {
         float r[3];
         const int ip[3] = {ia, ib, ic};
 #pragma unroll
@@ -178,6 +189,19 @@ __device__ __forceinline__ void refine_vertex_ff(const CellParams &P, const FS &
         vx = ff_two_sum(fx, (r[0] * bcx + r[1] * cax + r[2] * abx) * inv);
         vy = ff_two_sum(fy, (r[0] * bcy + r[1] * cay + r[2] * aby) * inv);
         vz = ff_two_sum(fz, (r[0] * bcz + r[1] * caz + r[2] * abz) * inv);
+        if (fabsf(D) <= kOneStepDet * scale) {   // a second step from the pair vertex
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                const float4 h = F.plh[ip[q]], l = F.pll[ip[q]];
+                FF acc = ff_mul({h.x, l.x}, vx);
+                acc = ff_add(acc, ff_mul({h.y, l.y}, vy));
+                acc = ff_add(acc, ff_mul({h.z, l.z}, vz));
+                r[q] = ff_sub({h.w, l.w}, acc).h;
+            }
+            vx = ff_add(vx, {(r[0] * bcx + r[1] * cax + r[2] * abx) * inv, 0.0f});
+            vy = ff_add(vy, {(r[0] * bcy + r[1] * cay + r[2] * aby) * inv, 0.0f});
+            vz = ff_add(vz, {(r[0] * bcz + r[1] * caz + r[2] * abz) * inv, 0.0f});
+        }
     } else {
         double x, y, z, DD;
         float kn;
@@ -315,193 +339,366 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
         }
     }
     __syncwarp();
-    // vertices (particle-relative): FP64 (vd) or float pairs (vf)
+    // vertices (particle-relative): FP64 (vd) or float pairs (vf).  Float-pair
+    // vertices are within about 2^-46 of their distance from the particle,
+    // which is far inside the tolerance for every cell but a tiny one far
+    // from its particle (a radical cell squeezed between large neighbours:
+    // volume 1e-11 at distance 2 in the 2M radical box, where it made a
+    // relative error of 4e-10).  A cell whose volume is below kTinyRel of
+    // the cube of its largest vertex distance is therefore done again with
+    // every vertex solved in FP64 from the FP64 planes (force64): both halves
+    // of the warp run the second pass when either needs it.  A cell that met
+    // the tolerance band (marginal) gets FP64 vertices from the start: its
+    // coincident vertices are merged below by their distance.
     unsigned tri[SL];
     double vd[SL][3];
     FF vf[SL][3];
     double mr2 = 0.0;
     FF mf = {0.0f, 0.0f};
-#pragma unroll
-    for (int s = 0; s < SL; s++) {
-        const int t = gl + G * s;
-        tri[s] = 0;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            vd[s][a] = 0.0;
-            vf[s][a] = {0.0f, 0.0f};
-        }
-        if (t < nv) {
-            tri[s] = rv[t];
-            F.tri[t] = tri[s];
-            F.adj[t] = rv[nv + t];
-            if (kFF) {
-                refine_vertex_ff(P, F, me, tri[s], __uint_as_float(rv[2 * nv + t]), __uint_as_float(rv[3 * nv + t]),
-                                 __uint_as_float(rv[4 * nv + t]), vf[s][0], vf[s][1], vf[s][2]);
-                const FF q = ff_add(ff_add(ff_mul(vf[s][0], vf[s][0]), ff_mul(vf[s][1], vf[s][1])),
-                                    ff_mul(vf[s][2], vf[s][2]));
-                if (ff_less(mf, q)) mf = q;
-            } else {
-#pragma unroll
-                for (int a = 0; a < 3; a++) vd[s][a] = rec_double(rv + (2 + 2 * a) * nv + 2 * t);
-                mr2 = fmax(mr2, vd[s][0] * vd[s][0] + vd[s][1] * vd[s][1] + vd[s][2] * vd[s][2]);
-            }
-#pragma unroll
-            for (int e = 0; e < 3; e++) {
-                atomicMin(&F.rep[tri_plane(tri[s], e)], t);
-                atomicAdd(&F.ford[tri_plane(tri[s], e)], 1);
-            }
-        }
-    }
-    // the largest |v|^2 over the group and, for the pairs, the power of two
-    // 2^sc (about 2 sqrt(max |v|^2) >= |v - c0|) that scales the relative
-    // coordinates to magnitude about 1, so that their products neither
-    // underflow nor overflow
     int sc = 0;
-    if (kFF) {
-#pragma unroll
-        for (int dd = G / 2; dd >= 1; dd >>= 1) {
-            const FF o = {__shfl_xor_sync(kFull, mf.h, dd, G), __shfl_xor_sync(kFull, mf.l, dd, G)};
-            if (ff_less(mf, o)) mf = o;
-        }
-        if (mf.h > 0.0f && mf.h < 3.0e38f) sc = (ilogbf(mf.h) + 2) / 2 + 1;
-    } else {
-        mr2 = group_max_nonneg<G>(mr2);
-    }
-    // origin of the sums: vertex 0
     double c0[3];
     FF c0f[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        if (kFF) {
-            c0f[a] = {__shfl_sync(kFull, vf[0][a].h, 0, G), __shfl_sync(kFull, vf[0][a].l, 0, G)};
-            c0[a] = ff_to_double(c0f[a]);
-        } else {
-            c0[a] = __shfl_sync(kFull, vd[0][a], 0, G);
-        }
-    }
-    const float down = pow2f(-sc);
-    int ne = 0;
-    unsigned own[SL];
-#pragma unroll
-    for (int s = 0; s < SL; s++) {
-        own[s] = 0;
-        const int t = gl + G * s;
-        if (t < nv) {
-#pragma unroll
+    double vol_out = 0.0, cen_out[3] = {0.0, 0.0, 0.0};
+    const bool marg = have && (fl & VGPU_CELL_MARGINAL) != 0u;
+    for (int pass = 0;; pass++) {
+        const bool force64 = pass > 0 || marg;
+        mr2 = 0.0;
+        mf = {0.0f, 0.0f};
+    #pragma unroll
+        for (int s = 0; s < SL; s++) {
+            const int t = gl + G * s;
+            tri[s] = 0;
+    #pragma unroll
             for (int a = 0; a < 3; a++) {
+                vd[s][a] = 0.0;
+                vf[s][a] = {0.0f, 0.0f};
+            }
+            if (t < nv) {
+                tri[s] = rv[t];
+                F.tri[t] = tri[s];
+                F.adj[t] = rv[nv + t];
                 if (kFF) {
-                    const FF q = ff_scale(ff_sub(vf[s][a], c0f[a]), down);
-                    F.v.f.vh[a][t] = q.h;
-                    F.v.f.vl[a][t] = q.l;
+                    refine_vertex_ff(P, F, me, tri[s], __uint_as_float(rv[2 * nv + t]), __uint_as_float(rv[3 * nv + t]),
+                                     __uint_as_float(rv[4 * nv + t]), force64, vf[s][0], vf[s][1], vf[s][2]);
+                    const FF q = ff_add(ff_add(ff_mul(vf[s][0], vf[s][0]), ff_mul(vf[s][1], vf[s][1])),
+                                        ff_mul(vf[s][2], vf[s][2]));
+                    if (ff_less(mf, q)) mf = q;
                 } else {
-                    (a == 0 ? F.v.d.vx : (a == 1 ? F.v.d.vy : F.v.d.vz))[t] = vd[s][a] - c0[a];
+    #pragma unroll
+                    for (int a = 0; a < 3; a++) vd[s][a] = rec_double(rv + (2 + 2 * a) * nv + 2 * t);
+                    mr2 = fmax(mr2, vd[s][0] * vd[s][0] + vd[s][1] * vd[s][1] + vd[s][2] * vd[s][2]);
+                }
+                if (pass == 0)
+    #pragma unroll
+                    for (int e = 0; e < 3; e++) {
+                        atomicMin(&F.rep[tri_plane(tri[s], e)], t);
+                        atomicAdd(&F.ford[tri_plane(tri[s], e)], 1);
+                    }
+            }
+        }
+        // the largest |v|^2 over the group and, for the pairs, the power of two
+        // 2^sc (about 2 sqrt(max |v|^2) >= |v - c0|) that scales the relative
+        // coordinates to magnitude about 1, so that their products neither
+        // underflow nor overflow
+        sc = 0;
+        if (kFF) {
+    #pragma unroll
+            for (int dd = G / 2; dd >= 1; dd >>= 1) {
+                const FF o = {__shfl_xor_sync(kFull, mf.h, dd, G), __shfl_xor_sync(kFull, mf.l, dd, G)};
+                if (ff_less(mf, o)) mf = o;
+            }
+            if (mf.h > 0.0f && mf.h < 3.0e38f) sc = (ilogbf(mf.h) + 2) / 2 + 1;
+        } else {
+            mr2 = group_max_nonneg<G>(mr2);
+        }
+        // origin of the sums: vertex 0
+    #pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (kFF) {
+                c0f[a] = {__shfl_sync(kFull, vf[0][a].h, 0, G), __shfl_sync(kFull, vf[0][a].l, 0, G)};
+                c0[a] = ff_to_double(c0f[a]);
+            } else {
+                c0[a] = __shfl_sync(kFull, vd[0][a], 0, G);
+            }
+        }
+        const float down = pow2f(-sc);
+        int ne = 0;
+        unsigned own[SL];
+    #pragma unroll
+        for (int s = 0; s < SL; s++) {
+            own[s] = 0;
+            const int t = gl + G * s;
+            if (t < nv) {
+    #pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    if (kFF) {
+                        const FF q = ff_scale(ff_sub(vf[s][a], c0f[a]), down);
+                        F.v.f.vh[a][t] = q.h;
+                        F.v.f.vl[a][t] = q.l;
+                    } else {
+                        (a == 0 ? F.v.d.vx : (a == 1 ? F.v.d.vy : F.v.d.vz))[t] = vd[s][a] - c0[a];
+                    }
+                }
+                const unsigned A3 = F.adj[t];
+    #pragma unroll
+                for (int e = 0; e < 3; e++)
+                    if ((int)((A3 >> (8 * e)) & 255u) > t) own[s] |= 1u << e;
+                ne += __popc(own[s]);
+            }
+        }
+        const int eincl = group_incl_scan<G>(ne, gl);
+        const int etot = __shfl_sync(kFull, eincl, G - 1, G);
+        {
+            int q = eincl - ne;
+    #pragma unroll
+            for (int s = 0; s < SL; s++)
+    #pragma unroll
+                for (int e = 0; e < 3; e++)
+                    if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(gl + G * s) | ((unsigned)e << 8);
+        }
+        __syncwarp();
+        // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
+        double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
+        if (kFF) {
+            FF s0 = {0.0f, 0.0f}, s1 = s0, s2 = s0, s3 = s0;
+            for (int i = gl; i < etot; i += G) {
+                const unsigned E = F.stage[i];
+                const int t = E & 255u, e = E >> 8;
+                const unsigned T = F.tri[t];
+                const int u = (F.adj[t] >> (8 * e)) & 255u;
+                const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
+                FF tv[3], uv[3], av[3], bv[3];
+    #pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    tv[c] = {F.v.f.vh[c][t], F.v.f.vl[c][t]};
+                    uv[c] = {F.v.f.vh[c][u], F.v.f.vl[c][u]};
+                    av[c] = {F.v.f.vh[c][rx], F.v.f.vl[c][rx]};
+                    bv[c] = {F.v.f.vh[c][ry], F.v.f.vl[c][ry]};
+                }
+                const FF w[3] = {ff_sub(ff_mul(tv[1], uv[2]), ff_mul(tv[2], uv[1])),
+                                 ff_sub(ff_mul(tv[2], uv[0]), ff_mul(tv[0], uv[2])),
+                                 ff_sub(ff_mul(tv[0], uv[1]), ff_mul(tv[1], uv[0]))};
+                const FF dy = ff_add(ff_add(ff_mul(bv[0], w[0]), ff_mul(bv[1], w[1])), ff_mul(bv[2], w[2]));
+                const FF dx = ff_add(ff_add(ff_mul(av[0], w[0]), ff_mul(av[1], w[1])), ff_mul(av[2], w[2]));
+                const FF dd = ff_sub(dy, dx);
+                s0 = ff_add(s0, dd);
+                s1 = ff_add(s1, ff_sub(ff_add(ff_mul(dd, ff_add(tv[0], uv[0])), ff_mul(dy, bv[0])), ff_mul(dx, av[0])));
+                s2 = ff_add(s2, ff_sub(ff_add(ff_mul(dd, ff_add(tv[1], uv[1])), ff_mul(dy, bv[1])), ff_mul(dx, av[1])));
+                s3 = ff_add(s3, ff_sub(ff_add(ff_mul(dd, ff_add(tv[2], uv[2])), ff_mul(dy, bv[2])), ff_mul(dx, av[2])));
+            }
+            // the group's sums, then the outputs from pairs with few FP64
+            // operations: vol = s0 / 6 * 2^(3 sc); centroid = c0 + 2^sc C / (4 s0)
+            group_sum4_ff<G>(s0, s1, s2, s3, gl);
+            if (have && gl == 0) {
+                constexpr float kSixthH = (float)(1.0 / 6.0);
+                constexpr float kSixthL = (float)(1.0 / 6.0 - (double)(float)(1.0 / 6.0));
+                vol_out = ff_to_double(ff_mul(s0, {kSixthH, kSixthL})) * pow2d(3 * sc);
+                if (48.0 * vol_out > P.g.tol_cu) {   // src/cell.cc:1895
+                    const FF inv = ff_div({1.0f, 0.0f}, ff_scale(s0, 4.0f));
+                    const float up = pow2f(sc);
+                    const FF sc3[3] = {s1, s2, s3};
+    #pragma unroll
+                    for (int a = 0; a < 3; a++) cen_out[a] = ff_to_double(ff_add(c0f[a], ff_scale(ff_mul(sc3[a], inv), up)));
+                } else {
+                    cen_out[0] = cen_out[1] = cen_out[2] = 0.0;
                 }
             }
-            const unsigned A3 = F.adj[t];
-#pragma unroll
-            for (int e = 0; e < 3; e++)
-                if ((int)((A3 >> (8 * e)) & 255u) > t) own[s] |= 1u << e;
-            ne += __popc(own[s]);
-        }
-    }
-    const int eincl = group_incl_scan<G>(ne, gl);
-    const int etot = __shfl_sync(kFull, eincl, G - 1, G);
-    {
-        int q = eincl - ne;
-#pragma unroll
-        for (int s = 0; s < SL; s++)
-#pragma unroll
-            for (int e = 0; e < 3; e++)
-                if ((own[s] >> e) & 1u) F.stage[q++] = (unsigned)(gl + G * s) | ((unsigned)e << 8);
-    }
-    __syncwarp();
-    // sum over edges (t,u) of (p_y - p_x).(v_t x v_u), p_f a vertex of face f
-    double vs = 0.0, cx = 0.0, cy = 0.0, cz = 0.0;
-    if (kFF) {
-        FF s0 = {0.0f, 0.0f}, s1 = s0, s2 = s0, s3 = s0;
-        for (int i = gl; i < etot; i += G) {
-            const unsigned E = F.stage[i];
-            const int t = E & 255u, e = E >> 8;
-            const unsigned T = F.tri[t];
-            const int u = (F.adj[t] >> (8 * e)) & 255u;
-            const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
-            FF tv[3], uv[3], av[3], bv[3];
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                tv[c] = {F.v.f.vh[c][t], F.v.f.vl[c][t]};
-                uv[c] = {F.v.f.vh[c][u], F.v.f.vl[c][u]};
-                av[c] = {F.v.f.vh[c][rx], F.v.f.vl[c][rx]};
-                bv[c] = {F.v.f.vh[c][ry], F.v.f.vl[c][ry]};
+        } else {
+            for (int i = gl; i < etot; i += G) {
+                const unsigned E = F.stage[i];
+                const int t = E & 255u, e = E >> 8;
+                const unsigned T = F.tri[t];
+                const int u = (F.adj[t] >> (8 * e)) & 255u;
+                const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
+                const double tx = F.v.d.vx[t], ty = F.v.d.vy[t], tz = F.v.d.vz[t];
+                const double ux = F.v.d.vx[u], uy = F.v.d.vy[u], uz = F.v.d.vz[u];
+                const double wx = ty * uz - tz * uy;
+                const double wy = tz * ux - tx * uz;
+                const double wz = tx * uy - ty * ux;
+                const double ax = F.v.d.vx[rx], ay = F.v.d.vy[rx], az = F.v.d.vz[rx];
+                const double bx = F.v.d.vx[ry], by = F.v.d.vy[ry], bz = F.v.d.vz[ry];
+                const double dy = bx * wx + by * wy + bz * wz;
+                const double dx = ax * wx + ay * wy + az * wz;
+                const double dd = dy - dx;
+                vs += dd;
+                cx += dd * (tx + ux) + dy * bx - dx * ax;
+                cy += dd * (ty + uy) + dy * by - dx * ay;
+                cz += dd * (tz + uz) + dy * bz - dx * az;
             }
-            const FF w[3] = {ff_sub(ff_mul(tv[1], uv[2]), ff_mul(tv[2], uv[1])),
-                             ff_sub(ff_mul(tv[2], uv[0]), ff_mul(tv[0], uv[2])),
-                             ff_sub(ff_mul(tv[0], uv[1]), ff_mul(tv[1], uv[0]))};
-            const FF dy = ff_add(ff_add(ff_mul(bv[0], w[0]), ff_mul(bv[1], w[1])), ff_mul(bv[2], w[2]));
-            const FF dx = ff_add(ff_add(ff_mul(av[0], w[0]), ff_mul(av[1], w[1])), ff_mul(av[2], w[2]));
-            const FF dd = ff_sub(dy, dx);
-            s0 = ff_add(s0, dd);
-            s1 = ff_add(s1, ff_sub(ff_add(ff_mul(dd, ff_add(tv[0], uv[0])), ff_mul(dy, bv[0])), ff_mul(dx, av[0])));
-            s2 = ff_add(s2, ff_sub(ff_add(ff_mul(dd, ff_add(tv[1], uv[1])), ff_mul(dy, bv[1])), ff_mul(dx, av[1])));
-            s3 = ff_add(s3, ff_sub(ff_add(ff_mul(dd, ff_add(tv[2], uv[2])), ff_mul(dy, bv[2])), ff_mul(dx, av[2])));
-        }
-        // the group's sums, then the outputs from pairs with few FP64
-        // operations: vol = s0 / 6 * 2^(3 sc); centroid = c0 + 2^sc C / (4 s0)
-        group_sum4_ff<G>(s0, s1, s2, s3, gl);
-        if (have && gl == 0) {
-            constexpr float kSixthH = (float)(1.0 / 6.0);
-            constexpr float kSixthL = (float)(1.0 / 6.0 - (double)(float)(1.0 / 6.0));
-            const double vol = ff_to_double(ff_mul(s0, {kSixthH, kSixthL})) * pow2d(3 * sc);
-            P.r.vol[out] = vol;
-            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
-                const FF inv = ff_div({1.0f, 0.0f}, ff_scale(s0, 4.0f));
-                const float up = pow2f(sc);
-                const FF sc3[3] = {s1, s2, s3};
-#pragma unroll
-                for (int a = 0; a < 3; a++)
-                    P.r.cen[3 * out + a] = ff_to_double(ff_add(c0f[a], ff_scale(ff_mul(sc3[a], inv), up)));
-            } else {
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
+            group_sum4<G>(vs, cx, cy, cz, gl);
+            if (have && gl == 0) {
+                vol_out = vs / 6.0;
+                if (48.0 * vol_out > P.g.tol_cu) {   // src/cell.cc:1895
+                    const double f = 1.0 / (4.0 * vs);
+                    cen_out[0] = c0[0] + cx * f;
+                    cen_out[1] = c0[1] + cy * f;
+                    cen_out[2] = c0[2] + cz * f;
+                } else {
+                    cen_out[0] = cen_out[1] = cen_out[2] = 0.0;
+                }
             }
         }
-    } else {
-        for (int i = gl; i < etot; i += G) {
-            const unsigned E = F.stage[i];
-            const int t = E & 255u, e = E >> 8;
-            const unsigned T = F.tri[t];
-            const int u = (F.adj[t] >> (8 * e)) & 255u;
-            const int rx = F.rep[tri_plane(T, e)], ry = F.rep[tri_plane(T, e == 2 ? 0 : e + 1)];
-            const double tx = F.v.d.vx[t], ty = F.v.d.vy[t], tz = F.v.d.vz[t];
-            const double ux = F.v.d.vx[u], uy = F.v.d.vy[u], uz = F.v.d.vz[u];
-            const double wx = ty * uz - tz * uy;
-            const double wy = tz * ux - tx * uz;
-            const double wz = tx * uy - ty * ux;
-            const double ax = F.v.d.vx[rx], ay = F.v.d.vy[rx], az = F.v.d.vz[rx];
-            const double bx = F.v.d.vx[ry], by = F.v.d.vy[ry], bz = F.v.d.vz[ry];
-            const double dy = bx * wx + by * wy + bz * wz;
-            const double dx = ax * wx + ay * wy + az * wz;
-            const double dd = dy - dx;
-            vs += dd;
-            cx += dd * (tx + ux) + dy * bx - dx * ax;
-            cy += dd * (ty + uy) + dy * by - dx * ay;
-            cz += dd * (tz + uz) + dy * bz - dx * az;
-        }
-        group_sum4<G>(vs, cx, cy, cz, gl);
-        if (have && gl == 0) {
-            const double vol = vs / 6.0;
-            P.r.vol[out] = vol;
-            if (48.0 * vol > P.g.tol_cu) {   // src/cell.cc:1895
-                const double f = 1.0 / (4.0 * vs);
-                P.r.cen[3 * out] = c0[0] + cx * f;
-                P.r.cen[3 * out + 1] = c0[1] + cy * f;
-                P.r.cen[3 * out + 2] = c0[2] + cz * f;
-            } else {
-                P.r.cen[3 * out] = P.r.cen[3 * out + 1] = P.r.cen[3 * out + 2] = 0.0;
-            }
-        }
+        const double r2 = kFF ? ff_to_double(mf) : mr2;
+        const bool tiny = kFF && !force64 && have && gl == 0 && vol_out < kTinyRel * r2 * sqrt(r2);
+        if (!__any_sync(kFull, tiny)) break;
+        __syncwarp();
     }
     if (have && gl == 0) {
-        P.r.nf[out] = nb_full ? 0 : nf;
-        P.r.nv[out] = nv;
+        P.r.vol[out] = vol_out;
+#pragma unroll
+        for (int a = 0; a < 3; a++) P.r.cen[3 * out + a] = cen_out[a];
+    }
+    // Coincident vertices.  Where a cut plane passes through an existing
+    // vertex within the reference's tolerance band, the reference makes that
+    // vertex a vertex of the new face, of higher order (create_facet and the
+    // marginal-vertex handling of nplane, src/cell.cc:1166-1355), while the
+    // engine keeps every vertex of order 3: its cut leaves new vertices at
+    // the same point, joined to the old one by edges of zero length.  Only a
+    // cell that met the band (VGPU_CELL_MARGINAL) can hold such edges; there
+    // every edge shorter than the band's width as a distance, tol / 2 over
+    // the cell's largest vertex distance R (a plane of the cell is at most 2R
+    // from the particle, and its band is tol_h / |d| wide, |d| <= 2R), is
+    // contracted (label propagation over the contracted edges): two vertices
+    // that close lie within the reference's band of each other's planes, so
+    // nothing the reference keeps apart is merged.  This gives the
+    // reference's vertex count and, in the polytope, its vertices of higher
+    // order; a face that the merge reduces to an edge or a point (a plane that
+    // touched the cell only there) is no face of the reference's cell and is
+    // dropped.  Both halves of a warp run this when either needs it (it holds
+    // collectives).  lab[t]: after the propagation, the lowest vertex of t's
+    // class; then a class's lowest vertex holds -(1 + its rank).
+    int nvm = nv, nfm = nf;
+    const bool any_marg = __any_sync(kFull, marg);
+    int *lab = reinterpret_cast<int *>(F.stage);   // (free once the sums are done)
+    if (any_marg) {
+        __syncwarp();
+        unsigned zero[SL];
+        const double r2 = kFF ? ff_to_double(mf) : mr2;
+        // contraction length squared in the units of the staged coordinates
+        // (float pairs: scaled by 2^-sc)
+        const double eps = P.g.tol_h / (2.0 * sqrt(r2));
+        const double eps2 = eps * eps * (kFF ? (double)pow2f(-2 * sc) : 1.0);
+#pragma unroll
+        for (int s = 0; s < SL; s++) {
+            const int t = gl + G * s;
+            zero[s] = 0;
+            if (t < nv) {
+                lab[t] = t;
+                if (marg) {
+                    const unsigned A3 = F.adj[t];
+#pragma unroll
+                    for (int e = 0; e < 3; e++) {
+                        const int u = (A3 >> (8 * e)) & 255u;
+                        if (u <= t || u >= nv) continue;
+                        double d2 = 0.0;
+#pragma unroll
+                        for (int a = 0; a < 3; a++) {
+                            double d;
+                            if (kFF) d = ((double)F.v.f.vh[a][t] - (double)F.v.f.vh[a][u]) +
+                                         ((double)F.v.f.vl[a][t] - (double)F.v.f.vl[a][u]);
+                            else d = (a == 0 ? F.v.d.vx : (a == 1 ? F.v.d.vy : F.v.d.vz))[t] -
+                                     (a == 0 ? F.v.d.vx : (a == 1 ? F.v.d.vy : F.v.d.vz))[u];
+                            d2 += d * d;
+                        }
+                        if (d2 <= eps2) zero[s] |= 1u << e;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // propagate the smallest label along contracted edges (classes hold a
+        // few vertices: a vertex of order k splits into k - 2)
+        for (int it = 0; it < 4 * kFinMaxV; it++) {
+            bool changed = false;
+#pragma unroll
+            for (int s = 0; s < SL; s++) {
+                const int t = gl + G * s;
+#pragma unroll
+                for (int e = 0; e < 3; e++) {
+                    if (!((zero[s] >> e) & 1u)) continue;
+                    const int u = (F.adj[t] >> (8 * e)) & 255u;
+                    const int a = lab[t], b = lab[u];
+                    if (a < b) {
+                        atomicMin(&lab[u], a);
+                        changed = true;
+                    } else if (b < a) {
+                        atomicMin(&lab[t], b);
+                        changed = true;
+                    }
+                }
+            }
+            __syncwarp();
+            if (!__any_sync(kFull, changed)) break;
+        }
+        // the classes' lowest vertices, ranked in vertex order
+        const int lane = threadIdx.x & 31;   // (the kernels' CTAs are one-dimensional)
+        const unsigned gmask = G == 32 ? kFull : (0xffffu << (lane & 16));
+        const unsigned below = (1u << lane) - 1u;
+        int before = 0;
+        int rank[SL];
+#pragma unroll
+        for (int s = 0; s < SL; s++) {
+            const int t = gl + G * s;
+            const bool rep = t < nv && lab[t] == t;
+            const unsigned b = __ballot_sync(kFull, rep) & gmask;
+            rank[s] = before + __popc(b & below);
+            before += __popc(b);
+        }
+        nvm = before;
+        __syncwarp();
+#pragma unroll
+        for (int s = 0; s < SL; s++) {
+            const int t = gl + G * s;
+            if (t < nv && lab[t] == t) lab[t] = -1 - rank[s];
+        }
+        __syncwarp();
+        // each face's loop without repeats of a merged vertex (consecutive
+        // equal indices, and the last equal to the first): its new order
+        for (int q = gl; q < nf; q += G) {
+            if (!marg) continue;
+            int t = F.rep[q], cnt = 0, first = -1, last = -1;
+            for (int j = 0; j < F.ford[q]; j++) {
+                const int l = lab[t];
+                const int o = l < 0 ? -1 - l : -1 - lab[l];
+                if (o != last) {
+                    cnt++;
+                    if (first < 0) first = o;
+                    last = o;
+                }
+                const unsigned T = F.tri[t];
+                const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
+                t = (F.adj[t] >> (8 * e)) & 255u;
+            }
+            if (cnt > 1 && last == first) cnt--;
+            F.ford[q] = cnt;
+        }
+        __syncwarp();
+        // the neighbour IDs of the faces that remain, compacted (rare: one lane)
+        if (marg && gl == 0 && !nb_full) {
+            nfm = 0;
+            for (int q = 0; q < nf; q++) nfm += F.ford[q] >= 3 ? 1 : 0;
+            if (nfm < nf) {
+                for (int q = 0, j = 0; q < nf; q++) {
+                    if (F.ford[q] < 3) continue;
+                    const int id = (int)rp[2 * nf + q];
+                    if (nfm <= kNbStride || j < kNbStride - 1) row[j] = id;
+                    else P.r.nb_ovf[ovf + j - (kNbStride - 1)] = id;
+                    j++;
+                }
+            }
+        }
+        nfm = __shfl_sync(kFull, nfm, 0, G);
+        __syncwarp();
+    }
+    // vertex t's index in the output (its class's rank where merged)
+    auto vmap = [&](int t) -> int {
+        if (!any_marg) return t;
+        const int l = lab[t];
+        return l < 0 ? -1 - l : -1 - lab[l];
+    };
+    if (have && gl == 0) {
+        P.r.nf[out] = nb_full ? 0 : nfm;
+        P.r.nv[out] = nvm;
         P.r.maxr2[out] = kFF ? ff_to_double(mf) : mr2;
         P.r.flags[out] = nb_full ? (VGPU_CELL_FAILED | (VGPU_FAIL_RECORDS << 8)) : (VGPU_CELL_OK | (int)fl);
         if (nb_full) atomicAdd(&P.cnt->nb_failed, 1ull);
@@ -512,6 +709,7 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
         // loop walks the face by the edges that start on it, which orders the
         // vertices clockwise seen from outside, as the reference's
         // face_vertices does (src/cell.cc:2285-2308)
+        // (an upper bound where vertices were merged: the stream is then shorter)
         const unsigned long long need = 2ull + 6ull * (unsigned long long)nv + 2ull * (unsigned long long)nf;
         unsigned long long po = 0;
         if (have && gl == 0) po = atomicAdd(P.poly_used, need);
@@ -520,28 +718,32 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
         double *D = P.poly + (fits ? po : 0);
         if (fits) {
             if (gl == 0) {
-                D[0] = (double)nv;
-                D[1] = (double)nf;
+                D[0] = (double)nvm;
+                D[1] = (double)nfm;
             }
 #pragma unroll
             for (int s = 0; s < SL; s++) {
                 const int t = gl + G * s;
-                if (t < nv)
+                if (t < nv && (!any_marg || lab[t] < 0)) {   // a merged class: its lowest vertex
+                    const int o = vmap(t);
 #pragma unroll
-                    for (int a = 0; a < 3; a++) D[2 + 3 * t + a] = kFF ? ff_to_double(vf[s][a]) : vd[s][a];
+                    for (int a = 0; a < 3; a++) D[2 + 3 * o + a] = kFF ? ff_to_double(vf[s][a]) : vd[s][a];
+                }
             }
         }
         // face loops; the loop over face chunks runs the same number of times
-        // in both halves, because it holds a group scan
-        double *DF = D + 2 + 3 * nv;
+        // in both halves, because it holds a group scan.  A merged cell
+        // (marg: its faces' orders are the merged ones, F.ford) is written by
+        // one lane below instead, skipping the faces the merge removed.
+        double *DF = D + 2 + 3 * nvm;
         const int nfmax = __reduce_max_sync(kFull, fits ? nf : 0);
         for (int q0 = 0; q0 < nfmax; q0 += G) {
             const int q = q0 + gl;
-            const bool mine = fits && q < nf;
+            const bool mine = fits && !marg && q < nf;
             const int ord = mine ? F.ford[q] : 0;
             // faces before q: q * 2 header words plus their orders
             int before = 0;
-            if (fits)
+            if (fits && !marg)
                 for (int j = 0; j < q0 && j < nf; j++) before += F.ford[j];
             const int incl = group_incl_scan<G>(ord, gl);
             if (mine) {
@@ -555,6 +757,27 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
                     const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
                     t = (F.adj[t] >> (8 * e)) & 255u;
                 }
+            }
+        }
+        if (fits && marg && gl == 0) {   // merged vertices (rare): the walks of the count above
+            double *df = DF;
+            for (int q = 0; q < nf; q++) {
+                const int ord = F.ford[q];
+                if (ord < 3) continue;   // removed by the merge
+                df[0] = (double)(int)rp[2 * nf + q];
+                df[1] = (double)ord;
+                int t = F.rep[q], w = 0, last = -1;
+                for (int j = 0; w < ord && j < kFinMaxV; j++) {
+                    const int o = vmap(t);
+                    if (o != last) {
+                        df[2 + w++] = (double)o;
+                        last = o;
+                    }
+                    const unsigned T = F.tri[t];
+                    const int e = tri_plane(T, 0) == q ? 0 : (tri_plane(T, 1) == q ? 1 : 2);
+                    t = (F.adj[t] >> (8 * e)) & 255u;
+                }
+                df += 2 + ord;
             }
         }
         if (fits) {
@@ -574,7 +797,7 @@ constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
 // 11.3 ms, 9 (96 registers, spills) 12.5 ms; 12.3 ms with two full-size
 // cells per warp (31.7 KB per CTA, 7 CTAs).
 #ifndef VGPU_FIN_MIN_BLOCKS
-#define VGPU_FIN_MIN_BLOCKS 7
+#define VGPU_FIN_MIN_BLOCKS 6
 #endif
 
 // Two cells per warp, one per 16-lane half, when both have at most 64

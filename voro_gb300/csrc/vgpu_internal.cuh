@@ -6,6 +6,17 @@
 namespace vgpu {
 
 constexpr int kWarp = 32;
+// Cells a warp of the clipping kernels takes from the work queue at a time by
+// default, and the largest CTA they are built for (threads); both can be
+// changed at build time (-D), the first also per container (vgpu_tuning).
+#ifndef VGPU_CELL_CHUNK
+#define VGPU_CELL_CHUNK 8
+#endif
+#ifndef VGPU_CTA_THREADS
+#define VGPU_CTA_THREADS 128
+#endif
+constexpr int kDefaultCellChunk = VGPU_CELL_CHUNK;
+constexpr int kBuiltCtaWarps = VGPU_CTA_THREADS / 32;
 constexpr int kMaxPlanes = 64;     // plane slots per cell (64-bit plane masks)
 constexpr int kCandBuf = 64;       // candidate buffer entries per warp
 // Neighbour IDs: kNbStride slots per cell in a fixed-stride array; a cell with
@@ -118,7 +129,9 @@ struct CellParams {
     Results r;
     Counters *cnt;
     int ncells;             // cells to compute (engine order), or overflow list length
-    const int *cell_list;   // NULL: all cells 0..ncells-1; else the list of engine indices
+    const int *cell_list;   // NULL: cells cell_begin..cell_begin+ncells-1; else the list of engine indices
+    int cell_begin;
+    int cell_chunk;         // consecutive cells a warp takes from the queue at once (0: the built-in default)
     int *overflow_list;     // cells that overflowed this engine's capacity
     const int *offsets;     // packed search offsets (engine table), sorted by lb2
     int noffsets;

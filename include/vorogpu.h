@@ -324,9 +324,14 @@ int vgpu_batch_destroy(vgpu_batch *b);
  * keeps its partial sums in a fixed 64 KB static device array, so n is limited
  * to 33,554,432 (larger n: VGPU_ERR_ARG).  The first call on each device, with
  * that device current, does a one-time set-up (the scratch address lookup);
- * make it before any stream capture.  Nothing has to be zeroed beforehand.
- * Calls that overlap on one device share the scratch and race: serialise them.
- * The summation order is fixed, so repeated calls give identical results. */
+ * make it before any stream capture, and do not use the entry point after a
+ * cudaDeviceReset in the same process (the cached address would be stale).
+ * Every call runs on the current device, which must own dev_vol, dev_out and
+ * the stream: a pointer of host memory or of another device is rejected with
+ * VGPU_ERR_ARG before anything is launched.  Nothing has to be zeroed
+ * beforehand.  Calls that overlap on one device share the scratch and race:
+ * serialise them.  The summation order is fixed, so repeated calls give
+ * identical results. */
 int vgpu_sum_volumes_noalloc(const double *dev_vol, int64_t n, double *dev_out, void *stream);
 
 #ifdef __cplusplus

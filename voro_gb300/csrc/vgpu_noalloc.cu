@@ -17,7 +17,15 @@
 // Set-up: the first call on each device (with that device current) looks up
 // the scratch's device address with cudaGetSymbolAddress, which can also load
 // this library's device code onto that device; make that first call before any
-// stream capture.  Later calls reuse the cached address.
+// stream capture.  Later calls reuse the cached address, so the entry point
+// must not be used after a cudaDeviceReset (or any other teardown of the
+// device's primary context) in the same process: the module, and with it the
+// scratch, may then live at another address.
+//
+// Device: every call runs on the current device, which must own dev_vol,
+// dev_out and the stream; the pointers are checked (cudaPointerGetAttributes,
+// which allocates nothing) and a pointer of another device or of host memory
+// is rejected with VGPU_ERR_ARG before anything is launched.
 //
 // Concurrency: there is one scratch array per device.  Two calls that overlap
 // on one device (different streams, or different host threads) race on it and
@@ -78,11 +86,27 @@ __global__ void __launch_bounds__(kThreads) total_kernel(const double *partials,
     if (threadIdx.x == 0) *out = t;
 }
 
-int scratch_for_current_device(double **out) {
+// VGPU_OK if p is device (or managed) memory of device dev.
+int check_on_device(const void *p, int dev, const char *what) {
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // clear it: the caller's pointer is what is wrong
+        return report_error(VGPU_ERR_ARG, "%s: not a CUDA pointer (%s)", what, cudaGetErrorString(e));
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        return report_error(VGPU_ERR_ARG, "%s is not device memory", what);
+    if (a.device != dev)
+        return report_error(VGPU_ERR_ARG, "%s lives on device %d but device %d is current", what, a.device, dev);
+    return VGPU_OK;
+}
+
+int scratch_for_current_device(double **out, int *dev_out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return report_error(VGPU_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return report_error(VGPU_ERR_ARG, "device ordinal %d out of range", dev);
+    *dev_out = dev;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch[dev]) {
         void *p = nullptr;
@@ -109,8 +133,11 @@ extern "C" int vgpu_sum_volumes_noalloc(const double *dev_vol, int64_t n, double
                             (long long)n, kMaxCells, kMaxPartials, kTile);
     if (n > 0 && !dev_vol) return report_error(VGPU_ERR_ARG, "null volume pointer");
     double *scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    int dev = -1;
+    int rc = scratch_for_current_device(&scratch, &dev);
     if (rc != VGPU_OK) return rc;
+    if (n > 0 && (rc = check_on_device(dev_vol, dev, "dev_vol")) != VGPU_OK) return rc;
+    if ((rc = check_on_device(dev_out, dev, "dev_out")) != VGPU_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int ntiles = (int)((n + kTile - 1) / kTile);
     if (ntiles > 0) {

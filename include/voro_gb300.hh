@@ -235,6 +235,9 @@ class voronoicell {
             v[k]++;
         }
     }
+    // voronoicell_base::output_custom (src/cell.cc:2485-2558): the
+    // print_custom fields of this cell, for particle i at (x, y, z), radius r
+    void output_custom(const char *format, int i, double x, double y, double z, double r, FILE *fp = stdout) const;
 
   protected:
     friend class container_gpu_base;
@@ -281,10 +284,113 @@ class voronoicell_neighbor : public voronoicell {
     explicit voronoicell_neighbor(C &) {}
     // one ID per face, ascending (the reference lists them in face order)
     void neighbors(std::vector<int> &v) const { v = nb_; }
+    void output_custom(const char *format, int i, double x, double y, double z, double r, FILE *fp = stdout) const;
 
   protected:
     friend class container_gpu_base;
     std::vector<int> nb_;
+};
+
+// The fields of output_custom (src/cell.cc:2485-2558), printed as the
+// reference's printers do (src/common.cc:37-136); nb: the neighbour IDs
+// (voronoicell_neighbor), NULL for a plain voronoicell (whose %n is empty).
+inline void gpu_detail_print_cell(const voronoicell &c, const std::vector<int> *nb, const char *format, int id,
+                                  double x, double y, double z, double r, FILE *fp) {
+    std::vector<double> d;
+    std::vector<int> iv;
+    auto print_d = [&](const std::vector<double> &v) {
+        for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %g" : "%g", v[i]);
+    };
+    auto print_i = [&](const std::vector<int> &v) {
+        for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %d" : "%d", v[i]);
+    };
+    auto print_xyz = [&](const std::vector<double> &v, double ox, double oy, double oz) {
+        for (size_t i = 0; i < v.size(); i += 3)
+            fprintf(fp, i ? " (%g,%g,%g)" : "(%g,%g,%g)", ox + v[i], oy + v[i + 1], oz + v[i + 2]);
+    };
+    for (const char *f = format; *f; f++) {
+        if (*f != '%') {
+            putc(*f, fp);
+            continue;
+        }
+        f++;
+        switch (*f) {
+            case 'i': fprintf(fp, "%d", id); break;
+            case 'x': fprintf(fp, "%g", x); break;
+            case 'y': fprintf(fp, "%g", y); break;
+            case 'z': fprintf(fp, "%g", z); break;
+            case 'q': fprintf(fp, "%g %g %g", x, y, z); break;
+            case 'r': fprintf(fp, "%g", r); break;
+            case 'w': fprintf(fp, "%d", c.p); break;
+            case 'p': c.vertices(d); print_xyz(d, 0, 0, 0); break;
+            case 'P': c.vertices(d); print_xyz(d, x, y, z); break;
+            case 'o': c.vertex_orders(iv); print_i(iv); break;
+            case 'm': fprintf(fp, "%g", 0.25 * c.max_radius_squared()); break;
+            case 'g': fprintf(fp, "%d", c.number_of_edges()); break;
+            case 'E': fprintf(fp, "%g", c.total_edge_distance()); break;
+            case 'e': c.face_perimeters(d); print_d(d); break;
+            case 's': fprintf(fp, "%d", c.number_of_faces()); break;
+            case 'F': fprintf(fp, "%g", c.surface_area()); break;
+            case 'A': c.face_freq_table(iv); print_i(iv); break;
+            case 'a': c.face_orders(iv); print_i(iv); break;
+            case 'f': c.face_areas(d); print_d(d); break;
+            case 't': {
+                c.face_vertices(iv);
+                size_t i = 0;
+                bool first = true;
+                while (i < iv.size()) {
+                    const int m = iv[i++];
+                    fputs(first ? "(" : " (", fp);
+                    first = false;
+                    for (int j = 0; j < m; j++) fprintf(fp, j ? ",%d" : "%d", iv[i + j]);
+                    fputs(")", fp);
+                    i += m;
+                }
+            } break;
+            case 'l': c.normals(d); print_xyz(d, 0, 0, 0); break;
+            case 'n':
+                if (nb) print_i(*nb);
+                break;
+            case 'v': fprintf(fp, "%g", c.volume()); break;
+            case 'c': {
+                double cx, cy, cz;
+                c.centroid(cx, cy, cz);
+                fprintf(fp, "%g %g %g", cx, cy, cz);
+            } break;
+            case 'C': {
+                double cx, cy, cz;
+                c.centroid(cx, cy, cz);
+                fprintf(fp, "%g %g %g", x + cx, y + cy, z + cz);
+            } break;
+            case 0: f--; break;
+            default:
+                putc('%', fp);
+                putc(*f, fp);
+        }
+    }
+    fputs("\n", fp);
+}
+inline void voronoicell::output_custom(const char *format, int i, double x, double y, double z, double r,
+                                       FILE *fp) const {
+    gpu_detail_print_cell(*this, nullptr, format, i, x, y, z, r, fp);
+}
+inline void voronoicell_neighbor::output_custom(const char *format, int i, double x, double y, double z, double r,
+                                                FILE *fp) const {
+    gpu_detail_print_cell(*this, &nb_, format, i, x, y, z, r, fp);
+}
+
+// particle_order (src/c_loops.hh:27-71): the order in which particles were
+// put through it (put / import with a particle_order); c_loop_order visits
+// their cells in that order.
+class particle_order {
+  public:
+    explicit particle_order(int init_size = 16) { idx_.reserve(init_size > 0 ? init_size : 16); }
+    void add(int64_t put_index) { idx_.push_back(put_index); }
+    size_t size() const { return idx_.size(); }
+    int64_t operator[](size_t i) const { return idx_[i]; }
+
+  private:
+    std::vector<int64_t> idx_;
 };
 
 // Shared implementation of the four container classes.
@@ -324,7 +430,20 @@ class container_gpu_base {
         ids_in_.clear();
         xyzr_in_.clear();
         gpu_detail::check(vgpu_clear(h_), "clear");
+        n_put_ = 0;
         dirty_ = true;
+    }
+
+    // For c_loop_order: per particle put since the last clear (put order), its
+    // row in the loop-order results, -1 where put() dropped it.
+    const std::vector<int32_t> &input_rows() {
+        ensure();
+        if (!rows_valid_) {
+            rows_.assign((size_t)n_put_, -1);
+            if (n_put_ > 0) gpu_detail::check(vgpu_get_input_rows(h_, rows_.data()), "input_rows");
+            rows_valid_ = true;
+        }
+        return rows_;
     }
 
     // container::compute_all_cells (src/container.cc:438-453)
@@ -350,6 +469,7 @@ class container_gpu_base {
             gpu_detail::check(vgpu_get_radii(h_, rad_.data()), "compute_all_cells");
         }
         have_nb_ = false;
+        rows_valid_ = false;
         poff_.clear();
         pdata_.clear();
         if (poly_on_ && n > 0) {
@@ -438,8 +558,19 @@ class container_gpu_base {
         if (needs_polytope(format) && !poly_on_) set_polytopes(true);
         ensure();
         if (contains_neighbor(format)) ensure_neighbors();
-        for (int64_t k = 0; k < n_; k++)
-            if (flags_[k] & VGPU_CELL_OK) output_custom(format, k, fp);
+        voronoicell_neighbor c;
+        for (int64_t k = 0; k < n_; k++) print_cell(c, format, k, fp);
+    }
+    // the same over the cells of a loop (c_loop_all, c_loop_order), as the
+    // reference's command-line utility prints them (src/cmd_line.cc:75-121)
+    template <class c_loop>
+    void print_custom_loop(c_loop &vl, const char *format, FILE *fp = stdout) {
+        if (needs_polytope(format) && !poly_on_) set_polytopes(true);
+        ensure();
+        if (contains_neighbor(format)) ensure_neighbors();
+        voronoicell_neighbor c;
+        if (vl.start()) do print_cell(c, format, vl.index(), fp);
+            while (vl.inc());
     }
     void print_custom(const char *format, const char *filename) {
         FILE *fp = fopen(filename, "w");
@@ -476,6 +607,7 @@ class container_gpu_base {
     double geom_[6];
 
     void stage(int n, double x, double y, double z, double r) {
+        n_put_++;
         ids_in_.push_back(n);
         xyzr_in_.push_back(x);
         xyzr_in_.push_back(y);
@@ -484,19 +616,28 @@ class container_gpu_base {
         dirty_ = true;
     }
 
+    // put with a particle_order (src/container.hh:294,516): the order records
+    // the particle's place in the put sequence
+    void stage(particle_order &vo, int n, double x, double y, double z, double r) {
+        vo.add(n_put_);
+        stage(n, x, y, z, r);
+    }
+
     // container::import (src/container.cc:333-376): "id x y z" (+ " r") per line
-    void import_stream(FILE *fp, bool with_r) {
+    void import_stream(FILE *fp, bool with_r, particle_order *vo = nullptr) {
         int i, j;
         double x, y, z, r = default_radius;
         while ((j = with_r ? fscanf(fp, "%d %lg %lg %lg %lg", &i, &x, &y, &z, &r)
-                           : fscanf(fp, "%d %lg %lg %lg", &i, &x, &y, &z)) == (with_r ? 5 : 4))
-            stage(i, x, y, z, r);
+                           : fscanf(fp, "%d %lg %lg %lg", &i, &x, &y, &z)) == (with_r ? 5 : 4)) {
+            if (vo) stage(*vo, i, x, y, z, r);
+            else stage(i, x, y, z, r);
+        }
         if (j != EOF) voro_fatal_error("File import error", VOROPP_FILE_ERROR);
     }
-    void import_file(const char *filename, bool with_r) {
+    void import_file(const char *filename, bool with_r, particle_order *vo = nullptr) {
         FILE *fp = fopen(filename, "r");
         if (!fp) voro_fatal_error("Unable to open file", VOROPP_FILE_ERROR);
-        import_stream(fp, with_r);
+        import_stream(fp, with_r, vo);
         fclose(fp);
     }
 
@@ -511,6 +652,9 @@ class container_gpu_base {
     std::vector<int32_t> ids_in_;
     std::vector<double> xyzr_in_;
     int64_t n_ = 0;
+    int64_t n_put_ = 0;          // particles put since the last clear
+    bool rows_valid_ = false;
+    std::vector<int32_t> rows_;  // input_rows() of the last compute
     std::vector<int32_t> ids_, nf_, nv_, flags_, nb_;
     std::vector<double> pos_, vol_, cen_, mr2_, rad_;
     std::vector<int64_t> off_;
@@ -614,89 +758,12 @@ class container_gpu_base {
             if (f[0] == '%' && f[1] == 'n') return true;
         return false;
     }
-    // the polytope fields of output_custom (src/cell.cc:2485-2558), printed
-    // as the reference's printers do (src/common.cc:37-136)
-    void poly_field(char f, int64_t k, double x, double y, double z, FILE *fp) {
-        voronoicell c;
-        load_polytope(c, &pdata_[poff_[k]]);
-        c.p = (int)(c.verts_.size() / 3);
-        std::vector<double> d;
-        std::vector<int> iv;
-        auto print_d = [&](const std::vector<double> &v) {
-            for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %g" : "%g", v[i]);
-        };
-        auto print_i = [&](const std::vector<int> &v) {
-            for (size_t i = 0; i < v.size(); i++) fprintf(fp, i ? " %d" : "%d", v[i]);
-        };
-        auto print_xyz = [&](const std::vector<double> &v, double ox, double oy, double oz) {
-            for (size_t i = 0; i < v.size(); i += 3)
-                fprintf(fp, i ? " (%g,%g,%g)" : "(%g,%g,%g)", ox + v[i], oy + v[i + 1], oz + v[i + 2]);
-        };
-        switch (f) {
-            case 'p': c.vertices(d); print_xyz(d, 0, 0, 0); break;
-            case 'P': c.vertices(d); print_xyz(d, x, y, z); break;
-            case 'o': c.vertex_orders(iv); print_i(iv); break;
-            case 'E': fprintf(fp, "%g", c.total_edge_distance()); break;
-            case 'e': c.face_perimeters(d); print_d(d); break;
-            case 'F': fprintf(fp, "%g", c.surface_area()); break;
-            case 'A': c.face_freq_table(iv); print_i(iv); break;
-            case 'a': c.face_orders(iv); print_i(iv); break;
-            case 'f': c.face_areas(d); print_d(d); break;
-            case 't': {
-                c.face_vertices(iv);
-                size_t i = 0;
-                bool first = true;
-                while (i < iv.size()) {
-                    const int m = iv[i++];
-                    fputs(first ? "(" : " (", fp);
-                    first = false;
-                    for (int j = 0; j < m; j++) fprintf(fp, j ? ",%d" : "%d", iv[i + j]);
-                    fputs(")", fp);
-                    i += m;
-                }
-            } break;
-            case 'l': c.normals(d); print_xyz(d, 0, 0, 0); break;
-        }
-    }
-
-    void output_custom(const char *format, int64_t k, FILE *fp) {
-        const double x = pos_[3 * k], y = pos_[3 * k + 1], z = pos_[3 * k + 2];
-        const double *c = &cen_[3 * k];
-        for (const char *f = format; *f; f++) {
-            if (*f != '%') {
-                putc(*f, fp);
-                continue;
-            }
-            f++;
-            switch (*f) {
-                case 'i': fprintf(fp, "%d", ids_[k]); break;
-                case 'x': fprintf(fp, "%g", x); break;
-                case 'y': fprintf(fp, "%g", y); break;
-                case 'z': fprintf(fp, "%g", z); break;
-                case 'q': fprintf(fp, "%g %g %g", x, y, z); break;
-                case 'r': fprintf(fp, "%g", radius_at(k)); break;
-                case 'w': fprintf(fp, "%d", nv_[k]); break;
-                case 'o': poly_field('o', k, x, y, z, fp); break;
-                case 'm': fprintf(fp, "%g", mr2_[k]); break;
-                case 'g': fprintf(fp, "%d", nv_[k] + nf_[k] - 2); break;   // Euler: E = V + F - 2
-                case 's': fprintf(fp, "%d", nf_[k]); break;
-                case 'n':
-                    for (int64_t q = off_[k]; q < off_[k + 1]; q++)
-                        fprintf(fp, q > off_[k] ? " %d" : "%d", nb_[q]);
-                    break;
-                case 'v': fprintf(fp, "%g", vol_[k]); break;
-                case 'c': fprintf(fp, "%g %g %g", c[0], c[1], c[2]); break;
-                case 'C': fprintf(fp, "%g %g %g", x + c[0], y + c[1], z + c[2]); break;
-                case 'p': case 'P': case 'E': case 'e': case 'F': case 'A': case 'a': case 'f': case 't': case 'l':
-                    poly_field(*f, k, x, y, z, fp);
-                    break;
-                case 0: f--; break;
-                default:
-                    putc('%', fp);
-                    putc(*f, fp);
-            }
-        }
-        fputs("\n", fp);
+    // cell k (loop order) as a voronoicell_neighbor, printed if it has a cell
+    void print_cell(voronoicell_neighbor &c, const char *format, int64_t k, FILE *fp) {
+        if (!fill(c, k)) return;
+        if (have_nb_) c.nb_.assign(nb_.begin() + off_[k], nb_.begin() + off_[k + 1]);
+        else c.nb_.clear();
+        c.output_custom(format, ids_[k], pos_[3 * k], pos_[3 * k + 1], pos_[3 * k + 2], radius_at(k), fp);
     }
 };
 
@@ -710,6 +777,9 @@ class container : public container_gpu_base {
     void put(int n, double x, double y, double z) { stage(n, x, y, z, default_radius); }
     void import(FILE *fp = stdin) { import_stream(fp, false); }
     void import(const char *filename) { import_file(filename, false); }
+    void put(particle_order &vo, int n, double x, double y, double z) { stage(vo, n, x, y, z, default_radius); }
+    void import(particle_order &vo, FILE *fp = stdin) { import_stream(fp, false, &vo); }
+    void import(particle_order &vo, const char *filename) { import_file(filename, false, &vo); }
     bool point_inside(double x, double y, double z) { return point_inside_box_and_walls(x, y, z); }
 };
 
@@ -723,6 +793,9 @@ class container_poly : public container_gpu_base {
     void put(int n, double x, double y, double z, double r) { stage(n, x, y, z, r); }
     void import(FILE *fp = stdin) { import_stream(fp, true); }
     void import(const char *filename) { import_file(filename, true); }
+    void put(particle_order &vo, int n, double x, double y, double z, double r) { stage(vo, n, x, y, z, r); }
+    void import(particle_order &vo, FILE *fp = stdin) { import_stream(fp, true, &vo); }
+    void import(particle_order &vo, const char *filename) { import_file(filename, true, &vo); }
     bool point_inside(double x, double y, double z) { return point_inside_box_and_walls(x, y, z); }
 };
 
@@ -737,6 +810,9 @@ class container_periodic : public container_gpu_base {
     void put(int n, double x, double y, double z) { stage(n, x, y, z, default_radius); }
     void import(FILE *fp = stdin) { import_stream(fp, false); }
     void import(const char *filename) { import_file(filename, false); }
+    void put(particle_order &vo, int n, double x, double y, double z) { stage(vo, n, x, y, z, default_radius); }
+    void import(particle_order &vo, FILE *fp = stdin) { import_stream(fp, false, &vo); }
+    void import(particle_order &vo, const char *filename) { import_file(filename, false, &vo); }
 };
 
 // container_periodic_poly (src/container_prd.hh:434-437)
@@ -749,6 +825,9 @@ class container_periodic_poly : public container_gpu_base {
     void put(int n, double x, double y, double z, double r) { stage(n, x, y, z, r); }
     void import(FILE *fp = stdin) { import_stream(fp, true); }
     void import(const char *filename) { import_file(filename, true); }
+    void put(particle_order &vo, int n, double x, double y, double z, double r) { stage(vo, n, x, y, z, r); }
+    void import(particle_order &vo, FILE *fp = stdin) { import_stream(fp, true, &vo); }
+    void import(particle_order &vo, const char *filename) { import_file(filename, true, &vo); }
 };
 
 // c_loop_all (src/c_loops.hh:165-210) and c_loop_all_periodic (325-393): the
@@ -784,6 +863,58 @@ class c_loop_all {
     int64_t k_ = 0;
 };
 typedef c_loop_all c_loop_all_periodic;
+
+// c_loop_order (src/c_loops.hh:268-317) and c_loop_order_periodic (398-446):
+// the cells of the particles of a particle_order, in its order (particles
+// that put() dropped have no cell and are skipped).
+class c_loop_order {
+  public:
+    template <class C>
+    c_loop_order(C &con, particle_order &vo) : con_(&con), vo_(&vo) {}
+    bool start() {
+        rows_ = &con_->input_rows();
+        i_ = 0;
+        return seek();
+    }
+    bool inc() {
+        i_++;
+        return seek();
+    }
+    int pid() const { return con_->pid_at(k_); }
+    void pos(double &x, double &y, double &z) const {
+        const double *p = con_->pos_at(k_);
+        x = p[0];
+        y = p[1];
+        z = p[2];
+    }
+    void pos(int &pid_, double &x, double &y, double &z, double &r) const {
+        pid_ = pid();
+        pos(x, y, z);
+        r = con_->radius_at(k_);
+    }
+    double x() const { return con_->pos_at(k_)[0]; }
+    double y() const { return con_->pos_at(k_)[1]; }
+    double z() const { return con_->pos_at(k_)[2]; }
+    int64_t index() const { return k_; }
+
+  private:
+    container_gpu_base *con_;
+    particle_order *vo_;
+    const std::vector<int32_t> *rows_ = nullptr;
+    size_t i_ = 0;
+    int64_t k_ = 0;
+    bool seek() {
+        for (; i_ < vo_->size(); i_++) {
+            const int64_t j = (*vo_)[i_];
+            if (j >= 0 && j < (int64_t)rows_->size() && (*rows_)[j] >= 0) {
+                k_ = (*rows_)[j];
+                return true;
+            }
+        }
+        return false;
+    }
+};
+typedef c_loop_order c_loop_order_periodic;
 
 }  // namespace voro
 

@@ -138,6 +138,11 @@ int vgpu_get_stats(vgpu_container *h, vgpu_stats *out);
  * reference's loop order (c_loop_all, src/c_loops.hh:165-210;
  * c_loop_all_periodic, src/c_loops.hh:325-393). */
 int vgpu_num_cells(vgpu_container *h, int64_t *n);
+/* Input order (particle_order with c_loop_order, src/c_loops.hh:268-317):
+ * rows[i] = the loop-order result row of the i-th particle put since the last
+ * vgpu_clear, or -1 if put() dropped it (outside a non-periodic wall).  One
+ * entry per particle put; valid after a compute (or point location). */
+int vgpu_get_input_rows(vgpu_container *h, int32_t *rows);
 /* Total neighbour entries over all cells (sum of face counts). */
 int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
 

@@ -271,9 +271,72 @@ def make_ghost_fixtures(ref, all_cases, seed0=4000):
         print(f"ghost_{name}: {len(gx)} ghosts, {int(rec.ok.sum())} cells, {os.path.getsize(out)} bytes")
 
 
+# Command-line fixtures (cli_*.npz): the reference's own voro++ utility
+# (oracle/_ref/voro++, built from src/cmd_line.cc) run on seeded particle
+# files with the flags of each case; stored: the arguments, the input file's
+# text, the .vol text, with -v the printed summary, and any drawing outputs.
+# A format's %n (face order: numbering dependent) is always its last field.
+def cli_cases():
+    rng = np.random.default_rng(5001)
+
+    def text(n, lo, hi, radii=None):
+        xyz = rng.uniform(lo, hi, size=(n, 3))
+        lines = []
+        for i in range(n):
+            row = "%d %.17g %.17g %.17g" % (i, xyz[i, 0], xyz[i, 1], xyz[i, 2])
+            if radii is not None:
+                row += " %.17g" % radii[i]
+            lines.append(row)
+        return "\n".join(lines) + "\n"
+
+    out = {}
+    out["cli_cube_default"] = (["0", "1", "0", "1", "0", "1"], text(1000, 0.0, 1.0))
+    out["cli_periodic_custom"] = (["-p", "-v", "-c", "%i %q %v %s %w %g %F %E %A %C %m %n", "0", "2", "0", "2", "0", "2"],
+                                  text(2000, 0.0, 2.0))
+    r = rng.uniform(0.02, 0.06, size=1500)
+    out["cli_poly_ordered_sphere"] = (["-r", "-o", "-ws", "1", "1", "1", "0.9", "-c", "%i %v %s %r %n",
+                                       "0", "2", "0", "2", "0", "2"], text(1500, -0.1, 2.1, radii=r))
+    out["cli_length_scale_xy_periodic"] = (["-l", "0.15", "-px", "-py", "-v", "0", "1.5", "0", "1.5", "0", "1.5"],
+                                           text(1200, -0.2, 1.7))
+    r = rng.uniform(0.3, 1.0, size=800)
+    out["cli_grid_ordered_poly"] = (["-n", "3", "4", "5", "-o", "-r", "-c", "%i %q %v %s %w %c", "0", "8", "0", "8",
+                                     "0", "8"], text(800, 0.0, 8.0, radii=r))
+    out["cli_box_walls"] = (["-wb", "0.1", "0.9", "0.15", "0.85", "0.2", "0.8", "-c", "%i %v %s %F %n",
+                             "0", "1", "0", "1", "0", "1"], text(900, 0.0, 1.0))
+    out["cli_cylinder_cone"] = (["-wc", "1", "1", "0", "0", "0", "1", "0.8", "-wo", "1", "1", "2.2", "0", "0", "-1",
+                                 "0.6", "-c", "%i %v %s %w", "0", "2", "0", "2", "0", "2"], text(1500, 0.0, 2.0))
+    out["cli_drawing"] = (["-g", "-y", "0", "1", "0", "1", "0", "1"], text(120, 0.0, 1.0))
+    return out
+
+
+def make_cli_fixtures():
+    import subprocess
+    import tempfile
+    exe = os.path.join(ROOT, "oracle", "_ref", "voro++")
+    if not os.path.exists(exe):
+        raise SystemExit("the reference command-line utility was not built (make -C oracle ref)")
+    for name, (args, txt) in cli_cases().items():
+        with tempfile.TemporaryDirectory() as td:
+            fn = os.path.join(td, "pts")
+            open(fn, "w").write(txt)
+            r = subprocess.run([exe] + args + [fn], capture_output=True, text=True, check=True)
+            vol = open(fn + ".vol").read()
+            extra = {}
+            for suffix, key in ((".gnu", "gnu"), ("_p.pov", "povp"), ("_v.pov", "povv")):
+                if os.path.exists(fn + suffix):
+                    extra[key] = np.array(open(fn + suffix).read())
+        out = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(out, args=np.array(args), input=np.array(txt), vol=np.array(vol),
+                            stdout=np.array(r.stdout.replace(td, "<dir>")), **extra)
+        print(f"{name}: {len(vol.splitlines())} cells, {os.path.getsize(out)} bytes")
+
+
 def main():
     if not build_ref():
         raise SystemExit("reference sources not available; cannot generate fixtures")
+    if "--cli-only" in sys.argv:
+        make_cli_fixtures()
+        return
     ref = RefLib()
     if "--poly-only" in sys.argv:
         make_poly_fixtures(ref, cases())
@@ -307,6 +370,7 @@ def main():
     make_wall_fixtures(ref)
     make_tric_fixtures(ref)
     make_tric_large_fixture(ref)
+    make_cli_fixtures()
 
 
 # A larger sheared box (cells only): 20,000 particles, so that the first

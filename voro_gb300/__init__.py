@@ -58,6 +58,7 @@ EXPORTED = [
     "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes", "vgpu_add_wall",
     "vgpu_clear_walls", "vgpu_point_inside_walls",
     "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts", "vgpu_set_fp64_fallback",
+    "vgpu_get_input_rows",
 ]
 
 
@@ -124,6 +125,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_set_ghost_depth.argtypes = [vp, ctypes.c_double]
     lib.vgpu_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_set_fp64_fallback.argtypes = [vp, ctypes.c_double]
+    lib.vgpu_get_input_rows.argtypes = [vp, vp]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_phase_counts.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
@@ -305,6 +307,7 @@ class _ContainerBase:
         self.mode = mode
         self._pending_ids = []
         self._pending_xyzr = []
+        self._n_put = 0
         self._dirty = True
         self._dev_keep = None
         self._polytopes = False
@@ -337,8 +340,15 @@ class _ContainerBase:
             ids = np.asarray(self._pending_ids, dtype=np.int32)
             xyzr = np.asarray(self._pending_xyzr, dtype=np.float64)
             _check(self._lib.vgpu_put(self._h, len(ids), _ptr(ids), _ptr(xyzr)))
+            self._count_put(len(ids))
             self._pending_ids = []
             self._pending_xyzr = []
+
+    def _count_put(self, n):
+        if self._dev_keep is not None:   # a host put() replaces device-resident input
+            self._dev_keep = None
+            self._n_put = 0
+        self._n_put += int(n)
 
     def put_array(self, ids, xyz, r=None):
         """Vectorised put(): ids (n,), xyz (n,3), optional radii (n,)."""
@@ -350,6 +360,7 @@ class _ContainerBase:
         xyzr[:, :3] = xyz
         xyzr[:, 3] = 0.5 if r is None else r
         _check(self._lib.vgpu_put(self._h, n, _ptr(ids), _ptr(xyzr)))
+        self._count_put(n)
         self._dirty = True
 
     # ---- walls: src/container.hh:56-103 (wall_list), src/wall.hh:25-130
@@ -409,6 +420,7 @@ class _ContainerBase:
         xyzr = np.ascontiguousarray(xyzr, dtype=np.float64)
         assert xyzr.shape == (len(ids), 4)
         _check(self._lib.vgpu_put(self._h, len(ids), _ptr(ids), _ptr(xyzr)))
+        self._count_put(len(ids))
         self._dirty = True
 
     def put_device(self, n, dev_ids_ptr, dev_xyzr_ptr, keepalive=None):
@@ -417,7 +429,8 @@ class _ContainerBase:
         self._pending_ids, self._pending_xyzr = [], []
         _check(self._lib.vgpu_put_device(self._h, int(n), ctypes.c_void_p(dev_ids_ptr),
                                          ctypes.c_void_p(dev_xyzr_ptr)))
-        self._dev_keep = keepalive
+        self._n_put = int(n)
+        self._dev_keep = keepalive if keepalive is not None else ()
         self._dirty = True
 
     def clear(self):
@@ -425,6 +438,7 @@ class _ContainerBase:
         self._pending_ids, self._pending_xyzr = [], []
         self._dev_keep = None
         _check(self._lib.vgpu_clear(self._h))
+        self._n_put = 0
         self._dirty = True
 
     def autotune(self, mode=None):
@@ -558,6 +572,16 @@ class _ContainerBase:
         names = ["flushes", "sorts64", "block_passes", "cand_passes", "cands_kept", "new_vertices",
                  "segments", "cells_run"]
         return dict(zip(names, list(out)))
+
+    def input_rows(self):
+        """particle_order / c_loop_order (src/c_loops.hh:268-317): for each
+        particle put since the last clear, in put order, its row in cells(),
+        or -1 where put() dropped it."""
+        self._flush_pending()
+        self._ensure()
+        rows = np.empty(self._n_put, np.int32)
+        _check(self._lib.vgpu_get_input_rows(self._h, _ptr(rows)))
+        return rows
 
     def total_particles(self):
         self._ensure()

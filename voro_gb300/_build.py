@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libvorogpu.so")
+CLI = os.path.join(LIBDIR, "voro++")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["vgpu_api.cu", "vgpu_bin.cu", "vgpu_sort.cu", "vgpu_cell.cu", "vgpu_clip_mixed.cu", "vgpu_clip_fp64.cu",
@@ -31,12 +32,13 @@ def _nvcc():
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
-    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith((".h", ".hh"))]
+    files += [os.path.join(HERE, "cli", f) for f in os.listdir(os.path.join(HERE, "cli")) if f.endswith(".cc")]
     return files
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(f) <= t for f in _deps())
@@ -91,7 +93,24 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None, out=None
             os.remove(o)
         except OSError:
             pass
+    if out is None:
+        build_cli()
     return target
+
+
+def build_cli() -> str:
+    """The command-line utility (voro_gb300/cli/voro++.cc, the reference's
+    voro++ on this engine): a host program over include/voro_gb300.hh, linked
+    against libvorogpu.so beside it."""
+    cxx = shutil.which("g++") or "g++"
+    src = os.path.join(HERE, "cli", "voro++.cc")
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-I", INCLUDE, src, "-L", LIBDIR, "-lvorogpu",
+                        "-Wl,-rpath,$ORIGIN", "-o", CLI + ".tmp"], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("voro++ build failed:\n" + r.stdout)
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

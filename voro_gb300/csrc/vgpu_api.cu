@@ -832,6 +832,7 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
     h->launches0 = launch_count();
     cudaEventRecord(h->ev[0], s);
     VG_CUDA(cudaMemsetAsync(h->kept.p, 0, 64, s));
+    if (n > 0) VG_CUDA(cudaMemsetAsync(h->outpos_in.p, 0xff, (size_t)n * 4, s));   // -1: dropped by put()
     BinParams bp;
     bp.g = g;
     bp.n = n;
@@ -1781,6 +1782,16 @@ int vgpu_find_voronoi_cells(vgpu_container *h, int64_t n, const double *xyz, int
 int vgpu_phase_cycles(vgpu_container *h, double out[8]) {
     if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
     for (int i = 0; i < 8; i++) out[i] = h->phase[i];
+    return VGPU_OK;
+}
+
+int vgpu_get_input_rows(vgpu_container *h, int32_t *rows) {
+    if (!h || !rows) return fail(VGPU_ERR_ARG, "null argument");
+    if (!h->binned) return fail(VGPU_ERR_NOT_COMPUTED, "no compute since the last put");
+    const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
+    if (n <= 0) return VGPU_OK;
+    VG_CUDA(cudaMemcpyAsync(rows, h->outpos_in.p, (size_t)n * 4, cudaMemcpyDeviceToHost, h->stream));
+    VG_CUDA(cudaStreamSynchronize(h->stream));
     return VGPU_OK;
 }
 

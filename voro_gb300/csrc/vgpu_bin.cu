@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const Small
                 if (g.poly) atomicMax(&s_rmax, (unsigned long long)__double_as_longlong(fmax(q.w, 0.0)));
             }
             J.rem[i] = r;
+            J.outpos_in[i] = -1;   // a dropped particle keeps -1 (kept ones: set below)
             key[i] = ((unsigned long long)uk << 32) | (unsigned)i;
             gk_in[i] = gk;
         } else {

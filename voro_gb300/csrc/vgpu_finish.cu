@@ -347,7 +347,8 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
     // relative error of 4e-10).  A cell whose volume is below kTinyRel of
     // the cube of its largest vertex distance is therefore done again with
     // every vertex solved in FP64 from the FP64 planes (force64): both halves
-    // of the warp run the second pass when either needs it.  A cell that met
+    // of the warp run a second pass when either needs it, the other half
+    // repeating its float-pair one.  A cell that met
     // the tolerance band (marginal) gets FP64 vertices from the start: its
     // coincident vertices are merged below by their distance.
     unsigned tri[SL];
@@ -360,8 +361,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
     FF c0f[3];
     double vol_out = 0.0, cen_out[3] = {0.0, 0.0, 0.0};
     const bool marg = have && (fl & VGPU_CELL_MARGINAL) != 0u;
+    bool redo64 = false;   // this group's cell is tiny: its second pass is in FP64
     for (int pass = 0;; pass++) {
-        const bool force64 = pass > 0 || marg;
+        const bool force64 = redo64 || marg;
         mr2 = 0.0;
         mf = {0.0f, 0.0f};
     #pragma unroll
@@ -541,6 +543,9 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
         const double r2 = kFF ? ff_to_double(mf) : mr2;
         const bool tiny = kFF && !force64 && have && gl == 0 && vol_out < kTinyRel * r2 * sqrt(r2);
         if (!__any_sync(kFull, tiny)) break;
+        // the other half of the warp repeats its own pass unchanged, so a
+        // cell's result never depends on the cell that shares its warp
+        redo64 = __shfl_sync(kFull, tiny, 0, G);
         __syncwarp();
     }
     if (have && gl == 0) {

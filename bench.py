@@ -408,7 +408,7 @@ def run_ours(args):
 
     tuned = None
     if args.density <= 0 and not args.no_tune:
-        tuned = con.autotune()   # the engine's own autotuner picks the engine-grid density
+        tuned = con.autotune()   # the engine's own autotuner: (tuning dict, ms)
     for _ in range(args.warmup):
         con.compute_all_cells()
     barrier()
@@ -445,7 +445,7 @@ def run_ours(args):
         if args.density > 0:
             con2.set_tuning(args.density, 0)
         elif tuned is not None:
-            con2.set_tuning(tuned[0], 0)
+            con2.set_tuning(tuned[0]["particles_per_block"], tuned[0]["warps_per_cta"], tuned[0]["cells_per_chunk"])
         h2d = ids_pin.nbytes + xyzr_pin.nbytes
         d2h = 0
         times = []
@@ -500,7 +500,9 @@ def run_ours(args):
         "dtype": "f32+f64" if args.mode == "mixed" else "f64", "data": "synthetic",
         "config": {"workload": workload_name(w), "engine": args.mode,
                    "cells_per_step": n, "l2": "flushed between steps (512 MiB write)",
-                   "engine_density": tuned[0] if tuned else (args.density if args.density > 0 else "default"),
+                   "engine_density": (tuned[0]["particles_per_block"] if tuned else
+                                      (args.density if args.density > 0 else "default")),
+                   "tuning": tuned[0] if tuned else con.tuning(),
                    "parallelism": f"{ws} independent replicas" if ws > 1 else "1 GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_kind": peak_kind,

@@ -160,10 +160,9 @@ int vgpu_num_neighbors(vgpu_container *h, int64_t *total);
  *   flags    VGPU_CELL_* bits */
 int vgpu_get_cells(vgpu_container *h, int32_t *ids, double *pos, double *vol, double *cen,
                    int32_t *nfaces, int32_t *nverts, double *maxr2, int32_t *flags);
-/* Autotuner: times vgpu_compute over a set of engine-grid densities
- * (particles per engine block) on this container's own particles, keeps the
- * fastest (as vgpu_set_tuning would) and leaves the results of a compute with
- * it.  No counterpart in the reference (a tuning choice of this engine). */
+/* Autotuner (vgpu_autotune_ex without the cache), returning the chosen
+ * engine-grid density.  No counterpart in the reference (a tuning choice of
+ * this engine). */
 int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms);
 
 /* Optional outputs of vgpu_compute (flags; default 0).  VGPU_OUTPUT_POLYTOPES
@@ -268,6 +267,39 @@ int vgpu_device_results(vgpu_container *h, const double **dev_vol, const int32_t
  * library was built for (0 = default 4).
  * Applies from the next compute. */
 int vgpu_set_tuning(vgpu_container *h, double particles_per_block, int warps_per_cta);
+
+/* The engine's tuning of one container (no counterpart in the reference,
+ * whose only knob is the block grid it is given):
+ *   particles_per_block  target density of the engine's own search grid
+ *   warps_per_cta        cells in flight per CTA of the clipping kernels
+ *                        (1 to the build's maximum, 4 by default)
+ *   cells_per_chunk      consecutive cells (neighbouring blocks) a warp
+ *                        takes from the work queue at once (1-64, default 8)
+ *   fp64_fallback        see vgpu_set_fp64_fallback
+ * In vgpu_set_tuning_ex a zero field keeps the current value.  None of them
+ * changes a cell's topology; volumes stay within the precision mode's bound. */
+typedef struct vgpu_tuning {
+    double particles_per_block;
+    int warps_per_cta;
+    int cells_per_chunk;
+    double fp64_fallback;
+} vgpu_tuning;
+int vgpu_get_tuning(vgpu_container *h, vgpu_tuning *out);
+int vgpu_set_tuning_ex(vgpu_container *h, const vgpu_tuning *t);
+
+/* The autotuner: times computes of the container's own particles over the
+ * engine-grid density, then warps per CTA, then cells per chunk (coordinate
+ * search, best of two computes each), keeps the fastest tuple and leaves the
+ * results of a compute with it.  Flags: VGPU_TUNE_USE_CACHE takes the tuple
+ * a previous search stored for the same GPU and workload signature (device
+ * name, container kind, precision, particle count to within a factor of two,
+ * box aspect ratio, walls) instead of searching; VGPU_TUNE_WRITE_CACHE
+ * stores the tuple it finds.  The cache is a text file:
+ * $VORO_GB300_TUNE_CACHE, else $XDG_CACHE_HOME/voro_gb300/autotune.txt, else
+ * ~/.cache/voro_gb300/autotune.txt.  *best_ms: the chosen tuple's step time. */
+#define VGPU_TUNE_USE_CACHE 1
+#define VGPU_TUNE_WRITE_CACHE 2
+int vgpu_autotune_ex(vgpu_container *h, int mode, int flags, vgpu_tuning *chosen, double *best_ms);
 
 /* Sheared container_periodic: depth of the ghost layers of images a compute
  * stores first, in mean particle spacings (0 = default 8; < 0: always the

@@ -53,14 +53,29 @@ def test_recompute_is_deterministic(gpu):
 
 
 @pytest.mark.gpu
-def test_autotune_keeps_results(gpu):
-    """The engine-grid density changes the search, never the cells."""
-    w, z = G.load("periodic_2000")
+@pytest.mark.parametrize("name", ["periodic_2000", "radical_1200", "wall_sphere_2000"])
+def test_autotune_keeps_results(gpu, tmp_path, monkeypatch, name):
+    """The tuning (engine-grid density, warps per CTA, cells per chunk)
+    changes the search, never the cells; a cached choice is reused."""
+    monkeypatch.setenv("VORO_GB300_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    w, z = G.load(name)
     con = vg.from_workload(w, mode="mixed")
-    d, ms = con.autotune()
-    assert 0.3 <= d <= 3.0 and ms > 0
+    t, ms = con.autotune(cache=True)
+    assert 0.3 <= t["particles_per_block"] <= 3.0 and ms > 0
+    assert 1 <= t["warps_per_cta"] <= 8 and 1 <= t["cells_per_chunk"] <= 16
+    assert con.tuning()["cells_per_chunk"] == t["cells_per_chunk"]
     errs = G.compare_cells(con.cells(), z, *TOL["mixed"], label="autotuned")
     assert not errs, "\n".join(errs)
+    # other tuples of the search space give the same cells too
+    for tup in [(0.35, 1, 1), (3.0, 2, 16), (1.0, 4, 4)]:
+        con.set_tuning(*tup)
+        errs = G.compare_cells(con.cells(), z, *TOL["mixed"], label=f"tuning {tup}")
+        assert not errs, "\n".join(errs)
+    # the cache: a second container of the same signature takes the stored tuple
+    assert len(open(tmp_path / "tune.txt").read().split()) == 5
+    con2 = vg.from_workload(w, mode="mixed")
+    t2, _ = con2.autotune(cache=True)
+    assert t2 == t
 
 
 @pytest.mark.gpu

@@ -58,8 +58,21 @@ EXPORTED = [
     "vgpu_get_ghost_cells", "vgpu_get_ghost_neighbors", "vgpu_get_ghost_polytopes", "vgpu_add_wall",
     "vgpu_clear_walls", "vgpu_point_inside_walls",
     "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts", "vgpu_set_fp64_fallback",
-    "vgpu_get_input_rows",
+    "vgpu_get_input_rows", "vgpu_get_tuning", "vgpu_set_tuning_ex", "vgpu_autotune_ex",
 ]
+
+
+class Tuning(ctypes.Structure):
+    """vgpu_tuning: the engine's per-container tuning (see include/vorogpu.h)."""
+    _fields_ = [("particles_per_block", ctypes.c_double), ("warps_per_cta", ctypes.c_int),
+                ("cells_per_chunk", ctypes.c_int), ("fp64_fallback", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+VGPU_TUNE_USE_CACHE = 1
+VGPU_TUNE_WRITE_CACHE = 2
 
 
 class VoroError(RuntimeError):
@@ -126,6 +139,9 @@ def load_library(build_if_missing=True):
     lib.vgpu_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_set_fp64_fallback.argtypes = [vp, ctypes.c_double]
     lib.vgpu_get_input_rows.argtypes = [vp, vp]
+    lib.vgpu_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.vgpu_set_tuning_ex.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.vgpu_autotune_ex.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Tuning), pd]
     lib.vgpu_phase_cycles.argtypes = [vp, pd]
     lib.vgpu_phase_counts.argtypes = [vp, pd]
     lib.vgpu_get_radii.argtypes = [vp, vp]
@@ -441,19 +457,28 @@ class _ContainerBase:
         self._n_put = 0
         self._dirty = True
 
-    def autotune(self, mode=None):
-        """Times the compute over a set of engine-grid densities on this
-        container's particles and keeps the fastest; returns
-        (particles per block, ms per compute)."""
+    def autotune(self, mode=None, cache=False):
+        """The engine's autotuner on this container's particles: engine-grid
+        density, warps per CTA and cells per chunk, fastest tuple kept (and,
+        with ``cache``, read from / written to the per-GPU cache file);
+        returns (tuning dict, ms per compute)."""
         self._flush_pending()
-        d, t = ctypes.c_double(0), ctypes.c_double(0)
-        _check(self._lib.vgpu_autotune(self._h, self._mode_code(mode), ctypes.byref(d), ctypes.byref(t)))
+        t, ms = Tuning(), ctypes.c_double(0)
+        flags = (VGPU_TUNE_USE_CACHE | VGPU_TUNE_WRITE_CACHE) if cache else 0
+        _check(self._lib.vgpu_autotune_ex(self._h, self._mode_code(mode), flags, ctypes.byref(t), ctypes.byref(ms)))
         self._dirty = False
-        return d.value, t.value
+        return t.as_dict(), ms.value
 
-    def set_tuning(self, particles_per_block=0.0, warps_per_cta=0):
-        _check(self._lib.vgpu_set_tuning(self._h, float(particles_per_block), int(warps_per_cta)))
+    def set_tuning(self, particles_per_block=0.0, warps_per_cta=0, cells_per_chunk=0, fp64_fallback=0.0):
+        """vgpu_set_tuning_ex: zero keeps a setting."""
+        t = Tuning(float(particles_per_block), int(warps_per_cta), int(cells_per_chunk), float(fp64_fallback))
+        _check(self._lib.vgpu_set_tuning_ex(self._h, ctypes.byref(t)))
         self._dirty = True
+
+    def tuning(self):
+        t = Tuning()
+        _check(self._lib.vgpu_get_tuning(self._h, ctypes.byref(t)))
+        return t.as_dict()
 
     def set_ghost_depth(self, spacings=0.0):
         """Sheared periodic boxes: depth of the image layers a compute stores

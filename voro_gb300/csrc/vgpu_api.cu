@@ -8,6 +8,7 @@
 #include <cstring>
 #include <chrono>
 #include <mutex>
+#include <sys/stat.h>
 #include <string>
 #include <vector>
 #include "vgpu_internal.cuh"
@@ -1378,30 +1379,179 @@ int compute_cells(vgpu_container *h, int mode, bool thin) {
 
 extern "C" {
 
-int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms) {
-    if (!h) return fail(VGPU_ERR_ARG, "null handle");
-    // engine-grid densities to try (particles per block); the search visits
-    // fewer, fuller blocks as the density grows, and the best point depends
-    // on the container's shape and particle count
-    static const double kDensities[] = {0.35, 0.5, 0.6, 0.75, 0.9, 1.0, 1.25, 1.5, 2.0, 3.0};
-    double best = h->target_density, best_t = 1e300;
-    for (double d : kDensities) {
-        h->target_density = d;
-        double t = 1e300;
-        for (int rep = 0; rep < 2; rep++) {   // the first compute of a size also allocates
-            int rc = vgpu_compute(h, mode);
-            if (rc != VGPU_OK) return rc;
-            t = std::min(t, (double)h->stats.step_ms);
-        }
-        if (t < best_t) {
-            best_t = t;
-            best = d;
+int vgpu_get_tuning(vgpu_container *h, vgpu_tuning *out) {
+    if (!h || !out) return fail(VGPU_ERR_ARG, "null argument");
+    out->particles_per_block = h->target_density;
+    out->warps_per_cta = h->warps_per_cta;
+    out->cells_per_chunk = h->cell_chunk > 0 ? h->cell_chunk : kDefaultCellChunk;
+    out->fp64_fallback = h->fp64_fallback;
+    return VGPU_OK;
+}
+
+int vgpu_set_tuning_ex(vgpu_container *h, const vgpu_tuning *t) {
+    if (!h || !t) return fail(VGPU_ERR_ARG, "null argument");
+    if (t->warps_per_cta < 0 || t->warps_per_cta > kBuiltCtaWarps)
+        return fail(VGPU_ERR_ARG, "warps per CTA must be 1-%d (got %d)", kBuiltCtaWarps, t->warps_per_cta);
+    if (t->cells_per_chunk < 0 || t->cells_per_chunk > 64)
+        return fail(VGPU_ERR_ARG, "cells per chunk must be 1-64 (got %d)", t->cells_per_chunk);
+    if (!(t->fp64_fallback >= 0.0)) return fail(VGPU_ERR_ARG, "bad fallback fraction");
+    int rc = vgpu_set_tuning(h, t->particles_per_block, t->warps_per_cta);
+    if (rc != VGPU_OK) return rc;
+    if (t->cells_per_chunk > 0) h->cell_chunk = t->cells_per_chunk;
+    if (t->fp64_fallback > 0.0) h->fp64_fallback = t->fp64_fallback;
+    return VGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The autotuner's cache: one line per (GPU, workload signature) with the
+// tuple it chose, in $VORO_GB300_TUNE_CACHE, else
+// $XDG_CACHE_HOME/voro_gb300/autotune.txt, else ~/.cache/voro_gb300/autotune.txt.
+// Unreadable or unwritable files only cost a fresh search.
+std::string tune_cache_path() {
+    if (const char *e = getenv("VORO_GB300_TUNE_CACHE")) return e;
+    std::string base;
+    if (const char *x = getenv("XDG_CACHE_HOME")) base = x;
+    else if (const char *home = getenv("HOME")) base = std::string(home) + "/.cache";
+    else return "";
+    return base + "/voro_gb300/autotune.txt";
+}
+
+// The signature the choice depends on: the device, the container kind and
+// precision, the particle count to within a factor of two, the box's shape
+// (its largest over smallest side, rounded) and its walls.
+std::string tune_key(vgpu_container *h, int mode) {
+    cudaDeviceProp prop;
+    std::string dev = cudaGetDeviceProperties(&prop, h->device) == cudaSuccess ? prop.name : "unknown";
+    for (char &c : dev)
+        if (c == ' ' || c == '\t') c = '_';
+    const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
+    int lg = 0;
+    while (lg < 62 && (int64_t(1) << (lg + 1)) <= n) lg++;
+    const double e0 = std::max({h->g.len[0], h->g.len[1], h->g.len[2]});
+    const double e1 = std::max(1e-300, std::min({h->g.len[0], h->g.len[1], h->g.len[2]}));
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s|kind%d|mode%d|n2^%d|aspect%d|walls%d|sm%d", dev.c_str(), h->g.kind, mode, lg,
+             (int)std::lround(e0 / e1), (int)h->walls.size(), h->sms);
+    return buf;
+}
+
+bool tune_cache_read(const std::string &key, vgpu_tuning &t) {
+    const std::string path = tune_cache_path();
+    if (path.empty()) return false;
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+        char k[300];
+        vgpu_tuning v{};
+        if (sscanf(line, "%299s %lf %d %d %lf", k, &v.particles_per_block, &v.warps_per_cta, &v.cells_per_chunk,
+                   &v.fp64_fallback) == 5 &&
+            key == k && v.particles_per_block > 0 && v.warps_per_cta >= 1 && v.warps_per_cta <= kBuiltCtaWarps &&
+            v.cells_per_chunk >= 1 && v.cells_per_chunk <= 64) {
+            t = v;   // the last matching line wins
+            found = true;
         }
     }
-    h->target_density = best;
-    int rc = vgpu_compute(h, mode);   // leave the results of the chosen setting
-    if (best_density) *best_density = best;
+    fclose(f);
+    return found;
+}
+
+void tune_cache_write(const std::string &key, const vgpu_tuning &t) {
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    const size_t slash = path.rfind('/');
+    if (slash != std::string::npos) {   // mkdir -p of the directory
+        const std::string dir = path.substr(0, slash);
+        for (size_t i = 1; i <= dir.size(); i++)
+            if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);
+    }
+    FILE *f = fopen(path.c_str(), "a");
+    if (!f) return;
+    fprintf(f, "%s %.17g %d %d %.17g\n", key.c_str(), t.particles_per_block, t.warps_per_cta, t.cells_per_chunk,
+            t.fp64_fallback);
+    fclose(f);
+}
+
+// the best step time of two computes at tuning t (the first compute of a new
+// size also allocates)
+int time_tuning(vgpu_container *h, int mode, const vgpu_tuning &t, double *ms) {
+    int rc = vgpu_set_tuning_ex(h, &t);
+    if (rc != VGPU_OK) return rc;
+    double best = 1e300;
+    for (int rep = 0; rep < 2; rep++) {
+        rc = vgpu_compute(h, mode);
+        if (rc != VGPU_OK) return rc;
+        best = std::min(best, (double)h->stats.step_ms);
+    }
+    *ms = best;
+    return VGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgpu_autotune_ex(vgpu_container *h, int mode, int flags, vgpu_tuning *chosen, double *best_ms) {
+    if (!h) return fail(VGPU_ERR_ARG, "null handle");
+    if (flags & ~(VGPU_TUNE_USE_CACHE | VGPU_TUNE_WRITE_CACHE)) return fail(VGPU_ERR_ARG, "unknown flags 0x%x", flags);
+    const std::string key = tune_key(h, mode);
+    vgpu_tuning best;
+    vgpu_get_tuning(h, &best);
+    double best_t = 1e300;
+    if ((flags & VGPU_TUNE_USE_CACHE) && tune_cache_read(key, best)) {
+        int rc = time_tuning(h, mode, best, &best_t);   // leaves the results of the cached choice
+        if (chosen) *chosen = best;
+        if (best_ms) *best_ms = best_t;
+        return rc;
+    }
+    // coordinate search: the engine-grid density (particles per block: the
+    // search visits fewer, fuller blocks as it grows), then the warps (cells
+    // in flight) per CTA, then the cells a warp takes from the queue at once
+    static const double kDensities[] = {0.35, 0.5, 0.6, 0.75, 0.9, 1.0, 1.25, 1.5, 2.0, 3.0};
+    static const int kWarps[] = {1, 2, 4, 8};
+    static const int kChunks[] = {1, 2, 4, 8, 16};
+    auto consider = [&](const vgpu_tuning &t) -> int {
+        double ms;
+        const int rc = time_tuning(h, mode, t, &ms);
+        if (rc == VGPU_OK && ms < best_t) {
+            best_t = ms;
+            best = t;
+        }
+        return rc;
+    };
+    for (double d : kDensities) {
+        vgpu_tuning t = best;
+        t.particles_per_block = d;
+        if (int rc = consider(t)) return rc;
+    }
+    for (int w : kWarps) {
+        if (w > kBuiltCtaWarps) continue;
+        vgpu_tuning t = best;
+        t.warps_per_cta = w;
+        if (int rc = consider(t)) return rc;
+    }
+    for (int c : kChunks) {
+        vgpu_tuning t = best;
+        t.cells_per_chunk = c;
+        if (int rc = consider(t)) return rc;
+    }
+    double ms;
+    int rc = time_tuning(h, mode, best, &ms);   // leave the results of the chosen setting
+    if (rc != VGPU_OK) return rc;
+    if (flags & VGPU_TUNE_WRITE_CACHE) tune_cache_write(key, best);
+    if (chosen) *chosen = best;
     if (best_ms) *best_ms = best_t;
+    return VGPU_OK;
+}
+
+int vgpu_autotune(vgpu_container *h, int mode, double *best_density, double *best_ms) {
+    vgpu_tuning t;
+    const int rc = vgpu_autotune_ex(h, mode, 0, &t, best_ms);
+    if (rc == VGPU_OK && best_density) *best_density = t.particles_per_block;
     return rc;
 }
 

@@ -23,7 +23,7 @@ extern "C" {
 #define VGPU_ERR_INTERNAL 3      /* VOROPP_INTERNAL_ERROR */
 #define VGPU_ERR_ARG 16          /* bad argument / handle */
 #define VGPU_ERR_CUDA 17         /* CUDA runtime error (see vgpu_last_error) */
-#define VGPU_ERR_UNSUPPORTED 18  /* not supported (walls on a periodic box; a sheared box in a batch) */
+#define VGPU_ERR_UNSUPPORTED 18  /* not supported (walls on a periodic box) */
 #define VGPU_ERR_DUPLICATE 19    /* container_periodic put of a duplicate point
                                     (src/common.cc:14-20 exits; we return this) */
 #define VGPU_ERR_NOT_COMPUTED 20 /* results requested before vgpu_compute */
@@ -335,8 +335,8 @@ int vgpu_set_fp64_fallback(vgpu_container *h, double fraction);
  * cell engine with a single device work queue, so thousands of small and
  * large containers share the GPU.  Results land in each member container and
  * are read with the usual getters.  Containers stay owned by the caller and
- * must outlive the batch's computes.  A sheared container_periodic is
- * computed on its own (vgpu_batch_add: VGPU_ERR_UNSUPPORTED). */
+ * must outlive the batch's computes.  A sheared container_periodic joins a
+ * batch with its images stored at the reference's depth. */
 typedef struct vgpu_batch vgpu_batch;
 int vgpu_batch_create(vgpu_batch **out);
 int vgpu_batch_add(vgpu_batch *b, vgpu_container *h);

@@ -24,7 +24,7 @@ def test_batch_needs_a_device():
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
 def test_batch_of_golden_fixtures_matches_reference(gpu, mode):
-    names = [n for n in G.names() if "tric_" not in n]   # sheared boxes: one at a time
+    names = G.names()   # every kind, sheared periodic boxes included
     cons, refs = [], []
     for name in names:
         w, z = G.load(name)
@@ -154,7 +154,23 @@ def test_batch_in_record_waves_matches_one_wave(gpu):
 
 
 @pytest.mark.gpu
-def test_batch_refuses_a_sheared_box(gpu):
-    w, _ = G.load("tric_dyadic_1500")
-    with pytest.raises(vg.VoroError):
-        vg.batch([vg.from_workload(w)])
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_sheared_members_in_a_batch_of_mixed_kinds(gpu, mode):
+    """Sheared container_periodic members (their images stored at the
+    reference's depth) beside rectangular, radical and walled ones, in waves
+    of the record store: the same cells as the reference."""
+    names = ["tric_dyadic_1500", "periodic_2000", "tric_poly_1000", "radical_1200", "tric_skew_800",
+             "wall_sphere_2000", "tric_generic_1200", "degenerate_tric_small_5"]
+    cons, refs = [], []
+    for name in names:
+        w, z = G.load(name)
+        cons.append(vg.from_workload(w, mode=mode))
+        refs.append(z)
+    b = vg.batch(cons)
+    b.set_record_budget(4 << 20)   # a few waves
+    b.compute_all_cells(mode=mode)
+    assert b.waves() > 1
+    assert b.stats()["failed_cells"] == 0
+    for name, con, z in zip(names, cons, refs):
+        errs = G.compare_cells(con.cells(), z, *TOL[mode], label=f"batch/{name}/{mode}")
+        assert not errs, "\n".join(errs)

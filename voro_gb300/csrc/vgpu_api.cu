@@ -1168,8 +1168,9 @@ int setup_member_records(vgpu_container *h, CellParams &cp, Counters *cnt, cudaS
     cp.rec = nullptr;
     cp.poly = nullptr;
     if (h->nkept <= 0) return VGPU_OK;
-    VG_CUDA(h->rec_off.ensure((size_t)h->nkept * 8));
-    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nkept * 8, s));
+    // by engine index: the particles, then (sheared boxes) their images
+    VG_CUDA(h->rec_off.ensure((size_t)h->nengine * 8));
+    VG_CUDA(cudaMemsetAsync(h->rec_off.p, 0xff, (size_t)h->nengine * 8, s));
     cp.rec_off = h->rec_off.as<unsigned long long>();
     if (h->output & VGPU_OUTPUT_POLYTOPES) {
         const unsigned long long pcap = (unsigned long long)h->nkept * kPolyDoublesPerCell + (1u << 16);
@@ -1998,7 +1999,6 @@ int vgpu_batch_create(vgpu_batch **out) {
 int vgpu_batch_add(vgpu_batch *b, vgpu_container *h) {
     if (!b || !h) return fail(VGPU_ERR_ARG, "null argument");
     if (h->device != b->device) return fail(VGPU_ERR_ARG, "container and batch are on different devices");
-    if (h->g.tric) return fail(VGPU_ERR_UNSUPPORTED, "sheared periodic boxes are computed one at a time");
     b->members.push_back(h);
     return VGPU_OK;
 }
@@ -2040,7 +2040,8 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     for (int i = 0; i < nc; i++) {
         const vgpu_container *h = b->members[i];
         const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
-        if (n <= kSmallBinMax) small.push_back(i);
+        // (a sheared box stores images of its particles: the multi-kernel binning)
+        if (n <= kSmallBinMax && !h->g.tric) small.push_back(i);
     }
     const int ns = (int)small.size();
     if (ns > 0) {
@@ -2087,7 +2088,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         }
     }
     for (int i = 0; i < nc; i++) {
-        cps[i].cell_list = nullptr;
+        if (!b->members[i]->g.tric) cps[i].cell_list = nullptr;   // (sheared: the particles among the images)
         cps[i].overflow_list = nullptr;
         cps[i].offsets = b->offsets.as<int>();   // the same table for every container
         starts[i + 1] = starts[i] + b->members[i]->nkept;

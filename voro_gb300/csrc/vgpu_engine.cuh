@@ -1272,7 +1272,8 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
             for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
             __syncwarp();
         }
-        const int k = (int)(gidx - cbeg);
+        // a sheared box's cells are its particles, not the images it stores
+        const int k = P.cell_list ? P.cell_list[gidx - cbeg] : (int)(gidx - cbeg);
         Engine<MODE, K, LEAN> eng(P, S, offsets, lane);
         eng.run(k);
         tests += eng.C.tests;

@@ -867,8 +867,10 @@ __global__ void __launch_bounds__(32 * kFinWarps, VGPU_FIN_MIN_BLOCKS) finish_ba
             __syncwarp();
         }
         // the pair (g, g+1); its second cell may belong to the next container
-        const int k0 = (int)(g - cbeg);
-        const int k1 = g + 1 < cend && g + 1 < gend ? (int)(g + 1 - cbeg) : -1;
+        // (a sheared box's cells: its particles, listed in cell_list)
+        const int i0 = (int)(g - cbeg);
+        const int k0 = P.cell_list ? P.cell_list[i0] : i0;
+        const int k1 = g + 1 < cend && g + 1 < gend ? (P.cell_list ? P.cell_list[i0 + 1] : i0 + 1) : -1;
         finish_pair<MODE>(P, fsh[wid], k0, k1, lane);
         if (k1 < 0 && g + 1 < gend) {
             // g + 1 starts the next container: finish it with that container's parameters
@@ -886,7 +888,8 @@ __global__ void __launch_bounds__(32 * kFinWarps, VGPU_FIN_MIN_BLOCKS) finish_ba
             unsigned *dst = reinterpret_cast<unsigned *>(&P);
             for (int i = lane; i < (int)(sizeof(CellParams) / 4); i += 32) dst[i] = src[i];
             __syncwarp();
-            finish_pair<MODE>(P, fsh[wid], (int)(g1 - cbeg), -1, lane);
+            const int j0 = (int)(g1 - cbeg);
+            finish_pair<MODE>(P, fsh[wid], P.cell_list ? P.cell_list[j0] : j0, -1, lane);
         }
     }
 }

@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--batch-count", type=int, default=1024, help="containers of the batched leg")
     ap.add_argument("--batch-nmax", type=int, default=100_000, help="largest container of the batched leg")
     ap.add_argument("--cpu-one-core-seconds", type=float, default=8.0)
+    ap.add_argument("--fp64-fallback", type=float, default=0.0,
+                    help="mixed engine's FP64 fallback fraction (0: the library default; >= 1: never sample)")
     return ap.parse_args()
 
 
@@ -397,6 +399,8 @@ def run_ours(args):
     con = vg.container_periodic(*w["geom"], *w["grid"], 8, mode=args.mode)
     if args.density > 0:
         con.set_tuning(args.density, 0)
+    if args.fp64_fallback > 0:
+        con.set_fp64_fallback(args.fp64_fallback)
     con.put_device(n, d_ids.data_ptr(), d_xyzr.data_ptr(), keepalive=(d_ids, d_xyzr))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 

@@ -42,6 +42,14 @@ namespace vgpu {
 
 namespace {
 
+// How the clipping kernels store the polytope records: streaming stores by
+// default (the records are read once, by the finish kernel, and would
+// otherwise push the particles and block starts that the searches re-read out
+// of the L2); -D'VGPU_RECORD_STORE(p,v)=(*(p)=(v))' builds plain stores.
+#ifndef VGPU_RECORD_STORE
+#define VGPU_RECORD_STORE(p, v) __stcs((p), (unsigned)(v))
+#endif
+
 // ------------------------------------------------------------------ masks
 // Slot s of lane l is bit l+32s.
 template <int K>
@@ -1031,6 +1039,7 @@ struct Engine {
     }
 
     // ---- the finished polytope as a compact record for the finish kernel
+    //      (stored by VGPU_RECORD_STORE)
     //      (layout in CellParams): valid vertices and live planes only, in
     //      slot order, with plane and vertex indices renumbered to match;
     //      false if the record store is full
@@ -1053,11 +1062,11 @@ struct Engine {
         if (off + words > P.rec_cap) return false;
         unsigned *R = P.rec + off;
         if (lane == 0) {
-            R[0] = (unsigned)nv;
-            R[1] = (unsigned)nf;
-            R[2] = (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0);
-            R[3] = 0;
-            R[4] = 0;
+            VGPU_RECORD_STORE(&R[0], (unsigned)nv);
+            VGPU_RECORD_STORE(&R[1], (unsigned)nf);
+            VGPU_RECORD_STORE(&R[2], (C.marginal ? VGPU_CELL_MARGINAL : 0) | (C.repaired ? VGPU_CELL_REPAIRED : 0));
+            VGPU_RECORD_STORE(&R[3], 0);
+            VGPU_RECORD_STORE(&R[4], 0);
         }
         // compact indices: vertex slot -> rank among valid slots (vmap),
         // plane slot -> rank among live planes (endN, free once the cell is done)
@@ -1080,22 +1089,22 @@ struct Engine {
                 const int r = S.vmap[t];
                 const unsigned T = V.tri[s];
                 const unsigned A3 = S.adj[t];
-                rv[r] = (unsigned)S.endN[tri_plane(T, 0)] | ((unsigned)S.endN[tri_plane(T, 1)] << 8) |
-                        ((unsigned)S.endN[tri_plane(T, 2)] << 16);
-                rv[nv + r] = (unsigned)S.vmap[A3 & 255u] | ((unsigned)S.vmap[(A3 >> 8) & 255u] << 8) |
-                             ((unsigned)S.vmap[(A3 >> 16) & 255u] << 16);
+                VGPU_RECORD_STORE(&rv[r], (unsigned)S.endN[tri_plane(T, 0)] | ((unsigned)S.endN[tri_plane(T, 1)] << 8) |
+                        ((unsigned)S.endN[tri_plane(T, 2)] << 16));
+                VGPU_RECORD_STORE(&rv[nv + r], (unsigned)S.vmap[A3 & 255u] | ((unsigned)S.vmap[(A3 >> 8) & 255u] << 8) |
+                             ((unsigned)S.vmap[(A3 >> 16) & 255u] << 16));
                 if (MODE == VGPU_FP64) {
                     const double c[3] = {V.dx[s], V.dy[s], V.dz[s]};
 #pragma unroll
                     for (int a = 0; a < 3; a++) {
                         const unsigned long long b = (unsigned long long)__double_as_longlong(c[a]);
-                        rv[(2 + 2 * a) * nv + 2 * r] = (unsigned)b;
-                        rv[(2 + 2 * a) * nv + 2 * r + 1] = (unsigned)(b >> 32);
+                        VGPU_RECORD_STORE(&rv[(2 + 2 * a) * nv + 2 * r], (unsigned)b);
+                        VGPU_RECORD_STORE(&rv[(2 + 2 * a) * nv + 2 * r + 1], (unsigned)(b >> 32));
                     }
                 } else {
-                    rv[2 * nv + r] = __float_as_uint(V.x[s]);
-                    rv[3 * nv + r] = __float_as_uint(V.y[s]);
-                    rv[4 * nv + r] = __float_as_uint(V.z[s]);
+                    VGPU_RECORD_STORE(&rv[2 * nv + r], __float_as_uint(V.x[s]));
+                    VGPU_RECORD_STORE(&rv[3 * nv + r], __float_as_uint(V.y[s]));
+                    VGPU_RECORD_STORE(&rv[4 * nv + r], __float_as_uint(V.z[s]));
                 }
             }
         }
@@ -1105,9 +1114,9 @@ struct Engine {
             const int q = lane + 32 * h;
             if ((live >> q) & 1ull) {
                 const int r = S.endN[q];
-                rp[r] = (unsigned)S.psrc[q];
-                rp[nf + r] = (unsigned)S.pshift[q];
-                rp[2 * nf + r] = (unsigned)S.pid[q];
+                VGPU_RECORD_STORE(&rp[r], (unsigned)S.psrc[q]);
+                VGPU_RECORD_STORE(&rp[nf + r], (unsigned)S.pshift[q]);
+                VGPU_RECORD_STORE(&rp[2 * nf + r], (unsigned)S.pid[q]);
             }
         }
         if (lane == 0) P.rec_off[C.k] = off;

@@ -175,6 +175,7 @@ struct vgpu_container {
     int64_t dev_n_ext = 0;
     bool use_device_input = false;
     DevBuf ids_in, xyzr_in;
+    DevBuf chk;   // put(): index of the first non-finite particle
     // work buffers
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, ovf_list2, counters, counters2;
@@ -539,31 +540,6 @@ int vgpu_container_destroy(vgpu_container *h) {
 
 }  // extern "C"
 
-namespace {
-
-// Index of the first particle whose x, y or z (or r, in a radical container)
-// is an infinity or a NaN; -1 if there is none.  Branch-free over the bit
-// patterns (an all-ones exponent) so that it runs at memory speed.
-int64_t first_nonfinite(const double *xyzr, int64_t n, bool poly) {
-    constexpr uint64_t kExp = 0x7ff0000000000000ull;
-    const uint64_t rmask = poly ? kExp : 0ull;
-    uint64_t bad = 0;
-    for (int64_t i = 0; i < n; i++) {
-        uint64_t b[4];
-        memcpy(b, xyzr + 4 * i, 32);
-        bad |= (uint64_t)((b[0] & kExp) == kExp) | (uint64_t)((b[1] & kExp) == kExp) |
-               (uint64_t)((b[2] & kExp) == kExp) | (uint64_t)(rmask != 0 && (b[3] & rmask) == rmask);
-    }
-    if (!bad) return -1;
-    for (int64_t i = 0; i < n; i++) {
-        const double *q = xyzr + 4 * i;
-        if (!(std::isfinite(q[0]) && std::isfinite(q[1]) && std::isfinite(q[2]) && (!poly || std::isfinite(q[3]))))
-            return i;
-    }
-    return -1;
-}
-
-}  // namespace
 
 extern "C" {
 
@@ -601,12 +577,18 @@ int vgpu_put(vgpu_container *h, int64_t n, const int32_t *ids, const double *xyz
                             h->stream));
     VG_CUDA(cudaMemcpyAsync(h->xyzr_in.as<double>() + 4 * h->staged, xyzr, (size_t)n * 32,
                             cudaMemcpyHostToDevice, h->stream));
-    // non-finite input is rejected here, while the copies run (from pinned
-    // memory they are asynchronous); the staged count does not advance, so
-    // nothing of this call is kept
-    const int64_t bad = first_nonfinite(xyzr, n, h->g.poly);
+    // non-finite input is rejected here, by a scan of what was just copied
+    // (on the device: the host's one-thread scan of 4M particles took longer
+    // than the copy); the staged count does not advance, so nothing of this
+    // call is kept
+    VG_CUDA(h->chk.ensure(sizeof(unsigned long long)));
+    VG_CUDA(cudaMemsetAsync(h->chk.p, 0xff, sizeof(unsigned long long), h->stream));
+    VG_CUDA(launch_first_nonfinite(h->xyzr_in.as<double>() + 4 * h->staged, n, h->g.poly,
+                                   h->chk.as<unsigned long long>(), h->stream));
+    unsigned long long bad = ~0ull;
+    VG_CUDA(cudaMemcpyAsync(&bad, h->chk.p, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
     VG_CUDA(cudaStreamSynchronize(h->stream));
-    if (bad >= 0)
+    if (bad != ~0ull)
         return fail(VGPU_ERR_ARG, "particle %lld (id %d) has a non-finite position or radius", (long long)bad,
                     (int)ids[bad]);
     h->staged += n;

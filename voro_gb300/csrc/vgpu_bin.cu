@@ -6,6 +6,7 @@
 //   container_periodic: put_locate_block   src/container_prd.cc:189-216
 // and computes two keys per particle: the reference block (which fixes the
 // loop order of results) and the engine block (which fixes the search grid).
+#include <algorithm>
 #include "vgpu_dev.cuh"
 
 namespace vgpu {
@@ -375,6 +376,29 @@ __global__ void duplicate_kernel(const unsigned *ukey_sorted, const int *uorder,
 }
 
 }  // namespace
+
+// The lowest index among n staged particles whose x, y or z (or r, when poly)
+// is an infinity or a NaN, by atomicMin into *first (left as it was when all
+// are finite).  put() runs it on the particles it has just copied, before it
+// counts them as staged.
+__global__ void first_nonfinite_kernel(const double4 *xyzr, long long n, int poly, unsigned long long *first) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double4 q = xyzr[i];
+        if (!(isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && (!poly || isfinite(q.w))))
+            atomicMin(first, (unsigned long long)i);
+    }
+}
+
+cudaError_t launch_first_nonfinite(const double *xyzr, long long n, bool poly, unsigned long long *first,
+                                   cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const long long blocks = std::min<long long>((n + 255) / 256, 4096);
+    first_nonfinite_kernel<<<(unsigned)blocks, 256, 0, s>>>(reinterpret_cast<const double4 *>(xyzr), n, poly ? 1 : 0,
+                                                             first);
+    note_launch();
+    return cudaGetLastError();
+}
 
 cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s) {
     int nub = bp.g.un[0] * bp.g.un[1] * bp.g.un[2];

@@ -9,6 +9,38 @@ static constexpr float kU32 = 5.9604645e-08f;          // 2^-24
 static constexpr double kU64 = 1.1102230246251565e-16; // 2^-53
 static constexpr unsigned kFull = 0xffffffffu;
 
+#if VGPU_GATHER_TMA
+// Bulk copies of candidate particle runs into shared memory, completed on a
+// per-warp mbarrier (cp.async.bulk, mbarrier.try_wait).  Every wait is bounded.
+static __device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+static __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+static __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+static __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+static __device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+static __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity) {
+    const unsigned a = smem_addr(bar);
+    for (int i = 0; i < (1 << 20); i++) {
+        unsigned done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+#endif
+
 // plane indices are always < kMaxPlanes; the mask keeps every shared-memory
 // index in bounds even if a slot held inconsistent data
 static __device__ __forceinline__ int tri_plane(unsigned t, int e) { return (t >> (8 * e)) & (kMaxPlanes - 1); }

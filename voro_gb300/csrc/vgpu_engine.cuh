@@ -45,8 +45,10 @@ namespace {
 // How the clipping kernels store the polytope records: streaming stores by
 // default (the records are read once, by the finish kernel, and would
 // otherwise push the particles and block starts that the searches re-read out
-// of the L2); -D'VGPU_RECORD_STORE(p,v)=(*(p)=(v))' builds plain stores.
-#ifndef VGPU_RECORD_STORE
+// of the L2); -DVGPU_PLAIN_RECORD_STORES=1 builds plain stores.
+#if VGPU_PLAIN_RECORD_STORES
+#define VGPU_RECORD_STORE(p, v) (*(p) = (unsigned)(v))
+#else
 #define VGPU_RECORD_STORE(p, v) __stcs((p), (unsigned)(v))
 #endif
 
@@ -114,6 +116,12 @@ __device__ __forceinline__ Mask<K> ballot_mask(const bool (&pred)[K]) {
 // ------------------------------------------------------------------ shared memory per warp
 template <int MODE, int K>
 struct WarpShared {
+#if VGPU_GATHER_TMA
+    float4 cstage[kStageEntries];   // staged particle runs (bulk copies)
+    unsigned long long cbar;        // their mbarrier
+    unsigned cbar_phase;            // its current phase parity; bit 31: staging off
+    unsigned cbar_pad;
+#endif
     float4 pl[kMaxPlanes];   // plane n.x, n.y, n.z, h  (n.v <= h inside)
     float4 pe[kMaxPlanes];   // |n|, en (abs error of n), eh (abs error of h), |h|
     // (pl and pe are contiguous: at the end of a cell they hold the FP64 planes)
@@ -818,6 +826,31 @@ struct Engine {
         __syncwarp();
     }
 
+#if VGPU_GATHER_TMA
+    // ---- candidates w0 .. w0+kStageEntries-1 of a block pass into S.cstage:
+    //      each lane copies the part of its block's run (16-byte particles,
+    //      contiguous in engine order) that falls in the window.  False (the
+    //      caller reads global memory) when staging is off for this warp; a
+    //      wait that runs out turns staging off for the rest of the launch.
+    __device__ bool stage_runs(int w0, int tot, int incl, int cnt, int st) {
+        const unsigned ph = S.cbar_phase;
+        if (ph & 0x80000000u) return false;
+        const int W = min(kStageEntries, tot - w0);
+        fence_proxy_async_smem();   // earlier reads of the window before the copies' writes
+        __syncwarp();
+        if (lane == 0) mbar_expect_tx(&S.cbar, (unsigned)W * 16u);
+        __syncwarp();
+        const int r0 = incl - cnt;
+        const int a = max(r0, w0), b = min(incl, w0 + W);
+        if (b > a) bulk_g2s(&S.cstage[a - w0], P.a.l32 + st + (a - r0), (unsigned)(b - a) * 16u, &S.cbar);
+        const bool ok = __all_sync(kFull, mbar_wait_bounded(&S.cbar, ph & 1u));
+        __syncwarp();
+        if (lane == 0) S.cbar_phase = ok ? (ph ^ 1u) : 0x80000000u;
+        __syncwarp();
+        return ok;
+    }
+#endif
+
     // ---- candidates from a range of block offsets: wrap/skip, block distance,
     //      then one lane per candidate particle
     __device__ void gather_offsets(int e_begin, int e_end, bool from_table, int shell_r) {
@@ -885,6 +918,10 @@ struct Engine {
             const int incl = warp_incl_scan(cnt, lane);
             const int tot = __shfl_sync(kFull, incl, 31);
             const int packed_d = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
+#if VGPU_GATHER_TMA
+            int w0 = 0;
+            bool staged = false;
+#endif
             for (int c0 = 0; c0 < tot; c0 += 32) {
                 PHASE_COUNT(3, 1);
                 if (C.ncand > kCandBuf - 32) {
@@ -893,6 +930,12 @@ struct Engine {
                     PHASE_END(t_nested, 6);
                 }
                 if (C.deleted || C.overflow) return;
+#if VGPU_GATHER_TMA
+                if ((c0 & (kStageEntries - 1)) == 0) {
+                    w0 = c0;
+                    staged = stage_runs(c0, tot, incl, cnt, st);
+                }
+#endif
                 const int c = c0 + lane;
                 // owner lane: number of lanes whose inclusive prefix is <= c
                 int pos = 0;
@@ -915,7 +958,11 @@ struct Engine {
                     const int ddi = (o_d & 31) - 16, ddj = ((o_d >> 5) & 31) - 16, ddk = ((o_d >> 10) & 31) - 16;
                     const bool self = (j == C.k) && ddi == 0 && ddj == 0 && ddk == 0;
                     if (!self) {
+#if VGPU_GATHER_TMA
+                        const float4 lj = staged ? S.cstage[c - w0] : P.a.l32[j];
+#else
                         const float4 lj = P.a.l32[j];
+#endif
                         const float dx = fmaf((float)ddi, P.g.gbs32[0], lj.x - l0);
                         const float dy = fmaf((float)ddj, P.g.gbs32[1], lj.y - l1);
                         const float dz = fmaf((float)ddk, P.g.gbs32[2], lj.z - l2);
@@ -1165,6 +1212,13 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
     __syncthreads();
     WarpShared<MODE, K> &S = ws[wid];
     if (lane < 6) S.stat[lane] = 0ull;
+#if VGPU_GATHER_TMA
+    if (lane == 0) {
+        mbar_init(&S.cbar, 1);
+        S.cbar_phase = 0;
+    }
+    __syncwarp();
+#endif
 #ifdef VGPU_PHASE_TIMING
     unsigned long long ph[16] = {};
     const long long t_kernel0 = clock64();
@@ -1235,6 +1289,13 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
     __syncthreads();
     CellParams &P = *reinterpret_cast<CellParams *>(reinterpret_cast<unsigned char *>(cps) + cp_slot * wid);
     WarpShared<MODE, K> &S = ws[wid];
+#if VGPU_GATHER_TMA
+    if (lane == 0) {
+        mbar_init(&S.cbar, 1);
+        S.cbar_phase = 0;
+    }
+    __syncwarp();
+#endif
     int cur = -1;
     long long cbeg = 0, cend = 0;
     unsigned long long tests = 0, repairs = 0, ptested = 0, pcut = 0, deleted = 0, marginal = 0, ovf = 0;

@@ -18,7 +18,11 @@ constexpr int kWarp = 32;
 constexpr int kDefaultCellChunk = VGPU_CELL_CHUNK;
 constexpr int kBuiltCtaWarps = VGPU_CTA_THREADS / 32;
 constexpr int kMaxPlanes = 64;     // plane slots per cell (64-bit plane masks)
-constexpr int kCandBuf = 64;       // candidate buffer entries per warp
+constexpr int kCandBuf = 64;
+#ifndef VGPU_GATHER_TMA
+#define VGPU_GATHER_TMA 0
+#endif
+constexpr int kStageEntries = 64;   // staged candidate particles per warp (VGPU_GATHER_TMA)       // candidate buffer entries per warp
 // Neighbour IDs: kNbStride slots per cell in a fixed-stride array; a cell with
 // more faces keeps kNbStride-1 there and the rest in an overflow store, whose
 // offset takes the row's last slot.
@@ -208,6 +212,8 @@ struct BinParams {
     int *idx;            // identity 0..n-1
 };
 cudaError_t launch_remap(const BinParams &bp, int *kept, unsigned long long *rmax_bits, cudaStream_t s);
+cudaError_t launch_first_nonfinite(const double *xyzr, long long n, bool poly, unsigned long long *first,
+                                   cudaStream_t s);
 // nkept particles in loop order (uorder) and nengine engine entries in engine
 // order (gorder; an index i >= nin is image i - nin of particle img_src[i - nin])
 cudaError_t launch_gather(const Geometry &g, int nkept, int nengine, int nin, const int *img_src,

@@ -245,8 +245,11 @@ def fp64_leg(con, n, flush, mixed):
 
 def c4_leg():
     """Near-degenerate lattice: 64^3 FCC (a = 1, periodic), every coordinate
-    jittered by N(0, (1e-7)^2).  One mixed and one FP64 compute; the rate at
-    which FP32 side tests fall back to FP64 and the topology agreement."""
+    jittered by N(0, (1e-7)^2).  The mixed compute as it runs by default (its
+    sample of the first pass hands the container to the FP64 engine), the
+    FP32 engine forced through every cell (the rate at which its side tests
+    fall back to FP64 and cells are handed on), the plain FP64 engine, and
+    the topology agreement of the three."""
     import voro_gb300 as vg
     from voro_gb300 import workloads as W
     w = W.fcc_jitter(cells=64, sigma=1e-7, seed=1004)
@@ -256,20 +259,31 @@ def c4_leg():
     con.compute_all_cells()
     st = con.stats()
     m = con.cells()
+    con.set_fp64_fallback(1.0)           # never hand the container over
+    con.compute_all_cells()
+    con.compute_all_cells()
+    stf = con.stats()
+    mf = con.cells()
+    con.set_fp64_fallback(0.25)
+    con.compute_all_cells(mode="fp64")
     con.compute_all_cells(mode="fp64")
     st64 = con.stats()
     f = con.cells()
-    topo = (np.array_equal(f.nf, m.nf) and np.array_equal(f.nv, m.nv) and np.array_equal(f.nb_off, m.nb_off)
-            and np.array_equal(f.nb, m.nb))
-    rel = np.abs(m.vol - f.vol) / f.vol
+    same = lambda a: (np.array_equal(f.nf, a.nf) and np.array_equal(f.nv, a.nv) and
+                      np.array_equal(f.nb_off, a.nb_off) and np.array_equal(f.nb, a.nb))
+    rel = max(float((np.abs(a.vol - f.vol) / f.vol).max()) for a in (m, mf))
     return {"workload": f"FCC 64^3 (a = 1, periodic cube L = 64), {n} particles, jitter sigma 1e-7 (seed 1004)",
-            "cells_per_s": n / (st["step_ms"] / 1000.0), "fp64_engine_cells_per_s": n / (st64["step_ms"] / 1000.0),
-            "side_tests": int(st["side_tests"]), "fp64_repairs": int(st["fp64_repairs"]),
-            "fp64_repairs_per_test": st["fp64_repairs"] / max(st["side_tests"], 1),
-            "cells_rerun_with_fp64": int(st["overflow_reruns"]),
-            "cells_rerun_fraction": st["overflow_reruns"] / n,
-            "marginal_cells": int(st["marginal_cells"]), "failed_cells": int(st["failed_cells"]),
-            "topology_equal_to_fp64": bool(topo), "max_rel_volume_diff_vs_fp64": float(rel.max())}
+            "cells_per_s": n / (st["step_ms"] / 1000.0),
+            "cells_on_fp64_engine": int(st["fp64_engine_cells"]),
+            "fp64_engine_cells_per_s": n / (st64["step_ms"] / 1000.0),
+            "fp32_engine_forced": {
+                "cells_per_s": n / (stf["step_ms"] / 1000.0),
+                "side_tests": int(stf["side_tests"]), "fp64_repairs": int(stf["fp64_repairs"]),
+                "fp64_repairs_per_test": stf["fp64_repairs"] / max(stf["side_tests"], 1),
+                "cells_handed_on": int(stf["overflow_reruns"]),
+                "cells_handed_on_fraction": stf["overflow_reruns"] / n},
+            "marginal_cells": int(stf["marginal_cells"]), "failed_cells": int(st["failed_cells"] + stf["failed_cells"]),
+            "topology_equal_to_fp64": bool(same(m) and same(mf)), "max_rel_volume_diff_vs_fp64": rel}
 
 
 def batched_leg(count, nmax, steps, warmup, mode="mixed"):

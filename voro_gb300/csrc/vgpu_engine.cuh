@@ -42,14 +42,16 @@ namespace vgpu {
 
 namespace {
 
-// How the clipping kernels store the polytope records: streaming stores by
-// default (the records are read once, by the finish kernel, and would
-// otherwise push the particles and block starts that the searches re-read out
-// of the L2); -DVGPU_PLAIN_RECORD_STORES=1 builds plain stores.
-#if VGPU_PLAIN_RECORD_STORES
-#define VGPU_RECORD_STORE(p, v) (*(p) = (unsigned)(v))
-#else
+// How the clipping kernels store the polytope records: plain stores by
+// default; -DVGPU_STREAMING_RECORD_STORES=1 builds streaming stores (st.cs,
+// meant to keep the once-read records from pushing the particles and block
+// starts out of the L2).  Measured on the 4M periodic box, clipping passes:
+// plain 76.2 ms, streaming 80.1 ms (the streaming form also costs the lean
+// pass registers: 100/160 spilled bytes against 56/80).
+#if VGPU_STREAMING_RECORD_STORES
 #define VGPU_RECORD_STORE(p, v) __stcs((p), (unsigned)(v))
+#else
+#define VGPU_RECORD_STORE(p, v) (*(p) = (unsigned)(v))
 #endif
 
 // ------------------------------------------------------------------ masks
@@ -809,6 +811,28 @@ struct Engine {
             k0 = bitonic32(k0, lane);
         }
         PHASE_END(t_sort, 2);
+#if VGPU_FLUSH_PREFETCH
+        // the next candidate's key and distance are read while this one is
+        // tested and cut (they do not change during the flush)
+        unsigned key = __shfl_sync(kFull, k0, 0);
+        float2 Ezw = *reinterpret_cast<const float2 *>(&S.u.c.ce[key & 63u].z);
+        for (int i = 0; i < n; i++) {
+            const int cb = key & 63u;
+            const float2 E = Ezw;
+            if (i + 1 < n) {
+                key = __shfl_sync(kFull, i + 1 < 32 ? k0 : k1, (i + 1) & 31);
+                Ezw = *reinterpret_cast<const float2 *>(&S.u.c.ce[key & 63u].z);
+            }
+            if (P.g.poly) {
+                const float rs = E.y;
+                if (!(rs <= 0.0f || rs * rs < 4.0f * C.R2 * E.x * E.x * (1.0f + 16.0f * kU32))) continue;
+            } else {
+                if (E.y >= C.cutoff2 * (1.0f + 1e-4f)) break;
+            }
+            test_and_cut(cb);
+            if (C.deleted || C.overflow) break;
+        }
+#else
         for (int i = 0; i < n; i++) {
             const unsigned key = __shfl_sync(kFull, i < 32 ? k0 : k1, i & 31);
             const int cb = key & 63u;
@@ -822,6 +846,7 @@ struct Engine {
             test_and_cut(cb);
             if (C.deleted || C.overflow) break;
         }
+#endif
         C.ncand = 0;
         __syncwarp();
     }

@@ -795,14 +795,15 @@ __device__ __forceinline__ void finish_record(const CellParams &P, FinishShared<
 }
 
 constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
-// CTAs kept resident per SM (the register bound of the launch): with 22 KB
+// CTAs kept resident per SM (the register bound of the launch).  With 22 KB
 // of shared memory per CTA (a warp's two 16-lane cells share the space of
-// one 128-vertex cell) the 124 registers the kernel wants decide, 8 CTAs.
-// Measured on the 4M periodic box, finish kernel: 7 (no cap) 11.0 ms, 8
-// 11.3 ms, 9 (96 registers, spills) 12.5 ms; 12.3 ms with two full-size
-// cells per warp (31.7 KB per CTA, 7 CTAs).
+// one 128-vertex cell) registers decide.  Measured on the 4M periodic box,
+// finish kernel: 6 (148 registers, so 6 CTAs resident) 14.1 ms; 7 (128
+// registers, a few spilled bytes, 8 CTAs resident) 12.3 ms.  (Before the
+// coincident-vertex merge and the second correction step the kernel fitted
+// 124 registers: 8 CTAs, 11.0 ms.)
 #ifndef VGPU_FIN_MIN_BLOCKS
-#define VGPU_FIN_MIN_BLOCKS 6
+#define VGPU_FIN_MIN_BLOCKS 7
 #endif
 
 // Two cells per warp, one per 16-lane half, when both have at most 64

@@ -89,8 +89,9 @@ def test_batch_edge_members(gpu):
         c.put_array(np.arange(n, dtype=np.int32), rng.uniform(0, 10, size=(n, 3)))
         return c
 
+    # sizes either side of the two shared-memory binning tiers (4096, 16384)
     makers = [lambda: walled(0), lambda: walled(3000), lambda: periodic(4096), lambda: periodic(4097),
-              lambda: walled(1)]
+              lambda: walled(1), lambda: periodic(16384), lambda: periodic(16385), lambda: walled(9000)]
     state = rng.bit_generator.state
     single = []
     for m in makers:

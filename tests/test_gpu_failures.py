@@ -93,7 +93,7 @@ def test_put_radius_checked_only_for_radical_containers(gpu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [500, 6000])   # the small-member and the multi-kernel binning
+@pytest.mark.parametrize("n", [500, 6000, 20000])   # both shared-memory binning tiers, the multi-kernel binning
 def test_put_device_nonfinite_refused_by_compute(gpu, n):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(9)
@@ -107,7 +107,7 @@ def test_put_device_nonfinite_refused_by_compute(gpu, n):
     with pytest.raises(vg.VoroError) as e:
         con.compute_all_cells()
     assert e.value.code == vg.VGPU_ERR_ARG
-    # in a batch, too (members of at most 4096 particles are binned together)
+    # in a batch, too (members of at most 16384 particles are binned together)
     con2 = vg.container_periodic(10, 0, 10, 0, 0, 10, 5, 5, 5, 8)
     con2.put_device(n, d_ids.data_ptr(), d_xyzr.data_ptr(), keepalive=(d_ids, d_xyzr))
     b = vg.batch([con2])

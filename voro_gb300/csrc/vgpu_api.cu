@@ -2017,13 +2017,22 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     }
     std::vector<CellParams> cps(nc);
     std::vector<long long> starts(nc + 1, 0);
-    // members of at most kSmallBinMax particles: binned together, one CTA each
+    // members of at most kSmallBinMax particles: binned together, one CTA
+    // each, in two launches by size (the jobs of at most kSmallBinTier
+    // particles first)
     std::vector<int> small;
-    for (int i = 0; i < nc; i++) {
-        const vgpu_container *h = b->members[i];
-        const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
-        // (a sheared box stores images of its particles: the multi-kernel binning)
-        if (n <= kSmallBinMax && !h->g.tric) small.push_back(i);
+    std::vector<char> is_small(nc, 0);
+    int ns_tier = 0;
+    for (int pass = 0; pass < 2; pass++) {
+        for (int i = 0; i < nc; i++) {
+            const vgpu_container *h = b->members[i];
+            const int64_t n = h->use_device_input ? h->dev_n_ext : h->staged;
+            // (a sheared box stores images of its particles: the multi-kernel binning)
+            if (h->g.tric || n > kSmallBinMax || (n <= kSmallBinTier) != (pass == 0)) continue;
+            small.push_back(i);
+            is_small[i] = 1;
+        }
+        if (pass == 0) ns_tier = (int)small.size();
     }
     const int ns = (int)small.size();
     if (ns > 0) {
@@ -2036,15 +2045,13 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         }
         VG_CUDA(cudaMemcpyAsync(b->jobs.p, jobs.data(), (size_t)ns * sizeof(SmallBinJob), cudaMemcpyHostToDevice, s));
         for (int j = 0; j < ns; j++) cudaEventRecord(b->members[small[j]]->ev[0], s);
-        VG_CUDA(launch_small_bin(b->jobs.as<SmallBinJob>(), ns, s));
+        VG_CUDA(launch_small_bin(b->jobs.as<SmallBinJob>(), ns_tier, kSmallBinTier, s));
+        VG_CUDA(launch_small_bin(b->jobs.as<SmallBinJob>() + ns_tier, ns - ns_tier, kSmallBinMax, s));
         for (int j = 0; j < ns; j++) cudaEventRecord(b->members[small[j]]->ev[1], s);
     }
     // the others on their own streams; the batch stream waits for each gather
-    for (int i = 0, j = 0; i < nc; i++) {
-        if (j < ns && small[j] == i) {
-            j++;
-            continue;
-        }
+    for (int i = 0; i < nc; i++) {
+        if (is_small[i]) continue;
         vgpu_container *h = b->members[i];
         int rc = prepare_cells(h, mode, cps[i]);
         if (rc != VGPU_OK) return rc;

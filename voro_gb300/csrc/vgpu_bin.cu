@@ -270,7 +270,7 @@ __device__ __forceinline__ void cta_bitonic(unsigned long long *key, int n2) {
     }
 }
 
-__global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const SmallBinJob *jobs) {
+__global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const SmallBinJob *jobs, int cap) {
     extern __shared__ unsigned long long sbin[];
     __shared__ int s_kept, s_dup, s_bad;
     __shared__ unsigned long long s_rmax;
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kSmallBinThreads) small_bin_kernel(const Small
     int n2 = 1;
     while (n2 < n) n2 <<= 1;
     unsigned long long *key = sbin;                                  // n2 keys
-    unsigned *gk_in = reinterpret_cast<unsigned *>(sbin + kSmallBinMax);   // engine key per input index
+    unsigned *gk_in = reinterpret_cast<unsigned *>(sbin + cap);   // engine key per input index
     if (threadIdx.x == 0) {
         s_kept = 0;
         s_dup = 0;
@@ -501,12 +501,13 @@ cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, int *fla
     return cudaGetLastError();
 }
 
-cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, cudaStream_t s) {
+cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, int cap, cudaStream_t s) {
     if (njobs <= 0) return cudaSuccess;
-    const size_t smem = kSmallBinMax * 8 + kSmallBinMax * 4;
+    if (cap <= 0 || cap > kSmallBinMax || (cap & (cap - 1)) != 0) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)cap * 8 + (size_t)cap * 4;
     cudaError_t e = cudaFuncSetAttribute(small_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    small_bin_kernel<<<njobs, kSmallBinThreads, smem, s>>>(jobs);
+    small_bin_kernel<<<njobs, kSmallBinThreads, smem, s>>>(jobs, cap);
     note_launch();
     return cudaGetLastError();
 }

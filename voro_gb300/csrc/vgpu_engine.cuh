@@ -811,28 +811,6 @@ struct Engine {
             k0 = bitonic32(k0, lane);
         }
         PHASE_END(t_sort, 2);
-#if VGPU_FLUSH_PREFETCH
-        // the next candidate's key and distance are read while this one is
-        // tested and cut (they do not change during the flush)
-        unsigned key = __shfl_sync(kFull, k0, 0);
-        float2 Ezw = *reinterpret_cast<const float2 *>(&S.u.c.ce[key & 63u].z);
-        for (int i = 0; i < n; i++) {
-            const int cb = key & 63u;
-            const float2 E = Ezw;
-            if (i + 1 < n) {
-                key = __shfl_sync(kFull, i + 1 < 32 ? k0 : k1, (i + 1) & 31);
-                Ezw = *reinterpret_cast<const float2 *>(&S.u.c.ce[key & 63u].z);
-            }
-            if (P.g.poly) {
-                const float rs = E.y;
-                if (!(rs <= 0.0f || rs * rs < 4.0f * C.R2 * E.x * E.x * (1.0f + 16.0f * kU32))) continue;
-            } else {
-                if (E.y >= C.cutoff2 * (1.0f + 1e-4f)) break;
-            }
-            test_and_cut(cb);
-            if (C.deleted || C.overflow) break;
-        }
-#else
         for (int i = 0; i < n; i++) {
             const unsigned key = __shfl_sync(kFull, i < 32 ? k0 : k1, i & 31);
             const int cb = key & 63u;
@@ -846,7 +824,6 @@ struct Engine {
             test_and_cut(cb);
             if (C.deleted || C.overflow) break;
         }
-#endif
         C.ncand = 0;
         __syncwarp();
     }

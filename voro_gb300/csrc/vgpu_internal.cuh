@@ -29,9 +29,6 @@ constexpr int kCandBuf = 64;
 #ifndef VGPU_GATHER_TMA
 #define VGPU_GATHER_TMA 0
 #endif
-#ifndef VGPU_FLUSH_PREFETCH
-#define VGPU_FLUSH_PREFETCH 0
-#endif
 constexpr int kStageEntries = 64;   // staged candidate particles per warp (VGPU_GATHER_TMA)       // candidate buffer entries per warp
 // Neighbour IDs: kNbStride slots per cell in a fixed-stride array; a cell with
 // more faces keeps kNbStride-1 there and the rest in an overflow store, whose
@@ -244,8 +241,12 @@ cudaError_t launch_image_write(const Geometry &g, int n, const double4 *rem, con
 // slot: nengine ints of scratch each; scan_tmp: scratch of exclusive_scan_int).
 cudaError_t launch_cell_list(const int *outpos, int nengine, int *list, int *flag, int *slot, int *scan_tmp,
                              size_t scan_tmp_ints_avail, cudaStream_t s);
-// One small container's binning in one CTA (batches): at most kSmallBinMax particles.
-constexpr int kSmallBinMax = 4096;
+// One small container's binning in one CTA (batches): at most kSmallBinMax
+// particles, sorted in shared memory (12 bytes per particle, rounded up to a
+// power of two).  Members of at most kSmallBinTier particles go in a launch
+// of 48 KB CTAs, the larger ones in a launch of 192 KB CTAs.
+constexpr int kSmallBinMax = 16384;
+constexpr int kSmallBinTier = 4096;
 constexpr int kSmallBinThreads = 512;
 struct SmallBinJob {
     Geometry g;
@@ -261,7 +262,8 @@ struct SmallBinJob {
     double *res_pos, *res_rad;
     unsigned long long *result;   // [0] kept | duplicate << 32, [1] largest radius (bits)
 };
-cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, cudaStream_t s);
+// jobs of at most cap particles each (cap a power of two, <= kSmallBinMax)
+cudaError_t launch_small_bin(const SmallBinJob *jobs, int njobs, int cap, cudaStream_t s);
 cudaError_t launch_ghost_setup(const Geometry &g, int n, const double4 *q, int base, double4 *p64, float4 *lffh,
                                float4 *lffl, int *pid, int *outpos, int *gblock, int *keep, cudaStream_t s);
 cudaError_t launch_duplicate_check(const unsigned *ukey_sorted, const int *uorder, const double4 *rem,

@@ -128,6 +128,36 @@ def test_batch_reports_duplicates_in_a_small_member(gpu):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("with_small", [False, True])
+def test_batch_reports_duplicates_in_a_large_member(gpu, with_small):
+    """A member binned by the multi-kernel path (more than 16384 particles),
+    whose duplicate check is read back only once the batch has waited for
+    every member's binning: the batch still fails with VGPU_ERR_DUPLICATE."""
+    rng = np.random.default_rng(5)
+    n = 20000
+    c = vg.container_periodic(30, 0, 30, 0, 0, 30, 16, 16, 16, mode="mixed")
+    xyz = rng.uniform(0, 30, size=(n, 3))
+    xyz[12345] = xyz[678]
+    c.put_array(np.arange(n, dtype=np.int32), xyz)
+    cons = [c]
+    if with_small:
+        s = vg.container_periodic(10, 0, 10, 0, 0, 10, 4, 4, 4, mode="mixed")
+        s.put_array(np.arange(300, dtype=np.int32), rng.uniform(0, 10, size=(300, 3)))
+        cons.append(s)
+    b = vg.batch(cons)
+    with pytest.raises(vg.VoroError) as e:
+        b.compute_all_cells(mode="mixed")
+    assert e.value.code == vg.VGPU_ERR_DUPLICATE
+    # the same member without the duplicate computes
+    xyz[12345] = rng.uniform(0, 30, size=3)
+    c2 = vg.container_periodic(30, 0, 30, 0, 0, 30, 16, 16, 16, mode="mixed")
+    c2.put_array(np.arange(n, dtype=np.int32), xyz)
+    b2 = vg.batch([c2] + cons[1:])
+    b2.compute_all_cells(mode="mixed")
+    assert abs(c2.sum_cell_volumes() - 27000.0) < 1e-8 * 27000.0
+
+
+@pytest.mark.gpu
 def test_batch_in_record_waves_matches_one_wave(gpu):
     """A record budget far below the batch's records runs it in waves of
     cells (each clipped and finished before the next): the same results."""

@@ -32,6 +32,7 @@ VGPU_OUTPUT_POLYTOPES = 1
 VGPU_CELL_FAILED = 8   # bits 8-11: reason (1 planes, 2 adjacency, 3 vertices, 4 search, 5 records)
 VGPU_FAIL_RECORDS = 5
 VGPU_ERR_ARG = 16
+VGPU_ERR_DUPLICATE = 19
 VGPU_ERR_CAPACITY = 21
 
 KIND_CONTAINER = 0

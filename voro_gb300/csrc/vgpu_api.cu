@@ -176,6 +176,10 @@ struct vgpu_container {
     bool use_device_input = false;
     DevBuf ids_in, xyzr_in;
     DevBuf chk;   // put(): index of the first non-finite particle
+    // pinned host words the binning reads back asynchronously: [0] kept and
+    // non-finite counts, [1] largest radius (bits), [2] duplicate flag
+    unsigned long long *host_rb = nullptr;
+    bool dup_pending = false;   // the duplicate flag of a deferred check is in host_rb[2]
     // work buffers
     DevBuf rem, ukey, gkey, idx, idx2, keys_alt, vals_alt, hist, scan_tmp, outpos_in, kept;
     DevBuf p64, lffh, lffl, pid, outpos, gblock, bstart, offsets, ovf_list, ovf_list2, counters, counters2;
@@ -532,6 +536,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->walls_dev,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
+    if (h->host_rb) cudaFreeHost(h->host_rb);
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -754,7 +759,13 @@ int upload_walls(vgpu_container *h) {
 // thin: a sheared periodic box may store its images only ghost_spacings mean
 // particle spacings deep (a compute checks afterwards that every cell's reach
 // stayed inside; see reach_check_kernel); else at the reference's depth.
-int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false) {
+// Binning runs in two parts around its one wait for the device: bin_begin
+// enqueues the remap and the read-back of its counts (into pinned memory),
+// bin_finish (once the container's stream has reached them) the sorts, the
+// gather and the engine's parameters.  A batch begins every large member
+// before it finishes any, so that their remaps run together instead of one
+// host round trip after another.
+int bin_begin(vgpu_container *h, int mode, bool thin) {
     if (mode != VGPU_FP64 && mode != VGPU_MIXED) return fail(VGPU_ERR_ARG, "bad mode %d", mode);
     if (int rc = upload_walls(h)) return rc;
     cudaStream_t s = h->stream;
@@ -779,7 +790,6 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
     }
     choose_engine_grid(g, n64, h->target_density);
     const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
-    const int nub = g.un[0] * g.un[1] * g.un[2];
     const size_t nn = (size_t)std::max(n, 1);
     // inputs
     const int32_t *d_ids;
@@ -828,20 +838,40 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
     int *d_kept = h->kept.as<int>();
     unsigned long long *d_rmax = reinterpret_cast<unsigned long long *>(h->kept.as<char>() + 16);
     VG_CUDA(launch_remap(bp, d_kept, d_rmax, s));
-    int kept2[2] = {0, 0};   // kept particles, particles with a non-finite position or radius
-    unsigned long long rmax_bits = 0;
-    VG_CUDA(cudaMemcpyAsync(kept2, d_kept, 8, cudaMemcpyDeviceToHost, s));
-    VG_CUDA(cudaMemcpyAsync(&rmax_bits, d_rmax, 8, cudaMemcpyDeviceToHost, s));
+    if (!h->host_rb) VG_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&h->host_rb), 64, cudaHostAllocDefault));
+    // kept particles and particles with a non-finite position or radius
+    // (two ints), then the largest radius
+    VG_CUDA(cudaMemcpyAsync(h->host_rb, d_kept, 8, cudaMemcpyDeviceToHost, s));
+    VG_CUDA(cudaMemcpyAsync(h->host_rb + 1, d_rmax, 8, cudaMemcpyDeviceToHost, s));
     // identity copy for the second sort
     if (n > 0) VG_CUDA(cudaMemcpyAsync(h->idx2.p, h->idx.p, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-    VG_CUDA(cudaStreamSynchronize(s));
+    return VGPU_OK;
+}
+
+// The rest of the binning, after bin_begin's read-back has landed (the
+// caller synchronised the container's stream).  defer_dup: the duplicate
+// check's flag is read back without waiting (dup_pending; the caller checks
+// it after its next synchronisation) instead of being waited for here.
+int bin_finish(vgpu_container *h, int mode, CellParams &cp, bool defer_dup) {
+    (void)mode;
+    cudaStream_t s = h->stream;
+    const int64_t n64 = h->use_device_input ? h->dev_n_ext : h->staged;
+    const int n = (int)n64;
+    Geometry &g = h->g;
+    const int nblocks = g.gn[0] * g.gn[1] * g.gn[2];
+    const int nub = g.un[0] * g.un[1] * g.un[2];
+    const size_t nn = (size_t)std::max(n, 1);
+    const int32_t *d_ids = h->use_device_input ? h->dev_ids_ext : h->ids_in.as<int32_t>();
+    int kept2[2];
+    memcpy(kept2, h->host_rb, 8);
     if (kept2[1] > 0)
         return fail(VGPU_ERR_ARG, "%d particles have a non-finite position or radius", kept2[1]);
     const int nkept = kept2[0];
     double rmax = 0.0;
-    memcpy(&rmax, &rmax_bits, 8);
+    memcpy(&rmax, h->host_rb + 1, 8);
     g.rmax = rmax;
     g.rmax32 = (float)rmax * (1.0f + 1e-6f);
+    h->dup_pending = false;
 
     int ubits = 1, gbits = 1;
     while ((1u << ubits) <= (unsigned)nub) ubits++;
@@ -902,10 +932,14 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
         int *dflag = h->kept.as<int>() + 8;
         VG_CUDA(cudaMemsetAsync(dflag, 0, 4, s));
         VG_CUDA(launch_duplicate_check(ukey_sorted, uorder, h->rem.as<double4>(), nkept, dflag, s));
-        int dup = 0;
-        VG_CUDA(cudaMemcpyAsync(&dup, dflag, 4, cudaMemcpyDeviceToHost, s));
-        VG_CUDA(cudaStreamSynchronize(s));
-        if (dup) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
+        h->host_rb[2] = 0;
+        VG_CUDA(cudaMemcpyAsync(h->host_rb + 2, dflag, 4, cudaMemcpyDeviceToHost, s));
+        if (defer_dup) {
+            h->dup_pending = true;
+        } else {
+            VG_CUDA(cudaStreamSynchronize(s));
+            if (h->host_rb[2]) return fail(VGPU_ERR_DUPLICATE, "duplicate particle positions (|d|^2 < 1e-10) in one block");
+        }
     }
 
     // engine order: the u-sort consumed idx, so sort (gkey, idx2)
@@ -975,6 +1009,13 @@ int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false
     h->binned = true;
     fill_cell_params(h, cp);
     return VGPU_OK;
+}
+
+int prepare_cells(vgpu_container *h, int mode, CellParams &cp, bool thin = false) {
+    int rc = bin_begin(h, mode, thin);
+    if (rc != VGPU_OK) return rc;
+    VG_CUDA(cudaStreamSynchronize(h->stream));
+    return bin_finish(h, mode, cp, false);
 }
 
 // The cell engine's parameters for the binned container h (h->nkept set).
@@ -2049,18 +2090,29 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         VG_CUDA(launch_small_bin(b->jobs.as<SmallBinJob>() + ns_tier, ns - ns_tier, kSmallBinMax, s));
         for (int j = 0; j < ns; j++) cudaEventRecord(b->members[small[j]]->ev[1], s);
     }
-    // the others on their own streams; the batch stream waits for each gather
+    // the others on their own streams: every remap first, then the rest of
+    // each member's binning as its remap's counts land; the batch stream
+    // waits for each gather
+    for (int i = 0; i < nc; i++) {
+        if (is_small[i]) continue;
+        int rc = bin_begin(b->members[i], mode, false);
+        if (rc != VGPU_OK) return rc;
+    }
+    bool dup_check = false;
     for (int i = 0; i < nc; i++) {
         if (is_small[i]) continue;
         vgpu_container *h = b->members[i];
-        int rc = prepare_cells(h, mode, cps[i]);
+        VG_CUDA(cudaStreamSynchronize(h->stream));
+        int rc = bin_finish(h, mode, cps[i], true);
         if (rc != VGPU_OK) return rc;
+        dup_check = dup_check || h->dup_pending;
         cps[i].cnt = b->counters.as<Counters>() + i;
         rc = setup_member_records(h, cps[i], cps[i].cnt, h->stream);
         if (rc != VGPU_OK) return rc;
         cudaEventRecord(h->ev[2], h->stream);   // after the gather and the record resets
         VG_CUDA(cudaStreamWaitEvent(s, h->ev[2], 0));
     }
+    if (dup_check && ns == 0) VG_CUDA(cudaStreamSynchronize(s));
     if (ns > 0) {
         std::vector<unsigned long long> res((size_t)ns * 2);
         VG_CUDA(cudaMemcpyAsync(res.data(), b->bin_res.p, (size_t)ns * 16, cudaMemcpyDeviceToHost, s));
@@ -2075,6 +2127,15 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
             rc = setup_member_records(h, cps[i], cps[i].cnt, s);
             if (rc != VGPU_OK) return rc;
         }
+    }
+    // the large members' deferred duplicate checks (the batch stream has
+    // passed every member's gather, which follows its check)
+    for (int i = 0; dup_check && i < nc; i++) {
+        vgpu_container *h = b->members[i];
+        if (!h->dup_pending) continue;
+        h->dup_pending = false;
+        if (h->host_rb[2])
+            return fail(VGPU_ERR_DUPLICATE, "member %d: duplicate particle positions (|d|^2 < 1e-10) in one block", i);
     }
     for (int i = 0; i < nc; i++) {
         if (!b->members[i]->g.tric) cps[i].cell_list = nullptr;   // (sheared: the particles among the images)

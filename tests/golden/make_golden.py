@@ -80,6 +80,54 @@ def degenerate_cases():
     return out
 
 
+# Edge cases of placement and of tiny inputs (edge_*.npz): coordinates
+# exactly on the box's faces and on block boundaries (put_remap's step_int
+# and its range checks, src/container.cc:174-191: a point at the upper face
+# of a non-periodic box is dropped), their neighbouring doubles, signed
+# zero, points many periods away (the remaps of src/container.cc:178-186
+# and src/container_prd.cc:189-216), and containers of one and two
+# particles (a periodic box's lone particle is its own neighbour).
+def edge_cases():
+    out = {}
+    rng = np.random.default_rng(2301)
+    special = [0.0, -0.0, 0.25, 0.5, 0.75, 1.0, np.nextafter(1.0, 0.0), np.nextafter(0.25, 0.0),
+               np.nextafter(0.25, 1.0), np.nextafter(0.75, 1.0), 1e-300, 0.5 + 2.0 ** -40]
+    rows = []
+    for v in special:
+        for a in range(3):
+            q = rng.uniform(0.05, 0.95, size=3)
+            q[a] = v
+            rows.append(q)
+    xyz = np.concatenate([rng.random((260, 3)), np.array(rows)])
+    out["edge_box_boundaries_296"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (4, 4, 4), (False,) * 3, xyz)
+    r = rng.uniform(0.02, 0.08, size=len(xyz))
+    out["edge_poly_boundaries_296"] = W._pack(W.KIND_CONTAINER_POLY, (0, 1, 0, 1, 0, 1), (4, 4, 4), (False,) * 3,
+                                              xyz, r=r)
+    # periodic: exact faces, one period and many periods away
+    L = 2.0
+    wrap = [0.0, L, -L, 2 * L + 0.3, -1000 * L + 0.7, np.nextafter(L, 0.0), np.nextafter(L, 4.0), -0.0, 1e-300,
+            1e6 * L + 0.123, 0.5 * L, -0.5 * L]
+    rows = []
+    for v in wrap:
+        for a in range(3):
+            q = rng.uniform(0.1, 1.9, size=3)
+            q[a] = v
+            rows.append(q)
+    xyz = np.concatenate([rng.uniform(0, L, size=(264, 3)), np.array(rows)])
+    out["edge_periodic_wraps_300"] = W._pack(W.KIND_PERIODIC, (L, 0, L, 0, 0, L), (4, 4, 4), (True,) * 3, xyz)
+    out["edge_flagperiodic_wraps_300"] = W._pack(W.KIND_CONTAINER, (0, L, 0, L, 0, L), (4, 4, 4), (True,) * 3, xyz)
+    # one and two particles
+    out["edge_single_1"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (1, 1, 1), (False,) * 3,
+                                   np.array([[0.3, 0.6, 0.2]]))
+    out["edge_pair_2"] = W._pack(W.KIND_CONTAINER, (0, 2, 0, 1, 0, 1), (2, 1, 1), (False,) * 3,
+                                 np.array([[0.4, 0.5, 0.5], [1.7, 0.2, 0.9]]))
+    out["edge_single_periodic_1"] = W._pack(W.KIND_PERIODIC, (3, 0, 3, 0, 0, 3), (2, 2, 2), (True,) * 3,
+                                            np.array([[1.1, 2.2, 0.4]]))
+    out["edge_pair_periodic_2"] = W._pack(W.KIND_PERIODIC, (3, 0, 3, 0, 0, 3), (2, 2, 2), (True,) * 3,
+                                          np.array([[1.1, 2.2, 0.4], [2.5, 0.9, 1.6]]))
+    return out
+
+
 # Sheared periodic boxes (tric_*.npz: the same per-cell records, plus
 # locate_tric_* and ghost_tric_*): container_periodic(_poly) with bxy, bxz,
 # byz != 0.  Positions are drawn over a larger range than the box, so put()
@@ -359,6 +407,10 @@ def main():
             make_cell_fixture(ref, name, w)
         make_poly_fixtures(ref, dc, names=list(dc))
         return
+    if "--edge-only" in sys.argv:
+        for name, w in edge_cases().items():
+            make_cell_fixture(ref, name, w)
+        return
     if "--tric-large-only" in sys.argv:
         make_tric_large_fixture(ref)
         return
@@ -370,6 +422,8 @@ def main():
     make_wall_fixtures(ref)
     make_tric_fixtures(ref)
     make_tric_large_fixture(ref)
+    for name, w in edge_cases().items():
+        make_cell_fixture(ref, name, w)
     make_cli_fixtures()
 
 

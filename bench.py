@@ -470,22 +470,32 @@ def run_ours(args):
         pinned = lambda shape, dt: torch.empty(tuple(shape), dtype=getattr(torch, np.dtype(dt).name),
                                                pin_memory=True).numpy()
         res = None
+        parts = {"put_ms": [], "compute_ms": [], "device_ms": [], "read_ms": []}
         for it in range(args.warmup + args.steps):
             barrier()
             t0 = time.perf_counter()
             con2.clear()
             con2.put_xyzr(ids_pin, xyzr_pin)
+            tp = time.perf_counter()
             con2.compute_all_cells()
+            tc = time.perf_counter()
             res = con2.cells(neighbors=True, out=res, alloc=pinned)
             torch.cuda.synchronize()
             t1 = time.perf_counter()
             if it >= args.warmup:
                 times.append(t1 - t0)
+                # where the wall clock went (the compute returns once its
+                # results are on the device; device_ms: its CUDA-event time)
+                parts["put_ms"].append(1000.0 * (tp - t0))
+                parts["compute_ms"].append(1000.0 * (tc - tp))
+                parts["device_ms"].append(con2.stats()["step_ms"])
+                parts["read_ms"].append(1000.0 * (t1 - tc))
             d2h = (res.vol.nbytes + res.nf.nbytes + res.nb.nbytes + res.nb_off.nbytes + res.ids.nbytes +
                    res.pos.nbytes + res.cen.nbytes + res.nv.nbytes + res.maxr2.nbytes + res.flags.nbytes)
         e2e_s = max_over_ranks(statistics.mean(times), ws, dev)
         e2e = {"value": job_throughput(n, ws, 1000.0 * e2e_s), "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s,
+               "split_ms": {k: statistics.mean(v) for k, v in parts.items()}}
 
     if rank != 0:
         if ws > 1:

@@ -55,50 +55,58 @@ namespace {
 #endif
 
 // ------------------------------------------------------------------ masks
-// Slot s of lane l is bit l+32s.
+// Slot l+32s (lane l, slot row s) is bit l of row word r[s]: one 32-bit word
+// per row, as a ballot returns it, so that a lane's test of its own slot is
+// one shift of a known word (a 64-bit word per two rows cost a wide shift).
 template <int K>
 struct Mask {
-    static constexpr int W = (K + 1) / 2;
-    unsigned long long w[W];
+    unsigned r[K];
     __device__ __forceinline__ void clear() {
 #pragma unroll
-        for (int i = 0; i < W; i++) w[i] = 0ull;
+        for (int i = 0; i < K; i++) r[i] = 0u;
     }
-    __device__ __forceinline__ bool test(int t) const { return (w[t >> 6] >> (t & 63)) & 1ull; }
+    __device__ __forceinline__ unsigned row(int t) const {
+        unsigned w = r[0];
+#pragma unroll
+        for (int i = 1; i < K; i++)
+            if ((t >> 5) == i) w = r[i];
+        return w;
+    }
+    __device__ __forceinline__ bool test(int t) const { return (row(t) >> (t & 31)) & 1u; }
     __device__ __forceinline__ int popc() const {
         int c = 0;
 #pragma unroll
-        for (int i = 0; i < W; i++) c += __popcll(w[i]);
+        for (int i = 0; i < K; i++) c += __popc(r[i]);
         return c;
     }
     __device__ __forceinline__ bool any() const {
-        unsigned long long o = 0;
+        unsigned o = 0u;
 #pragma unroll
-        for (int i = 0; i < W; i++) o |= w[i];
-        return o != 0ull;
+        for (int i = 0; i < K; i++) o |= r[i];
+        return o != 0u;
     }
     __device__ __forceinline__ bool equals(const Mask &o) const {
         bool e = true;
 #pragma unroll
-        for (int i = 0; i < W; i++) e = e && (w[i] == o.w[i]);
+        for (int i = 0; i < K; i++) e = e && (r[i] == o.r[i]);
         return e;
     }
     // number of set bits below bit t
     __device__ __forceinline__ int rank(int t) const {
         int c = 0;
-        const int wi = t >> 6;
+        const int wi = t >> 5;
 #pragma unroll
-        for (int i = 0; i < W; i++) {
-            if (i < wi) c += __popcll(w[i]);
-            else if (i == wi) c += __popcll(w[i] & ((1ull << (t & 63)) - 1ull));
+        for (int i = 0; i < K; i++) {
+            if (i < wi) c += __popc(r[i]);
+            else if (i == wi) c += __popc(r[i] & ((1u << (t & 31)) - 1u));
         }
         return c;
     }
     // lowest set bit, or -1
     __device__ __forceinline__ int first() const {
 #pragma unroll
-        for (int i = 0; i < W; i++)
-            if (w[i]) return i * 64 + __ffsll((long long)w[i]) - 1;
+        for (int i = 0; i < K; i++)
+            if (r[i]) return i * 32 + __ffs((int)r[i]) - 1;
         return -1;
     }
 };
@@ -106,12 +114,8 @@ struct Mask {
 template <int K>
 __device__ __forceinline__ Mask<K> ballot_mask(const bool (&pred)[K]) {
     Mask<K> m;
-    m.clear();
 #pragma unroll
-    for (int s = 0; s < K; s++) {
-        unsigned b = __ballot_sync(kFull, pred[s]);
-        m.w[s >> 1] |= (unsigned long long)b << (32 * (s & 1));
-    }
+    for (int s = 0; s < K; s++) m.r[s] = __ballot_sync(kFull, pred[s]);
     return m;
 }
 
@@ -467,7 +471,7 @@ struct Engine {
             S.pshift[lane] = lane;
         }
         Vm.clear();
-        Vm.w[0] = 0xffull;
+        Vm.r[0] = 0xffu;
 #pragma unroll
         for (int s = 0; s < K; s++) clear_slot(s);
         if (lane < 8) {
@@ -695,7 +699,7 @@ struct Engine {
         PHASE_COUNT(5, total);
         Mask<K> Fm;
 #pragma unroll
-        for (int i = 0; i < Mask<K>::W; i++) Fm.w[i] = ~Vm.w[i] | Rm.w[i];
+        for (int i = 0; i < K; i++) Fm.r[i] = ~Vm.r[i] | Rm.r[i];
         if (Fm.popc() < total) {
             C.overflow = true;
             C.fail_reason = VGPU_FAIL_VERTICES;
@@ -726,7 +730,7 @@ struct Engine {
         // solves run in one pass; across all free slots only when no row has room.
         unsigned fw[K];   // free lanes of each slot row
 #pragma unroll
-        for (int s = 0; s < K; s++) fw[s] = (unsigned)(Fm.w[s >> 1] >> (32 * (s & 1)));
+        for (int s = 0; s < K; s++) fw[s] = Fm.r[s];
         int hs = -1;
 #pragma unroll
         for (int s = K - 1; s >= 0; s--)
@@ -788,7 +792,7 @@ struct Engine {
         if (__any_sync(kFull, bad)) C.marginal = true;
         const Mask<K> Nm = ballot_mask<K>(host);
 #pragma unroll
-        for (int i = 0; i < Mask<K>::W; i++) Vm.w[i] = (Vm.w[i] & ~Rm.w[i]) | Nm.w[i];
+        for (int i = 0; i < K; i++) Vm.r[i] = (Vm.r[i] & ~Rm.r[i]) | Nm.r[i];
         __syncwarp();
         update_radius();
     }

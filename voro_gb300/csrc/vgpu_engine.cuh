@@ -183,7 +183,7 @@ struct CellCtx {
     bool deleted, overflow, marginal, repaired;
     bool needs_fp64;  // this lane's vertex solve was ill-conditioned (first pass: the cell is rerun)
     int fail_reason;  // why overflow was set (VGPU_FAIL_*)
-    unsigned long long freeplanes;
+    unsigned freeplanes[2];   // plane slots not in use: slots 0-31, 32-63
     int ncand;
     unsigned tests, repairs, ptested, pcut;
 #ifdef VGPU_PHASE_TIMING
@@ -457,7 +457,8 @@ struct Engine {
         C.ri2 = C.me32.w * C.me32.w;
         C.deleted = C.overflow = C.marginal = C.repaired = C.needs_fp64 = false;
         C.fail_reason = 0;
-        C.freeplanes = ~0x3full;
+        C.freeplanes[0] = ~0x3fu;
+        C.freeplanes[1] = ~0u;
         C.ncand = 0;
         C.tests = C.repairs = C.ptested = C.pcut = 0;
         if (lane < 6) {
@@ -538,8 +539,10 @@ struct Engine {
     }
 
     // ---- plane slot allocation with recycling of dead planes
+    //      (32-bit halves: the lowest free slot and its removal are single
+    //      32-bit operations)
     __device__ __forceinline__ int alloc_plane() {
-        if (C.freeplanes == 0ull) {
+        if ((C.freeplanes[0] | C.freeplanes[1]) == 0u) {
             unsigned long long live = 0ull;
 #pragma unroll
             for (int s = 0; s < K; s++)
@@ -547,11 +550,18 @@ struct Engine {
                     const unsigned t = V.tri[s];
                     live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
                 }
-            C.freeplanes = ~warp_or64(live);
-            if (C.freeplanes == 0ull) return -1;
+            const unsigned long long fr = ~warp_or64(live);
+            C.freeplanes[0] = (unsigned)fr;
+            C.freeplanes[1] = (unsigned)(fr >> 32);
+            if (fr == 0ull) return -1;
         }
-        const int p = __ffsll((long long)C.freeplanes) - 1;
-        C.freeplanes &= ~(1ull << p);
+        if (C.freeplanes[0]) {
+            const int p = __ffs((int)C.freeplanes[0]) - 1;
+            C.freeplanes[0] &= C.freeplanes[0] - 1u;
+            return p;
+        }
+        const int p = 32 + __ffs((int)C.freeplanes[1]) - 1;
+        C.freeplanes[1] &= C.freeplanes[1] - 1u;
         return p;
     }
 

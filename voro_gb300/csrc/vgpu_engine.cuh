@@ -617,6 +617,10 @@ struct Engine {
             const float Cq = fmaf(3.0f * kU32, fabsf(Q.w), E.y) + P.g.tol_h32;
 #pragma unroll
             for (int s = 0; s < K; s++) {
+                out[s] = false;
+                // a slot row with no vertex is skipped (the branch is the
+                // warp's: Vm is the same in every lane); row 0 always holds some
+                if (s > 0 && Vm.r[s] == 0u) continue;
                 const float v = fmaf(Q.x, V.x[s], fmaf(Q.y, V.y[s], fmaf(Q.z, V.z[s], -Q.w)));
                 const float bnd = 1.5f * fmaf(A, V.a[s], fmaf(E.z, V.e[s], Cq));
                 out[s] = v > bnd;
@@ -726,9 +730,11 @@ struct Engine {
 #pragma unroll
                     for (int e = 0; e < 3; e++)
                         if ((bnd[s] >> e) & 1u) {
-                            const int a = tri_plane(T, e), b = tri_plane(T, e == 2 ? 0 : e + 1);
-                            const unsigned u = (A3 >> (8 * e)) & 255u;
-                            S.stage[q++] = (unsigned)a | ((unsigned)b << 8) | (u << 16);
+                            // bytes e and e+1 (mod 3) of T, byte e of A3, and T's
+                            // zero top byte, in one byte permutation; the planes
+                            // masked to their 6 bits as tri_plane does
+                            constexpr unsigned kSel[3] = {0x3410u, 0x3521u, 0x3602u};
+                            S.stage[q++] = __byte_perm(T, A3, kSel[e]) & 0x00ff3f3fu;
                         }
                 }
             }
@@ -759,8 +765,8 @@ struct Engine {
                 if (r < total) {
                     host[s] = true;
                     const unsigned E = S.stage[r];
-                    const int a = E & 255u, b = (E >> 8) & 255u, u = (E >> 16) & 255u;
-                    const unsigned T = (unsigned)a | ((unsigned)b << 8) | ((unsigned)p << 16);
+                    const int a = E & 255u, b = (E >> 8) & 255u, u = E >> 16;   // (E's top byte is 0)
+                    const unsigned T = __byte_perm(E, (unsigned)p, 0x5410u);   // a | b << 8 | p << 16
                     V.tri[s] = T;
                     S.tri[t] = T;
                     S.adj[t] = (unsigned)u;

@@ -1195,12 +1195,15 @@ struct Engine {
 
 // CTAs of 4 warps kept resident per SM by the main (mixed, 64-slot, FP64-free)
 // engine; it fixes the register budget (65536 / (128 * blocks)).  Measured on
-// the 4M periodic box (both clipping passes): 6 (80 registers, 24 warps per
-// SM) 82.2 ms, 5 (96) 83.5 ms, 7 (72) 84.2 ms, 4 (103, no spills) 88.9 ms,
-// 3 (118) 86.8 ms.  (With the FP64 repair and vertex calls in this engine it
-// needed 224 registers: 3 CTAs at 168 registers, 102 ms.)
+// the 4M periodic box (both clipping passes): with the slot masks as 64-bit
+// words 6 (80 registers, 24 warps per SM) 82.2 ms, 5 (96) 83.5 ms, 7 (72)
+// 84.2 ms, 4 (103, no spills) 88.9 ms, 3 (118) 86.8 ms; with one 32-bit word
+// per slot row (no spills at 80 registers) 6: 66.49 ms, 7: 66.34 ms (72
+// registers, 44 bytes spilled); shared memory allows no more than 7.  (With
+// the FP64 repair and vertex calls in this engine it needed 224 registers:
+// 3 CTAs at 168 registers, 102 ms.)
 #ifndef VGPU_MIN_BLOCKS
-#define VGPU_MIN_BLOCKS 6
+#define VGPU_MIN_BLOCKS 7
 #endif
 // Largest CTA the clipping kernels are built for (VGPU_CTA_THREADS, in
 // vgpu_internal.cuh); the default launch uses 4 warps.

@@ -175,7 +175,6 @@ struct vgpu_container {
     int64_t dev_n_ext = 0;
     bool use_device_input = false;
     DevBuf ids_in, xyzr_in;
-    DevBuf seg_work;   // per-SM work queues of the clipping kernels
     DevBuf chk;   // put(): index of the first non-finite particle
     // pinned host words the binning reads back asynchronously: [0] kept and
     // non-finite counts, [1] largest radius (bits), [2] duplicate flag
@@ -535,8 +534,7 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->gh_ovf, &h->gh_ovf2, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
                       &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
                       &h->walls_dev,
-                      &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp,
-                      &h->seg_work, &h->chk};
+                      &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
     for (DevBuf *b : bufs) b->release();
     if (h->host_rb) cudaFreeHost(h->host_rb);
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
@@ -823,7 +821,6 @@ int bin_begin(vgpu_container *h, int mode, bool thin) {
     VG_CUDA(h->kept.ensure(64));
     VG_CUDA(h->counters.ensure(sizeof(Counters)));
     VG_CUDA(h->counters2.ensure(2 * sizeof(Counters)));
-    VG_CUDA(h->seg_work.ensure(kMaxSegments * sizeof(unsigned long long)));
 
     h->launches0 = launch_count();
     cudaEventRecord(h->ev[0], s);
@@ -1028,8 +1025,6 @@ void fill_cell_params(vgpu_container *h, CellParams &cp) {
     const int nkept = h->nkept;
     memset(&cp, 0, sizeof(cp));
     cp.cell_chunk = h->cell_chunk;
-    cp.seg_work = h->seg_work.p ? h->seg_work.as<unsigned long long>() : nullptr;
-    cp.nseg = std::min(std::max(h->sms, 1), kMaxSegments);
     cp.g = g;
     cp.a.p64 = h->p64.as<double4>();
     cp.a.l32 = h->lffh.as<float4>();
@@ -1090,7 +1085,6 @@ int prepare_small(vgpu_container *h, int mode, SmallBinJob &job, unsigned long l
     VG_CUDA(h->outpos_in.ensure(nn * 4));
     VG_CUDA(h->counters.ensure(sizeof(Counters)));
     VG_CUDA(h->counters2.ensure(2 * sizeof(Counters)));
-    VG_CUDA(h->seg_work.ensure(kMaxSegments * sizeof(unsigned long long)));
     VG_CUDA(h->r_vol.ensure(nn * 8));
     VG_CUDA(h->r_cen.ensure(nn * 24));
     VG_CUDA(h->r_nf.ensure(nn * 4));

@@ -1252,47 +1252,12 @@ __global__ void __launch_bounds__(VGPU_CTA_THREADS, min_blocks<MODE, K, LEAN>())
     const int chunk = max(1, min(P.cell_chunk > 0 ? P.cell_chunk : VGPU_CELL_CHUNK,
                                  P.ncells / (int)(4 * gridDim.x * (blockDim.x >> 5))));
     int w = 0, wend = 0;
-#if VGPU_SM_LOCAL
-    const bool seg_queues = P.seg_work != nullptr && P.nseg > 1;
-    unsigned smid;
-    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    const int home = seg_queues ? (int)(smid % (unsigned)P.nseg) : 0;
-    int probe = 0;   // segments found exhausted so far, from the home one on
-#endif
     for (;;) {
         if (w == wend) {
-#if VGPU_SM_LOCAL
-            if (seg_queues) {
-                bool got = false;
-                while (probe < P.nseg) {
-                    const int g = home + probe < P.nseg ? home + probe : home + probe - P.nseg;
-                    const int lo = (int)((long long)P.ncells * g / P.nseg);
-                    const int hi = (int)((long long)P.ncells * (g + 1) / P.nseg);
-                    long long t = -1;
-                    if (lane == 0) {
-                        // a plain read first: an exhausted queue costs no atomic
-                        const unsigned long long cur = *reinterpret_cast<volatile unsigned long long *>(&P.seg_work[g]);
-                        if (cur < (unsigned long long)(hi - lo))
-                            t = (long long)atomicAdd(&P.seg_work[g], (unsigned long long)chunk);
-                    }
-                    t = __shfl_sync(kFull, t, 0);
-                    if (t >= 0 && t < hi - lo) {
-                        w = lo + (int)t;
-                        wend = min(w + chunk, hi);
-                        got = true;
-                        break;
-                    }
-                    probe++;
-                }
-                if (!got) break;
-            } else
-#endif
-            {
-                if (lane == 0) w = (int)atomicAdd(work, (unsigned long long)chunk);
-                w = __shfl_sync(kFull, w, 0);
-                if (w >= P.ncells) break;
-                wend = min(w + chunk, P.ncells);
-            }
+            if (lane == 0) w = (int)atomicAdd(work, (unsigned long long)chunk);
+            w = __shfl_sync(kFull, w, 0);
+            if (w >= P.ncells) break;
+            wend = min(w + chunk, P.ncells);
         }
         const int k = P.cell_list ? P.cell_list[w] : P.cell_begin + w;
         w++;
@@ -1439,12 +1404,6 @@ cudaError_t launch_one(const CellParams &cp, int warps, int sms, cudaStream_t s)
     const long long need = (cp.ncells + warps - 1) / warps;
     int grid = (int)(want < need ? want : need);
     if (grid < 1) grid = 1;
-#if VGPU_SM_LOCAL
-    if (cp.seg_work) {
-        e = cudaMemsetAsync(cp.seg_work, 0, (size_t)cp.nseg * sizeof(unsigned long long), s);
-        if (e != cudaSuccess) return e;
-    }
-#endif
     cell_kernel<MODE, K, LEAN><<<grid, warps * 32, smem, s>>>(cp);
     note_launch();
     return cudaGetLastError();

@@ -29,13 +29,6 @@ constexpr int kCandBuf = 64;
 #ifndef VGPU_GATHER_TMA
 #define VGPU_GATHER_TMA 0
 #endif
-// VGPU_SM_LOCAL=1: the clipping kernels' warps take cells from a queue per
-// SM (a contiguous range of cells each, then the other SMs' leftovers), so
-// that the warps sharing an SM's L1 work on neighbouring cells
-#ifndef VGPU_SM_LOCAL
-#define VGPU_SM_LOCAL 0
-#endif
-constexpr int kMaxSegments = 256;
 constexpr int kStageEntries = 64;   // staged candidate particles per warp (VGPU_GATHER_TMA)       // candidate buffer entries per warp
 // Neighbour IDs: kNbStride slots per cell in a fixed-stride array; a cell with
 // more faces keeps kNbStride-1 there and the rest in an overflow store, whose
@@ -150,10 +143,6 @@ struct CellParams {
     const int *cell_list;   // NULL: cells cell_begin..cell_begin+ncells-1; else the list of engine indices
     int cell_begin;
     int cell_chunk;         // consecutive cells a warp takes from the queue at once (0: the built-in default)
-    // per-SM work queues (VGPU_SM_LOCAL builds): nseg counters, zeroed before
-    // each launch; segment g holds cells [ncells*g/nseg, ncells*(g+1)/nseg)
-    unsigned long long *seg_work;
-    int nseg;
     int *overflow_list;     // cells that overflowed this engine's capacity
     const int *offsets;     // packed search offsets (engine table), sorted by lb2
     int noffsets;

@@ -210,6 +210,10 @@ struct vgpu_container {
     unsigned long long poly_used = 0;   // doubles of polytope output of the last compute
     long long launches0 = 0;    // launch counter at its start
     bool computed = false;
+    // the CSR neighbour offsets of the last compute are in nb_off (csr_total
+    // neighbours), so that get_neighbors after num_neighbors scans once
+    bool csr_valid = false;
+    int64_t csr_total = 0;
     bool binned = false;        // engine-order arrays match the particles (after a compute or a locate)
     vgpu_stats stats{};
     double phase[16] = {};
@@ -534,7 +538,8 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->gh_ovf, &h->gh_ovf2, &h->gh_cnt, &h->gh_vol, &h->gh_cen, &h->gh_nf, &h->gh_nv, &h->gh_mr2, &h->gh_flags,
                       &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
                       &h->walls_dev,
-                      &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp};
+                      &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp,
+                      &h->chk};
     for (DevBuf *b : bufs) b->release();
     if (h->host_rb) cudaFreeHost(h->host_rb);
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);
@@ -1295,6 +1300,7 @@ int finish_compute(vgpu_container *h, const Counters &c, float cell_ms) {
     h->stats.step_ms = step_ms;
     h->stats.kernel_launches = launch_count() - h->launches0;
     h->computed = true;
+    h->csr_valid = false;
     if (h->stats.failed_cells > 0)
         return fail(VGPU_ERR_CAPACITY, "%lld cells exceeded the engine capacity", (long long)h->stats.failed_cells);
     return VGPU_OK;
@@ -1682,6 +1688,10 @@ int vgpu_get_radii(vgpu_container *h, double *radii) {
 }
 
 static int build_csr(vgpu_container *h, int64_t *total_out) {
+    if (h->csr_valid) {
+        *total_out = h->csr_total;
+        return VGPU_OK;
+    }
     size_t n = (size_t)h->ncells;
     cudaStream_t s = h->stream;
     VG_CUDA(h->nb_off.ensure((n + 1) * 8));
@@ -1694,6 +1704,8 @@ static int build_csr(vgpu_container *h, int64_t *total_out) {
     VG_CUDA(cudaMemcpyAsync(&total, h->nb_off.as<long long>() + n, 8, cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
     *total_out = total;
+    h->csr_total = total;
+    h->csr_valid = true;
     return VGPU_OK;
 }
 

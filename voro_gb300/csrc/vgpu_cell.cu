@@ -25,7 +25,23 @@ __global__ void compact_nb_kernel(const int *nf, const int *nb, const int *ovf, 
     if (i >= n) return;
     int m = nf[i];
     long long o = off[i];
-    // ascending order of neighbour IDs
+    // ascending order of neighbour IDs: a cell of at most 32 faces (nearly
+    // all) by a bitonic sort across the warp's lanes, a larger one by ranks
+    if (m <= 32) {
+        // signed order as unsigned: flip the sign bit; the pads sort last
+        unsigned x = lane < m ? (unsigned)nb_get(nb, ovf, i, m, lane) ^ 0x80000000u : 0xffffffffu;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const unsigned y = __shfl_xor_sync(0xffffffffu, x, j);
+                const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+                x = (lower == up) ? min(x, y) : max(x, y);
+            }
+        }
+        if (lane < m) out[o + lane] = (int)(x ^ 0x80000000u);
+        return;
+    }
     for (int q = lane; q < m; q += 32) {
         int v = nb_get(nb, ovf, i, m, q);
         int rank = 0;

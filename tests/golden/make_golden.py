@@ -125,6 +125,26 @@ def edge_cases():
                                             np.array([[1.1, 2.2, 0.4]]))
     out["edge_pair_periodic_2"] = W._pack(W.KIND_PERIODIC, (3, 0, 3, 0, 0, 3), (2, 2, 2), (True,) * 3,
                                           np.array([[1.1, 2.2, 0.4], [2.5, 0.9, 1.6]]))
+    # a box far from the origin (coordinates near 1e5, spacing about 0.13)
+    x0 = 100000.0
+    xyz = x0 + rng.random((500, 3))
+    out["edge_far_box_500"] = W._pack(W.KIND_CONTAINER, (x0, x0 + 1, x0, x0 + 1, x0, x0 + 1), (4, 4, 4),
+                                      (False,) * 3, xyz)
+    # strongly anisotropic boxes, walled and periodic
+    xyz = rng.random((600, 3)) * np.array([20.0, 1.0, 0.5])
+    out["edge_aniso_600"] = W._pack(W.KIND_CONTAINER, (0, 20, 0, 1, 0, 0.5), (20, 2, 1), (False,) * 3, xyz)
+    xyz = rng.random((500, 3)) * np.array([5.0, 1.0, 0.7])
+    out["edge_periodic_aniso_500"] = W._pack(W.KIND_PERIODIC, (5.0, 0, 1.0, 0, 0, 0.7), (10, 2, 2), (True,) * 3, xyz)
+    # radical: zero radii among a wide spread, and all radii equal (the
+    # power diagram is then the plain Voronoi diagram)
+    xyz = rng.random((400, 3)) * 2.0
+    r = rng.uniform(0.0, 0.3, size=400)
+    r[::7] = 0.0
+    out["edge_radical_zero_r_400"] = W._pack(W.KIND_CONTAINER_POLY, (0, 2, 0, 2, 0, 2), (4, 4, 4), (False,) * 3,
+                                             xyz, r=r)
+    xyz = rng.random((400, 3)) * 3.0
+    out["edge_periodic_poly_equal_r_400"] = W._pack(W.KIND_PERIODIC_POLY, (3, 0, 3, 0, 0, 3), (4, 4, 4),
+                                                    (True,) * 3, xyz, r=np.full(400, 0.25))
     return out
 
 

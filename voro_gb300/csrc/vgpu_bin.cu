@@ -100,11 +100,15 @@ __device__ __forceinline__ void gather_one(const Geometry &g, int k, int b, doub
     int bx = b % g.gn[0];
     int by = (b / g.gn[0]) % g.gn[1];
     int bz = b / (g.gn[0] * g.gn[1]);
-    double ox = g.lo[0] + bx * g.gbs[0];
-    double oy = g.lo[1] + by * g.gbs[1];
-    double oz = g.lo[2] + bz * g.gbs[2];
     p64[k] = p;
-    const double d[4] = {p.x - ox, p.y - oy, p.z - oz, p.w};
+    // (p - lo) - b * bs rather than p - (lo + b * bs): the block origin
+    // rounded at the magnitude of lo would put an error of ulp(lo) into the
+    // local positions (a box near 1e5 lost 1e-10 of its cells' volumes in
+    // the float-pair planes); p - lo is exact within a container far from
+    // the origin (p and lo within a factor two) and otherwise errs by an ulp
+    // of the box's size, and it is the same difference the engine key uses
+    const double d[4] = {(p.x - g.lo[0]) - bx * g.gbs[0], (p.y - g.lo[1]) - by * g.gbs[1],
+                         (p.z - g.lo[2]) - bz * g.gbs[2], p.w};
     float h[4], l[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) {

@@ -7,6 +7,28 @@ import numpy as np
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+# Fixtures whose per-cell topology the engine does not reproduce, with the
+# reason; their geometry is checked instead (test_gpu_parity.py).
+KNOWN_LIMIT = {
+    "edge_cubic_jitter_1e-12_216":
+        "a lattice jittered at the scale of the reference's tolerance: which of the split "
+        "vertices' tiny faces survive is decided inside the band, cell by cell (the reference's "
+        "own neighbour lists are not symmetric there)",
+}
+
+# Fixtures whose volumes are determined only to u * kappa: vertices where two
+# nearly parallel bisectors meet (a pair of particles 3e-9 apart seen from a
+# third one: kappa about spacing / separation, 5e7 here), computed by the
+# reference along its edges and by the engine from three planes.
+CONDITIONING_TOL = {
+    "edge_near_coincident_300": {"fp64": (1e-9, 1e-9), "mixed": (1e-7, 1e-7)},
+}
+
+
+def tolerance(name, mode, default):
+    return CONDITIONING_TOL.get(name, {}).get(mode, default)
+
+
 def names():
     """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly;
     locate_*.npz point-location answers, see load_locate; ghost_*.npz ghost

@@ -145,6 +145,24 @@ def edge_cases():
     xyz = rng.random((400, 3)) * 3.0
     out["edge_periodic_poly_equal_r_400"] = W._pack(W.KIND_PERIODIC_POLY, (3, 0, 3, 0, 0, 3), (4, 4, 4),
                                                     (True,) * 3, xyz, r=np.full(400, 0.25))
+    # radical cells cut away entirely (compute_cell false): a few large
+    # particles among many small ones
+    xyz = rng.random((300, 3)) * 2.0
+    r = np.full(300, 0.02)
+    r[:6] = 0.9
+    out["edge_radical_deleted_300"] = W._pack(W.KIND_CONTAINER_POLY, (0, 2, 0, 2, 0, 2), (4, 4, 4), (False,) * 3,
+                                              xyz, r=r)
+    # nearly coincident pairs (1e-7 and 1e-9 apart) in a walled box: tiny cells
+    xyz = rng.random((300, 3))
+    xyz[1] = xyz[0] + np.array([1e-7, 0.0, 0.0])
+    xyz[3] = xyz[2] + np.array([3e-9, -2e-9, 1e-9])
+    out["edge_near_coincident_300"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (4, 4, 4), (False,) * 3, xyz)
+    # a simple-cubic lattice jittered by 1e-12: vertices of order 4 split by
+    # far less than the reference's tolerance (about 1e-13 of the box here)
+    g = np.arange(6, dtype=float) + 0.5
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1) + rng.normal(0.0, 1e-12, size=(216, 3))
+    out["edge_cubic_jitter_1e-12_216"] = W._pack(W.KIND_CONTAINER, (0, 6, 0, 6, 0, 6), (3, 3, 3), (False,) * 3, xyz)
     return out
 
 
@@ -213,6 +231,13 @@ def wall_cases():
     w["geom"] = (0.0, 2.0, 0.0, 1.0, 0.0, 1.0)
     w["walls"] = [(1, [0.0, -1.0, 0.0, -0.1], -7), (1, [0.0, 1.0, 0.0, 0.9], -8)]
     out["wall_planes_xperiodic_1000"] = w
+    # a sphere wall on a box far from the origin
+    x0 = 50000.0
+    rng = np.random.default_rng(2104)
+    w = W._pack(W.KIND_CONTAINER, (x0, x0 + 2, x0, x0 + 2, x0, x0 + 2), (5, 5, 5), (False,) * 3,
+                x0 + rng.random((800, 3)) * 2.0)
+    w["walls"] = [(0, [x0 + 1.0, x0 + 1.0, x0 + 1.0, 0.95], -7)]
+    out["wall_far_sphere_800"] = w
     return out
 
 

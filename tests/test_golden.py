@@ -21,8 +21,16 @@ def test_volumes_tile_the_box(name):
     assert abs(z["vol"][ok].sum() - G.box_volume(w)) <= 1e-11 * G.box_volume(w)
 
 
+# Fixtures whose reference output is itself not symmetric: on a lattice
+# jittered by far less than its face sizes, the reference decides each cell's
+# tiny faces within its own tolerance, independently of the neighbour's cell.
+REFERENCE_ASYMMETRIC = {"edge_cubic_jitter_1e-12_216"}
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_neighbour_relation_is_symmetric(name):
+    if name in REFERENCE_ASYMMETRIC:
+        pytest.skip("the reference's own neighbour lists are not symmetric here")
     w, z = G.load(name)
     ids = z["ids"]
     pairs = set()

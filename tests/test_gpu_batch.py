@@ -24,7 +24,9 @@ def test_batch_needs_a_device():
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
 def test_batch_of_golden_fixtures_matches_reference(gpu, mode):
-    names = G.names()   # every kind, sheared periodic boxes included
+    # every kind, sheared periodic boxes included (not the known limits: a
+    # batch has no per-member FP64 rerun)
+    names = [n for n in G.names() if n not in G.KNOWN_LIMIT]
     cons, refs = [], []
     for name in names:
         w, z = G.load(name)
@@ -36,7 +38,7 @@ def test_batch_of_golden_fixtures_matches_reference(gpu, mode):
     assert st["cells"] == sum(len(z["ids"]) for _, z in refs)
     assert st["failed_cells"] == 0
     for name, con, (w, z) in zip(names, cons, refs):
-        errs = G.compare_cells(con.cells(), z, *TOL[mode], label=f"batch/{name}/{mode}")
+        errs = G.compare_cells(con.cells(), z, *G.tolerance(name, mode, TOL[mode]), label=f"batch/{name}/{mode}")
         assert not errs, "\n".join(errs)
         assert abs(con.sum_cell_volumes() - G.box_volume(w)) <= 1e-9 * G.box_volume(w)
 

@@ -1223,8 +1223,12 @@ int setup_member_records(vgpu_container *h, CellParams &cp, Counters *cnt, cudaS
 // run could not complete.
 // first: cells at the start of cp's range whose first pass has already run
 // (with the same counters, whose work counters the caller has reset).
+// clip_passes' answer when a mixed first pass handed on more than switch_above
+// of its cells (the caller reruns the container on the FP64 engine)
+constexpr int kSwitchToFp64 = -1;
+
 int clip_passes(cudaStream_t s, int sms, int warps, int mode, const CellParams &cp, Counters *cnt1, Counters *cnt2,
-                int *list2, Counters &sum, int first = 0) {
+                int *list2, Counters &sum, int first = 0, double switch_above = -1.0) {
     Counters c[3];
     memset(c, 0, sizeof(c));
     CellParams p0 = cp;
@@ -1237,6 +1241,8 @@ int clip_passes(cudaStream_t s, int sms, int warps, int mode, const CellParams &
     VG_CUDA(cudaMemcpyAsync(&c[0], cp.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     VG_CUDA(cudaStreamSynchronize(s));
     unsigned long long pending = c[0].overflow;
+    if (mode == VGPU_MIXED && switch_above >= 0.0 && (double)pending > switch_above * p0.ncells)
+        return kSwitchToFp64;
     const int *list = cp.overflow_list;
     if (pending > 0 && mode == VGPU_MIXED) {
         CellParams p1 = cp;
@@ -1382,8 +1388,24 @@ int compute_cells(vgpu_container *h, int mode, bool thin) {
         }
     }
     Counters c1;
+    // a container below the sampled size is judged by its whole first pass:
+    // with the band saturated (a lattice jittered at the tolerance's scale,
+    // where the FP32 engine's band handling met its limits) it reruns on the
+    // FP64 engine like a sampled one
+    const bool judge_first = mode == VGPU_MIXED && h->fp64_fallback < 1.0 && cp.ncells < kSampleMinCells;
     rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, h->counters2.as<Counters>(),
-                     h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1, first);
+                     h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1, first,
+                     judge_first ? h->fp64_fallback : -1.0);
+    if (rc == kSwitchToFp64) {
+        mode = VGPU_FP64;
+        switched = true;
+        VG_CUDA(cudaMemsetAsync(cp.cnt, 0, sizeof(Counters), s));
+        VG_CUDA(cudaMemsetAsync(h->counters2.p, 0, 2 * sizeof(Counters), s));
+        rc = setup_records(h, mode, cp, cp.cnt, s, store.buf);
+        if (rc != VGPU_OK) return rc;
+        rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, h->counters2.as<Counters>(),
+                         h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1, 0);
+    }
     if (rc != VGPU_OK) return rc;
     cudaEventRecord(h->ev[4], s);
     VG_CUDA(launch_finish(cp, mode, h->sms, s));

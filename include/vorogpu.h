@@ -46,7 +46,7 @@ extern "C" {
                         tolerance band and cells below 1e-4 of the cube of
                         their radius solved in FP64); volume and centroid
                         summed in float pairs.  Per-cell volume and centroid
-                        within 1e-10 of the FP64 engine's.  Large containers
+                        within 1e-10 of the FP64 engine's.  Containers
                         whose FP32 filter band is saturated run on the FP64
                         engine (vgpu_set_fp64_fallback) */
 
@@ -82,8 +82,9 @@ typedef struct vgpu_stats {
     int64_t kernel_launches;  /* engine kernels launched by the last compute */
     double clip_ms;           /* of kernel_ms: the main clipping kernel alone */
     double finish_ms;         /* of kernel_ms: the FP64 finish kernel (mixed engine) */
-    int64_t fp64_engine_cells; /* mixed compute: cells the FP64 engine computed because a
-                                  sample showed the FP32 filter band saturated (0 or all) */
+    int64_t fp64_engine_cells; /* mixed compute: cells the FP64 engine computed because the
+                                  first pass (or its sample) showed the FP32 filter band
+                                  saturated (0 or all of a container's) */
 } vgpu_stats;
 
 /* Library / device. */
@@ -318,14 +319,17 @@ int vgpu_set_ghost_depth(vgpu_container *h, double spacings);
  * vgpu_compute returns VGPU_ERR_CAPACITY.  Applies from the next compute. */
 int vgpu_set_record_budget(vgpu_container *h, int64_t bytes);
 
-/* Mixed computes of large containers (at least 262,144 cells) first run the
- * FP32 engine's first pass on 1/64 of the cells.  If more than this fraction
- * of them need FP64 (tests inside the filter band or ill-conditioned
- * vertices, as in jittered lattices where three near-coplanar bisectors meet),
- * the whole container is computed by the FP64 engine instead, which is faster
- * there and gives the same topology; vgpu_stats.fp64_engine_cells reports it.
- * Default 0.25; a value >= 1 never switches.  No counterpart in the reference
- * (it computes in FP64 throughout). */
+/* Mixed computes judge the FP32 engine's first pass: a large container (at
+ * least 262,144 cells) runs it first on 1/64 of its cells, a smaller one on
+ * all of them (and a batch member by its share of the batch's first pass).
+ * If more than this fraction of those cells need FP64 (tests inside the
+ * filter band or ill-conditioned vertices, as in jittered lattices where
+ * three near-coplanar bisectors meet), the whole container is computed by the
+ * FP64 engine instead, which is faster there, gives the same topology and
+ * stays exact where a lattice is jittered at the tolerance's own scale;
+ * vgpu_stats.fp64_engine_cells reports it.  Default 0.25; a value >= 1 never
+ * switches.  No counterpart in the reference (it computes in FP64
+ * throughout). */
 int vgpu_set_fp64_fallback(vgpu_container *h, double fraction);
 
 /* ---- batches: many containers computed by one persistent launch ----

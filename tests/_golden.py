@@ -25,6 +25,16 @@ CONDITIONING_TOL = {
 }
 
 
+# Fixtures with a cell beyond the engines' capacity (the 128-vertex engine's
+# slots): the compute returns VGPU_ERR_CAPACITY with exactly these cells
+# flagged VGPU_CELL_FAILED and this reason (bits 8-11), every other cell as
+# the reference's.  A large radical particle among small ones: its cell of 84
+# vertices and 44 faces needs more than 128 vertex slots while it is cut.
+CAPACITY_LIMIT = {
+    "edge_radical_deleted_300": {"ids": [1], "reason": 3},
+}
+
+
 def tolerance(name, mode, default):
     return CONDITIONING_TOL.get(name, {}).get(mode, default)
 
@@ -157,9 +167,10 @@ def box_volume(w):
     return g[0] * g[2] * g[5]
 
 
-def compare_cells(got, ref, vol_rtol, cen_rtol, label=""):
+def compare_cells(got, ref, vol_rtol, cen_rtol, label="", skip=None):
     """got: object with ids,pos,vol,cen,nf,nv,ok and neighbors(k) sorted;
-    ref: the fixture arrays.  Returns a list of human-readable mismatches."""
+    ref: the fixture arrays; skip: a mask of cells left out (the cells of a
+    known capacity limit).  Returns a list of human-readable mismatches."""
     errs = []
     n = len(ref["ids"])
     if len(got.ids) != n:
@@ -170,6 +181,9 @@ def compare_cells(got, ref, vol_rtol, cen_rtol, label=""):
         errs.append(f"{label}: stored positions differ (max {np.abs(got.pos - ref['pos']).max():.3g})")
     ok_ref = ref["ok"] != 0
     ok_got = np.asarray(got.ok, dtype=bool)
+    if skip is not None:
+        ok_ref = ok_ref & ~skip
+        ok_got = ok_got & ~skip
     if not np.array_equal(ok_got, ok_ref):
         errs.append(f"{label}: deleted-cell flags differ at {np.nonzero(ok_got != ok_ref)[0][:10]}")
     m = ok_ref & ok_got

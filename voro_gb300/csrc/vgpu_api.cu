@@ -2269,8 +2269,18 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
     int first_err = VGPU_OK;
     for (int i = 0; i < nc; i++) {
         vgpu_container *h = b->members[i];
-        h->poly_used = cs[i].poly_used;
-        int rc = finish_compute(h, cs[i], cell_ms);
+        int rc;
+        if (mode == VGPU_MIXED && h->fp64_fallback < 1.0 && h->nkept > 0 &&
+            (double)cs[i].overflow > h->fp64_fallback * h->nkept) {
+            // the member's filter band was saturated (more than the fallback
+            // fraction of its cells handed on, as a single compute judges
+            // it): the member alone again, on the FP64 engine
+            rc = compute_cells(h, VGPU_FP64, false);
+            h->stats.fp64_engine_cells = h->nkept;
+        } else {
+            h->poly_used = cs[i].poly_used;
+            rc = finish_compute(h, cs[i], cell_ms);
+        }
         if (rc != VGPU_OK && first_err == VGPU_OK) first_err = rc;
         vgpu_stats &t = b->stats;
         t.cells += h->stats.cells;
@@ -2282,6 +2292,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         t.planes_cut += h->stats.planes_cut;
         t.overflow_reruns += h->stats.overflow_reruns;
         t.failed_cells += h->stats.failed_cells;
+        t.fp64_engine_cells += h->stats.fp64_engine_cells;
     }
     const auto t2 = std::chrono::steady_clock::now();
     b->stats.kernel_ms = cell_ms;

@@ -41,9 +41,10 @@ static __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar
 }
 #endif
 
-// plane indices are always < kMaxPlanes; the mask keeps every shared-memory
+// plane indices are always below the engine's plane slots (64 or 128); the
+// mask (to the larger) keeps every shared-memory
 // index in bounds even if a slot held inconsistent data
-static __device__ __forceinline__ int tri_plane(unsigned t, int e) { return (t >> (8 * e)) & (kMaxPlanes - 1); }
+static __device__ __forceinline__ int tri_plane(unsigned t, int e) { return (t >> (8 * e)) & (kMaxPlanesWide - 1); }
 
 // Sortable key of a float (total order as unsigned)
 static __device__ __forceinline__ unsigned float_key(float f) {

@@ -120,6 +120,24 @@ __device__ __forceinline__ Mask<K> ballot_mask(const bool (&pred)[K]) {
 }
 
 // ------------------------------------------------------------------ shared memory per warp
+// plane slots of an engine with K vertex slot rows: 64, or 128 for the
+// 128-vertex engines (a cell that outgrows 64 vertices can also hold more
+// than 64 live planes at once: a radical cell of a large particle among
+// small ones)
+template <int K>
+struct PlaneSlots {
+    static constexpr int N = K >= 4 ? kMaxPlanesWide : kMaxPlanes;
+    static constexpr int W = N / 32;   // 32-bit words of a set of planes
+};
+
+// set bit p of a set of planes held as 32-bit words
+template <int NW>
+__device__ __forceinline__ void plane_set_add(unsigned (&m)[NW], int p) {
+#pragma unroll
+    for (int i = 0; i < NW; i++)
+        if ((p >> 5) == i) m[i] |= 1u << (p & 31);
+}
+
 template <int MODE, int K>
 struct WarpShared {
 #if VGPU_GATHER_TMA
@@ -128,19 +146,19 @@ struct WarpShared {
     unsigned cbar_phase;            // its current phase parity; bit 31: staging off
     unsigned cbar_pad;
 #endif
-    float4 pl[kMaxPlanes];   // plane n.x, n.y, n.z, h  (n.v <= h inside)
-    float4 pe[kMaxPlanes];   // |n|, en (abs error of n), eh (abs error of h), |h|
+    float4 pl[PlaneSlots<K>::N];   // plane n.x, n.y, n.z, h  (n.v <= h inside)
+    float4 pe[PlaneSlots<K>::N];   // |n|, en (abs error of n), eh (abs error of h), |h|
     // (pl and pe are contiguous: at the end of a cell they hold the FP64 planes)
-    double4 pl64x[MODE == VGPU_FP64 ? kMaxPlanes : 1];   // FP64 planes (FP64 engine, during the search)
-    int pid[kMaxPlanes];     // neighbour ID of the plane
-    int psrc[kMaxPlanes];    // engine index of the generating particle, -1 for initial faces
-    int pshift[kMaxPlanes];  // packed periodic image counts (initial faces: face index)
+    double4 pl64x[MODE == VGPU_FP64 ? PlaneSlots<K>::N : 1];   // FP64 planes (FP64 engine, during the search)
+    int pid[PlaneSlots<K>::N];     // neighbour ID of the plane
+    int psrc[PlaneSlots<K>::N];    // engine index of the generating particle, -1 for initial faces
+    int pshift[PlaneSlots<K>::N];  // packed periodic image counts (initial faces: face index)
     unsigned tri[32 * K];
     unsigned adj[32 * K];
     unsigned stage[48 * K];  // boundary edges of a cut (a | b<<8 | u<<16); final stage: edge list
     unsigned char vmap[32 * K];   // finished cell: vertex slot -> compact index
-    unsigned char startN[kMaxPlanes];
-    unsigned char endN[kMaxPlanes];
+    unsigned char startN[PlaneSlots<K>::N];
+    unsigned char endN[PlaneSlots<K>::N];
     // the warp's counters over its cells (side tests, repairs, planes tested,
     // planes cut, deleted, marginal): kept here rather than in registers,
     // which the clipping loop needs more
@@ -157,7 +175,7 @@ struct WarpShared {
         } c;
         struct {
             double vx[32 * K], vy[32 * K], vz[32 * K];   // FP64 vertices relative to c0
-            double fx[kMaxPlanes], fy[kMaxPlanes], fz[kMaxPlanes];  // face points relative to c0
+            double fx[PlaneSlots<K>::N], fy[PlaneSlots<K>::N], fz[PlaneSlots<K>::N];  // face points relative to c0
         } f;
     } u;
 };
@@ -183,7 +201,7 @@ struct CellCtx {
     bool deleted, overflow, marginal, repaired;
     bool needs_fp64;  // this lane's vertex solve was ill-conditioned (first pass: the cell is rerun)
     int fail_reason;  // why overflow was set (VGPU_FAIL_*)
-    unsigned freeplanes[2];   // plane slots not in use: slots 0-31, 32-63
+    unsigned freeplanes[2];   // plane slots not in use: slots 0-31, 32-63 (128-vertex engines: also fp_hi)
     int ncand;
     unsigned tests, repairs, ptested, pcut;
 #ifdef VGPU_PHASE_TIMING
@@ -387,6 +405,7 @@ struct Engine {
     Verts<MODE, K> V;
     Mask<K> Vm;           // valid vertex slots
     CellCtx C;
+    unsigned fp_hi[PlaneSlots<K>::W > 2 ? 2 : 1];   // free plane slots 64-127 (128-vertex engines)
 
     __device__ Engine(const CellParams &p, WarpShared<MODE, K> &s, const int *off, int l)
         : P(p), S(s), offsets(off), lane(l) {}
@@ -459,6 +478,7 @@ struct Engine {
         C.fail_reason = 0;
         C.freeplanes[0] = ~0x3fu;
         C.freeplanes[1] = ~0u;
+        if constexpr (PlaneSlots<K>::W > 2) fp_hi[0] = fp_hi[1] = ~0u;
         C.ncand = 0;
         C.tests = C.repairs = C.ptested = C.pcut = 0;
         if (lane < 6) {
@@ -542,27 +562,57 @@ struct Engine {
     //      (32-bit halves: the lowest free slot and its removal are single
     //      32-bit operations)
     __device__ __forceinline__ int alloc_plane() {
-        if ((C.freeplanes[0] | C.freeplanes[1]) == 0u) {
-            unsigned long long live = 0ull;
+        if constexpr (PlaneSlots<K>::W == 2) {
+            if ((C.freeplanes[0] | C.freeplanes[1]) == 0u) {
+                unsigned long long live = 0ull;
 #pragma unroll
-            for (int s = 0; s < K; s++)
-                if (Vm.test(lane + 32 * s)) {
-                    const unsigned t = V.tri[s];
-                    live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
-                }
-            const unsigned long long fr = ~warp_or64(live);
-            C.freeplanes[0] = (unsigned)fr;
-            C.freeplanes[1] = (unsigned)(fr >> 32);
-            if (fr == 0ull) return -1;
-        }
-        if (C.freeplanes[0]) {
-            const int p = __ffs((int)C.freeplanes[0]) - 1;
-            C.freeplanes[0] &= C.freeplanes[0] - 1u;
+                for (int s = 0; s < K; s++)
+                    if (Vm.test(lane + 32 * s)) {
+                        const unsigned t = V.tri[s];
+                        live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+                    }
+                const unsigned long long fr = ~warp_or64(live);
+                C.freeplanes[0] = (unsigned)fr;
+                C.freeplanes[1] = (unsigned)(fr >> 32);
+                if (fr == 0ull) return -1;
+            }
+            if (C.freeplanes[0]) {
+                const int p = __ffs((int)C.freeplanes[0]) - 1;
+                C.freeplanes[0] &= C.freeplanes[0] - 1u;
+                return p;
+            }
+            const int p = 32 + __ffs((int)C.freeplanes[1]) - 1;
+            C.freeplanes[1] &= C.freeplanes[1] - 1u;
             return p;
+        } else {
+            // 128 slots: words 0-1 in C.freeplanes, 2-3 in fp_hi
+            unsigned *fw[4] = {&C.freeplanes[0], &C.freeplanes[1], &fp_hi[0], &fp_hi[1]};
+            if ((C.freeplanes[0] | C.freeplanes[1] | fp_hi[0] | fp_hi[1]) == 0u) {
+                unsigned live[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+                for (int s = 0; s < K; s++)
+                    if (Vm.test(lane + 32 * s)) {
+                        const unsigned t = V.tri[s];
+#pragma unroll
+                        for (int e = 0; e < 3; e++) plane_set_add(live, tri_plane(t, e));
+                    }
+                unsigned any = 0u;
+#pragma unroll
+                for (int w = 0; w < 4; w++) {
+                    *fw[w] = ~__reduce_or_sync(kFull, live[w]);
+                    any |= *fw[w];
+                }
+                if (any == 0u) return -1;
+            }
+#pragma unroll
+            for (int w = 0; w < 4; w++)
+                if (*fw[w]) {
+                    const int p = 32 * w + __ffs((int)*fw[w]) - 1;
+                    *fw[w] &= *fw[w] - 1u;
+                    return p;
+                }
+            return -1;
         }
-        const int p = 32 + __ffs((int)C.freeplanes[1]) - 1;
-        C.freeplanes[1] &= C.freeplanes[1] - 1u;
-        return p;
     }
 
     // ---- a candidate plane that cuts nothing but holds every vertex of a
@@ -573,20 +623,26 @@ struct Engine {
     //      through vertices on the plane relabels it (src/cell.cc:1166-1355).
     //      band: this lane's slots in the band.
     __device__ void relabel_coplanar(int cb, unsigned band) {
-        unsigned long long on = 0ull, off = 0ull;
+        constexpr int NW = PlaneSlots<K>::W;
+        unsigned on[NW], off[NW];
+#pragma unroll
+        for (int w = 0; w < NW; w++) on[w] = off[w] = 0u;
 #pragma unroll
         for (int s = 0; s < K; s++)
             if (Vm.test(lane + 32 * s)) {
                 const unsigned t = V.tri[s];
-                const unsigned long long f =
-                    (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
-                if ((band >> s) & 1u) on |= f;
-                else off |= f;
+#pragma unroll
+                for (int e = 0; e < 3; e++) {
+                    if ((band >> s) & 1u) plane_set_add(on, tri_plane(t, e));
+                    else plane_set_add(off, tri_plane(t, e));
+                }
             }
-        const unsigned long long faces = warp_or64(on) & ~warp_or64(off);
-        if (lane == 0 && faces) {
-            const int id = S.u.c.cpid[cb];
-            for (unsigned long long m = faces; m; m &= m - 1ull) S.pid[__ffsll((long long)m) - 1] = id;
+        const int id = S.u.c.cpid[cb];
+#pragma unroll
+        for (int w = 0; w < NW; w++) {
+            const unsigned faces = __reduce_or_sync(kFull, on[w]) & ~__reduce_or_sync(kFull, off[w]);
+            if (lane == 0)
+                for (unsigned m = faces; m; m &= m - 1u) S.pid[32 * w + __ffs((int)m) - 1] = id;
         }
         __syncwarp();
     }
@@ -732,9 +788,9 @@ struct Engine {
                         if ((bnd[s] >> e) & 1u) {
                             // bytes e and e+1 (mod 3) of T, byte e of A3, and T's
                             // zero top byte, in one byte permutation; the planes
-                            // masked to their 6 bits as tri_plane does
+                            // masked to their 7 bits as tri_plane does
                             constexpr unsigned kSel[3] = {0x3410u, 0x3521u, 0x3602u};
-                            S.stage[q++] = __byte_perm(T, A3, kSel[e]) & 0x00ff3f3fu;
+                            S.stage[q++] = __byte_perm(T, A3, kSel[e]) & 0x00ff7f7fu;
                         }
                 }
             }
@@ -1114,15 +1170,38 @@ struct Engine {
     //      false if the record store is full
     __device__ bool emit_record() {
         constexpr int VW = MODE == VGPU_FP64 ? 6 : 3;   // words per vertex position
-        unsigned long long live = 0ull;
+        constexpr int NW = PlaneSlots<K>::W;
+        // the live planes as NW 32-bit words (64 slots: built as one 64-bit word)
+        unsigned live[NW];
+        int nf = 0;
+        if constexpr (NW == 2) {
+            unsigned long long l64 = 0ull;
 #pragma unroll
-        for (int s = 0; s < K; s++)
-            if (Vm.test(lane + 32 * s)) {
-                const unsigned t = V.tri[s];
-                live |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+            for (int s = 0; s < K; s++)
+                if (Vm.test(lane + 32 * s)) {
+                    const unsigned t = V.tri[s];
+                    l64 |= (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+                }
+            l64 = warp_or64(l64);
+            live[0] = (unsigned)l64;
+            live[1] = (unsigned)(l64 >> 32);
+            nf = __popcll(l64);
+        } else {
+#pragma unroll
+            for (int w = 0; w < NW; w++) live[w] = 0u;
+#pragma unroll
+            for (int s = 0; s < K; s++)
+                if (Vm.test(lane + 32 * s)) {
+                    const unsigned t = V.tri[s];
+#pragma unroll
+                    for (int e = 0; e < 3; e++) plane_set_add(live, tri_plane(t, e));
+                }
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                live[w] = __reduce_or_sync(kFull, live[w]);
+                nf += __popc(live[w]);
             }
-        live = warp_or64(live);
-        const int nf = __popcll(live);
+        }
         const int nv = Vm.popc();
         const unsigned words = (unsigned)(kRecHeader + (2 + VW) * nv + 3 * nf);
         unsigned long long off = 0;
@@ -1144,10 +1223,21 @@ struct Engine {
             const int t = lane + 32 * s;
             if (Vm.test(t)) S.vmap[t] = (unsigned char)Vm.rank(t);
         }
+        if constexpr (NW == 2) {
+            const unsigned long long l64 = ((unsigned long long)live[1] << 32) | live[0];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int q = lane + 32 * h;
-            if ((live >> q) & 1ull) S.endN[q] = (unsigned char)__popcll(live & ((1ull << q) - 1ull));
+            for (int h = 0; h < 2; h++) {
+                const int q = lane + 32 * h;
+                if ((l64 >> q) & 1ull) S.endN[q] = (unsigned char)__popcll(l64 & ((1ull << q) - 1ull));
+            }
+        } else {
+            const unsigned lt = (1u << lane) - 1u;
+            int before = 0;
+#pragma unroll
+            for (int h = 0; h < NW; h++) {
+                if ((live[h] >> lane) & 1u) S.endN[lane + 32 * h] = (unsigned char)(before + __popc(live[h] & lt));
+                before += __popc(live[h]);
+            }
         }
         __syncwarp();
         unsigned *rv = R + kRecHeader;
@@ -1179,9 +1269,9 @@ struct Engine {
         }
         unsigned *rp = rv + (2 + VW) * nv;
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < NW; h++) {
             const int q = lane + 32 * h;
-            if ((live >> q) & 1ull) {
+            if ((live[h] >> lane) & 1u) {
                 const int r = S.endN[q];
                 VGPU_RECORD_STORE(&rp[r], (unsigned)S.psrc[q]);
                 VGPU_RECORD_STORE(&rp[nf + r], (unsigned)S.pshift[q]);

@@ -20,17 +20,20 @@ namespace {
 constexpr int kFinMaxV = 128;   // vertices (the 128-slot engine's capacity)
 
 // One cell's shared arrays for cells of at most NV vertices (a whole warp:
-// 128; a 16-lane half: 64).  Planes: at most 64 either way (the record's
-// planes are numbered compactly, and a cell of 64 vertices has 34 faces).
+// 128; a 16-lane half: 64).  Planes (the record's, numbered compactly): 128
+// for a whole warp, as the 128-vertex engines allow; 64 for a half, whose
+// cell of at most 64 vertices has at most 34 faces.  (The two halves' space
+// is the larger: the whole warp's extra planes cost no shared memory.)
 template <int NV>
 struct FinishShared {
     static constexpr int kNV = NV;
+    static constexpr int kNP = NV >= 128 ? kMaxPlanesWide : kMaxPlanes;
     unsigned tri[NV];
     unsigned adj[NV];
-    int psrc[kMaxPlanes], pshift[kMaxPlanes];
-    int rep[kMaxPlanes];             // per face: its lowest vertex
-    int ford[kMaxPlanes];            // per face: its vertex count
-    float4 plh[kMaxPlanes], pll[kMaxPlanes];   // the FP64 planes as float pairs (MIXED engine)
+    int psrc[kNP], pshift[kNP];
+    int rep[kNP];             // per face: its lowest vertex
+    int ford[kNP];            // per face: its vertex count
+    float4 plh[kNP], pll[kNP];   // the FP64 planes as float pairs (MIXED engine)
     // vertices relative to c0: FP64 (FP64 engine) or scaled float pairs
     // (MIXED engine: vh + vl, see the edge sums)
     union {
@@ -813,6 +816,8 @@ template <int MODE>
 __device__ __forceinline__ void finish_pair(const CellParams &P, FinishWarp &W, int k0, int k1, int lane) {
     const int half = lane >> 4, gl = lane & 15;
     const int mine = half ? k1 : k0;
+    // (a record's vertices all have order 3, so a cell of at most 64
+    // vertices has at most 34 faces: within a half's 64 planes)
     int nv = 0;
     if (mine >= 0) {
         const unsigned long long off = P.rec_off[mine];

@@ -17,7 +17,8 @@ constexpr int kWarp = 32;
 #endif
 constexpr int kDefaultCellChunk = VGPU_CELL_CHUNK;
 constexpr int kBuiltCtaWarps = VGPU_CTA_THREADS / 32;
-constexpr int kMaxPlanes = 64;     // plane slots per cell (64-bit plane masks)
+constexpr int kMaxPlanes = 64;       // plane slots per cell of the 64-vertex engines
+constexpr int kMaxPlanesWide = 128;  // ... of the 128-vertex engines (cells of up to 128 live planes)
 constexpr int kCandBuf = 64;
 // VGPU_GATHER_TMA=1 builds the candidate gather with the block runs of each
 // 64-candidate window bulk-copied (cp.async.bulk, one copy per block run,

@@ -163,6 +163,18 @@ def edge_cases():
     X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
     xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1) + rng.normal(0.0, 1e-12, size=(216, 3))
     out["edge_cubic_jitter_1e-12_216"] = W._pack(W.KIND_CONTAINER, (0, 6, 0, 6, 0, 6), (3, 3, 3), (False,) * 3, xyz)
+    # a dense cluster in a mostly empty box: most blocks empty, a few holding
+    # hundreds of particles (the search's long runs of candidates per block)
+    xyz = np.concatenate([0.5 + 0.02 * rng.standard_normal((1500, 3)), rng.random((60, 3))])
+    out["edge_cluster_1560"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (5, 5, 5), (False,) * 3, xyz)
+    # particles on a line and on a plane: every bisector parallel to the
+    # others (slabs), or to one axis (prisms), the box closing the cells
+    t = np.sort(rng.random(80))
+    xyz = np.stack([t, np.full(80, 0.37), np.full(80, 0.61)], 1)
+    out["edge_line_80"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (4, 2, 2), (False,) * 3, xyz)
+    uv = rng.random((150, 2))
+    xyz = np.stack([uv[:, 0], uv[:, 1], np.full(150, 0.5)], 1)
+    out["edge_plane_150"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (4, 4, 2), (False,) * 3, xyz)
     return out
 
 

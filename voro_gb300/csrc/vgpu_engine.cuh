@@ -624,25 +624,43 @@ struct Engine {
     //      band: this lane's slots in the band.
     __device__ void relabel_coplanar(int cb, unsigned band) {
         constexpr int NW = PlaneSlots<K>::W;
-        unsigned on[NW], off[NW];
+        if constexpr (NW == 2) {
+            unsigned long long on = 0ull, off = 0ull;
 #pragma unroll
-        for (int w = 0; w < NW; w++) on[w] = off[w] = 0u;
-#pragma unroll
-        for (int s = 0; s < K; s++)
-            if (Vm.test(lane + 32 * s)) {
-                const unsigned t = V.tri[s];
-#pragma unroll
-                for (int e = 0; e < 3; e++) {
-                    if ((band >> s) & 1u) plane_set_add(on, tri_plane(t, e));
-                    else plane_set_add(off, tri_plane(t, e));
+            for (int s = 0; s < K; s++)
+                if (Vm.test(lane + 32 * s)) {
+                    const unsigned t = V.tri[s];
+                    const unsigned long long f =
+                        (1ull << tri_plane(t, 0)) | (1ull << tri_plane(t, 1)) | (1ull << tri_plane(t, 2));
+                    if ((band >> s) & 1u) on |= f;
+                    else off |= f;
                 }
+            const unsigned long long faces = warp_or64(on) & ~warp_or64(off);
+            if (lane == 0 && faces) {
+                const int id = S.u.c.cpid[cb];
+                for (unsigned long long m = faces; m; m &= m - 1ull) S.pid[__ffsll((long long)m) - 1] = id;
             }
-        const int id = S.u.c.cpid[cb];
+        } else {
+            unsigned on[NW], off[NW];
 #pragma unroll
-        for (int w = 0; w < NW; w++) {
-            const unsigned faces = __reduce_or_sync(kFull, on[w]) & ~__reduce_or_sync(kFull, off[w]);
-            if (lane == 0)
-                for (unsigned m = faces; m; m &= m - 1u) S.pid[32 * w + __ffs((int)m) - 1] = id;
+            for (int w = 0; w < NW; w++) on[w] = off[w] = 0u;
+#pragma unroll
+            for (int s = 0; s < K; s++)
+                if (Vm.test(lane + 32 * s)) {
+                    const unsigned t = V.tri[s];
+#pragma unroll
+                    for (int e = 0; e < 3; e++) {
+                        if ((band >> s) & 1u) plane_set_add(on, tri_plane(t, e));
+                        else plane_set_add(off, tri_plane(t, e));
+                    }
+                }
+            const int id = S.u.c.cpid[cb];
+#pragma unroll
+            for (int w = 0; w < NW; w++) {
+                const unsigned faces = __reduce_or_sync(kFull, on[w]) & ~__reduce_or_sync(kFull, off[w]);
+                if (lane == 0)
+                    for (unsigned m = faces; m; m &= m - 1u) S.pid[32 * w + __ffs((int)m) - 1] = id;
+            }
         }
         __syncwarp();
     }

@@ -175,6 +175,14 @@ def edge_cases():
     uv = rng.random((150, 2))
     xyz = np.stack([uv[:, 0], uv[:, 1], np.full(150, 0.5)], 1)
     out["edge_plane_150"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (4, 4, 2), (False,) * 3, xyz)
+    # a sheared periodic box with positions up to fifty periods away (the
+    # z-y-x remap along the lattice vectors, src/container_prd.cc:189-216)
+    geom = (7.3, -1.9, 6.1, 2.7, 1.3, 5.9)
+    xyz = rng.uniform(-50.0, 50.0, size=(800, 3)) * np.array([geom[0], geom[2], geom[5]])
+    out["edge_tric_far_800"] = W._pack(W.KIND_PERIODIC, geom, (4, 3, 4), (True,) * 3, xyz)
+    # a periodic box so small that a cell's neighbours are mostly images
+    xyz = rng.random((20, 3)) * 0.5
+    out["edge_periodic_small_box_20"] = W._pack(W.KIND_PERIODIC, (0.5, 0, 0.5, 0, 0, 0.5), (2, 2, 2), (True,) * 3, xyz)
     return out
 
 
@@ -250,6 +258,13 @@ def wall_cases():
                 x0 + rng.random((800, 3)) * 2.0)
     w["walls"] = [(0, [x0 + 1.0, x0 + 1.0, x0 + 1.0, 0.95], -7)]
     out["wall_far_sphere_800"] = w
+    # a plane wall with particles lying exactly on it
+    rng = np.random.default_rng(2105)
+    xyz = rng.random((600, 3)) * 2.0
+    xyz[:25, 0] = 1.25
+    w = W._pack(W.KIND_CONTAINER, (0, 2, 0, 2, 0, 2), (4, 4, 4), (False,) * 3, xyz)
+    w["walls"] = [(1, [1.0, 0.0, 0.0, 1.25], -7)]
+    out["wall_plane_through_600"] = w
     return out
 
 

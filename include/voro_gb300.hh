@@ -192,15 +192,40 @@ class voronoicell {
             v[f] = per;
         }
     }
-    // outward unit normals, three per face
+    // outward unit normals, three per face, by the rule of
+    // voronoicell_base::normals_search (src/cell.cc:2108-2164): from the
+    // loop's second edge on, the first edge longer than the tolerance is
+    // paired with each later edge until their vector product is above it;
+    // a face without such a pair (a sliver) gets (0, 0, 0).  The tests are
+    // on the reference's doubled coordinates, 2x these vertices.
     void normals(std::vector<double> &v) const {
         need_poly();
-        v.resize(3 * fstart_.size());
+        v.assign(3 * fstart_.size(), 0.0);
         for (size_t f = 0; f < fstart_.size(); f++) {
-            double n[3];
-            newell(f, n);
-            const double l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-            for (int a = 0; a < 3; a++) v[3 * f + a] = l > 0 ? -n[a] / l : 0.0;
+            const int m = forder(f);
+            auto edge = [&](int t, double e[3]) {
+                const double *a = vert(floops_[fstart_[f] + t]);
+                const double *b = vert(floops_[fstart_[f] + (t + 1) % m]);
+                for (int c = 0; c < 3; c++) e[c] = b[c] - a[c];
+            };
+            for (int t = 1; t < m; t++) {
+                double u[3];
+                edge(t, u);
+                if (4.0 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) <= tol_) continue;
+                for (int s = t + 1; s < m; s++) {
+                    double e[3];
+                    edge(s, e);
+                    const double w[3] = {e[1] * u[2] - e[2] * u[1], e[2] * u[0] - e[0] * u[2],
+                                         e[0] * u[1] - e[1] * u[0]};
+                    const double wm = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+                    if (16.0 * wm > tol_) {
+                        const double r = 1.0 / std::sqrt(wm);
+                        for (int c = 0; c < 3; c++) v[3 * f + c] = w[c] * r;
+                        break;
+                    }
+                }
+                break;
+            }
         }
     }
     double surface_area() const {
@@ -242,6 +267,7 @@ class voronoicell {
   protected:
     friend class container_gpu_base;
     double vol_ = 0, cen_[3] = {0, 0, 0}, mr2_ = 0;
+    double tol_ = 0;   // the container's length tolerance, for normals()
     int nf_ = 0;
     bool has_poly_ = false;
     std::vector<double> verts_;   // 3 per vertex, particle-relative
@@ -594,6 +620,7 @@ class container_gpu_base {
     container_gpu_base(int kind, const double geom[6], const int grid[3], const int per[3])
         : poly_(kind == VGPU_CONTAINER_POLY || kind == VGPU_CONTAINER_PERIODIC_POLY) {
         gpu_detail::check(vgpu_container_create(&h_, kind, geom, grid, per), "container");
+        gpu_detail::check(vgpu_get_tolerance(h_, &tol_), "container");
         for (int i = 0; i < 6; i++) geom_[i] = geom[i];
     }
 
@@ -643,6 +670,7 @@ class container_gpu_base {
 
   private:
     vgpu_container *h_ = nullptr;
+    double tol_ = 0;   // the reference cell's length tolerance (vgpu_get_tolerance)
     bool poly_;
     bool poly_on_ = false;
     std::vector<int64_t> poff_;
@@ -706,13 +734,13 @@ class container_gpu_base {
             gpu_detail::check(vgpu_get_ghost_polytopes(h_, off, nullptr), "compute_ghost_cell");
             std::vector<double> d((size_t)std::max<int64_t>(off[1], 1));
             gpu_detail::check(vgpu_get_ghost_polytopes(h_, off, d.data()), "compute_ghost_cell");
-            if (off[1] > 0) load_polytope(c, d.data());
+            if (off[1] > 0) load_polytope(c, d.data(), tol_);
         }
         return true;
     }
     bool fill(voronoicell &c, int64_t k) {
         c.has_poly_ = false;
-        if (poly_on_ && !poff_.empty() && poff_[k + 1] > poff_[k]) load_polytope(c, &pdata_[poff_[k]]);
+        if (poly_on_ && !poff_.empty() && poff_[k + 1] > poff_[k]) load_polytope(c, &pdata_[poff_[k]], tol_);
         c.p = nv_[k];
         c.vol_ = vol_[k];
         c.cen_[0] = cen_[3 * k];
@@ -723,8 +751,9 @@ class container_gpu_base {
         return (flags_[k] & VGPU_CELL_OK) != 0;
     }
     // [nv, nf, vertices, per face: neighbour, m, loop] -> faces in neighbour order
-    static void load_polytope(voronoicell &c, const double *d) {
+    static void load_polytope(voronoicell &c, const double *d, double tol) {
         const int nv = (int)d[0], nf = (int)d[1];
+        c.tol_ = tol;
         c.verts_.assign(d + 2, d + 2 + 3 * nv);
         std::vector<int> fs(nf), order(nf);
         int i = 2 + 3 * nv;

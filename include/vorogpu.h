@@ -331,6 +331,14 @@ int vgpu_set_record_budget(vgpu_container *h, int64_t bytes);
  * switches.  No counterpart in the reference (it computes in FP64
  * throughout). */
 int vgpu_set_fp64_fallback(vgpu_container *h, double fraction);
+/* The container's length tolerance as the reference's cells hold it:
+ * tol = 10 * DBL_EPSILON * max_len_sq (src/cell.cc:26, src/config.hh:80),
+ * max_len_sq from the container's geometry (src/container.cc:34-35 for
+ * container / container_poly, the unit cell's max_radius_squared for the
+ * periodic kinds, src/container_prd.cc:32), in the reference's doubled
+ * vertex coordinates.  It is the threshold of voronoicell_base::normals
+ * (src/cell.cc:2108-2164), which the host-side polytope queries follow. */
+int vgpu_get_tolerance(vgpu_container *h, double *tol);
 
 /* ---- batches: many containers computed by one persistent launch ----
  * The reference computes containers one at a time (compute_all_cells per

@@ -160,6 +160,20 @@ def load(name):
     return w, z
 
 
+def reference_tol(w):
+    """The reference cell's length tolerance for workload ``w``:
+    10 * DBL_EPSILON * max_len_sq (src/cell.cc:26), max_len_sq by
+    src/container.cc:34-35 or, for a rectangular periodic box, the unit
+    cell's max_radius_squared in doubled coordinates (bx^2 + by^2 + bz^2)."""
+    g = w["geom"]
+    if w["kind"] in (0, 1):
+        m = sum((g[2 * a + 1] - g[2 * a]) ** 2 * (0.25 if w["periodic"][a] else 1.0) for a in range(3))
+    else:
+        assert g[1] == g[3] == g[4] == 0.0, "sheared unit cells need the engine's unit-cell computation"
+        m = g[0] ** 2 + g[2] ** 2 + g[5] ** 2
+    return 10.0 * np.finfo(np.float64).eps * m
+
+
 def box_volume(w):
     g = w["geom"]
     if w["kind"] in (0, 1):

@@ -297,6 +297,11 @@ def make_wall_fixtures(ref):
 POLY_NAMES = ["unit_cube_1000", "radical_1200", "periodic_poly_800", "sparse_dropped_40", "degenerate_cubic_216",
               "degenerate_fcc_256", "degenerate_fcc_walled_256"]
 POLY_CELLS = 200
+# polytopes of the edge cases (vertices near 1e5, a dense cluster, slabs and
+# prisms of collinear and coplanar particles, a box's faces and block
+# boundaries)
+EDGE_POLY_NAMES = ["edge_far_box_500", "edge_cluster_1560", "edge_line_80", "edge_plane_150",
+                   "edge_box_boundaries_296"]
 CUSTOM_FORMAT = "%i %q %r %w %s %v %c %C %m %g %F %E %A %o"
 
 
@@ -480,8 +485,10 @@ def main():
         make_poly_fixtures(ref, dc, names=list(dc))
         return
     if "--edge-only" in sys.argv:
-        for name, w in edge_cases().items():
+        ec = edge_cases()
+        for name, w in ec.items():
             make_cell_fixture(ref, name, w)
+        make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
         return
     if "--tric-large-only" in sys.argv:
         make_tric_large_fixture(ref)
@@ -494,8 +501,10 @@ def main():
     make_wall_fixtures(ref)
     make_tric_fixtures(ref)
     make_tric_large_fixture(ref)
-    for name, w in edge_cases().items():
+    ec = edge_cases()
+    for name, w in ec.items():
         make_cell_fixture(ref, name, w)
+    make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
     make_cli_fixtures()
 
 

@@ -60,6 +60,7 @@ EXPORTED = [
     "vgpu_clear_walls", "vgpu_point_inside_walls",
     "vgpu_autotune", "vgpu_set_record_budget", "vgpu_phase_counts", "vgpu_set_fp64_fallback",
     "vgpu_get_input_rows", "vgpu_get_tuning", "vgpu_set_tuning_ex", "vgpu_autotune_ex",
+    "vgpu_get_tolerance",
 ]
 
 
@@ -139,6 +140,7 @@ def load_library(build_if_missing=True):
     lib.vgpu_set_ghost_depth.argtypes = [vp, ctypes.c_double]
     lib.vgpu_set_record_budget.argtypes = [vp, ctypes.c_int64]
     lib.vgpu_set_fp64_fallback.argtypes = [vp, ctypes.c_double]
+    lib.vgpu_get_tolerance.argtypes = [vp, pd]
     lib.vgpu_get_input_rows.argtypes = [vp, vp]
     lib.vgpu_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
     lib.vgpu_set_tuning_ex.argtypes = [vp, ctypes.POINTER(Tuning)]
@@ -199,6 +201,7 @@ class CellResults:
         self.rad = None   # stored radii (put's r), filled by cells()
         self.poly_off = None   # polytope CSR (VGPU_OUTPUT_POLYTOPES), filled by cells()
         self.poly_data = None
+        self.poly_tol = 0.0    # the container's length tolerance (vgpu_get_tolerance)
 
     def __len__(self):
         return len(self.ids)
@@ -215,21 +218,24 @@ class CellResults:
         if self.poly_off is None:
             raise ValueError("polytope output was not requested: call set_polytopes(True) before computing")
         a, b = self.poly_off[k], self.poly_off[k + 1]
-        return Polytope.from_stream(self.poly_data[a:b]) if b > a else None
+        return Polytope.from_stream(self.poly_data[a:b], self.poly_tol) if b > a else None
 
 
 class Polytope:
     """One cell's polytope as the engine returns it (VGPU_OUTPUT_POLYTOPES):
     vertices relative to the particle and faces as vertex loops, ordered by
     neighbour ID like ``neighbors()``.  The query names follow
-    voronoicell_base (src/cell.hh:132-211) and compute the same quantities."""
+    voronoicell_base (src/cell.hh:132-211) and compute the same quantities.
+    ``tol`` is the container's length tolerance (vgpu_get_tolerance), the
+    threshold below which normals() reports a face's normal as zero."""
 
-    def __init__(self, verts, faces):
+    def __init__(self, verts, faces, tol=0.0):
         self.verts = verts                      # (nv, 3)
         self.faces = faces                      # [(neighbour, [vertex indices])]
+        self.tol = float(tol)
 
     @classmethod
-    def from_stream(cls, d):
+    def from_stream(cls, d, tol=0.0):
         nv, nf = int(d[0]), int(d[1])
         verts = np.asarray(d[2:2 + 3 * nv]).reshape(nv, 3)
         faces = []
@@ -239,7 +245,7 @@ class Polytope:
             faces.append((nb, [int(v) for v in d[i + 2:i + 2 + m]]))
             i += 2 + m
         faces.sort(key=lambda f: f[0])          # stable: the order of neighbors()
-        return cls(verts, faces)
+        return cls(verts, faces, tol)
 
     @property
     def p(self):
@@ -267,12 +273,31 @@ class Polytope:
         return [0.5 * float(np.linalg.norm(self._newell(f[1]))) for f in self.faces]
 
     def normals(self):
-        """Outward unit normals (the loops run clockwise seen from outside)."""
+        """Outward unit normals, by the rule of voronoicell_base::normals_search
+        (src/cell.cc:2108-2164): walking the loop from its second edge, the
+        first edge longer than the tolerance is paired with each later edge
+        until their vector product is above it; that product, normalised, is
+        the normal.  A face with no such pair (a sliver, or one whose edges
+        are all shorter than the tolerance) gets (0, 0, 0).  The tests are on
+        the reference's doubled coordinates (2x these vertices)."""
         out = []
         for f in self.faces:
-            nrm = -self._newell(f[1])
-            ln = float(np.linalg.norm(nrm))
-            out.append(tuple(nrm / ln) if ln > 0 else (0.0, 0.0, 0.0))
+            loop = f[1]
+            P = self.verts[loop]
+            E = np.roll(P, -1, axis=0) - P             # edge t: loop[t] -> loop[t+1]
+            n = len(loop)
+            nrm = (0.0, 0.0, 0.0)
+            for t in range(1, n):
+                u = E[t]
+                if 4.0 * float(u @ u) > self.tol:
+                    for s in range(t + 1, n):
+                        w = np.cross(E[s], u)
+                        wm = 16.0 * float(w @ w)
+                        if wm > self.tol:
+                            nrm = tuple(w / np.sqrt(float(w @ w)))
+                            break
+                    break
+            out.append(nrm)
         return out
 
     def face_perimeters(self):
@@ -317,6 +342,9 @@ class _ContainerBase:
         gr = (ctypes.c_int * 3)(*[int(v) for v in grid])
         pe = (ctypes.c_int * 3)(*[1 if p else 0 for p in periodic])
         _check(self._lib.vgpu_container_create(ctypes.byref(self._h), kind, g, gr, pe))
+        t = ctypes.c_double(0.0)
+        _check(self._lib.vgpu_get_tolerance(self._h, ctypes.byref(t)))
+        self.tol = t.value
         self.kind = kind
         self.geom = tuple(float(v) for v in geom)
         self.grid = tuple(int(v) for v in grid)
@@ -571,7 +599,7 @@ class _ContainerBase:
             _check(self._lib.vgpu_get_ghost_polytopes(self._h, _ptr(poff), None))
             data = np.zeros(max(int(poff[-1]), 1))
             _check(self._lib.vgpu_get_ghost_polytopes(self._h, _ptr(poff), _ptr(data)))
-            res.poly_off, res.poly_data = poff, data
+            res.poly_off, res.poly_data, res.poly_tol = poff, data, self.tol
         return res
 
     def find_voronoi_cell(self, x, y, z):
@@ -656,7 +684,7 @@ class _ContainerBase:
             _check(self._lib.vgpu_get_polytopes(self._h, _ptr(poff), None))
             data = np.zeros(max(int(poff[-1]), 1))
             _check(self._lib.vgpu_get_polytopes(self._h, _ptr(poff), _ptr(data)))
-            res.poly_off, res.poly_data = poff, data
+            res.poly_off, res.poly_data, res.poly_tol = poff, data, self.tol
         return res
 
     # ---- print_custom: src/container.hh:434-451, src/cell.cc:2485-2558

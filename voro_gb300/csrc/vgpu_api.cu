@@ -719,6 +719,12 @@ int vgpu_set_fp64_fallback(vgpu_container *h, double fraction) {
     return VGPU_OK;
 }
 
+int vgpu_get_tolerance(vgpu_container *h, double *tol) {
+    if (!h || !tol) return fail(VGPU_ERR_ARG, "null argument");
+    *tol = 2.0 * h->g.tol_h;   // tol_h holds half of it (exact in binary)
+    return VGPU_OK;
+}
+
 int vgpu_set_record_budget(vgpu_container *h, int64_t bytes) {
     if (!h || bytes < 0) return fail(VGPU_ERR_ARG, "bad record budget");
     h->record_bytes = bytes;

@@ -195,36 +195,42 @@ class voronoicell {
     // outward unit normals, three per face, by the rule of
     // voronoicell_base::normals_search (src/cell.cc:2108-2164): from the
     // loop's second edge on, the first edge longer than the tolerance is
-    // paired with each later edge until their vector product is above it;
-    // a face without such a pair (a sliver) gets (0, 0, 0).  The tests are
-    // on the reference's doubled coordinates, 2x these vertices.
+    // paired with each later edge until their vector product is above it.
+    // The tests are on the reference's doubled coordinates, 2x these
+    // vertices.  The reference starts at its lowest-numbered vertex of the
+    // face, a numbering the engine does not share: each start is tried in
+    // turn, and a face gets (0, 0, 0) only when none finds such a pair.
     void normals(std::vector<double> &v) const {
         need_poly();
         v.assign(3 * fstart_.size(), 0.0);
         for (size_t f = 0; f < fstart_.size(); f++) {
             const int m = forder(f);
             auto edge = [&](int t, double e[3]) {
-                const double *a = vert(floops_[fstart_[f] + t]);
+                const double *a = vert(floops_[fstart_[f] + t % m]);
                 const double *b = vert(floops_[fstart_[f] + (t + 1) % m]);
                 for (int c = 0; c < 3; c++) e[c] = b[c] - a[c];
             };
-            for (int t = 1; t < m; t++) {
-                double u[3];
-                edge(t, u);
-                if (4.0 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) <= tol_) continue;
-                for (int s = t + 1; s < m; s++) {
-                    double e[3];
-                    edge(s, e);
-                    const double w[3] = {e[1] * u[2] - e[2] * u[1], e[2] * u[0] - e[0] * u[2],
-                                         e[0] * u[1] - e[1] * u[0]};
-                    const double wm = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
-                    if (16.0 * wm > tol_) {
-                        const double r = 1.0 / std::sqrt(wm);
-                        for (int c = 0; c < 3; c++) v[3 * f + c] = w[c] * r;
-                        break;
+            bool found = false;
+            for (int r = 0; r < m && !found; r++) {
+                for (int t = 1; t < m; t++) {
+                    double u[3];
+                    edge(r + t, u);
+                    if (4.0 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) <= tol_) continue;
+                    for (int s = t + 1; s < m; s++) {
+                        double e[3];
+                        edge(r + s, e);
+                        const double w[3] = {e[1] * u[2] - e[2] * u[1], e[2] * u[0] - e[0] * u[2],
+                                             e[0] * u[1] - e[1] * u[0]};
+                        const double wm = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+                        if (16.0 * wm > tol_) {
+                            const double q = 1.0 / std::sqrt(wm);
+                            for (int c = 0; c < 3; c++) v[3 * f + c] = w[c] * q;
+                            found = true;
+                            break;
+                        }
                     }
+                    break;
                 }
-                break;
             }
         }
     }

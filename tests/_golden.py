@@ -174,6 +174,25 @@ def reference_tol(w):
     return 10.0 * np.finfo(np.float64).eps * m
 
 
+def normal_start_dependent(verts, loop, tol):
+    """Whether the reference's normals_search (src/cell.cc:2108-2164) finds
+    a normal for this face from some loop vertices and none from others: its
+    answer then rests on its own vertex numbering."""
+    P = np.asarray(verts)[loop]
+    E = np.roll(P, -1, axis=0) - P
+    n = len(loop)
+
+    def found(r):
+        for t in range(1, n):
+            u = E[(r + t) % n]
+            if 4.0 * (u @ u) > tol:
+                return any(16.0 * float(np.sum(np.cross(E[(r + s) % n], u) ** 2)) > tol for s in range(t + 1, n))
+        return False
+
+    outcomes = {found(r) for r in range(n)}
+    return len(outcomes) == 2
+
+
 def box_volume(w):
     g = w["geom"]
     if w["kind"] in (0, 1):

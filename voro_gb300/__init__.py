@@ -277,28 +277,38 @@ class Polytope:
         (src/cell.cc:2108-2164): walking the loop from its second edge, the
         first edge longer than the tolerance is paired with each later edge
         until their vector product is above it; that product, normalised, is
-        the normal.  A face with no such pair (a sliver, or one whose edges
-        are all shorter than the tolerance) gets (0, 0, 0).  The tests are on
-        the reference's doubled coordinates (2x these vertices)."""
+        the normal.  The tests are on the reference's doubled coordinates (2x
+        these vertices).  The reference walks from its lowest-numbered vertex
+        of the face, a numbering the engine does not share; so each start is
+        tried in turn, and a face gets (0, 0, 0) only when no start finds
+        such a pair (a sliver, or a face whose edges are all shorter than the
+        tolerance), where the reference's answer cannot depend on its start."""
         out = []
         for f in self.faces:
-            loop = f[1]
-            P = self.verts[loop]
+            P = self.verts[f[1]]
             E = np.roll(P, -1, axis=0) - P             # edge t: loop[t] -> loop[t+1]
-            n = len(loop)
+            n = len(P)
             nrm = (0.0, 0.0, 0.0)
-            for t in range(1, n):
-                u = E[t]
-                if 4.0 * float(u @ u) > self.tol:
-                    for s in range(t + 1, n):
-                        w = np.cross(E[s], u)
-                        wm = 16.0 * float(w @ w)
-                        if wm > self.tol:
-                            nrm = tuple(w / np.sqrt(float(w @ w)))
-                            break
+            for r in range(n):
+                w = self._normal_walk(E, n, r)
+                if w is not None:
+                    nrm = tuple(w / np.sqrt(float(w @ w)))
                     break
             out.append(nrm)
         return out
+
+    def _normal_walk(self, E, n, r):
+        """normals_search from loop vertex r: the first edge product above the
+        tolerance, or None."""
+        for t in range(1, n):
+            u = E[(r + t) % n]
+            if 4.0 * float(u @ u) > self.tol:
+                for s in range(t + 1, n):
+                    w = np.cross(E[(r + s) % n], u)
+                    if 16.0 * float(w @ w) > self.tol:
+                        return w
+                return None
+        return None
 
     def face_perimeters(self):
         out = []

@@ -150,8 +150,7 @@ struct WarpShared {
     float4 pe[PlaneSlots<K>::N];   // |n|, en (abs error of n), eh (abs error of h), |h|
     // (pl and pe are contiguous: at the end of a cell they hold the FP64 planes)
     double4 pl64x[MODE == VGPU_FP64 ? PlaneSlots<K>::N : 1];   // FP64 planes (FP64 engine, during the search)
-    int pid[PlaneSlots<K>::N];     // neighbour ID of an initial face or wall, or of a relabelled face
-    unsigned relab[PlaneSlots<K>::W];   // planes whose face took another ID (pid holds it)
+    int pid[PlaneSlots<K>::N];     // neighbour ID of the plane
     int psrc[PlaneSlots<K>::N];    // engine index of the generating particle, -1 for initial faces
     int pshift[PlaneSlots<K>::N];  // packed periodic image counts (initial faces: face index)
     unsigned tri[32 * K];
@@ -169,6 +168,7 @@ struct WarpShared {
             unsigned ck[kCandBuf];    // sort keys
             int cj[kCandBuf];         // engine index
             int cs[kCandBuf];         // packed periodic image counts
+            int cpid[kCandBuf];       // neighbour ID
             float4 cd[kCandBuf];      // plane (FP32): n, h
             float4 ce[kCandBuf];      // en, eh, |n|, rs
             double4 cd64[MODE == VGPU_FP64 ? kCandBuf : 1];  // plane (FP64), FP64 engine
@@ -491,7 +491,6 @@ struct Engine {
             S.psrc[lane] = -1;
             S.pshift[lane] = lane;
         }
-        if (!kLean && lane < PlaneSlots<K>::W) S.relab[lane] = 0u;
         Vm.clear();
         Vm.r[0] = 0xffu;
 #pragma unroll
@@ -551,6 +550,7 @@ struct Engine {
             S.u.c.ck[slot] = (float_key(ce.w) & ~63u) | (unsigned)slot;
             S.u.c.cj[slot] = -1;
             S.u.c.cs[slot] = 6 + lane;
+            S.u.c.cpid[slot] = P.walls[lane].id;
             S.u.c.cd[slot] = cd;
             S.u.c.ce[slot] = ce;
             if (MODE == VGPU_FP64) S.u.c.cd64[slot] = q;
@@ -622,10 +622,6 @@ struct Engine {
     //      takes the candidate's ID, as the reference's facet construction
     //      through vertices on the plane relabels it (src/cell.cc:1166-1355).
     //      band: this lane's slots in the band.
-    __device__ __forceinline__ int candidate_id(int cb) const {
-        const int cj = S.u.c.cj[cb];
-        return cj >= 0 ? P.a.pid[cj] : P.walls[S.u.c.cs[cb] - 6].id;
-    }
     __device__ void relabel_coplanar(int cb, unsigned band) {
         constexpr int NW = PlaneSlots<K>::W;
         if constexpr (NW == 2) {
@@ -641,10 +637,8 @@ struct Engine {
                 }
             const unsigned long long faces = warp_or64(on) & ~warp_or64(off);
             if (lane == 0 && faces) {
-                const int id = candidate_id(cb);
+                const int id = S.u.c.cpid[cb];
                 for (unsigned long long m = faces; m; m &= m - 1ull) S.pid[__ffsll((long long)m) - 1] = id;
-                S.relab[0] |= (unsigned)faces;
-                S.relab[1] |= (unsigned)(faces >> 32);
             }
         } else {
             unsigned on[NW], off[NW];
@@ -660,14 +654,12 @@ struct Engine {
                         else plane_set_add(off, tri_plane(t, e));
                     }
                 }
-            const int id = lane == 0 ? candidate_id(cb) : 0;
+            const int id = S.u.c.cpid[cb];
 #pragma unroll
             for (int w = 0; w < NW; w++) {
                 const unsigned faces = __reduce_or_sync(kFull, on[w]) & ~__reduce_or_sync(kFull, off[w]);
-                if (lane == 0) {
+                if (lane == 0)
                     for (unsigned m = faces; m; m &= m - 1u) S.pid[32 * w + __ffs((int)m) - 1] = id;
-                    S.relab[w] |= faces;
-                }
             }
         }
         __syncwarp();
@@ -749,9 +741,7 @@ struct Engine {
             const int j = S.u.c.cj[cb];
             S.pl[p] = Q;
             S.pe[p] = make_float4(E.z, E.x, E.y, fabsf(Q.w));
-            // a particle's ID is read when the record is written; a wall's is here
-            if (j < 0) S.pid[p] = P.walls[S.u.c.cs[cb] - 6].id;
-            if (!kLean) S.relab[p >> 5] &= ~(1u << (p & 31));
+            S.pid[p] = S.u.c.cpid[cb];
             S.psrc[p] = j;
             S.pshift[p] = S.u.c.cs[cb];
             if (MODE == VGPU_FP64) S.pl64x[p] = S.u.c.cd64[cb];
@@ -1099,6 +1089,7 @@ struct Engine {
                     S.u.c.ck[slot] = (key & ~63u) | (unsigned)slot;
                     S.u.c.cj[slot] = j;
                     S.u.c.cs[slot] = o_code;
+                    S.u.c.cpid[slot] = P.a.pid[j];
                     S.u.c.cd[slot] = cd;
                     S.u.c.ce[slot] = ce;
                     if (MODE == VGPU_FP64) S.u.c.cd64[slot] = plane64_from(P, C.me64, j, o_code);
@@ -1302,10 +1293,7 @@ struct Engine {
                 const int r = S.endN[q];
                 VGPU_RECORD_STORE(&rp[r], (unsigned)S.psrc[q]);
                 VGPU_RECORD_STORE(&rp[nf + r], (unsigned)S.pshift[q]);
-                const int src = S.psrc[q];
-                bool own = src >= 0;
-                if (!kLean && own) own = ((S.relab[h] >> lane) & 1u) == 0u;
-                VGPU_RECORD_STORE(&rp[2 * nf + r], (unsigned)(own ? P.a.pid[src] : S.pid[q]));
+                VGPU_RECORD_STORE(&rp[2 * nf + r], (unsigned)S.pid[q]);
             }
         }
         if (lane == 0) P.rec_off[C.k] = off;

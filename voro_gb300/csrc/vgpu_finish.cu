@@ -802,7 +802,8 @@ constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
 // of shared memory per CTA (a warp's two 16-lane cells share the space of
 // one 128-vertex cell) registers decide.  Measured on the 4M periodic box,
 // finish kernel: 6 (148 registers, so 6 CTAs resident) 14.1 ms; 7 (128
-// registers, a few spilled bytes, 8 CTAs resident) 12.3 ms.  (Before the
+// registers, a few spilled bytes, 8 CTAs resident) 12.3 ms; 9 (96 registers,
+// 468 bytes spilled, 10 CTAs resident) 15.1 ms against 12.2.  (Before the
 // coincident-vertex merge and the second correction step the kernel fitted
 // 124 registers: 8 CTAs, 11.0 ms.)
 #ifndef VGPU_FIN_MIN_BLOCKS

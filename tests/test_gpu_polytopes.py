@@ -76,6 +76,14 @@ def test_polytopes_match_reference(gpu, tmp_path, name, mode):
     assert not errs, "\n".join(errs[:10])
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", G.poly_names())
+def test_container_tolerance_is_the_references(gpu, name):
+    w, _ = G.load(name)
+    con = vg.from_workload(w, mode="mixed")
+    assert con.tol == pytest.approx(G.reference_tol(w), rel=1e-15, abs=0.0)
+
+
 def _orders_sorted(text, fmt):
     """The vertex-order list %o (the format's last field, one entry per vertex
     in vertex-numbering order) as a sorted multiset: the engine numbers the

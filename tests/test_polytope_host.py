@@ -37,3 +37,16 @@ def test_polytope_queries_match_reference(name):
         assert sum(pt.face_freq_table()) == len(c["faces"])
         checked += 1
     assert checked > 0
+
+
+def test_normals_follow_the_tolerance():
+    # the z = 0 face of the unit cube, clockwise seen from below (outside)
+    verts = np.array([[x, y, 0.0] for y in (0.0, 1.0) for x in (0.0, 1.0)])
+    face = [(-5, [0, 1, 3, 2])]
+    assert np.allclose(vg.Polytope(verts, face).normals()[0], (0.0, 0.0, -1.0))
+    # edges of doubled length 2 (4 |e|^2 = 4) and products of 16: a
+    # tolerance above both leaves no pair, one between them none either
+    assert vg.Polytope(verts, face, tol=5.0).normals()[0] == (0.0, 0.0, 0.0)
+    assert vg.Polytope(verts, face, tol=17.0).normals()[0] == (0.0, 0.0, 0.0)
+    assert np.allclose(vg.Polytope(verts, face, tol=3.0).normals()[0], (0.0, 0.0, -1.0))
+

@@ -44,8 +44,9 @@ def test_normals_follow_the_tolerance():
     verts = np.array([[x, y, 0.0] for y in (0.0, 1.0) for x in (0.0, 1.0)])
     face = [(-5, [0, 1, 3, 2])]
     assert np.allclose(vg.Polytope(verts, face).normals()[0], (0.0, 0.0, -1.0))
-    # edges of doubled length 2 (4 |e|^2 = 4) and products of 16: a
-    # tolerance above both leaves no pair, one between them none either
+    # in doubled coordinates the edges' squared lengths are 4 and their
+    # products' 16: a tolerance of 5 (or 17) leaves no first edge, one of 3
+    # keeps the normal
     assert vg.Polytope(verts, face, tol=5.0).normals()[0] == (0.0, 0.0, 0.0)
     assert vg.Polytope(verts, face, tol=17.0).normals()[0] == (0.0, 0.0, 0.0)
     assert np.allclose(vg.Polytope(verts, face, tol=3.0).normals()[0], (0.0, 0.0, -1.0))

@@ -172,6 +172,21 @@ def load_profile_summary():
     return None
 
 
+def issue_roof(prof, n, clip_ms, sms, sm_mhz):
+    """The clipping kernel against the warp-instruction issue rate, the roof
+    that binds it (four warp instructions per cycle per SM): the first
+    pass's warp instructions per cell from the ncu capture in profiles/,
+    times the cells, over the clipping time of both passes (CUDA events)."""
+    ipc = prof.get("warp_instructions_per_cell")
+    if ipc is None:
+        return None
+    peak = sms * 4 * sm_mhz * 1e6 / 1e12
+    achieved = ipc * n / (clip_ms / 1000.0) / 1e12
+    return {"unit": "T warp instructions/s", "achieved": achieved, "peak": peak, "frac": achieved / peak,
+            "instructions_per_cell": ipc, "peak_kind": f"nominal issue ({sms} SMs x 4 x {sm_mhz:.0f} MHz)",
+            "capture_issue_active": prof.get("issue_active")}
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -544,7 +559,8 @@ def run_ours(args):
                               "flops_per_cell": flops_cell,
                               "model": "F_cell = 6 T_cell + 40 V_cell; T_cell = reference side tests per cell "
                                        f"({t_ref if t_ref is not None else float('nan'):.1f}, CPU port on "
-                                       f"{t_cells} cells), V_cell = mean vertices ({v_mean:.2f})"}},
+                                       f"{t_cells} cells), V_cell = mean vertices ({v_mean:.2f})"},
+                     "issue": issue_roof(prof, n, cms, props.multi_processor_count, sm_mhz)},
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clocks,

@@ -319,7 +319,7 @@ int vgpu_set_ghost_depth(vgpu_container *h, double spacings);
  * vgpu_compute returns VGPU_ERR_CAPACITY.  Applies from the next compute. */
 int vgpu_set_record_budget(vgpu_container *h, int64_t bytes);
 
-/* Mixed computes judge the FP32 engine's first pass: a large container (at
+/* Mixed computes assess the FP32 engine's first pass: a large container (at
  * least 262,144 cells) runs it first on 1/64 of its cells, a smaller one on
  * all of them (and a batch member by its share of the batch's first pass).
  * If more than this fraction of those cells need FP64 (tests inside the

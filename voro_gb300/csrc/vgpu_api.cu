@@ -1394,14 +1394,14 @@ int compute_cells(vgpu_container *h, int mode, bool thin) {
         }
     }
     Counters c1;
-    // a container below the sampled size is judged by its whole first pass:
+    // a container below the sampled size is assessed on its whole first pass:
     // with the band saturated (a lattice jittered at the tolerance's scale,
     // where the FP32 engine's band handling met its limits) it reruns on the
     // FP64 engine like a sampled one
-    const bool judge_first = mode == VGPU_MIXED && h->fp64_fallback < 1.0 && cp.ncells < kSampleMinCells;
+    const bool whole_first = mode == VGPU_MIXED && h->fp64_fallback < 1.0 && cp.ncells < kSampleMinCells;
     rc = clip_passes(s, h->sms, h->warps_per_cta, mode, cp, h->counters2.as<Counters>(),
                      h->counters2.as<Counters>() + 1, h->ovf_list2.as<int>(), c1, first,
-                     judge_first ? h->fp64_fallback : -1.0);
+                     whole_first ? h->fp64_fallback : -1.0);
     if (rc == kSwitchToFp64) {
         mode = VGPU_FP64;
         switched = true;
@@ -2279,7 +2279,7 @@ int vgpu_batch_compute(vgpu_batch *b, int mode) {
         if (mode == VGPU_MIXED && h->fp64_fallback < 1.0 && h->nkept > 0 &&
             (double)cs[i].overflow > h->fp64_fallback * h->nkept) {
             // the member's filter band was saturated (more than the fallback
-            // fraction of its cells handed on, as a single compute judges
+            // fraction of its cells handed on, as a single compute assesses
             // it): the member alone again, on the FP64 engine
             rc = compute_cells(h, VGPU_FP64, false);
             h->stats.fp64_engine_cells = h->nkept;

@@ -42,9 +42,41 @@ def tolerance(name, mode, default):
 def names():
     """The per-cell record fixtures (poly_*.npz hold polytopes, see load_poly;
     locate_*.npz point-location answers, see load_locate; ghost_*.npz ghost
-    cells, see load_ghost)."""
+    cells, see load_ghost; normals_*.npz print_custom normals, see
+    load_normals)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "*.npz"))
-                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_", "wall_", "cli_")))
+                  if not os.path.basename(p).startswith(("poly_", "locate_", "ghost_", "wall_", "cli_", "normals_")))
+
+
+def normal_names():
+    return sorted(os.path.basename(p)[8:-4] for p in glob.glob(os.path.join(HERE, "normals_*.npz")))
+
+
+def load_normals(name):
+    """The reference's print_custom text of fixture ``name`` for "%i %n %l"
+    (format, text)."""
+    with np.load(os.path.join(HERE, f"normals_{name}.npz")) as z:
+        return str(z["custom_format"]), str(z["custom_text"])
+
+
+def face_normals_by_neighbour(text):
+    """Per particle ID of a "%i %n %l" print_custom text: its faces as
+    (neighbour, (nx, ny, nz)) pairs, sorted."""
+    out = {}
+    for line in text.splitlines():
+        f = line.split()
+        if not f:
+            continue
+        pid = int(f[0])
+        rest = f[1:]
+        nf = len(rest) // 2   # nf neighbour IDs, then nf "(x,y,z)" normals
+        nbs = [int(v) for v in rest[:nf]]
+        nrms = []
+        for tok in rest[nf:]:
+            x, y, z = (float(v) for v in tok.strip("()").split(","))
+            nrms.append((x, y, z))
+        out[pid] = sorted(zip(nbs, nrms))
+    return out
 
 
 def wall_names():

@@ -326,6 +326,27 @@ def make_poly_fixtures(ref, all_cases, names=None):
         print(f"poly_{name}: {len(cells)} cells, {os.path.getsize(out)} bytes")
 
 
+# Normal fixtures: the reference's print_custom of "%i %n %l" over every cell,
+# each face's neighbour beside its normal, so that a test can pair them
+# whatever the face order (faces whose normals_search finds no pair above
+# the tolerance print 0 0 0).
+NORMAL_FORMAT = "%i %n %l"
+NORMAL_NAMES = ["unit_cube_1000", "radical_1200", "periodic_poly_800", "edge_box_boundaries_296",
+                "edge_far_box_500"]
+
+
+def make_normal_fixtures(ref, all_cases):
+    import tempfile
+    for name in NORMAL_NAMES:
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "custom.txt")
+            ref.print_custom(all_cases[name], NORMAL_FORMAT, path)
+            text = open(path).read()
+        out = os.path.join(HERE, f"normals_{name}.npz")
+        np.savez_compressed(out, custom_format=np.array(NORMAL_FORMAT), custom_text=np.array(text))
+        print(f"normals_{name}: {os.path.getsize(out)} bytes")
+
+
 # Point-location fixtures: query points and the reference's find_voronoi_cell
 # answer for each (found flag, particle ID, returned particle position): points
 # spread over the domain grown by 20% on every side (outside a non-periodic
@@ -490,12 +511,16 @@ def main():
             make_cell_fixture(ref, name, w)
         make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
         return
+    if "--normals-only" in sys.argv:
+        make_normal_fixtures(ref, {**cases(), **edge_cases()})
+        return
     if "--tric-large-only" in sys.argv:
         make_tric_large_fixture(ref)
         return
     for name, w in cases().items():
         make_cell_fixture(ref, name, w)
     make_poly_fixtures(ref, cases())
+    make_normal_fixtures(ref, {**cases(), **edge_cases()})
     make_locate_fixtures(ref, cases())
     make_ghost_fixtures(ref, cases())
     make_wall_fixtures(ref)

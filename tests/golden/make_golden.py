@@ -183,6 +183,17 @@ def edge_cases():
     # a periodic box so small that a cell's neighbours are mostly images
     xyz = rng.random((20, 3)) * 0.5
     out["edge_periodic_small_box_20"] = W._pack(W.KIND_PERIODIC, (0.5, 0, 0.5, 0, 0, 0.5), (2, 2, 2), (True,) * 3, xyz)
+    # voids: a slab of particles in a box periodic across it (the cells
+    # reach through the empty part to the slab's images, some 20 engine
+    # blocks away), and three tight clusters in a periodic box with a few
+    # particles between them (cells spanning much of the box)
+    xyz = rng.random((9000, 3)) * np.array([0.2, 1.0, 1.0])
+    out["edge_slab_periodic_9000"] = W._pack(W.KIND_CONTAINER, (0, 1, 0, 1, 0, 1), (14, 14, 14),
+                                             (True, False, False), xyz)
+    cen = rng.random((3, 3))
+    xyz = np.mod(cen[rng.integers(0, 3, 6000)] + rng.normal(0.0, 0.02, (6000, 3)), 1.0)
+    xyz = np.concatenate([xyz, rng.random((8, 3))])
+    out["edge_voids_periodic_6008"] = W._pack(W.KIND_PERIODIC, (1, 0, 1, 0, 0, 1), (12, 12, 12), (True,) * 3, xyz)
     return out
 
 

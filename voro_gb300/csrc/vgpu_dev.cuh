@@ -5,6 +5,23 @@
 
 namespace vgpu {
 
+// Block offset e (0 <= e < 6 (2r+1)^2) on the surface of the cube of
+// Chebyshev radius r, walked face by face (face e / (2r+1)^2: axis f >> 1,
+// side f & 1) without branches.  Returns false for the copies of an edge or
+// corner block: each surface block is taken once, by the face of its lowest
+// axis.
+__device__ __forceinline__ bool shell_offset(int e, int r, int &di, int &dj, int &dk) {
+    const int A = 2 * r + 1, AA = A * A;
+    const int f = e / AA, q = e - f * AA;
+    const int u = q % A - r, v = q / A - r;
+    const int ax = f >> 1, s = (f & 1) ? r : -r;
+    di = ax == 0 ? s : u;
+    dj = ax == 1 ? s : (ax == 0 ? u : v);
+    dk = ax == 2 ? s : v;
+    return !(ax > 0 && abs(di) == r) && !(ax > 1 && abs(dj) == r);
+}
+
+
 static constexpr float kU32 = 5.9604645e-08f;          // 2^-24
 static constexpr double kU64 = 1.1102230246251565e-16; // 2^-53
 static constexpr unsigned kFull = 0xffffffffu;

@@ -398,6 +398,13 @@ struct Engine {
     // the two FP64 calls the kernel needs 80 registers instead of 168 (6 CTAs
     // per SM instead of 3).
     static constexpr bool kLean = LEAN && MODE == VGPU_MIXED;
+    // The 64-slot engines walk each shell beyond the table as its whole cube
+    // (no branches: the fastest at the small radii nearly every search ends
+    // at) up to kNarrowShellRadius, and hand on a cell that searches further;
+    // the 128-slot engines walk only the cubes' faces, up to kMaxShellRadius.
+    // (The face walk in the 64-slot engines cost 1.2 ms of 66.4 on the 4M
+    // periodic box, a branching one 7 ms.)
+    static constexpr bool kWideSearch = K >= 4;
     const CellParams &P;
     WarpShared<MODE, K> &S;
     const int *offsets;   // shared copy of the offset table
@@ -947,6 +954,11 @@ struct Engine {
     }
 #endif
 
+    // a block offset in one word: 10 bits per axis (|offset| <= kMaxShellRadius)
+    __device__ __forceinline__ static int pack_offset(int di, int dj, int dk) {
+        return (di + kShellPack) | ((dj + kShellPack) << 10) | ((dk + kShellPack) << 20);
+    }
+
     // ---- candidates from a range of block offsets: wrap/skip, block distance,
     //      then one lane per candidate particle
     __device__ void gather_offsets(int e_begin, int e_end, bool from_table, int shell_r) {
@@ -963,13 +975,19 @@ struct Engine {
                     dj = ((code >> 5) & 31) - 16;
                     dk = ((code >> 10) & 31) - 16;
                 } else {
-                    const int w = 2 * shell_r + 1;
-                    di = e % w - shell_r;
-                    dj = (e / w) % w - shell_r;
-                    dk = e / (w * w) - shell_r;
-                    const int m = max(abs(di), max(abs(dj), abs(dk)));
+                    // (at radius kOffsetRadius the table already holds the
+                    // offsets of lower bound <= kTableLb2Max)
+                    if constexpr (kWideSearch) {
+                        ok = shell_offset(e, shell_r, di, dj, dk);   // the cube's faces
+                    } else {   // the whole cube, without branches
+                        const int w = 2 * shell_r + 1;
+                        di = e % w - shell_r;
+                        dj = (e / w) % w - shell_r;
+                        dk = e / (w * w) - shell_r;
+                        ok = max(abs(di), max(abs(dj), abs(dk))) == shell_r;
+                    }
                     const int a = max(abs(di) - 1, 0), b = max(abs(dj) - 1, 0), c = max(abs(dk) - 1, 0);
-                    ok = (m == shell_r) && (a * a + b * b + c * c > kTableLb2Max);
+                    ok = ok && (a * a + b * b + c * c > kTableLb2Max);
                 }
             }
             int cnt = 0, st = 0, code = 0;
@@ -1013,7 +1031,7 @@ struct Engine {
             }
             const int incl = warp_incl_scan(cnt, lane);
             const int tot = __shfl_sync(kFull, incl, 31);
-            const int packed_d = (di + 16) | ((dj + 16) << 5) | ((dk + 16) << 10);
+            const int packed_d = pack_offset(di, dj, dk);
 #if VGPU_GATHER_TMA
             int w0 = 0;
             bool staged = false;
@@ -1051,7 +1069,8 @@ struct Engine {
                 float4 cd = make_float4(0, 0, 0, 0), ce = make_float4(0, 0, 0, 0);
                 const int j = o_st + (c - (o_incl - o_cnt));
                 if (c < tot) {
-                    const int ddi = (o_d & 31) - 16, ddj = ((o_d >> 5) & 31) - 16, ddk = ((o_d >> 10) & 31) - 16;
+                    const int ddi = (o_d & 1023) - kShellPack, ddj = ((o_d >> 10) & 1023) - kShellPack,
+                              ddk = ((o_d >> 20) & 1023) - kShellPack;
                     const bool self = (j == C.k) && ddi == 0 && ddj == 0 && ddk == 0;
                     if (!self) {
 #if VGPU_GATHER_TMA
@@ -1108,7 +1127,7 @@ struct Engine {
         const float bmin2 = P.g.gbs_min * P.g.gbs_min;
         const int rmax_grid = max(P.g.gn[0], max(P.g.gn[1], P.g.gn[2]));
         const bool any_periodic = P.g.per[0] || P.g.per[1] || P.g.per[2];
-        const int rlim = min(4 * rmax_grid + 8, 40);
+        const int rlim = min(4 * rmax_grid + 8, kWideSearch ? kMaxShellRadius : kNarrowShellRadius);
         for (int seg = 0;; seg++) {
             const bool table = seg < P.ngroups;
             int b0 = 0, b1 = 0, r = 0;
@@ -1126,7 +1145,7 @@ struct Engine {
                 }
                 if (!any_periodic && r > rmax_grid + 1) return;
                 lb2 = (float)((r - 1) * (r - 1)) * bmin2;
-                b1 = (2 * r + 1) * (2 * r + 1) * (2 * r + 1);
+                b1 = kWideSearch ? 6 * (2 * r + 1) * (2 * r + 1) : (2 * r + 1) * (2 * r + 1) * (2 * r + 1);
             }
             if (lb2 >= C.cutoff2 * (1.0f + 1e-5f)) return;
             PHASE_COUNT(6, 1);

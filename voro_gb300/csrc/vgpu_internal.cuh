@@ -37,6 +37,14 @@ constexpr int kStageEntries = 64;   // staged candidate particles per warp (VGPU
 constexpr int kNbStride = 32;
 constexpr int kOffsetRadius = 4;   // engine search table covers Chebyshev radius <= 4
 constexpr int kTableLb2Max = 15;   // ... and lower-bound shells lb2 <= 15 (complete there)
+// Beyond the table the search walks Chebyshev shells of blocks: the 64-slot
+// engines up to kNarrowShellRadius (they hand a cell that reaches further to
+// the next engine), the 128-slot engines up to kMaxShellRadius (a cell
+// reaching further fails with VGPU_FAIL_SEARCH).  A candidate's block offset
+// travels packed in 10 bits per axis, offset by kShellPack.
+constexpr int kNarrowShellRadius = 40;
+constexpr int kMaxShellRadius = 500;
+constexpr int kShellPack = 512;
 constexpr int kMaxGroups = 16;
 
 // Geometry of one container, in the reference's own terms plus the engine's

@@ -164,14 +164,13 @@ __global__ void locate_kernel(const __grid_constant__ CellParams P, int n, const
         // offsets the table leaves out)
         const int rmax_grid = max(g.gn[0], max(g.gn[1], g.gn[2]));
         const bool any_periodic = g.per[0] || g.per[1] || g.per[2];
-        const int rlim = min(4 * rmax_grid + 8, 40);
+        const int rlim = min(4 * rmax_grid + 8, kMaxShellRadius);
         for (int r = kOffsetRadius; !done && r < rlim; r++) {
             if (!any_periodic && r > rmax_grid + 1) break;
             if ((double)((r - 1) * (r - 1)) * bmin2 * (1.0 - 1e-12) > B.d + rmax2) break;
-            const int w = 2 * r + 1;
-            for (int e = 0; e < w * w * w; e++) {
-                const int di = e % w - r, dj = (e / w) % w - r, dk = e / (w * w) - r;
-                if (max(abs(di), max(abs(dj), abs(dk))) != r) continue;
+            for (int e = 0; e < 6 * (2 * r + 1) * (2 * r + 1); e++) {
+                int di, dj, dk;
+                if (!shell_offset(e, r, di, dj, dk)) continue;
                 const int x = max(abs(di) - 1, 0), y = max(abs(dj) - 1, 0), z = max(abs(dk) - 1, 0);
                 if (r == kOffsetRadius && x * x + y * y + z * z <= kTableLb2Max) continue;
                 scan_block(P, eb, c, loc, di, dj, dk, rmax2, B);

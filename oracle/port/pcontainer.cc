@@ -395,10 +395,9 @@ struct Container {
     // Flat block storage.  For periodic boxes the ghost blocks are shifted
     // copies of the primary blocks, in their order (src/container_prd.cc:
     // 551-554,583-774, rectangular case).  The reference creates them lazily;
-    // here they are built up front, all of them when that is cheap, else the
-    // first `kGhostDepth` layers (cells reaching further are not expected for
-    // the inputs this oracle is used on, and are reported by deep_access).
-    static constexpr int kGhostDepth = 6;
+    // here they are all built up front (for a rectangular box at most about
+    // nine times the primary particles): a cell beside a void reaches across
+    // most of the box, to images many layers deep.
     void finalize() {
         bstart.assign(nblocks + 1, 0);
         auto src_of = [&](int b, int &sb, int &aj, int &ak) {
@@ -414,11 +413,8 @@ struct Container {
             return true;
         };
         if (prd) {
-            long long full = 0, primary = 0;
-            for (auto &v : sid) primary += (long long)v.size();
-            full = primary * (long long)oy * oz / ((long long)ny * nz);
-            if (full <= 4 * primary + 100000) { ghost_y = ey; ghost_z = ez; }
-            else { ghost_y = std::min(ey, kGhostDepth); ghost_z = std::min(ez, kGhostDepth); }
+            ghost_y = ey;
+            ghost_z = ez;
         }
         for (int b = 0; b < nblocks; b++) {
             int sb, aj, ak;

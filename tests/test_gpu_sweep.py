@@ -58,3 +58,21 @@ def test_sweep_matches_port(gpu, port, c):
         errs = G.compare_cells(con.cells(), z, *TOL[mode], label=f"sweep {c}/{mode}")
         assert not errs, "\n".join(errs) + f"\nstats {st}"
         assert st["marginal_cells"] == 0 and st["failed_cells"] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_sweep_as_one_batch_matches_port(gpu, port, mode):
+    """The same containers as members of one batch (binned together, one
+    launch per pass): every member against the port."""
+    ws = [sweep_case(c) for c in range(CASES)]
+    cons = [vg.from_workload(w, mode=mode) for w in ws]
+    b = vg.batch(cons)
+    b.compute_all_cells(mode=mode)
+    for c, (w, con) in enumerate(zip(ws, cons)):
+        ref = port.compute(w)
+        nb = np.concatenate([np.sort(ref.neighbors(k)) for k in range(len(ref))])
+        z = {"ids": ref.ids, "pos": ref.pos, "vol": ref.vol, "cen": ref.cen, "nf": ref.nf, "nv": ref.nv,
+             "ok": ref.ok, "nb": nb, "nb_off": ref.nb_off}
+        errs = G.compare_cells(con.cells(), z, *TOL[mode], label=f"batch sweep {c}/{mode}")
+        assert not errs, "\n".join(errs)

@@ -313,6 +313,8 @@ POLY_CELLS = 200
 # boundaries)
 EDGE_POLY_NAMES = ["edge_far_box_500", "edge_cluster_1560", "edge_line_80", "edge_plane_150",
                    "edge_box_boundaries_296"]
+# point location in the void containers (queries deep inside the voids)
+EDGE_LOCATE_NAMES = ["edge_slab_periodic_9000", "edge_voids_periodic_6008"]
 CUSTOM_FORMAT = "%i %q %r %w %s %v %c %C %m %g %F %E %A %o"
 
 
@@ -521,6 +523,7 @@ def main():
         for name, w in ec.items():
             make_cell_fixture(ref, name, w)
         make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
+        make_locate_fixtures(ref, {k: ec[k] for k in EDGE_LOCATE_NAMES}, seed0=3900)
         return
     if "--normals-only" in sys.argv:
         make_normal_fixtures(ref, {**cases(), **edge_cases()})
@@ -541,6 +544,7 @@ def main():
     for name, w in ec.items():
         make_cell_fixture(ref, name, w)
     make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
+    make_locate_fixtures(ref, {k: ec[k] for k in EDGE_LOCATE_NAMES}, seed0=3900)
     make_cli_fixtures()
 
 

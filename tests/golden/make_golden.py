@@ -313,8 +313,12 @@ POLY_CELLS = 200
 # boundaries)
 EDGE_POLY_NAMES = ["edge_far_box_500", "edge_cluster_1560", "edge_line_80", "edge_plane_150",
                    "edge_box_boundaries_296"]
-# point location in the void containers (queries deep inside the voids)
+# point location and ghost cells in the void containers (queries and ghosts
+# deep inside the voids; a ghost in the slab container's void touches up to
+# 327 of the slab's particles, beyond the engines' 128 vertices, so only the
+# clustered one gets ghosts)
 EDGE_LOCATE_NAMES = ["edge_slab_periodic_9000", "edge_voids_periodic_6008"]
+EDGE_GHOST_NAMES = ["edge_voids_periodic_6008"]
 CUSTOM_FORMAT = "%i %q %r %w %s %v %c %C %m %g %F %E %A %o"
 
 
@@ -416,10 +420,10 @@ def ghost_particles(w, seed):
     return np.concatenate([xyz, rad[:, None]], 1)
 
 
-def make_ghost_fixtures(ref, all_cases, seed0=4000):
+def make_ghost_fixtures(ref, all_cases, seed0=4000, nb_per_cell=60):
     for i, (name, w) in enumerate(all_cases.items()):
         gx = ghost_particles(w, seed0 + i)
-        rec = ref.ghost_cells(w, gx)
+        rec = ref.ghost_cells(w, gx, nb_per_cell=nb_per_cell)
         nb = [np.sort(rec.neighbors(k)) for k in range(len(rec))]
         nb_off = np.zeros(len(rec) + 1, np.int64)
         nb_off[1:] = np.cumsum([len(x) for x in nb])
@@ -524,6 +528,7 @@ def main():
             make_cell_fixture(ref, name, w)
         make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
         make_locate_fixtures(ref, {k: ec[k] for k in EDGE_LOCATE_NAMES}, seed0=3900)
+        make_ghost_fixtures(ref, {k: ec[k] for k in EDGE_GHOST_NAMES}, seed0=4901, nb_per_cell=1000)
         return
     if "--normals-only" in sys.argv:
         make_normal_fixtures(ref, {**cases(), **edge_cases()})
@@ -545,6 +550,7 @@ def main():
         make_cell_fixture(ref, name, w)
     make_poly_fixtures(ref, ec, names=EDGE_POLY_NAMES)
     make_locate_fixtures(ref, {k: ec[k] for k in EDGE_LOCATE_NAMES}, seed0=3900)
+    make_ghost_fixtures(ref, {k: ec[k] for k in EDGE_GHOST_NAMES}, seed0=4901, nb_per_cell=1000)
     make_cli_fixtures()
 
 

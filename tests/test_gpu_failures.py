@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import voro_gb300 as vg
+from voro_gb300 import workloads as W
 from tests import _golden as G
 
 TOL = {"fp64": 1e-12, "mixed": 1e-10}
@@ -118,3 +119,31 @@ def test_put_device_nonfinite_refused_by_compute(gpu, n):
     d_xyzr[n // 3, 2] = 5.0
     con.compute_all_cells()
     assert abs(con.sum_cell_volumes() - 1000.0) < 1e-9 * 1000.0
+
+
+@pytest.mark.gpu
+def test_destroyed_containers_free_their_device_memory(gpu):
+    """Every device buffer a container allocates (binning, images, hand-on
+    lists) goes back when it is destroyed: a run of periodic and plain
+    containers created, computed and dropped leaves device memory where it
+    was."""
+    import gc
+    import torch
+    ws = [W.small_random(20000, kind=k, L=10.0, seed=s) for s, k in enumerate((2, 3, 0, 1))]
+    for w in ws:   # warm: the library's own one-off allocations
+        c = vg.from_workload(w, mode="mixed")
+        c.compute_all_cells()
+        del c
+    gc.collect()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(12):
+        for w in ws:
+            c = vg.from_workload(w, mode="mixed")
+            c.compute_all_cells()
+            c.cells()
+            del c
+    gc.collect()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < 64 << 20, f"{(free0 - free1) >> 20} MiB not returned"

@@ -539,7 +539,8 @@ int vgpu_container_destroy(vgpu_container *h) {
                       &h->gh_nb, &h->gh_nb_ovf, &h->gh_nb_off, &h->gh_nb_out, &h->gh_poly, &h->gh_poly_off,
                       &h->walls_dev,
                       &h->r_pos, &h->r_rad, &h->rec_off, &h->poly, &h->poly_off, &h->nb_off, &h->nb_out, &h->nb_tmp, &h->sum_tmp,
-                      &h->chk};
+                      &h->chk, &h->cell_list, &h->img_cnt, &h->img_off, &h->img_src, &h->x_gkey, &h->x_idx,
+                      &h->x_kalt, &h->x_rem, &h->x_valt};
     for (DevBuf *b : bufs) b->release();
     if (h->host_rb) cudaFreeHost(h->host_rb);
     for (int i = 0; i < 6; i++) cudaEventDestroy(h->ev[i]);

@@ -123,13 +123,14 @@ def test_put_device_nonfinite_refused_by_compute(gpu, n):
 
 @pytest.mark.gpu
 def test_destroyed_containers_free_their_device_memory(gpu):
-    """Every device buffer a container allocates (binning, images, hand-on
-    lists) goes back when it is destroyed: a run of periodic and plain
-    containers created, computed and dropped leaves device memory where it
-    was."""
+    """Every device buffer a container allocates (binning, a sheared box's
+    images, hand-on lists) goes back when it is destroyed: a run of sheared,
+    periodic and plain containers created, computed and dropped leaves
+    device memory where it was."""
     import gc
     import torch
     ws = [W.small_random(20000, kind=k, L=10.0, seed=s) for s, k in enumerate((2, 3, 0, 1))]
+    ws.append(W.sheared_periodic(n=20000, L=30.0, seed=7))
     for w in ws:   # warm: the library's own one-off allocations
         c = vg.from_workload(w, mode="mixed")
         c.compute_all_cells()

@@ -810,6 +810,54 @@ constexpr int kFinWarps = 2;   // warps per CTA (two cell slots per warp)
 #define VGPU_FIN_MIN_BLOCKS 7
 #endif
 
+// A record is checked before finish_record indexes the shared arrays by it:
+// its face count within the planes held there and, for a cell that met the
+// tolerance band (where a cut can leave links that do not return), every
+// vertex's planes below the face count, its neighbours below the vertex
+// count and its edges (links to a higher vertex) within the edge list's
+// room.  A record that fails is a failed cell (VGPU_FAIL_ADJACENCY),
+// written here; the caller then passes no cell (-1).  Every lane of the
+// G-lane group calls it (group collectives).
+template <int G>
+__device__ __forceinline__ int checked_cell(const CellParams &P, int k, int gl, int lane) {
+    const unsigned long long off = k >= 0 ? P.rec_off[k] : kNoRecord;
+    bool bad = false;
+    int owned = 0;
+    if (off != kNoRecord) {
+        const unsigned *R = P.rec + off;
+        const int nv = (int)R[0], nf = (int)R[1];
+        const unsigned *rv = R + kRecHeader;
+        if (nf > FinishShared<4 * G>::kNP || nf < 0 || nv < 0) {
+            bad = true;
+        } else if ((R[2] & VGPU_CELL_MARGINAL) != 0u) {
+            for (int t = gl; t < nv; t += G) {
+                const unsigned T = rv[t], A3 = rv[nv + t];
+                for (int e = 0; e < 3; e++) {
+                    const int q = (int)tri_plane(T, e), u = (int)((A3 >> (8 * e)) & 255u);
+                    if (q >= nf || u >= nv) bad = true;
+                    owned += u > t ? 1 : 0;
+                }
+            }
+        }
+    }
+    for (int dd = G / 2; dd >= 1; dd >>= 1) owned += __shfl_xor_sync(kFull, owned, dd, G);
+    if (owned > 3 * (4 * G) / 2) bad = true;   // FinishShared::stage
+    const unsigned gm = G == 32 ? kFull : (0xffffu << (lane & 16));
+    bad = (__ballot_sync(kFull, bad) & gm) != 0u;
+    if (!bad) return k;
+    if (gl == 0) {
+        const int o = P.a.outpos[k];
+        P.r.vol[o] = 0.0;
+        P.r.cen[3 * o] = P.r.cen[3 * o + 1] = P.r.cen[3 * o + 2] = 0.0;
+        P.r.nf[o] = 0;
+        P.r.nv[o] = 0;
+        P.r.maxr2[o] = 0.0;
+        P.r.flags[o] = VGPU_CELL_FAILED | (VGPU_FAIL_ADJACENCY << 8);
+        atomicAdd(&P.cnt->nb_failed, 1ull);
+    }
+    return -1;
+}
+
 // Two cells per warp, one per 16-lane half, when both have at most 64
 // vertices (nearly always: their FP64 work then fills the lanes better);
 // otherwise the whole warp does one cell after the other.
@@ -825,10 +873,10 @@ __device__ __forceinline__ void finish_pair(const CellParams &P, FinishWarp &W, 
         if (off != kNoRecord) nv = (int)P.rec[off];
     }
     if (!__any_sync(kFull, nv > 64)) {
-        finish_record<MODE, 16>(P, W.half[half], mine, gl);
+        finish_record<MODE, 16>(P, W.half[half], checked_cell<16>(P, mine, gl, lane), gl);
     } else {
-        finish_record<MODE, 32>(P, W.whole, k0, lane);
-        finish_record<MODE, 32>(P, W.whole, k1, lane);
+        finish_record<MODE, 32>(P, W.whole, checked_cell<32>(P, k0, lane, lane), lane);
+        finish_record<MODE, 32>(P, W.whole, checked_cell<32>(P, k1, lane, lane), lane);
     }
 }
 

@@ -58,7 +58,8 @@ extern "C" {
 #define VGPU_CELL_REPAIRED 4  /* at least one FP32 test was redone in FP64 */
 #define VGPU_CELL_FAILED 8    /* the cell exceeded every engine capacity; bits 8-11 give why: */
 #define VGPU_FAIL_PLANES 1    /*   more live planes than the last engine's 128 slots */
-#define VGPU_FAIL_ADJACENCY 2 /*   inconsistent vertex adjacency after a cut */
+#define VGPU_FAIL_ADJACENCY 2 /*   inconsistent vertex adjacency (after a cut, or in a
+                                   cell record the finish kernel checks) */
 #define VGPU_FAIL_VERTICES 3  /*   more vertices than the last engine's 128 slots */
 #define VGPU_FAIL_SEARCH 4    /*   the neighbour search did not terminate */
 #define VGPU_FAIL_RECORDS 5   /*   the polytope record store was full */
